@@ -1,0 +1,360 @@
+"""Benchmark of the CDE query path: collision queries/s on one GB300.
+
+Workload (one "step" = one batch): the star-container layout — a 64-vertex star container of
+radius 2000 with 4 rectangular holes and 2 inferior-quality zones, 300 placed items of 40 star
+types with 8-200 vertices — and 1,048,576 uniform queries (item, rotation, translation) checked
+with the HazardFilter that ignores the quality-1 zone.  A query's verdict is
+detect_surrogate_collision || detect_poly_collision (lbf/benches/ci_bench.rs:107-121).
+
+  value   — device throughput: queries resident in HBM, one kernel launch per step, CUDA events on
+            the launching stream, L2 flushed (256 MB write) between steps;
+  e2e     — the same metric through the C ABI's host entry point (jcde_detect_batch_host) from
+            pinned host memory: host->device copy, kernel, device->host copy every step;
+  roofline— algorithmic bytes per launch (oracle-counted per-query work of the same workload)
+            over the kernel's event time, against the measured HBM peak;
+  cpu_baseline — the oracle (C++ restatement of the reference CDE) on all host cores, bounded sample.
+
+`--impl reference` times the CPU restatement of the reference on the host cores instead (the
+reference itself is Rust and cannot be built here).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+sys.path.insert(0, os.path.join(REPO, "jagua-rs_gb300"))
+
+N_QUERIES = 1 << 20
+SEED = 0xC1
+WORKLOAD = ("star container r=2000 (64 v) + 4 rect holes + 2 quality zones; 300 placed items of 40 star "
+            "types (8-200 v); 1,048,576 uniform queries; HazKeyFilter ignoring the quality-1 zone")
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def host_cores() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+# ----------------------------------------------------------------------------------------------
+# clocks: nvidia-smi sampled during the timed region
+# ----------------------------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap,power.draw")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 8:
+                continue
+            try:
+                sm.append(float(p[0]))
+                mx.append(float(p[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------------------------
+# workload
+# ----------------------------------------------------------------------------------------------
+def make_layout(backend):
+    from jcde import workload as W
+
+    t = time.time()
+    lay, eng = W.star_container_layout(backend)
+    log(f"[bench] layout: {len(lay.hazards)} hazards, {len(lay.items)} item types, "
+        f"{lay.n_failed_placements} failed placements ({time.time() - t:.1f}s, {backend.name})")
+    return lay, eng
+
+
+def gpu_engine_for(lay):
+    import jcde
+
+    eng = jcde.CDEngine(lay.cde_bbox, (), jcde.CDEConfig(quadtree_depth=lay.depth, cd_threshold=lay.cd_threshold))
+    for it in lay.items:
+        eng.register_item(it.xy, it.poi, it.poles)
+    for hz in lay.hazards:
+        eng.register_hazard(jcde.Hazard(hz.kind, hz.xy, hz.poi, hz.dynamic, hz.tag))
+    return eng
+
+
+def oracle_engine_for(lay):
+    from jcde import workload as W
+    from oracle import oracle as O
+
+    O.build()
+    return W.replay(O.OracleBackend, lay)
+
+
+def bytes_per_query(counts: np.ndarray, n: int, lay, q) -> float:
+    """Algorithmic bytes per query: 20 B query + 1 B verdict, 8 B per item vertex, 12 B per ff pole,
+    16 B per quadtree node visited, 8 B per node-hazard entry scanned, 16 B per hazard edge tested,
+    16 B per point-in-polygon edge (counted by the oracle on the same queries)."""
+    nv = np.array([len(it.xy) for it in lay.items], np.float64)[q["item"]].mean()
+    nff = np.array([it.n_ff_poles for it in lay.items], np.float64)[q["item"]].mean()
+    c = counts.astype(np.float64) / n
+    return 21.0 + 8.0 * nv + 12.0 * nff + 16.0 * c[0] + 8.0 * c[1] + 16.0 * c[2] + 16.0 * c[3]
+
+
+def cpu_baseline(lay, queries, n_sample: int, repeats: int = 3):
+    oeng = oracle_engine_for(lay)
+    q = queries[:n_sample]
+    cores = host_cores()
+    counts = np.zeros(4, np.uint64)
+    oeng.detect_batch(q, ignored=lay.filter_keys, n_threads=cores, counts=counts)   # warm-up + work counts
+    best = float("inf")
+    verdicts = None
+    for _ in range(repeats):
+        t = time.perf_counter()
+        verdicts = oeng.detect_batch(q, ignored=lay.filter_keys, n_threads=cores)
+        best = min(best, time.perf_counter() - t)
+    return {"value": n_sample / best, "unit": "queries/s", "cores": cores, "kind": "port",
+            "sample": f"first {n_sample} queries of the batch, best of {repeats}"}, counts, verdicts
+
+
+def read_traffic(n_queries: int):
+    """DRAM bytes per launch of k_detect from the committed ncu summary, scaled to n_queries."""
+    path = os.path.join(REPO, "profiles", "k_detect_star.txt")
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_query"):
+                return float(line.split("=")[1]) * n_queries
+    except OSError:
+        pass
+    return None
+
+
+# ----------------------------------------------------------------------------------------------
+# arms
+# ----------------------------------------------------------------------------------------------
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    from jcde import workload as W
+    from oracle import oracle as O
+
+    O.build()
+    lay, oeng = make_layout(O.OracleBackend)
+    q = W.queries_for(lay, N_QUERIES, SEED)
+    cores = host_cores()
+    sample = 1 << 17
+    for i in range(args.warmup):
+        oeng.detect_batch(q[:sample], ignored=lay.filter_keys, n_threads=cores)
+    times = []
+    for i in range(args.steps):
+        s = q[(i * sample) % N_QUERIES:][:sample]
+        t = time.perf_counter()
+        oeng.detect_batch(s, ignored=lay.filter_keys, n_threads=cores)
+        times.append(time.perf_counter() - t)
+    value = sample * args.steps / sum(times)
+    desc = f"{sample} queries per step of the {N_QUERIES}-query batch"
+    line = {
+        "metric": "collision queries/s", "value": value, "unit": "queries/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "impl": "reference",
+        "config": {"workload": WORKLOAD, "queries_per_step": sample, "quadtree_depth": lay.depth,
+                   "cd_threshold": lay.cd_threshold},
+        "cpu_baseline": {"value": value, "unit": "queries/s", "cores": cores, "kind": "port", "sample": desc},
+        "e2e": {"value": value, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "CPU restatement of the reference CDE (Rust reference not buildable here), all host cores",
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args):
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    import jcde
+    from jcde import workload as W
+
+    jcde.lib()
+    lay, _ = make_layout(jcde.GpuBackend)
+    eng = gpu_engine_for(lay)
+    # weak scaling: every rank answers its own batch of N_QUERIES (distinct query stream per rank)
+    q = W.queries_for(lay, N_QUERIES, SEED, sid=3 + rank)
+    dq = torch.from_numpy(q.view(np.uint8).copy()).cuda()
+    out = torch.empty(N_QUERIES, dtype=torch.uint8, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    filt = lay.filter_keys
+
+    for _ in range(args.warmup):
+        eng.detect_batch(dq, filter=filt, out=out, stream=stream)
+    torch.cuda.synchronize()
+
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    launches0 = eng.kernel_launches()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            flush.zero_()
+            ev[i][0].record(stream)
+            eng.detect_batch(dq, filter=filt, out=out, stream=stream)
+            ev[i][1].record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    launches = eng.kernel_launches() - launches0
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    dev_s = sum(step_ms) / 1e3
+    if world > 1:
+        t = torch.tensor([dev_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        dev_s = float(t.item())
+    value = world * N_QUERIES * args.steps / dev_s
+    verdicts = out.cpu().numpy()
+
+    # e2e: host buffers through the C ABI, copies inside the timed region
+    hq = torch.from_numpy(q.view(np.uint8).copy()).pin_memory()
+    hout = torch.empty(N_QUERIES, dtype=torch.uint8).pin_memory()
+    import ctypes as C
+
+    from jcde._ffi import lib
+
+    fobj = jcde.engine._Filter(filt)
+    for _ in range(args.warmup):
+        lib().jcde_detect_batch_host(eng.h, hq.data_ptr(), N_QUERIES, fobj.ref, hout.data_ptr())
+    e2e_times = []
+    for i in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        st = lib().jcde_detect_batch_host(eng.h, hq.data_ptr(), N_QUERIES, fobj.ref, hout.data_ptr())
+        e2e_times.append(time.perf_counter() - t)
+        assert st == 0
+    e2e_s = sum(e2e_times)
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * N_QUERIES * args.steps / e2e_s
+    e2e_same = bool(np.array_equal(hout.numpy(), verdicts))
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return 0
+
+    # CPU baseline + algorithmic bytes per query (oracle on a bounded sample of the same queries)
+    cpu, counts, cpu_verdicts = cpu_baseline(lay, q, n_sample=args.cpu_sample)
+    sample_ok = bool(np.array_equal(cpu_verdicts, verdicts[: args.cpu_sample]))
+    bpq = bytes_per_query(counts, args.cpu_sample, lay, q[: args.cpu_sample])
+    avg_launch_s = dev_s / args.steps
+    achieved = bpq * N_QUERIES / avg_launch_s / 1e9
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    traffic = read_traffic(N_QUERIES)
+    clocks = clk.summary()
+    line = {
+        "metric": "collision queries/s", "value": value, "unit": "queries/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "queries_per_step": N_QUERIES, "quadtree_depth": lay.depth,
+                   "cd_threshold": lay.cd_threshold, "l2": "flushed between steps (256 MB write)",
+                   "parallelism": f"{world} rank(s), queries per rank, layout replicated"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback",
+                     "bytes_per_query": bpq, "kernel": "k_detect<3>"},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": N_QUERIES * 20,
+                "d2h_bytes_per_step": N_QUERIES, "same_verdicts": e2e_same},
+        "gpu_launches": launches,
+        "clocks": clocks,
+        "wall_s_timed": wall,
+        "parity_sample": {"queries": args.cpu_sample, "bit_exact": sample_ok},
+        "collision_rate": float(verdicts.mean()),
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="jcde", choices=["jcde", "reference"])
+    ap.add_argument("--cpu-sample", type=int, default=1 << 17)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,182 @@
+/*
+ * jcde — C ABI of the GB300 collision detection engine for 2D irregular nesting.
+ *
+ * One jcde_engine replaces one jagua-rs `CDEngine` (jagua-rs/src/collision_detection/cd_engine.rs:22-31):
+ * it owns the hazard registry, the quadtree (kept on the host and mirrored into device memory as a
+ * flat structure of arrays) and the item shapes with their surrogates.  Queries run as sm_103a
+ * kernels; every verdict and every collected hazard set equals the reference's f32 answer.
+ *
+ * Conventions
+ *   - every entry point returns a jcde_status (0 = JCDE_OK) and never aborts the process;
+ *   - hazard keys are dense uint32 slots (the reference's slotmap HazKey, hazards/hazard.rs:8-11);
+ *     a freed key is reused last-in first-out;
+ *   - a jcde_query carries the transformation as matrix entries (cos, sin, tx, ty) — the matrix
+ *     [[cos, -sin, tx], [sin, cos, ty]] of rot_transl_m (geometry/transformation.rs:475-483), which
+ *     is what the reference's CDE consumes (`&Transformation`); sin/cos are the caller's;
+ *   - `stream` arguments are cudaStream_t values passed as void* (NULL = legacy default stream);
+ *     "device" pointers must be CUDA device (or managed) memory, "host" pointers plain host memory;
+ *   - mutations (register / deregister / restore) must not overlap queries on the same engine.
+ */
+#ifndef JCDE_H
+#define JCDE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t jcde_status;
+#define JCDE_OK 0
+#define JCDE_ERR_ARG (-1)        /* invalid argument (null pointer, bad size, bad polygon, ...) */
+#define JCDE_ERR_CUDA (-2)       /* a CUDA runtime call failed */
+#define JCDE_ERR_CAPACITY (-3)   /* an output buffer is too small; sizes are reported */
+#define JCDE_ERR_NOT_FOUND (-4)  /* unknown hazard key / entity / item */
+#define JCDE_ERR_TIMEOUT (-5)    /* a bounded device wait gave up */
+#define JCDE_ERR_STATE (-6)      /* engine in a state that forbids the call */
+
+/* query verdicts */
+#define JCDE_FREE 0u       /* no collision */
+#define JCDE_COLLIDES 1u   /* collision */
+#define JCDE_INVALID 2u    /* the query names an unknown item */
+
+/* HazardEntity kinds (collision_detection/hazards/hazard.rs:38-51); Exterior has exterior scope */
+#define JCDE_PLACED_ITEM 0
+#define JCDE_EXTERIOR 1
+#define JCDE_HOLE 2
+#define JCDE_QUALITY_ZONE 3
+
+typedef struct jcde_engine jcde_engine;
+typedef struct jcde_snapshot jcde_snapshot;
+
+typedef struct { float x_min, y_min, x_max, y_max; } jcde_rect;   /* Rect (primitives/rect.rs:12-19) */
+
+/* CDEConfig (cd_engine.rs:346-353) incl. SPSurrogateConfig (fail_fast/sp_surrogate.rs:120-131) */
+typedef struct {
+    uint8_t quadtree_depth;        /* <= 15 */
+    uint8_t cd_threshold;
+    uint8_t reserved[2];
+    uint32_t n_pole_limits;        /* entries used in pole_limit_n / pole_limit_coverage (<= 3) */
+    uint32_t pole_limit_n[3];
+    float pole_limit_coverage[3];
+    uint32_t n_ff_poles;
+    uint32_t n_ff_piers;
+} jcde_config;
+
+/* Hazard (hazards/hazard.rs:16-23): entity kind + final shape.  `xy` holds n_vertices (x, y)
+ * pairs, `poi` the shape's pole of inaccessibility (x, y, r) — SPolygon::poi — used by the
+ * containment test (cd_engine.rs:231-255).  `tag` identifies the entity for deregistration by
+ * entity (cd_engine.rs:72-85); `dynamic` marks hazards that snapshots track (cd_engine.rs:98-106). */
+typedef struct {
+    int32_t kind;
+    int32_t dynamic;
+    const float* xy;
+    uint32_t n_vertices;
+    float poi[3];
+    uint64_t tag;
+} jcde_hazard;
+
+/* One candidate placement: item type + transformation matrix entries (20 bytes, packed). */
+#pragma pack(push, 1)
+typedef struct {
+    uint32_t item;
+    float cos_r, sin_r, tx, ty;
+} jcde_query;
+#pragma pack(pop)
+
+/* HazKeyFilter (hazards/filter.rs:13-48); n_ignored == 0 is NoFilter (filter.rs:58-65). */
+typedef struct {
+    const uint32_t* ignored;
+    uint32_t n_ignored;
+} jcde_filter;
+
+const char* jcde_status_string(jcde_status s);
+/* default CDEConfig of lbf (lbf/src/config.rs:37-45): depth 5, threshold 16, poles (100,0),(20,.75),(10,.9), 2 ff poles, 0 piers */
+void jcde_default_config(jcde_config* out);
+
+/* --- engine lifetime: CDEngine::new (cd_engine.rs:34-56) ------------------------------------ */
+jcde_status jcde_create(const jcde_config* cfg, jcde_rect bbox, const jcde_hazard* static_hazards,
+                        uint32_t n_static, jcde_engine** out);
+void jcde_destroy(jcde_engine* e);
+jcde_status jcde_bbox(const jcde_engine* e, jcde_rect* out);                     /* cd_engine.rs:329-331 */
+
+/* --- hazards --------------------------------------------------------------------------------- */
+jcde_status jcde_register_hazard(jcde_engine* e, const jcde_hazard* h, uint32_t* out_key);  /* cd_engine.rs:59-70 */
+jcde_status jcde_deregister_hazard(jcde_engine* e, uint32_t key);                            /* cd_engine.rs:87-96 */
+jcde_status jcde_deregister_hazard_by_entity(jcde_engine* e, int32_t kind, uint64_t tag,
+                                             uint32_t* out_key);                             /* cd_engine.rs:72-85 */
+jcde_status jcde_n_hazard_slots(const jcde_engine* e, uint32_t* out);
+
+/* --- items: shape_cd + surrogate of an Item (entities/item.rs:27-48) -------------------------- */
+/* poles_xyr: all surrogate poles (x, y, r), poles[0] = poi; the first cfg.n_ff_poles are probed
+ * (sp_surrogate.rs:55-57).  piers_xyxy: ff piers (sp_surrogate.rs:59-61), may be NULL. */
+jcde_status jcde_register_item(jcde_engine* e, const float* xy, uint32_t n_vertices, const float poi[3],
+                               const float* poles_xyr, uint32_t n_poles, const float* piers_xyxy,
+                               uint32_t n_piers, uint32_t* out_item);
+
+/* --- batched queries (device buffers, stream ordered) ----------------------------------------- */
+/* verdict[i] = detect_surrogate_collision(item.surrogate, T_i) || detect_poly_collision(T_i(item.shape))
+ * (cd_engine.rs:204-223 then :160-197, in the protocol of lbf/benches/ci_bench.rs:107-121). */
+jcde_status jcde_detect_batch(jcde_engine* e, const jcde_query* d_queries, uint32_t n,
+                              const jcde_filter* filter, uint8_t* d_verdicts, void* stream);
+/* Surrogate-only and polygon-only halves of the verdict (cd_engine.rs:204-223 / :160-197). */
+jcde_status jcde_detect_surrogate_batch(jcde_engine* e, const jcde_query* d_queries, uint32_t n,
+                                        const jcde_filter* filter, uint8_t* d_verdicts, void* stream);
+jcde_status jcde_detect_poly_batch(jcde_engine* e, const jcde_query* d_queries, uint32_t n,
+                                   const jcde_filter* filter, uint8_t* d_verdicts, void* stream);
+/* Same as jcde_detect_batch with host buffers: copies in, kernel, copies out, synchronises. */
+jcde_status jcde_detect_batch_host(jcde_engine* e, const jcde_query* h_queries, uint32_t n,
+                                   const jcde_filter* filter, uint8_t* h_verdicts);
+
+/* All colliding hazards per query: collect_surrogate_collisions then collect_poly_collisions into
+ * one collector (cd_engine.rs:296-310, :261-289; lbf/benches/ci_bench.rs:56-68).  A filter acts as
+ * keys pre-seeded into the collector (hazards/filter.rs:69-76): they are skipped and not reported.
+ * Keys of query i are d_ids[d_offsets[i] .. d_offsets[i] + d_counts[i]), ascending.  The order of
+ * the per-query runs inside d_ids is unspecified.  *d_total receives the number of keys needed; if
+ * it exceeds ids_cap, runs that did not fit are not written (d_counts still holds their sizes) and
+ * the host entry point returns JCDE_ERR_CAPACITY. */
+jcde_status jcde_collect_batch(jcde_engine* e, const jcde_query* d_queries, uint32_t n,
+                               const jcde_filter* filter, uint32_t* d_offsets, uint32_t* d_counts,
+                               uint32_t* d_ids, uint32_t ids_cap, uint32_t* d_total, void* stream);
+
+/* --- single queries with the reference's signatures (host buffers, synchronous) -------------- */
+/* detect_poly_collision (cd_engine.rs:160-197) of an already transformed shape with its poi. */
+jcde_status jcde_detect_poly(jcde_engine* e, const float* xy, uint32_t n_vertices, const float poi[3],
+                             const jcde_filter* filter, uint8_t* out);
+/* detect_surrogate_collision (cd_engine.rs:204-223) of an item's surrogate under a transformation. */
+jcde_status jcde_detect_surrogate(jcde_engine* e, uint32_t item, const float transform[4],
+                                  const jcde_filter* filter, uint8_t* out);
+/* collect_poly_collisions (cd_engine.rs:261-289); *n_out receives the count (even when > cap). */
+jcde_status jcde_collect_poly(jcde_engine* e, const float* xy, uint32_t n_vertices, const float poi[3],
+                              const jcde_filter* filter, uint32_t* keys, uint32_t cap, uint32_t* n_out);
+/* collect_surrogate_collisions (cd_engine.rs:296-310). */
+jcde_status jcde_collect_surrogate(jcde_engine* e, uint32_t item, const float transform[4],
+                                   const jcde_filter* filter, uint32_t* keys, uint32_t cap, uint32_t* n_out);
+
+/* --- snapshots: CDEngine::save / restore (cd_engine.rs:98-149) ------------------------------- */
+jcde_status jcde_save(const jcde_engine* e, jcde_snapshot** out);
+jcde_status jcde_restore(jcde_engine* e, const jcde_snapshot* s);
+void jcde_snapshot_free(jcde_snapshot* s);
+
+/* --- shape preparation (host): SPolygon::new (simple_polygon.rs:41-71) and surrogate poles
+ *     (fail_fast/pole.rs:12-47) — what Item::new / Container::new compute once per shape ------ */
+/* xy_out: n_vertices (x, y) in internal counter-clockwise order; bbox_out[4]; area_diam[2]; poi[3] */
+jcde_status jcde_spolygon_new(const float* xy, uint32_t n_vertices, float* xy_out, float* bbox_out,
+                              float* area_diam, float* poi);
+/* poles of an internal shape with the given area and poi; *n_out receives the count (even when > cap) */
+jcde_status jcde_surrogate_poles(const float* xy, uint32_t n_vertices, float area, const float poi[3],
+                                 const jcde_config* cfg, float* poles_xyr, uint32_t cap, uint32_t* n_out);
+
+/* --- introspection (tests, tooling) ----------------------------------------------------------- */
+/* canonical dump of the quadtree (pre-order, hazards by key, edges sorted); *n_words always set */
+jcde_status jcde_tree_dump(const jcde_engine* e, uint32_t* out, uint64_t cap, uint64_t* n_words);
+/* node count and flattened sizes currently mirrored on the device */
+jcde_status jcde_device_stats(jcde_engine* e, uint64_t* out5);
+/* number of kernels this engine has launched since creation (bench accounting) */
+uint64_t jcde_kernel_launches(const jcde_engine* e);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* JCDE_H */

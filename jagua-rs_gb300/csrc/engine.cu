@@ -1,0 +1,636 @@
+// jcde engine: C ABI (include/jcde.h), device mirror of the quadtree, kernel launches.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <list>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/jcde.h"
+#include "kernels.cuh"
+#include "prep.hpp"
+#include "qtree.hpp"
+
+using namespace jcde;
+
+namespace {
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    ~DevBuf() {
+        if (p) cudaFree(p);
+    }
+    bool ensure(size_t bytes) {
+        if (bytes <= cap) return true;
+        if (p) cudaFree(p);
+        p = nullptr;
+        size_t want = std::max<size_t>(bytes, cap + cap / 2);
+        want = (want + 255) & ~size_t(255);
+        if (cudaMalloc(&p, want) != cudaSuccess) {
+            cap = 0;
+            p = nullptr;
+            return false;
+        }
+        cap = want;
+        return true;
+    }
+    template <class T>
+    T* as() const { return reinterpret_cast<T*>(p); }
+};
+
+// One distinct filter: its ignored-key bitmask and per-node strongest presence on the device.
+struct FilterSlot {
+    std::vector<uint32_t> words;
+    uint64_t version = ~0ull;   // tree version the strength array was computed for
+    DevBuf d_mask, d_strength;
+};
+
+}  // namespace
+
+struct jcde_snapshot {
+    std::vector<HazardRec> dynamic_hazards;
+};
+
+struct jcde_engine {
+    jcde_config cfg{};
+    QuadTree tree;
+    // items (shape_cd + surrogate) on the host
+    std::vector<DItem> items;
+    std::vector<float2> iverts;
+    std::vector<float4> poles, piers;
+    bool items_dirty = true;
+    // device mirror
+    uint64_t tree_version = ~0ull;
+    FlatTree flat;
+    std::vector<DHaz> haz;
+    std::vector<float2> hverts;
+    DevBuf d_nodes, d_nedges, d_strength0, d_entries, d_edges, d_haz, d_hverts;
+    DevBuf d_items, d_iverts, d_poles, d_piers;
+    uint32_t n_nodes = 0;
+    // filters
+    std::list<FilterSlot> filters;
+    // staging for host entry points and single queries
+    DevBuf d_q, d_out, d_raw, d_coll;
+    cudaStream_t last_stream = nullptr;
+    bool have_last_stream = false;
+    cudaStream_t own[2] = {nullptr, nullptr};
+    int n_sms = 0;
+    int detect_blocks_per_sm = 0, collect_blocks_per_sm = 0;
+    uint64_t launches = 0;
+
+    jcde_engine(const jcde_config& c, Box bbox) : cfg(c), tree(c.quadtree_depth, c.cd_threshold, bbox) {}
+    ~jcde_engine() {
+        for (auto& s : own)
+            if (s) cudaStreamDestroy(s);
+    }
+};
+
+#define CUDA_TRY(x)                                   \
+    do {                                              \
+        if ((x) != cudaSuccess) return JCDE_ERR_CUDA; \
+    } while (0)
+
+static jcde_status upload(DevBuf& b, const void* src, size_t bytes) {
+    if (!b.ensure(std::max<size_t>(bytes, 16))) return JCDE_ERR_CUDA;
+    if (bytes) CUDA_TRY(cudaMemcpy(b.p, src, bytes, cudaMemcpyHostToDevice));
+    return JCDE_OK;
+}
+
+// Bring the device mirror up to date with the host quadtree and item table.
+static jcde_status sync_device(jcde_engine* e) {
+    if (e->tree_version == e->tree.version() && !e->items_dirty) return JCDE_OK;
+    // queries already queued on the caller's stream may still read the old image
+    if (e->have_last_stream) CUDA_TRY(cudaStreamSynchronize(e->last_stream));
+    if (e->tree_version != e->tree.version()) {
+        e->tree.flatten(e->flat);
+        e->haz.assign(e->tree.n_slots(), DHaz{});
+        e->hverts.clear();
+        const auto& hs = e->tree.hazards();
+        for (uint32_t k = 0; k < hs.size(); k++) {
+            if (!hs[k].alive) continue;
+            const Polygon& s = hs[k].shape;
+            DHaz& d = e->haz[k];
+            d.box = s.bbox;
+            d.poi_x = s.poi.c.x;
+            d.poi_y = s.poi.c.y;
+            d.v_off = (uint32_t)e->hverts.size();
+            d.v_cnt_scope = (uint32_t)s.v.size() | (kind_is_exterior(hs[k].kind) ? 0x80000000u : 0u);
+            for (const Pt& p : s.v) e->hverts.push_back(make_float2(p.x, p.y));
+        }
+        jcde_status st;
+        if ((st = upload(e->d_nodes, e->flat.nodes.data(), e->flat.nodes.size() * sizeof(DNode)))) return st;
+        if ((st = upload(e->d_nedges, e->flat.nedges.data(), e->flat.nedges.size() * 4))) return st;
+        if ((st = upload(e->d_strength0, e->flat.strength.data(), e->flat.strength.size()))) return st;
+        if ((st = upload(e->d_entries, e->flat.entries.data(), e->flat.entries.size() * sizeof(DEntry)))) return st;
+        if ((st = upload(e->d_edges, e->flat.edges.data(), e->flat.edges.size() * 4))) return st;
+        if ((st = upload(e->d_haz, e->haz.data(), e->haz.size() * sizeof(DHaz)))) return st;
+        if ((st = upload(e->d_hverts, e->hverts.data(), e->hverts.size() * sizeof(float2)))) return st;
+        e->n_nodes = (uint32_t)e->flat.nodes.size();
+        e->tree_version = e->tree.version();
+    }
+    if (e->items_dirty) {
+        jcde_status st;
+        if ((st = upload(e->d_items, e->items.data(), e->items.size() * sizeof(DItem)))) return st;
+        if ((st = upload(e->d_iverts, e->iverts.data(), e->iverts.size() * sizeof(float2)))) return st;
+        if ((st = upload(e->d_poles, e->poles.data(), e->poles.size() * sizeof(float4)))) return st;
+        if ((st = upload(e->d_piers, e->piers.data(), e->piers.size() * sizeof(float4)))) return st;
+        e->items_dirty = false;
+    }
+    return JCDE_OK;
+}
+
+static View base_view(const jcde_engine* e) {
+    View v;
+    v.nodes = e->d_nodes.as<DNode>();
+    v.entries = e->d_entries.as<DEntry>();
+    v.edges = e->d_edges.as<float4>();
+    v.haz = e->d_haz.as<DHaz>();
+    v.hverts = e->d_hverts.as<float2>();
+    v.items = e->d_items.as<DItem>();
+    v.iverts = e->d_iverts.as<float2>();
+    v.poles = e->d_poles.as<float4>();
+    v.piers = e->d_piers.as<float4>();
+    v.strength = e->d_strength0.as<uint8_t>();
+    v.mask = nullptr;
+    v.nedges = e->d_nedges.as<uint32_t>();
+    v.cde = e->tree.bbox();
+    v.n_items = (uint32_t)e->items.size();
+    v.n_slots = e->tree.n_slots();
+    v.cd_threshold = e->cfg.cd_threshold;
+    v.exterior = e->tree.exterior_key();
+    return v;
+}
+
+static uint32_t mask_words(const jcde_engine* e) { return std::max<uint32_t>(1, (e->tree.n_slots() + 31) / 32); }
+
+// Resolve a filter into the view: NoFilter uses the strength array built with the tree; any other
+// filter gets a cached device bitmask and a strength array recomputed by k_strength when needed.
+static jcde_status apply_filter(jcde_engine* e, const jcde_filter* f, cudaStream_t s, View& v) {
+    if (!f || f->n_ignored == 0) return JCDE_OK;
+    if (!f->ignored) return JCDE_ERR_ARG;
+    const uint32_t W = mask_words(e);
+    std::vector<uint32_t> words(W, 0u);
+    for (uint32_t i = 0; i < f->n_ignored; i++) {
+        uint32_t k = f->ignored[i];
+        if (k < e->tree.n_slots()) words[k >> 5] |= 1u << (k & 31);   // unknown keys ignore nothing
+    }
+    FilterSlot* slot = nullptr;
+    for (auto it = e->filters.begin(); it != e->filters.end(); ++it)
+        if (it->words == words) {
+            e->filters.splice(e->filters.begin(), e->filters, it);
+            slot = &e->filters.front();
+            break;
+        }
+    if (!slot) {
+        if (e->filters.size() >= 8) {
+            // the evicted slot may still be read by queued queries
+            if (e->have_last_stream) CUDA_TRY(cudaStreamSynchronize(e->last_stream));
+            e->filters.pop_back();
+        }
+        e->filters.emplace_front();
+        slot = &e->filters.front();
+        slot->words = words;
+        if (!slot->d_mask.ensure(W * 4)) return JCDE_ERR_CUDA;
+        CUDA_TRY(cudaMemcpy(slot->d_mask.p, words.data(), W * 4, cudaMemcpyHostToDevice));
+    }
+    v.mask = slot->d_mask.as<uint32_t>();
+    if (slot->version != e->tree.version()) {
+        if (!slot->d_strength.ensure(std::max<uint32_t>(e->n_nodes, 16))) return JCDE_ERR_CUDA;
+        k_strength<<<(e->n_nodes + 255) / 256, 256, 0, s>>>(v, e->n_nodes, slot->d_strength.as<uint8_t>());
+        CUDA_TRY(cudaGetLastError());
+        e->launches++;
+        slot->version = e->tree.version();
+    }
+    v.strength = slot->d_strength.as<uint8_t>();
+    return JCDE_OK;
+}
+
+static void init_launch_shape(jcde_engine* e) {
+    if (e->n_sms) return;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&e->n_sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&e->detect_blocks_per_sm, k_detect<3>, DETECT_WARPS * 32, 0);
+    if (e->detect_blocks_per_sm < 1) e->detect_blocks_per_sm = 1;
+    if (e->n_sms < 1) e->n_sms = 1;
+}
+
+static jcde_status launch_detect(jcde_engine* e, int mode, const jcde_query* dq, uint32_t n, const jcde_filter* f,
+                                 uint8_t* dout, cudaStream_t s, RawShape raw) {
+    jcde_status st = sync_device(e);
+    if (st) return st;
+    init_launch_shape(e);
+    View v = base_view(e);
+    if ((st = apply_filter(e, f, s, v))) return st;
+    if (n == 0) return JCDE_OK;
+    uint32_t want = (n + DETECT_WARPS - 1) / DETECT_WARPS;
+    uint32_t grid = std::min<uint32_t>(want, (uint32_t)(e->n_sms * e->detect_blocks_per_sm));
+    const uint32_t* q = reinterpret_cast<const uint32_t*>(dq);
+    switch (mode) {
+        case 1: k_detect<1><<<grid, DETECT_WARPS * 32, 0, s>>>(v, q, n, dout, raw); break;
+        case 2: k_detect<2><<<grid, DETECT_WARPS * 32, 0, s>>>(v, q, n, dout, raw); break;
+        default: k_detect<3><<<grid, DETECT_WARPS * 32, 0, s>>>(v, q, n, dout, raw); break;
+    }
+    CUDA_TRY(cudaGetLastError());
+    e->launches++;
+    e->last_stream = s;
+    e->have_last_stream = true;
+    return JCDE_OK;
+}
+
+static jcde_status launch_collect(jcde_engine* e, int mode, const jcde_query* dq, uint32_t n, const jcde_filter* f,
+                                  uint32_t* d_off, uint32_t* d_cnt, uint32_t* d_ids, uint32_t cap, uint32_t* d_total,
+                                  cudaStream_t s, RawShape raw) {
+    jcde_status st = sync_device(e);
+    if (st) return st;
+    init_launch_shape(e);
+    View v = base_view(e);
+    if ((st = apply_filter(e, f, s, v))) return st;
+    CUDA_TRY(cudaMemsetAsync(d_total, 0, 4, s));
+    if (n == 0) return JCDE_OK;
+    const uint32_t words = mask_words(e);
+    const size_t smem = (size_t)COLLECT_WARPS * words * 4;
+    if (smem > 200 * 1024) return JCDE_ERR_CAPACITY;   // > ~1.6M hazard slots
+    static bool attr_set[4] = {false, false, false, false};
+    const void* fn = mode == 1 ? (const void*)k_collect<1> : mode == 2 ? (const void*)k_collect<2> : (const void*)k_collect<3>;
+    if (smem > 48 * 1024 && !attr_set[mode]) {
+        CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        attr_set[mode] = true;
+    }
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, COLLECT_WARPS * 32, smem);
+    if (per_sm < 1) per_sm = 1;
+    uint32_t want = (n + COLLECT_WARPS - 1) / COLLECT_WARPS;
+    uint32_t grid = std::min<uint32_t>(want, (uint32_t)(e->n_sms * per_sm));
+    const uint32_t* q = reinterpret_cast<const uint32_t*>(dq);
+    switch (mode) {
+        case 1: k_collect<1><<<grid, COLLECT_WARPS * 32, smem, s>>>(v, q, n, words, d_off, d_cnt, d_ids, cap, d_total, raw); break;
+        case 2: k_collect<2><<<grid, COLLECT_WARPS * 32, smem, s>>>(v, q, n, words, d_off, d_cnt, d_ids, cap, d_total, raw); break;
+        default: k_collect<3><<<grid, COLLECT_WARPS * 32, smem, s>>>(v, q, n, words, d_off, d_cnt, d_ids, cap, d_total, raw); break;
+    }
+    CUDA_TRY(cudaGetLastError());
+    e->launches++;
+    e->last_stream = s;
+    e->have_last_stream = true;
+    return JCDE_OK;
+}
+
+static bool valid_config(const jcde_config* c) {
+    return c && c->quadtree_depth <= MAX_DEPTH && c->n_pole_limits <= 3;
+}
+
+static jcde_status make_hazard(const jcde_hazard* h, HazardRec& r) {
+    if (!h || !h->xy || h->n_vertices < 3) return JCDE_ERR_ARG;
+    if (h->kind < 0 || h->kind > 3) return JCDE_ERR_ARG;
+    r.kind = h->kind;
+    r.dynamic = h->dynamic != 0;
+    r.tag = h->tag;
+    r.shape.v.resize(h->n_vertices);
+    for (uint32_t i = 0; i < h->n_vertices; i++) r.shape.v[i] = Pt{h->xy[2 * i], h->xy[2 * i + 1]};
+    r.shape.poi = Disk{Pt{h->poi[0], h->poi[1]}, h->poi[2]};
+    return JCDE_OK;
+}
+
+extern "C" {
+
+const char* jcde_status_string(jcde_status s) {
+    switch (s) {
+        case JCDE_OK: return "ok";
+        case JCDE_ERR_ARG: return "invalid argument";
+        case JCDE_ERR_CUDA: return "CUDA runtime error";
+        case JCDE_ERR_CAPACITY: return "output capacity exceeded";
+        case JCDE_ERR_NOT_FOUND: return "not found";
+        case JCDE_ERR_TIMEOUT: return "device wait timed out";
+        case JCDE_ERR_STATE: return "invalid engine state";
+        default: return "unknown status";
+    }
+}
+
+void jcde_default_config(jcde_config* c) {
+    if (!c) return;
+    std::memset(c, 0, sizeof(*c));
+    c->quadtree_depth = 5;
+    c->cd_threshold = 16;
+    c->n_pole_limits = 3;
+    c->pole_limit_n[0] = 100; c->pole_limit_coverage[0] = 0.0f;
+    c->pole_limit_n[1] = 20;  c->pole_limit_coverage[1] = 0.75f;
+    c->pole_limit_n[2] = 10;  c->pole_limit_coverage[2] = 0.90f;
+    c->n_ff_poles = 2;
+    c->n_ff_piers = 0;
+}
+
+jcde_status jcde_create(const jcde_config* cfg, jcde_rect bbox, const jcde_hazard* hs, uint32_t n, jcde_engine** out) {
+    if (!out || !valid_config(cfg) || (n && !hs)) return JCDE_ERR_ARG;
+    if (!(bbox.x_min < bbox.x_max && bbox.y_min < bbox.y_max)) return JCDE_ERR_ARG;
+    *out = nullptr;
+    jcde_engine* e = new (std::nothrow) jcde_engine(*cfg, Box{bbox.x_min, bbox.y_min, bbox.x_max, bbox.y_max});
+    if (!e) return JCDE_ERR_CUDA;
+    for (uint32_t i = 0; i < n; i++) {
+        HazardRec r;
+        if (make_hazard(&hs[i], r)) {
+            delete e;
+            return JCDE_ERR_ARG;
+        }
+        e->tree.insert(std::move(r));
+    }
+    *out = e;
+    return JCDE_OK;
+}
+
+void jcde_destroy(jcde_engine* e) {
+    if (!e) return;
+    if (e->have_last_stream) cudaStreamSynchronize(e->last_stream);
+    delete e;
+}
+
+jcde_status jcde_bbox(const jcde_engine* e, jcde_rect* out) {
+    if (!e || !out) return JCDE_ERR_ARG;
+    Box b = e->tree.bbox();
+    *out = jcde_rect{b.x0, b.y0, b.x1, b.y1};
+    return JCDE_OK;
+}
+
+jcde_status jcde_register_hazard(jcde_engine* e, const jcde_hazard* h, uint32_t* out_key) {
+    if (!e) return JCDE_ERR_ARG;
+    HazardRec r;
+    jcde_status st = make_hazard(h, r);
+    if (st) return st;
+    uint32_t k = e->tree.insert(std::move(r));
+    if (out_key) *out_key = k;
+    return JCDE_OK;
+}
+
+jcde_status jcde_deregister_hazard(jcde_engine* e, uint32_t key) {
+    if (!e) return JCDE_ERR_ARG;
+    return e->tree.remove(key) ? JCDE_OK : JCDE_ERR_NOT_FOUND;
+}
+
+jcde_status jcde_deregister_hazard_by_entity(jcde_engine* e, int32_t kind, uint64_t tag, uint32_t* out_key) {
+    if (!e) return JCDE_ERR_ARG;
+    const auto& hs = e->tree.hazards();
+    for (uint32_t k = 0; k < hs.size(); k++)
+        if (hs[k].alive && hs[k].kind == kind && hs[k].tag == tag) {
+            e->tree.remove(k);
+            if (out_key) *out_key = k;
+            return JCDE_OK;
+        }
+    return JCDE_ERR_NOT_FOUND;
+}
+
+jcde_status jcde_n_hazard_slots(const jcde_engine* e, uint32_t* out) {
+    if (!e || !out) return JCDE_ERR_ARG;
+    *out = e->tree.n_slots();
+    return JCDE_OK;
+}
+
+jcde_status jcde_register_item(jcde_engine* e, const float* xy, uint32_t nv, const float poi[3], const float* poles,
+                               uint32_t n_poles, const float* piers, uint32_t n_piers, uint32_t* out_item) {
+    if (!e || !xy || nv < 3 || !poi || (n_poles && !poles) || (n_piers && !piers)) return JCDE_ERR_ARG;
+    DItem it{};
+    it.v_off = (uint32_t)e->iverts.size();
+    it.v_cnt = nv;
+    it.pole_off = (uint32_t)e->poles.size();
+    it.n_ff_poles = std::min<uint32_t>(e->cfg.n_ff_poles, n_poles);   // SPSurrogate::ff_poles (sp_surrogate.rs:55-57)
+    it.pier_off = (uint32_t)e->piers.size();
+    it.n_piers = n_piers;
+    it.poi_x = poi[0];
+    it.poi_y = poi[1];
+    for (uint32_t i = 0; i < nv; i++) e->iverts.push_back(make_float2(xy[2 * i], xy[2 * i + 1]));
+    for (uint32_t i = 0; i < n_poles; i++) e->poles.push_back(make_float4(poles[3 * i], poles[3 * i + 1], poles[3 * i + 2], 0.0f));
+    for (uint32_t i = 0; i < n_piers; i++)
+        e->piers.push_back(make_float4(piers[4 * i], piers[4 * i + 1], piers[4 * i + 2], piers[4 * i + 3]));
+    e->items.push_back(it);
+    e->items_dirty = true;
+    if (out_item) *out_item = (uint32_t)e->items.size() - 1;
+    return JCDE_OK;
+}
+
+jcde_status jcde_detect_batch(jcde_engine* e, const jcde_query* dq, uint32_t n, const jcde_filter* f, uint8_t* dout,
+                              void* stream) {
+    if (!e || (n && (!dq || !dout))) return JCDE_ERR_ARG;
+    return launch_detect(e, 3, dq, n, f, dout, (cudaStream_t)stream, RawShape{nullptr, 0, 0, 0, 0});
+}
+jcde_status jcde_detect_surrogate_batch(jcde_engine* e, const jcde_query* dq, uint32_t n, const jcde_filter* f,
+                                        uint8_t* dout, void* stream) {
+    if (!e || (n && (!dq || !dout))) return JCDE_ERR_ARG;
+    return launch_detect(e, 1, dq, n, f, dout, (cudaStream_t)stream, RawShape{nullptr, 0, 0, 0, 0});
+}
+jcde_status jcde_detect_poly_batch(jcde_engine* e, const jcde_query* dq, uint32_t n, const jcde_filter* f,
+                                   uint8_t* dout, void* stream) {
+    if (!e || (n && (!dq || !dout))) return JCDE_ERR_ARG;
+    return launch_detect(e, 2, dq, n, f, dout, (cudaStream_t)stream, RawShape{nullptr, 0, 0, 0, 0});
+}
+
+jcde_status jcde_detect_batch_host(jcde_engine* e, const jcde_query* hq, uint32_t n, const jcde_filter* f,
+                                   uint8_t* hout) {
+    if (!e || (n && (!hq || !hout))) return JCDE_ERR_ARG;
+    if (n == 0) return JCDE_OK;
+    for (auto& s : e->own)
+        if (!s) CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    if (!e->d_q.ensure((size_t)n * sizeof(jcde_query)) || !e->d_out.ensure(n)) return JCDE_ERR_CUDA;
+    jcde_status st = sync_device(e);
+    if (st) return st;
+    // resolve the filter once, on the first stream, before the pipelined chunks
+    View probe = base_view(e);
+    if ((st = apply_filter(e, f, e->own[0], probe))) return st;
+    CUDA_TRY(cudaStreamSynchronize(e->own[0]));
+    // chunks alternate between two streams so that copies overlap the other chunk's kernel
+    const uint32_t n_chunks = n >= (1u << 18) ? 4u : 1u;
+    const uint32_t chunk = (n + n_chunks - 1) / n_chunks;
+    jcde_query* dq = e->d_q.as<jcde_query>();
+    uint8_t* dout = e->d_out.as<uint8_t>();
+    for (uint32_t c = 0; c < n_chunks; c++) {
+        uint32_t a = c * chunk, b = std::min<uint32_t>(n, a + chunk);
+        if (a >= b) break;
+        cudaStream_t s = e->own[c & 1];
+        CUDA_TRY(cudaMemcpyAsync(dq + a, hq + a, (size_t)(b - a) * sizeof(jcde_query), cudaMemcpyHostToDevice, s));
+        if ((st = launch_detect(e, 3, dq + a, b - a, f, dout + a, s, RawShape{nullptr, 0, 0, 0, 0}))) return st;
+        CUDA_TRY(cudaMemcpyAsync(hout + a, dout + a, b - a, cudaMemcpyDeviceToHost, s));
+    }
+    CUDA_TRY(cudaStreamSynchronize(e->own[0]));
+    CUDA_TRY(cudaStreamSynchronize(e->own[1]));
+    e->have_last_stream = false;
+    return JCDE_OK;
+}
+
+jcde_status jcde_collect_batch(jcde_engine* e, const jcde_query* dq, uint32_t n, const jcde_filter* f, uint32_t* d_off,
+                               uint32_t* d_cnt, uint32_t* d_ids, uint32_t cap, uint32_t* d_total, void* stream) {
+    if (!e || !d_total || (n && (!dq || !d_off || !d_cnt)) || (cap && !d_ids)) return JCDE_ERR_ARG;
+    return launch_collect(e, 3, dq, n, f, d_off, d_cnt, d_ids, cap, d_total, (cudaStream_t)stream,
+                          RawShape{nullptr, 0, 0, 0, 0});
+}
+
+static jcde_status single_detect(jcde_engine* e, int mode, const jcde_query* hq, const float* xy, uint32_t nv,
+                                 const float* poi, const jcde_filter* f, uint8_t* out) {
+    if (!e->d_q.ensure(sizeof(jcde_query)) || !e->d_out.ensure(16)) return JCDE_ERR_CUDA;
+    RawShape raw{nullptr, 0, 0, 0, 0};
+    if (xy) {
+        if (!e->d_raw.ensure((size_t)nv * 8)) return JCDE_ERR_CUDA;
+        CUDA_TRY(cudaMemcpy(e->d_raw.p, xy, (size_t)nv * 8, cudaMemcpyHostToDevice));
+        raw = RawShape{e->d_raw.as<float2>(), nv, poi[0], poi[1], poi[2]};
+    } else {
+        CUDA_TRY(cudaMemcpy(e->d_q.p, hq, sizeof(jcde_query), cudaMemcpyHostToDevice));
+    }
+    jcde_status st = launch_detect(e, mode, e->d_q.as<jcde_query>(), 1, f, e->d_out.as<uint8_t>(), 0, raw);
+    if (st) return st;
+    uint8_t v = 0;
+    CUDA_TRY(cudaMemcpy(&v, e->d_out.p, 1, cudaMemcpyDeviceToHost));
+    *out = v;
+    return JCDE_OK;
+}
+
+jcde_status jcde_detect_poly(jcde_engine* e, const float* xy, uint32_t nv, const float poi[3], const jcde_filter* f,
+                             uint8_t* out) {
+    if (!e || !xy || nv < 3 || !poi || !out) return JCDE_ERR_ARG;
+    return single_detect(e, 2, nullptr, xy, nv, poi, f, out);
+}
+
+jcde_status jcde_detect_surrogate(jcde_engine* e, uint32_t item, const float t[4], const jcde_filter* f, uint8_t* out) {
+    if (!e || !t || !out) return JCDE_ERR_ARG;
+    if (item >= e->items.size()) return JCDE_ERR_NOT_FOUND;
+    jcde_query q{item, t[0], t[1], t[2], t[3]};
+    return single_detect(e, 1, &q, nullptr, 0, nullptr, f, out);
+}
+
+static jcde_status single_collect(jcde_engine* e, int mode, const jcde_query* hq, const float* xy, uint32_t nv,
+                                  const float* poi, const jcde_filter* f, uint32_t* keys, uint32_t cap, uint32_t* n_out) {
+    const uint32_t slots = std::max<uint32_t>(1, e->tree.n_slots());
+    if (!e->d_q.ensure(sizeof(jcde_query)) || !e->d_coll.ensure((size_t)(3 + slots) * 4)) return JCDE_ERR_CUDA;
+    RawShape raw{nullptr, 0, 0, 0, 0};
+    if (xy) {
+        if (!e->d_raw.ensure((size_t)nv * 8)) return JCDE_ERR_CUDA;
+        CUDA_TRY(cudaMemcpy(e->d_raw.p, xy, (size_t)nv * 8, cudaMemcpyHostToDevice));
+        raw = RawShape{e->d_raw.as<float2>(), nv, poi[0], poi[1], poi[2]};
+    } else {
+        CUDA_TRY(cudaMemcpy(e->d_q.p, hq, sizeof(jcde_query), cudaMemcpyHostToDevice));
+    }
+    uint32_t* c = e->d_coll.as<uint32_t>();
+    jcde_status st = launch_collect(e, mode, e->d_q.as<jcde_query>(), 1, f, c, c + 1, c + 3, slots, c + 2, 0, raw);
+    if (st) return st;
+    std::vector<uint32_t> h(3 + slots);
+    CUDA_TRY(cudaMemcpy(h.data(), c, h.size() * 4, cudaMemcpyDeviceToHost));
+    const uint32_t cnt = h[1];
+    *n_out = cnt;
+    if (cnt > cap) return JCDE_ERR_CAPACITY;
+    for (uint32_t i = 0; i < cnt; i++) keys[i] = h[3 + h[0] + i];
+    return JCDE_OK;
+}
+
+jcde_status jcde_collect_poly(jcde_engine* e, const float* xy, uint32_t nv, const float poi[3], const jcde_filter* f,
+                              uint32_t* keys, uint32_t cap, uint32_t* n_out) {
+    if (!e || !xy || nv < 3 || !poi || !n_out || (cap && !keys)) return JCDE_ERR_ARG;
+    return single_collect(e, 2, nullptr, xy, nv, poi, f, keys, cap, n_out);
+}
+
+jcde_status jcde_collect_surrogate(jcde_engine* e, uint32_t item, const float t[4], const jcde_filter* f, uint32_t* keys,
+                                   uint32_t cap, uint32_t* n_out) {
+    if (!e || !t || !n_out || (cap && !keys)) return JCDE_ERR_ARG;
+    if (item >= e->items.size()) return JCDE_ERR_NOT_FOUND;
+    jcde_query q{item, t[0], t[1], t[2], t[3]};
+    return single_collect(e, 1, &q, nullptr, 0, nullptr, f, keys, cap, n_out);
+}
+
+jcde_status jcde_save(const jcde_engine* e, jcde_snapshot** out) {
+    if (!e || !out) return JCDE_ERR_ARG;
+    jcde_snapshot* s = new (std::nothrow) jcde_snapshot();
+    if (!s) return JCDE_ERR_CUDA;
+    for (const HazardRec& h : e->tree.hazards())
+        if (h.alive && h.dynamic) s->dynamic_hazards.push_back(h);
+    *out = s;
+    return JCDE_OK;
+}
+
+// CDEngine::restore (cd_engine.rs:109-149): diff by entity, deregister the surplus, register the rest.
+jcde_status jcde_restore(jcde_engine* e, const jcde_snapshot* s) {
+    if (!e || !s) return JCDE_ERR_ARG;
+    std::vector<std::pair<uint32_t, std::pair<int32_t, uint64_t>>> to_remove;
+    const auto& hs = e->tree.hazards();
+    for (uint32_t k = 0; k < hs.size(); k++)
+        if (hs[k].alive && hs[k].dynamic) to_remove.push_back({k, {hs[k].kind, hs[k].tag}});
+    std::vector<const HazardRec*> to_add;
+    for (const HazardRec& h : s->dynamic_hazards) {
+        auto it = std::find_if(to_remove.begin(), to_remove.end(),
+                               [&](const auto& r) { return r.second.first == h.kind && r.second.second == h.tag; });
+        if (it != to_remove.end()) {
+            *it = to_remove.back();   // Vec::swap_remove
+            to_remove.pop_back();
+        } else {
+            to_add.push_back(&h);
+        }
+    }
+    for (const auto& r : to_remove) e->tree.remove(r.first);
+    for (const HazardRec* h : to_add) {
+        HazardRec c = *h;
+        e->tree.insert(std::move(c));
+    }
+    return JCDE_OK;
+}
+
+void jcde_snapshot_free(jcde_snapshot* s) { delete s; }
+
+jcde_status jcde_spolygon_new(const float* xy, uint32_t nv, float* xy_out, float* bbox_out, float* area_diam, float* poi) {
+    if (!xy || !xy_out || !bbox_out || !area_diam || !poi || nv < 3) return JCDE_ERR_ARG;
+    std::vector<Pt> pts(nv);
+    for (uint32_t i = 0; i < nv; i++) pts[i] = Pt{xy[2 * i], xy[2 * i + 1]};
+    PreparedPolygon p;
+    if (spolygon_new(std::move(pts), &p)) return JCDE_ERR_ARG;
+    for (uint32_t i = 0; i < nv; i++) {
+        xy_out[2 * i] = p.v[i].x;
+        xy_out[2 * i + 1] = p.v[i].y;
+    }
+    bbox_out[0] = p.bbox.x0; bbox_out[1] = p.bbox.y0; bbox_out[2] = p.bbox.x1; bbox_out[3] = p.bbox.y1;
+    area_diam[0] = p.area;
+    area_diam[1] = p.diameter;
+    poi[0] = p.poi.c.x; poi[1] = p.poi.c.y; poi[2] = p.poi.r;
+    return JCDE_OK;
+}
+
+jcde_status jcde_surrogate_poles(const float* xy, uint32_t nv, float area, const float poi[3], const jcde_config* cfg,
+                                 float* poles_xyr, uint32_t cap, uint32_t* n_out) {
+    if (!xy || nv < 3 || !poi || !valid_config(cfg) || !n_out || (cap && !poles_xyr)) return JCDE_ERR_ARG;
+    std::vector<Pt> pts(nv);
+    for (uint32_t i = 0; i < nv; i++) pts[i] = Pt{xy[2 * i], xy[2 * i + 1]};
+    PoleLimit lim[3];
+    for (uint32_t i = 0; i < cfg->n_pole_limits; i++) lim[i] = PoleLimit{cfg->pole_limit_n[i], cfg->pole_limit_coverage[i]};
+    std::vector<Disk> poles;
+    if (surrogate_poles(pts, area, Disk{Pt{poi[0], poi[1]}, poi[2]}, lim, (int)cfg->n_pole_limits, &poles))
+        return JCDE_ERR_ARG;
+    *n_out = (uint32_t)poles.size();
+    if (poles.size() > cap) return JCDE_ERR_CAPACITY;
+    for (size_t i = 0; i < poles.size(); i++) {
+        poles_xyr[3 * i] = poles[i].c.x;
+        poles_xyr[3 * i + 1] = poles[i].c.y;
+        poles_xyr[3 * i + 2] = poles[i].r;
+    }
+    return JCDE_OK;
+}
+
+jcde_status jcde_tree_dump(const jcde_engine* e, uint32_t* out, uint64_t cap, uint64_t* n_words) {
+    if (!e || !n_words) return JCDE_ERR_ARG;
+    std::vector<uint32_t> d;
+    e->tree.dump(d);
+    *n_words = d.size();
+    if (d.size() > cap) return out ? JCDE_ERR_CAPACITY : JCDE_OK;
+    if (out) std::memcpy(out, d.data(), d.size() * 4);
+    return JCDE_OK;
+}
+
+jcde_status jcde_device_stats(jcde_engine* e, uint64_t* out5) {
+    if (!e || !out5) return JCDE_ERR_ARG;
+    jcde_status st = sync_device(e);
+    if (st) return st;
+    out5[0] = e->flat.nodes.size();
+    out5[1] = e->flat.entries.size();
+    out5[2] = e->flat.edges.size() / 4;
+    out5[3] = e->hverts.size();
+    out5[4] = e->iverts.size();
+    return JCDE_OK;
+}
+
+uint64_t jcde_kernel_launches(const jcde_engine* e) { return e ? e->launches : 0; }
+
+}  // extern "C"

@@ -1,0 +1,261 @@
+// Geometry predicates of the CDE query path, compiled both for the host (quadtree builder, pole
+// generation) and for sm_103a kernels, so that both sides round every operation identically.
+//
+// Every function restates an f32 routine of jagua-rs (path:line in the comment).  Rules that keep
+// the device bit-identical with the reference's f32 arithmetic:
+//   * device code is compiled with -fmad=false -prec-div=true -prec-sqrt=true -ftz=false, host code
+//     with -ffp-contract=off: Rust never contracts a*b+c into a fused multiply-add;
+//   * expressions keep the reference's evaluation order ((a*b) - (c*d), left-to-right sums);
+//   * f32::min / f32::max are fminf / fmaxf (a NaN operand is ignored);
+//   * sin/cos are never evaluated here: transforms arrive as matrix entries.
+#pragma once
+#include <cstdint>
+#include <cstring>
+#include <cmath>
+
+#ifdef __CUDACC__
+#define JHD __host__ __device__ __forceinline__
+#define JCDE_UNROLL _Pragma("unroll")
+#else
+#define JHD inline
+#define JCDE_UNROLL
+#endif
+
+namespace jcde {
+
+struct Pt { float x, y; };
+struct Seg { Pt s, e; };
+struct Box { float x0, y0, x1, y1; };
+struct Disk { Pt c; float r; };
+
+enum Rel : int { REL_INTERSECTING = 0, REL_ENCLOSED = 1, REL_SURROUNDING = 2, REL_DISJOINT = 3 };
+
+JHD float fmn(float a, float b) { return fminf(a, b); }
+JHD float fmx(float a, float b) { return fmaxf(a, b); }
+
+JHD int32_t f2i(float f) {
+#ifdef __CUDA_ARCH__
+    return __float_as_int(f);
+#else
+    int32_t i;
+    std::memcpy(&i, &f, 4);
+    return i;
+#endif
+}
+
+// util/fpa.rs:18-31 — FPA equality is float-cmp's approx_eq!(f32) with the default margin:
+// exactly equal, or |a-b| <= f32::EPSILON, or at most 4 ULPs apart (bit patterns as i32).
+JHD bool fpa_eq(float a, float b) {
+    if (a == b) return true;
+    if (fabsf(a - b) <= 1.1920928955078125e-07f) return true;
+    int32_t d = (int32_t)((uint32_t)f2i(a) - (uint32_t)f2i(b));
+    int32_t ad = d < 0 ? (d == INT32_MIN ? INT32_MAX : -d) : d;
+    return ad <= 4;
+}
+JHD bool fpa_le(float a, float b) { return fpa_eq(a, b) || a < b; }
+JHD bool fpa_ge(float a, float b) { return fpa_eq(a, b) || a > b; }
+JHD bool fpa_lt(float a, float b) { return !fpa_eq(a, b) && a < b; }
+JHD bool fpa_gt(float a, float b) { return !fpa_eq(a, b) && a > b; }
+
+// rect.rs:266-271
+JHD bool box_hits_box(const Box& a, const Box& b) {
+    return fmx(a.x0, b.x0) <= fmn(a.x1, b.x1) && fmx(a.y0, b.y0) <= fmn(a.y1, b.y1);
+}
+// rect.rs:46-65 — relation of `s` to `o`
+JHD int box_relation(const Box& s, const Box& o) {
+    if (!box_hits_box(s, o)) return REL_DISJOINT;
+    if (s.x0 <= o.x0 && s.y0 <= o.y0 && s.x1 >= o.x1 && s.y1 >= o.y1) return REL_SURROUNDING;
+    if (s.x0 >= o.x0 && s.y0 >= o.y0 && s.x1 <= o.x1 && s.y1 <= o.y1) return REL_ENCLOSED;
+    return REL_INTERSECTING;
+}
+// rect.rs:46-65 restricted to the Surrounding answer (get_virtual_root, detect_poly_collision)
+JHD bool box_surrounds(const Box& s, const Box& o) {
+    return box_hits_box(s, o) && s.x0 <= o.x0 && s.y0 <= o.y0 && s.x1 >= o.x1 && s.y1 >= o.y1;
+}
+// rect.rs:70-89 + rect.rs:274-279
+JHD int box_almost_relation(const Box& s, const Box& o) {
+    bool hit = fpa_le(fmx(s.x0, o.x0), fmn(s.x1, o.x1)) && fpa_le(fmx(s.y0, o.y0), fmn(s.y1, o.y1));
+    if (!hit) return REL_DISJOINT;
+    if (fpa_le(s.x0, o.x0) && fpa_le(s.y0, o.y0) && fpa_ge(s.x1, o.x1) && fpa_ge(s.y1, o.y1))
+        return REL_SURROUNDING;
+    if (fpa_ge(s.x0, o.x0) && fpa_ge(s.y0, o.y0) && fpa_le(s.x1, o.x1) && fpa_le(s.y1, o.y1))
+        return REL_ENCLOSED;
+    return REL_INTERSECTING;
+}
+// rect.rs:282-288
+JHD bool box_hits_pt(const Box& r, Pt p) { return p.x >= r.x0 && p.x <= r.x1 && p.y >= r.y0 && p.y <= r.y1; }
+// rect.rs:248-253
+JHD Pt box_mid(const Box& r) { return Pt{(r.x0 + r.x1) / 2.0f, (r.y0 + r.y1) / 2.0f}; }
+// rect.rs:259-263
+JHD float box_diameter(const Box& r) {
+    float dx = r.x1 - r.x0;
+    float dy = r.y1 - r.y0;
+    return sqrtf(dx * dx + dy * dy);
+}
+// rect.rs:93-109
+JHD Box box_square(const Box& r) {
+    float w = r.x1 - r.x0, h = r.y1 - r.y0;
+    float dx = 0.0f, dy = 0.0f;
+    if (h < w) dy = (w - h) / 2.0f;
+    else if (w < h) dx = (h - w) / 2.0f;
+    return Box{r.x0 - dx, r.y0 - dy, r.x1 + dx, r.y1 + dy};
+}
+// rect.rs:154-161 corner i (quadrant order: ++, -+, --, +-)
+JHD Pt box_corner(const Box& r, int i) {
+    return Pt{(i == 0 || i == 3) ? r.x1 : r.x0, (i == 0 || i == 1) ? r.y1 : r.y0};
+}
+// rect.rs:141-151 with rect.rs:35-41 — quadrant i of r (from_diagonal_corners(corner_i, mid))
+JHD Box box_quadrant(const Box& r, int i) {
+    Pt m = box_mid(r);
+    Pt c = box_corner(r, i);
+    return Box{fmn(c.x, m.x), fmn(c.y, m.y), fmx(c.x, m.x), fmx(c.y, m.y)};
+}
+
+// rect.rs:301-345 — Rect collides with Edge
+JHD bool box_hits_seg(const Box& r, const Seg& e) {
+    float ex0 = fmn(e.s.x, e.e.x), ex1 = fmx(e.s.x, e.e.x);
+    float ey0 = fmn(e.s.y, e.e.y), ey1 = fmx(e.s.y, e.e.y);
+    if (fmx(ex0, r.x0) > fmn(ex1, r.x1) || fmx(ey0, r.y0) > fmn(ey1, r.y1)) return false;
+    if (box_hits_pt(r, e.s) || box_hits_pt(r, e.e)) return true;
+    float sx = e.s.x, sy = e.s.y;
+    float dx = e.e.x - sx, dy = e.e.y - sy;
+    bool all_pos = true, all_neg = true;
+JCDE_UNROLL
+    for (int i = 0; i < 4; i++) {
+        Pt c = box_corner(r, i);
+        float side = (c.x - sx) * dy - (c.y - sy) * dx;
+        all_pos = all_pos && side > 0.0f;
+        all_neg = all_neg && side < 0.0f;
+    }
+    return !(all_pos || all_neg);
+}
+
+// edge.rs:180-228 (location not requested) — e1 is the querying edge, e2 the hazard edge
+JHD bool seg_hits_seg(const Seg& e1, const Seg& e2) {
+    float x1 = e1.s.x, y1 = e1.s.y, x2 = e1.e.x, y2 = e1.e.y;
+    float x3 = e2.s.x, y3 = e2.s.y, x4 = e2.e.x, y4 = e2.e.y;
+    if (fmx(fmn(x1, x2), fmn(x3, x4)) > fmn(fmx(x1, x2), fmx(x3, x4))) return false;
+    if (fmx(fmn(y1, y2), fmn(y3, y4)) > fmn(fmx(y1, y2), fmx(y3, y4))) return false;
+    float t_nom = (x2 - x4) * (y4 - y3) - (y2 - y4) * (x4 - x3);
+    float t_den = (x2 - x1) * (y4 - y3) - (y2 - y1) * (x4 - x3);
+    float u_nom = (x2 - x4) * (y2 - y1) - (y2 - y4) * (x2 - x1);
+    float u_den = t_den;  // edge.rs:210 is the same expression as edge.rs:208
+    if (t_den == 0.0f || u_den == 0.0f) return false;
+    float t = t_nom / t_den;
+    float u = u_nom / u_den;
+    return 0.0f <= t && t <= 1.0f && 0.0f <= u && u <= 1.0f;
+}
+
+// qt_traits.rs:144-177 — half of e2 hit by e1: -1 none, 0 first half, 1 halfway, 2 second half
+JHD int seg_hit_half(const Seg& e1, const Seg& e2) {
+    float x1 = e1.s.x, y1 = e1.s.y, x2 = e1.e.x, y2 = e1.e.y;
+    float x3 = e2.s.x, y3 = e2.s.y, x4 = e2.e.x, y4 = e2.e.y;
+    float t_nom = (x2 - x4) * (y4 - y3) - (y2 - y4) * (x4 - x3);
+    float t_den = (x2 - x1) * (y4 - y3) - (y2 - y1) * (x4 - x3);
+    float u_nom = (x2 - x4) * (y2 - y1) - (y2 - y4) * (x2 - x1);
+    if (t_den == 0.0f) return -1;
+    float t = t_nom / t_den;
+    float u = u_nom / t_den;
+    if (0.0f <= t && t <= 1.0f && 0.0f <= u && u <= 1.0f) return u > 0.5f ? 0 : (u < 0.5f ? 2 : 1);
+    return -1;
+}
+
+// qt_traits.rs:19-106 — which of the 4 quadrants of node box r the edge touches (bit i = quadrant i)
+JHD uint32_t seg_quadrant_mask(const Seg& e, const Box& r) {
+    float ex0 = fmn(e.s.x, e.e.x), ex1 = fmx(e.s.x, e.e.x);
+    float ey0 = fmn(e.s.y, e.e.y), ey1 = fmx(e.s.y, e.e.y);
+    uint32_t hit = 0, undet = 0;
+JCDE_UNROLL
+    for (int i = 0; i < 4; i++) {
+        Box q = box_quadrant(r, i);
+        bool no = fmx(ex0, q.x0) > fmn(ex1, q.x1) || fmx(ey0, q.y0) > fmn(ey1, q.y1);
+        if (!no) {
+            if (box_hits_pt(q, e.s) || box_hits_pt(q, e.e)) hit |= 1u << i;
+            else undet |= 1u << i;
+        }
+    }
+    if (!undet) return hit;
+    Pt c = box_mid(r);
+    // sides (rect.rs:164-184): top c0->c1, left c1->c2, bottom c2->c3, right c3->c0; bisectors
+    // (qt_traits.rs:123-130).  half_intersect (qt_traits.rs:110-140) runs only while a quadrant it
+    // could set is undetermined, and sets the quadrants of the half of the side that was hit.
+    const Seg sides[6] = {
+        Seg{Pt{r.x0, r.y1}, Pt{r.x0, r.y0}},  // left:   first half -> q1, second -> q2
+        Seg{Pt{r.x1, r.y0}, Pt{r.x1, r.y1}},  // right:  q3 | q0
+        Seg{Pt{r.x1, r.y1}, Pt{r.x0, r.y1}},  // top:    q0 | q1
+        Seg{Pt{r.x0, r.y0}, Pt{r.x1, r.y0}},  // bottom: q2 | q3
+        Seg{Pt{r.x0, c.y}, Pt{r.x1, c.y}},    // h-bisector: q1,q2 | q0,q3
+        Seg{Pt{c.x, r.y0}, Pt{c.x, r.y1}},    // v-bisector: q2,q3 | q0,q1
+    };
+    const uint32_t fst[6] = {0x2, 0x8, 0x1, 0x4, 0x6, 0xC};
+    const uint32_t sec[6] = {0x4, 0x1, 0x2, 0x8, 0x9, 0x3};
+JCDE_UNROLL
+    for (int k = 0; k < 6; k++) {
+        if ((fst[k] | sec[k]) & undet) {
+            int h = seg_hit_half(e, sides[k]);
+            uint32_t set = (h == 0 ? fst[k] : 0u) | (h == 2 ? sec[k] : 0u) | (h == 1 ? (fst[k] | sec[k]) : 0u);
+            hit |= set;
+            undet &= ~set;
+        }
+    }
+    return hit;
+}
+
+// edge.rs:63-87 + edge.rs:152-159 — squared distance from p to the segment
+JHD float seg_sq_dist(const Seg& e, Pt p) {
+    float x1 = e.s.x, y1 = e.s.y, x2 = e.e.x, y2 = e.e.y;
+    float a = p.x - x1, b = p.y - y1, c = x2 - x1, d = y2 - y1;
+    float dot = a * c + b * d;
+    float len_sq = c * c + d * d;
+    float param = -1.0f;
+    if (len_sq != 0.0f) param = dot / len_sq;
+    float xx, yy;
+    if (param < 0.0f) { xx = x1; yy = y1; }
+    else if (param > 1.0f) { xx = x2; yy = y2; }
+    else { xx = x1 + param * c; yy = y1 + param * d; }
+    float dx = p.x - xx, dy = p.y - yy;
+    return dx * dx + dy * dy;
+}
+// circle.rs:506-510
+JHD bool disk_hits_seg(const Disk& c, const Seg& e) { return seg_sq_dist(e, c.c) <= c.r * c.r; }
+// circle.rs:512-525
+JHD bool disk_hits_box(const Disk& c, const Box& r) {
+    float nx = fmx(r.x0, fmn(c.c.x, r.x1));
+    float ny = fmx(r.y0, fmn(c.c.y, r.y1));
+    float dx = nx - c.c.x, dy = ny - c.c.y;
+    return dx * dx + dy * dy <= c.r * c.r;
+}
+// circle.rs:527-531 (point.sq_distance_to(center) <= r^2)
+JHD bool disk_hits_pt(const Disk& c, Pt p) {
+    float dx = p.x - c.c.x, dy = p.y - c.c.y;
+    return dx * dx + dy * dy <= c.r * c.r;
+}
+// circle.rs:551-560 — separation distance (either side) from the circle to p
+JHD float disk_sep_dist(const Disk& c, Pt p) {
+    float dx = p.x - c.c.x, dy = p.y - c.c.y;
+    float d = sqrtf(dx * dx + dy * dy);
+    return d <= c.r ? c.r - d : d - c.r;
+}
+JHD uint32_t disk_quadrant_mask(const Disk& c, const Box& r) {  // qt_traits.rs:9-13 default
+    uint32_t m = 0;
+JCDE_UNROLL
+    for (int i = 0; i < 4; i++) m |= disk_hits_box(c, box_quadrant(r, i)) ? (1u << i) : 0u;
+    return m;
+}
+
+// point.rs:259-264 with the rot_transl_m matrix [[c, -s, tx], [s, c, ty]] (transformation.rs:475-483)
+JHD Pt xform(Pt p, float c, float s, float tx, float ty) {
+    float ms = -s;
+    return Pt{c * p.x + ms * p.y + tx * 1.0f, s * p.x + c * p.y + ty * 1.0f};
+}
+
+// One edge's contribution to the ray-cast point-in-polygon test of simple_polygon.rs:255-292.
+// `ray` runs from p to the right, past the polygon's bbox; returns 1 when the edge counts.
+JHD int pip_edge_term(const Seg& ray, const Seg& e, Pt p) {
+    if ((fpa_eq(e.s.y, p.y) && fpa_gt(e.s.x, p.x)) || (fpa_eq(e.e.y, p.y) && fpa_gt(e.e.x, p.x)))
+        return (fpa_lt(e.s.y, p.y) || fpa_lt(e.e.y, p.y)) ? 1 : 0;
+    return seg_hits_seg(ray, e) ? 1 : 0;
+}
+JHD Seg pip_ray(const Box& bbox, Pt p) { return Seg{p, Pt{bbox.x1 + (bbox.x1 - bbox.x0), p.y}}; }
+
+}  // namespace jcde

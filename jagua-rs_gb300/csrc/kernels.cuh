@@ -1,0 +1,557 @@
+// sm_103a kernels of the CDE query path.
+//
+// One warp resolves one candidate placement (item, transformation).  The reference answers a query
+// sequentially (lbf/benches/ci_bench.rs:107-121): the fail-fast poles of the surrogate are walked
+// down the quadtree from the root (cd_engine.rs:204-223), then every edge of the transformed item
+// is walked down from the virtual root (cd_engine.rs:160-173), then the partially present hazards of
+// the virtual root are tested for containment (cd_engine.rs:176-193).  Its answer is the OR of all
+// those tests, so the warp spreads them over lanes:
+//   * probes (poles, piers, item edges) — one per lane, each lane walks its own descent with a
+//     4-bit pending-children mask per level packed into one 64-bit register (no stack memory); a
+//     lane that hits raises a per-warp shared-memory flag and every other lane abandons its walk at
+//     its next node (early exit at node granularity);
+//   * containment — lanes evaluate the FPA bounding-box relation of one hazard each, then the
+//     warp runs each needed ray-cast point-in-polygon test cooperatively (edges over lanes,
+//     crossing counts by ballot + popc).
+// Collect queries (cd_engine.rs:261-310) walk the same probes with the collect rule of
+// qt_node.rs:151-191 and gather hazard keys in a per-warp shared-memory bitset, which is emitted
+// in ascending key order after one warp-aggregated atomicAdd reserves the output range.
+#pragma once
+#include <cfloat>
+#include <cstdint>
+
+#include "geom.cuh"
+#include "qtree.hpp"
+
+namespace jcde {
+
+constexpr uint32_t FULL = 0xffffffffu;
+constexpr int MAX_DEPTH = 15;   // 4 pending bits per level in a 64-bit register
+
+struct View {
+    const DNode* __restrict__ nodes;
+    const DEntry* __restrict__ entries;
+    const float4* __restrict__ edges;
+    const DHaz* __restrict__ haz;
+    const float2* __restrict__ hverts;
+    const DItem* __restrict__ items;
+    const float2* __restrict__ iverts;
+    const float4* __restrict__ poles;
+    const float4* __restrict__ piers;
+    const uint8_t* __restrict__ strength;   // strongest unfiltered presence per node
+    const uint32_t* __restrict__ mask;      // ignored-key bitmask, nullptr = NoFilter
+    const uint32_t* __restrict__ nedges;    // active edges per node (collect)
+    Box cde;
+    uint32_t n_items, n_slots, cd_threshold;
+    int32_t exterior;
+};
+
+// A raw (already transformed) query shape for the single-polygon entry points.
+struct RawShape {
+    const float2* verts;   // nullptr: shapes come from items + transformations
+    uint32_t nv;
+    float poi_x, poi_y, poi_r;
+};
+
+__device__ __forceinline__ bool filtered(const View& v, uint32_t k) {
+    return v.mask != nullptr && ((__ldg(&v.mask[k >> 5]) >> (k & 31)) & 1u);
+}
+__device__ __forceinline__ Box ld_box(const float4* p) {
+    float4 f = __ldg(p);
+    return Box{f.x, f.y, f.z, f.w};
+}
+__device__ __forceinline__ DNode ld_node(const View& v, int i) {
+    const float4* p = reinterpret_cast<const float4*>(v.nodes + i);
+    float4 a = __ldg(p);
+    int4 b = __ldg(reinterpret_cast<const int4*>(p + 1));
+    DNode d;
+    d.box = Box{a.x, a.y, a.z, a.w};
+    d.child = b.x;
+    d.parent = b.y;
+    d.hz_off = (uint32_t)b.z;
+    d.hz_cnt = (uint32_t)b.w;
+    return d;
+}
+__device__ __forceinline__ int4 ld_node_links(const View& v, int i) {
+    return __ldg(reinterpret_cast<const int4*>(v.nodes + i) + 1);
+}
+__device__ __forceinline__ DEntry ld_entry(const View& v, uint32_t i) {
+    const float4* p = reinterpret_cast<const float4*>(v.entries + i);
+    float4 a = __ldg(p);
+    uint4 b = __ldg(reinterpret_cast<const uint4*>(p + 1));
+    DEntry e;
+    e.ff = Box{a.x, a.y, a.z, a.w};
+    e.hkey = b.x;
+    e.edge_off = b.y;
+    e.edge_cnt = b.z;
+    e.presence = b.w;
+    return e;
+}
+__device__ __forceinline__ Seg ld_edge(const View& v, uint32_t i) {
+    float4 f = __ldg(&v.edges[i]);
+    return Seg{Pt{f.x, f.y}, Pt{f.z, f.w}};
+}
+
+// Probe-type dispatch: the queryable entities of qt_traits.rs (Circle for poles, Edge otherwise).
+__device__ __forceinline__ bool p_hits_box(const Disk& d, const Box& b) { return disk_hits_box(d, b); }
+__device__ __forceinline__ bool p_hits_box(const Seg& s, const Box& b) { return box_hits_seg(b, s); }
+__device__ __forceinline__ bool p_hits_seg(const Disk& d, const Seg& e) { return disk_hits_seg(d, e); }
+__device__ __forceinline__ bool p_hits_seg(const Seg& s, const Seg& e) { return seg_hits_seg(s, e); }
+__device__ __forceinline__ uint32_t p_quad_mask(const Disk& d, const Box& b) { return disk_quadrant_mask(d, b); }
+__device__ __forceinline__ uint32_t p_quad_mask(const Seg& s, const Box& b) { return seg_quadrant_mask(s, b); }
+
+// Advance the pending-children walk: returns the next node or -1 when the walk is finished.
+__device__ __forceinline__ int walk_next(const View& v, uint64_t& pend, int& depth, int& parent) {
+    while (depth > 0) {
+        const int sh = 4 * (depth - 1);
+        uint32_t m = (uint32_t)(pend >> sh) & 0xFu;
+        if (m) {
+            int i = __ffs(m) - 1;
+            pend &= ~(1ull << (sh + i));
+            return ld_node_links(v, parent).x + i;
+        }
+        depth--;
+        parent = ld_node_links(v, parent).y;
+    }
+    return -1;
+}
+
+// QTNode::collides (qt_node.rs:99-147) for one probe from node `start`.
+template <class P>
+__device__ bool detect_walk(const View& v, const P& p, int node, volatile int* flag) {
+    uint64_t pend = 0;
+    int depth = 0, parent = -1;
+    while (node >= 0) {
+        if (*flag) return false;
+        const uint32_t st = __ldg(&v.strength[node]);
+        if (st == PRES_ENTIRE) {
+            *flag = 1;
+            return true;
+        }
+        if (st == PRES_PARTIAL) {
+            DNode nd = ld_node(v, node);
+            if (nd.child >= 0) {
+                uint32_t m = p_quad_mask(p, nd.box);
+                if (m) {
+                    pend = (pend & ~(0xFull << (4 * depth))) | ((uint64_t)m << (4 * depth));
+                    parent = node;
+                    depth++;
+                }
+            } else {
+                for (uint32_t k = 0; k < nd.hz_cnt; k++) {
+                    DEntry e = ld_entry(v, nd.hz_off + k);
+                    if (e.presence != PRES_PARTIAL || filtered(v, e.hkey)) continue;
+                    if (!p_hits_box(p, e.ff)) continue;   // qt_partial_hazard.rs:67-71
+                    for (uint32_t j = 0; j < e.edge_cnt; j++)
+                        if (p_hits_seg(p, ld_edge(v, e.edge_off + j))) {
+                            *flag = 1;
+                            return true;
+                        }
+                    if (*flag) return false;
+                }
+            }
+        }
+        node = walk_next(v, pend, depth, parent);
+    }
+    return false;
+}
+
+__device__ __forceinline__ void bit_set(uint32_t* bits, uint32_t k) { atomicOr(&bits[k >> 5], 1u << (k & 31)); }
+__device__ __forceinline__ bool bit_get(const uint32_t* bits, uint32_t k) {
+    return (((volatile const uint32_t*)bits)[k >> 5] >> (k & 31)) & 1u;
+}
+
+// QTNode::collect_collisions (qt_node.rs:151-191) for one probe from node `start`.
+template <class P>
+__device__ void collect_walk(const View& v, const P& p, int node, uint32_t* bits) {
+    uint64_t pend = 0;
+    int depth = 0, parent = -1;
+    while (node >= 0) {
+        DNode nd = ld_node(v, node);
+        const bool now = __ldg(&v.nedges[node]) <= v.cd_threshold;
+        if (nd.child >= 0 && !now) {
+            uint32_t m = p_quad_mask(p, nd.box);
+            if (m) {
+                pend = (pend & ~(0xFull << (4 * depth))) | ((uint64_t)m << (4 * depth));
+                parent = node;
+                depth++;
+            }
+        } else {
+            for (uint32_t k = 0; k < nd.hz_cnt; k++) {
+                DEntry e = ld_entry(v, nd.hz_off + k);
+                if (bit_get(bits, e.hkey)) continue;
+                if (e.presence == PRES_ENTIRE) {
+                    bit_set(bits, e.hkey);
+                } else if (e.presence == PRES_PARTIAL && p_hits_box(p, e.ff)) {
+                    for (uint32_t j = 0; j < e.edge_cnt; j++)
+                        if (p_hits_seg(p, ld_edge(v, e.edge_off + j))) {
+                            bit_set(bits, e.hkey);
+                            break;
+                        }
+                }
+            }
+        }
+        node = walk_next(v, pend, depth, parent);
+    }
+}
+
+// Per-query shape: item vertices under the query's transformation, or a raw polygon.
+struct QShape {
+    const float2* verts;
+    uint32_t nv;
+    float c, s, tx, ty;
+    bool raw;
+    __device__ __forceinline__ Pt vtx(uint32_t k) const {
+        float2 f = __ldg(&verts[k]);
+        Pt p{f.x, f.y};
+        return raw ? p : xform(p, c, s, tx, ty);
+    }
+    __device__ __forceinline__ Seg edge(uint32_t k) const { return Seg{vtx(k), vtx(k + 1 == nv ? 0 : k + 1)}; }
+};
+
+// SPolygon::generate_bounding_box (simple_polygon.rs:122-133) as a warp reduction.
+__device__ __forceinline__ Box warp_bbox(const QShape& sh, int lane) {
+    float x0 = FLT_MAX, y0 = FLT_MAX, x1 = -FLT_MAX, y1 = -FLT_MAX;
+    for (uint32_t k = lane; k < sh.nv; k += 32) {
+        Pt p = sh.vtx(k);
+        x0 = fminf(x0, p.x);
+        y0 = fminf(y0, p.y);
+        x1 = fmaxf(x1, p.x);
+        y1 = fmaxf(y1, p.y);
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        x0 = fminf(x0, __shfl_xor_sync(FULL, x0, o));
+        y0 = fminf(y0, __shfl_xor_sync(FULL, y0, o));
+        x1 = fmaxf(x1, __shfl_xor_sync(FULL, x1, o));
+        y1 = fmaxf(y1, __shfl_xor_sync(FULL, y1, o));
+    }
+    return Box{x0, y0, x1, y1};
+}
+
+// CDEngine::get_virtual_root (cd_engine.rs:314-327); children boxes are Rect::quadrants of the parent.
+__device__ __forceinline__ int virtual_root(const View& v, const Box& sb) {
+    int n = 0;
+    for (;;) {
+        DNode nd = ld_node(v, n);
+        if (nd.child < 0) return n;
+        int next = -1;
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+            if (next < 0 && box_surrounds(box_quadrant(nd.box, i), sb)) next = nd.child + i;
+        if (next < 0) return n;
+        n = next;
+    }
+}
+
+// Ray-cast point-in-polygon (simple_polygon.rs:255-292) with the polygon's edges over the lanes.
+__device__ __forceinline__ bool warp_pip_hazard(const View& v, const DHaz& h, Pt p, int lane) {
+    if (!box_hits_pt(h.box, p)) return false;
+    const Seg ray = pip_ray(h.box, p);
+    const uint32_t nv = h.v_cnt_scope & 0x7fffffffu;
+    uint32_t n = 0;
+    for (uint32_t base = 0; base < nv; base += 32) {
+        uint32_t k = base + lane;
+        int t = 0;
+        if (k < nv) {
+            float2 a = __ldg(&v.hverts[h.v_off + k]);
+            float2 b = __ldg(&v.hverts[h.v_off + (k + 1 == nv ? 0 : k + 1)]);
+            t = pip_edge_term(ray, Seg{Pt{a.x, a.y}, Pt{b.x, b.y}}, p);
+        }
+        n += __popc(__ballot_sync(FULL, t));
+    }
+    return (n & 1u) == 1u;
+}
+__device__ __forceinline__ bool warp_pip_shape(const QShape& sh, const Box& sb, Pt p, int lane) {
+    if (!box_hits_pt(sb, p)) return false;
+    const Seg ray = pip_ray(sb, p);
+    uint32_t n = 0;
+    for (uint32_t base = 0; base < sh.nv; base += 32) {
+        uint32_t k = base + lane;
+        int t = 0;
+        if (k < sh.nv) t = pip_edge_term(ray, sh.edge(k), p);
+        n += __popc(__ballot_sync(FULL, t));
+    }
+    return (n & 1u) == 1u;
+}
+
+// CDEngine::detect_containment_collision (cd_engine.rs:231-255) for a hazard whose FPA bbox
+// relation needs a point-in-polygon test: 1 = Surrounding, 2 = Enclosed.
+__device__ __forceinline__ bool warp_containment(const View& v, const QShape& sh, const Box& sb, Pt spoi,
+                                                 uint32_t hkey, int need, int lane) {
+    DHaz h;
+    {
+        const float4* p = reinterpret_cast<const float4*>(v.haz + hkey);
+        float4 a = __ldg(p), b = __ldg(p + 1);
+        h.box = Box{a.x, a.y, a.z, a.w};
+        h.poi_x = b.x;
+        h.poi_y = b.y;
+        h.v_off = __float_as_uint(b.z);
+        h.v_cnt_scope = __float_as_uint(b.w);
+    }
+    bool contained = need == 1 ? warp_pip_hazard(v, h, spoi, lane) : warp_pip_shape(sh, sb, Pt{h.poi_x, h.poi_y}, lane);
+    bool ext = (h.v_cnt_scope >> 31) != 0;
+    return ext ? !contained : contained;
+}
+
+// Shape of query `qi`, loaded by 5 lanes and broadcast.
+struct QueryHead {
+    uint32_t item;
+    float c, s, tx, ty;
+};
+__device__ __forceinline__ QueryHead load_query(const uint32_t* __restrict__ q, uint32_t qi, int lane) {
+    uint32_t w = lane < 5 ? __ldg(&q[(size_t)qi * 5 + lane]) : 0u;
+    QueryHead h;
+    h.item = __shfl_sync(FULL, w, 0);
+    h.c = __uint_as_float(__shfl_sync(FULL, w, 1));
+    h.s = __uint_as_float(__shfl_sync(FULL, w, 2));
+    h.tx = __uint_as_float(__shfl_sync(FULL, w, 3));
+    h.ty = __uint_as_float(__shfl_sync(FULL, w, 4));
+    return h;
+}
+
+constexpr int MODE_SURROGATE = 1;
+constexpr int MODE_POLY = 2;
+constexpr int DETECT_WARPS = 8;
+
+// Detect: verdict per query (JCDE_FREE / JCDE_COLLIDES / JCDE_INVALID).
+template <int MODE>
+__global__ void __launch_bounds__(DETECT_WARPS * 32) k_detect(View v, const uint32_t* __restrict__ q, uint32_t n,
+                                                              uint8_t* __restrict__ out, RawShape raw) {
+    __shared__ int flags[DETECT_WARPS];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    volatile int* flag = &flags[warp];
+    const uint32_t stride = gridDim.x * DETECT_WARPS;
+    for (uint32_t qi = blockIdx.x * DETECT_WARPS + warp; qi < n; qi += stride) {
+        QShape sh;
+        DItem it{};
+        Pt spoi;
+        if (raw.verts) {
+            sh = QShape{raw.verts, raw.nv, 1.0f, 0.0f, 0.0f, 0.0f, true};
+            spoi = Pt{raw.poi_x, raw.poi_y};
+        } else {
+            QueryHead qh = load_query(q, qi, lane);
+            if (qh.item >= v.n_items) {
+                if (lane == 0) out[qi] = 2;
+                continue;
+            }
+            it = v.items[qh.item];
+            sh = QShape{v.iverts + it.v_off, it.v_cnt, qh.c, qh.s, qh.tx, qh.ty, false};
+            spoi = xform(Pt{it.poi_x, it.poi_y}, qh.c, qh.s, qh.tx, qh.ty);
+        }
+        if (lane == 0) *flag = 0;
+        __syncwarp();
+        bool hit = false;
+        Box sb{0, 0, 0, 0};
+        int vr = 0;
+        if (MODE & MODE_POLY) {
+            sb = warp_bbox(sh, lane);
+            // detect_poly_collision: a shape not surrounded by the CDE box collides (cd_engine.rs:161-163)
+            hit = !box_surrounds(v.cde, sb);
+            if (!hit) vr = virtual_root(v, sb);
+        }
+        const uint32_t n_pole = (MODE & MODE_SURROGATE) ? it.n_ff_poles : 0u;
+        const uint32_t n_pier = (MODE & MODE_SURROGATE) ? it.n_piers : 0u;
+        const uint32_t n_edge = (MODE & MODE_POLY) ? sh.nv : 0u;
+        const uint32_t np = n_pole + n_pier + n_edge;
+        for (uint32_t base = 0; !hit && base < np; base += 32) {
+            const uint32_t p = base + lane;
+            bool h = false;
+            if (p < np) {
+                if (p < n_pole) {
+                    float4 pl = __ldg(&v.poles[it.pole_off + p]);
+                    Disk d{xform(Pt{pl.x, pl.y}, sh.c, sh.s, sh.tx, sh.ty), pl.z};
+                    h = detect_walk(v, d, 0, flag);
+                } else if (p < n_pole + n_pier) {
+                    float4 pr = __ldg(&v.piers[it.pier_off + (p - n_pole)]);
+                    Seg sg{xform(Pt{pr.x, pr.y}, sh.c, sh.s, sh.tx, sh.ty), xform(Pt{pr.z, pr.w}, sh.c, sh.s, sh.tx, sh.ty)};
+                    h = detect_walk(v, sg, 0, flag);
+                } else {
+                    h = detect_walk(v, sh.edge(p - n_pole - n_pier), vr, flag);
+                }
+            }
+            hit = __any_sync(FULL, h);
+        }
+        if ((MODE & MODE_POLY) && !hit) {
+            // containment of the shape in (or of) the partially present hazards of the virtual root
+            DNode vn = ld_node(v, vr);
+            for (uint32_t base = 0; !hit && base < vn.hz_cnt; base += 32) {
+                const uint32_t k = base + lane;
+                int need = 0;
+                bool res = false;
+                uint32_t hk = 0;
+                if (k < vn.hz_cnt) {
+                    DEntry e = ld_entry(v, vn.hz_off + k);
+                    // an Entire entry here is an ignored one (qt_node.rs:104), and is skipped
+                    if (e.presence == PRES_PARTIAL && !filtered(v, e.hkey)) {
+                        hk = e.hkey;
+                        const float4* hp = reinterpret_cast<const float4*>(v.haz + hk);
+                        float4 a = __ldg(hp), b = __ldg(hp + 1);
+                        int rel = box_almost_relation(Box{a.x, a.y, a.z, a.w}, sb);
+                        if (rel == REL_SURROUNDING) need = 1;
+                        else if (rel == REL_ENCLOSED) need = 2;
+                        else res = (__float_as_uint(b.w) >> 31) != 0;   // not contained: exterior scope collides
+                    }
+                }
+                if (__any_sync(FULL, res)) {
+                    hit = true;
+                    break;
+                }
+                uint32_t todo = __ballot_sync(FULL, need != 0);
+                while (todo && !hit) {
+                    const int src = __ffs(todo) - 1;
+                    todo &= todo - 1;
+                    const int nd = __shfl_sync(FULL, need, src);
+                    const uint32_t hkk = __shfl_sync(FULL, hk, src);
+                    hit = warp_containment(v, sh, sb, spoi, hkk, nd, lane);
+                }
+            }
+        }
+        if (lane == 0) out[qi] = hit ? 1 : 0;
+    }
+}
+
+constexpr int COLLECT_WARPS = 4;
+
+// Collect: sorted colliding hazard keys per query, compacted with one atomicAdd per query.
+template <int MODE>
+__global__ void __launch_bounds__(COLLECT_WARPS * 32) k_collect(View v, const uint32_t* __restrict__ q, uint32_t n,
+                                                                uint32_t words, uint32_t* __restrict__ offsets,
+                                                                uint32_t* __restrict__ counts, uint32_t* __restrict__ ids,
+                                                                uint32_t cap, uint32_t* __restrict__ total, RawShape raw) {
+    extern __shared__ uint32_t smem[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    uint32_t* bits = smem + (size_t)warp * words;
+    const uint32_t stride = gridDim.x * COLLECT_WARPS;
+    for (uint32_t qi = blockIdx.x * COLLECT_WARPS + warp; qi < n; qi += stride) {
+        QShape sh;
+        DItem it{};
+        Pt spoi;
+        bool valid = true;
+        if (raw.verts) {
+            sh = QShape{raw.verts, raw.nv, 1.0f, 0.0f, 0.0f, 0.0f, true};
+            spoi = Pt{raw.poi_x, raw.poi_y};
+        } else {
+            QueryHead qh = load_query(q, qi, lane);
+            valid = qh.item < v.n_items;
+            if (valid) {
+                it = v.items[qh.item];
+                sh = QShape{v.iverts + it.v_off, it.v_cnt, qh.c, qh.s, qh.tx, qh.ty, false};
+                spoi = xform(Pt{it.poi_x, it.poi_y}, qh.c, qh.s, qh.tx, qh.ty);
+            } else {
+                sh = QShape{v.iverts, 0, 1.0f, 0.0f, 0.0f, 0.0f, true};
+                spoi = Pt{0, 0};
+            }
+        }
+        // the ignored keys are pre-seeded into the collector (hazards/filter.rs:69-76)
+        for (uint32_t w = lane; w < words; w += 32) bits[w] = v.mask ? __ldg(&v.mask[w]) : 0u;
+        __syncwarp();
+        if (valid) {
+            Box sb{0, 0, 0, 0};
+            int vr = 0;
+            if (MODE & MODE_POLY) {
+                sb = warp_bbox(sh, lane);
+                if (!box_surrounds(v.cde, sb) && v.exterior >= 0 && lane == 0) bit_set(bits, (uint32_t)v.exterior);
+                vr = virtual_root(v, sb);
+            }
+            const uint32_t n_pole = (MODE & MODE_SURROGATE) ? it.n_ff_poles : 0u;
+            const uint32_t n_pier = (MODE & MODE_SURROGATE) ? it.n_piers : 0u;
+            const uint32_t n_edge = (MODE & MODE_POLY) ? sh.nv : 0u;
+            const uint32_t np = n_pole + n_pier + n_edge;
+            for (uint32_t p = lane; p < np; p += 32) {
+                if (p < n_pole) {
+                    float4 pl = __ldg(&v.poles[it.pole_off + p]);
+                    Disk d{xform(Pt{pl.x, pl.y}, sh.c, sh.s, sh.tx, sh.ty), pl.z};
+                    collect_walk(v, d, 0, bits);
+                } else if (p < n_pole + n_pier) {
+                    float4 pr = __ldg(&v.piers[it.pier_off + (p - n_pole)]);
+                    Seg sg{xform(Pt{pr.x, pr.y}, sh.c, sh.s, sh.tx, sh.ty), xform(Pt{pr.z, pr.w}, sh.c, sh.s, sh.tx, sh.ty)};
+                    collect_walk(v, sg, 0, bits);
+                } else {
+                    collect_walk(v, sh.edge(p - n_pole - n_pier), vr, bits);
+                }
+            }
+            __syncwarp();
+            if (MODE & MODE_POLY) {
+                DNode vn = ld_node(v, vr);
+                for (uint32_t base = 0; base < vn.hz_cnt; base += 32) {
+                    const uint32_t k = base + lane;
+                    int need = 0;
+                    uint32_t hk = 0;
+                    if (k < vn.hz_cnt) {
+                        DEntry e = ld_entry(v, vn.hz_off + k);
+                        if (e.presence == PRES_PARTIAL && !bit_get(bits, e.hkey)) {
+                            hk = e.hkey;
+                            const float4* hp = reinterpret_cast<const float4*>(v.haz + hk);
+                            float4 a = __ldg(hp), b = __ldg(hp + 1);
+                            int rel = box_almost_relation(Box{a.x, a.y, a.z, a.w}, sb);
+                            if (rel == REL_SURROUNDING) need = 1;
+                            else if (rel == REL_ENCLOSED) need = 2;
+                            else if ((__float_as_uint(b.w) >> 31) != 0) bit_set(bits, hk);
+                        }
+                    }
+                    uint32_t todo = __ballot_sync(FULL, need != 0);
+                    while (todo) {
+                        const int src = __ffs(todo) - 1;
+                        todo &= todo - 1;
+                        const int nd = __shfl_sync(FULL, need, src);
+                        const uint32_t hkk = __shfl_sync(FULL, hk, src);
+                        if (warp_containment(v, sh, sb, spoi, hkk, nd, lane) && lane == 0) bit_set(bits, hkk);
+                    }
+                }
+            }
+        }
+        __syncwarp();
+        // emit keys in ascending order: bits minus the pre-seeded ignored keys
+        uint32_t cnt = 0;
+        for (uint32_t w = lane; w < words; w += 32) cnt += __popc(bits[w] & ~(v.mask ? __ldg(&v.mask[w]) : 0u));
+#pragma unroll
+        for (int o = 16; o; o >>= 1) cnt += __shfl_xor_sync(FULL, cnt, o);
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(total, cnt);
+        base = __shfl_sync(FULL, base, 0);
+        if (lane == 0) {
+            offsets[qi] = base;
+            counts[qi] = valid ? cnt : 0xffffffffu;
+        }
+        if ((uint64_t)base + cnt <= cap) {
+            uint32_t run = base;
+            for (uint32_t w0 = 0; w0 < words; w0 += 32) {
+                const uint32_t w = w0 + lane;
+                uint32_t m = w < words ? (bits[w] & ~(v.mask ? __ldg(&v.mask[w]) : 0u)) : 0u;
+                uint32_t c = __popc(m), incl = c;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    uint32_t t = __shfl_up_sync(FULL, incl, o);
+                    if (lane >= o) incl += t;
+                }
+                uint32_t pos = run + incl - c;
+                while (m) {
+                    int b = __ffs(m) - 1;
+                    m &= m - 1;
+                    ids[pos++] = w * 32 + b;
+                }
+                run += __shfl_sync(FULL, incl, 31);
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// Strongest presence per node under a filter (QTHazardVec::strongest, qt_hazard_vec.rs:60-63).
+__global__ void k_strength(View v, uint32_t n_nodes, uint8_t* __restrict__ out) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_nodes) return;
+    DNode nd = ld_node(v, i);
+    uint8_t s = PRES_NONE;
+    for (uint32_t k = 0; k < nd.hz_cnt; k++) {
+        DEntry e = ld_entry(v, nd.hz_off + k);
+        if (!filtered(v, e.hkey)) {
+            s = (uint8_t)e.presence;
+            break;
+        }
+    }
+    out[i] = s;
+}
+
+}  // namespace jcde

@@ -1,0 +1,30 @@
+// Host preparation of shapes (see prep.cpp).
+#pragma once
+#include <cstdint>
+#include <vector>
+
+#include "geom.cuh"
+
+namespace jcde {
+
+struct PreparedPolygon {
+    std::vector<Pt> v;   // counter-clockwise
+    Box bbox;
+    float area;
+    float diameter;
+    Disk poi;            // pole of inaccessibility
+};
+
+struct PoleLimit {
+    uint32_t n;
+    float coverage;
+};
+
+float polygon_area(const Pt* v, size_t n);
+// SPolygon::new (simple_polygon.rs:41-71): 0 on success, -1 for an invalid polygon
+int spolygon_new(std::vector<Pt> pts, PreparedPolygon* out);
+// generate_surrogate_poles (pole.rs:12-47) of an internal shape with the given area and poi
+int surrogate_poles(const std::vector<Pt>& v, float area, Disk poi, const PoleLimit* lim, int n_lim,
+                    std::vector<Disk>* poles);
+
+}  // namespace jcde

@@ -1,0 +1,23 @@
+"""jcde — GB300-native collision detection engine for 2D irregular nesting.
+
+A drop-in for the query path of jagua-rs's ``CDEngine``: the quadtree of hazards is mirrored into
+GPU memory and detect / collect queries run as hand-written sm_103a kernels behind the C ABI of
+``include/jcde.h``.  This package is the Python host side over that ABI.
+"""
+from ._ffi import JcdeError, build, lib
+from .engine import CDEConfig, CDEngine, GpuBackend, GpuEngine, Hazard, spolygon_new, surrogate_poles
+from .workload import QUERY_DTYPE
+
+__all__ = [
+    "CDEConfig",
+    "CDEngine",
+    "GpuBackend",
+    "GpuEngine",
+    "Hazard",
+    "JcdeError",
+    "QUERY_DTYPE",
+    "build",
+    "lib",
+    "spolygon_new",
+    "surrogate_poles",
+]

@@ -1,0 +1,358 @@
+"""Python mirror of the reference's ``CDEngine`` over the jcde C ABI.
+
+The method names, argument meanings and failure behaviour follow
+jagua-rs/src/collision_detection/cd_engine.rs: ``register_hazard`` / ``deregister_hazard_by_key`` /
+``deregister_hazard_by_entity`` / ``detect_poly_collision`` / ``detect_surrogate_collision`` /
+``collect_poly_collisions`` / ``collect_surrogate_collisions`` / ``save`` / ``restore`` / ``bbox``.
+Where the reference panics (unknown key, cd_engine.rs:78 and :91) these raise ``KeyError``.
+
+Every query runs on the GPU through libjcde.so; nothing here answers a query on the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _ffi
+from ._ffi import check, jcde_config, jcde_filter, jcde_hazard, jcde_rect, lib
+from .workload import QUERY_DTYPE
+
+PLACED_ITEM, EXTERIOR, HOLE, QUALITY_ZONE = 0, 1, 2, 3
+
+
+@dataclass
+class CDEConfig:
+    """CDEConfig (cd_engine.rs:346-353) with its SPSurrogateConfig (sp_surrogate.rs:120-131)."""
+
+    quadtree_depth: int = 5
+    cd_threshold: int = 16
+    n_pole_limits: tuple = ((100, 0.0), (20, 0.75), (10, 0.90))
+    n_ff_poles: int = 2
+    n_ff_piers: int = 0
+
+    def to_c(self) -> jcde_config:
+        c = jcde_config()
+        c.quadtree_depth = self.quadtree_depth
+        c.cd_threshold = self.cd_threshold
+        c.n_pole_limits = len(self.n_pole_limits)
+        for i, (n, cov) in enumerate(self.n_pole_limits):
+            c.pole_limit_n[i] = n
+            c.pole_limit_coverage[i] = cov
+        c.n_ff_poles = self.n_ff_poles
+        c.n_ff_piers = self.n_ff_piers
+        return c
+
+
+@dataclass
+class Hazard:
+    """Hazard (hazards/hazard.rs:16-23): entity kind + tag, final shape (vertices + poi), dynamic."""
+
+    kind: int
+    xy: np.ndarray
+    poi: np.ndarray
+    dynamic: bool = False
+    tag: int = 0
+
+
+def _f32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _fp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def _c_hazard(h: Hazard, keep: list) -> jcde_hazard:
+    xy = _f32(h.xy).reshape(-1, 2)
+    keep.append(xy)
+    ch = jcde_hazard()
+    ch.kind = int(h.kind)
+    ch.dynamic = int(bool(h.dynamic))
+    ch.xy = _fp(xy)
+    ch.n_vertices = len(xy)
+    for i in range(3):
+        ch.poi[i] = float(h.poi[i])
+    ch.tag = int(h.tag)
+    return ch
+
+
+class _Filter:
+    """HazardFilter as a jcde_filter: None/empty = NoFilter, else a HazKeyFilter of keys."""
+
+    def __init__(self, ignored):
+        keys = [] if ignored is None else [int(k) for k in (ignored if hasattr(ignored, "__iter__") else [ignored])]
+        self.arr = np.ascontiguousarray(np.asarray(keys, dtype=np.uint32))
+        self.c = jcde_filter()
+        self.c.ignored = self.arr.ctypes.data_as(C.POINTER(C.c_uint32))
+        self.c.n_ignored = len(self.arr)
+
+    @property
+    def ref(self):
+        return C.byref(self.c)
+
+
+def _stream_handle(stream) -> int | None:
+    if stream is None:
+        try:
+            import torch
+
+            return torch.cuda.current_stream().cuda_stream
+        except Exception:
+            return None
+    return int(getattr(stream, "cuda_stream", stream))
+
+
+class CDEngine:
+    """GPU collision detection engine with the reference's query surface (cd_engine.rs:22-341)."""
+
+    def __init__(self, bbox, static_hazards=(), config: CDEConfig | None = None):
+        self.config = config or CDEConfig()
+        self._cfg = self.config.to_c()
+        keep: list = []
+        arr = (jcde_hazard * max(1, len(static_hazards)))()
+        for i, h in enumerate(static_hazards):
+            arr[i] = _c_hazard(h, keep)
+        handle = C.c_void_p()
+        check(lib().jcde_create(C.byref(self._cfg), jcde_rect(*[float(v) for v in bbox]), arr, len(static_hazards),
+                                C.byref(handle)), "jcde_create")
+        self.h = handle
+        self.n_items = 0
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h:
+            try:
+                lib().jcde_destroy(h)
+            except Exception:
+                pass
+            self.h = None
+
+    # --- hazards -------------------------------------------------------------------------------
+    def register_hazard(self, hazard: Hazard) -> int:
+        keep: list = []
+        ch = _c_hazard(hazard, keep)
+        k = C.c_uint32()
+        check(lib().jcde_register_hazard(self.h, C.byref(ch), C.byref(k)), "register_hazard")
+        return k.value
+
+    def deregister_hazard_by_key(self, key: int) -> None:
+        st = lib().jcde_deregister_hazard(self.h, int(key))
+        if st == _ffi.ERR_NOT_FOUND:
+            raise KeyError(f"Cannot deregister hazard that is not registered: {key}")
+        check(st, "deregister_hazard_by_key")
+
+    def deregister_hazard_by_entity(self, kind: int, tag: int) -> int:
+        k = C.c_uint32()
+        st = lib().jcde_deregister_hazard_by_entity(self.h, int(kind), int(tag), C.byref(k))
+        if st == _ffi.ERR_NOT_FOUND:
+            raise KeyError(f"Cannot deregister hazard that is not registered: kind {kind} tag {tag}")
+        check(st, "deregister_hazard_by_entity")
+        return k.value
+
+    def n_hazard_slots(self) -> int:
+        n = C.c_uint32()
+        check(lib().jcde_n_hazard_slots(self.h, C.byref(n)), "n_hazard_slots")
+        return n.value
+
+    def bbox(self):
+        r = jcde_rect()
+        check(lib().jcde_bbox(self.h, C.byref(r)), "bbox")
+        return (r.x_min, r.y_min, r.x_max, r.y_max)
+
+    # --- items ---------------------------------------------------------------------------------
+    def register_item(self, xy, poi, poles, piers=None) -> int:
+        xy, poi = _f32(xy).reshape(-1, 2), _f32(poi)
+        poles = _f32(np.asarray(poles).reshape(-1, 3))
+        piers = _f32(np.zeros((0, 4)) if piers is None else np.asarray(piers).reshape(-1, 4))
+        out = C.c_uint32()
+        check(lib().jcde_register_item(self.h, _fp(xy), len(xy), _fp(poi), _fp(poles), len(poles),
+                                       _fp(piers) if len(piers) else None, len(piers), C.byref(out)), "register_item")
+        self.n_items += 1
+        return out.value
+
+    # --- single queries (reference signatures) ---------------------------------------------------
+    def detect_poly_collision(self, xy, poi, filter=None) -> bool:
+        xy, poi = _f32(xy).reshape(-1, 2), _f32(poi)
+        f = _Filter(filter)
+        out = C.c_uint8()
+        check(lib().jcde_detect_poly(self.h, _fp(xy), len(xy), _fp(poi), f.ref, C.byref(out)), "detect_poly_collision")
+        return bool(out.value)
+
+    def detect_surrogate_collision(self, item: int, transform, filter=None) -> bool:
+        t = _f32(transform)
+        f = _Filter(filter)
+        out = C.c_uint8()
+        st = lib().jcde_detect_surrogate(self.h, int(item), _fp(t), f.ref, C.byref(out))
+        if st == _ffi.ERR_NOT_FOUND:
+            raise KeyError(f"unknown item {item}")
+        check(st, "detect_surrogate_collision")
+        return bool(out.value)
+
+    def collect_poly_collisions(self, xy, poi, filter=None) -> list:
+        xy, poi = _f32(xy).reshape(-1, 2), _f32(poi)
+        f = _Filter(filter)
+        cap = max(1, self.n_hazard_slots())
+        keys = np.zeros(cap, np.uint32)
+        n = C.c_uint32()
+        check(lib().jcde_collect_poly(self.h, _fp(xy), len(xy), _fp(poi), f.ref,
+                                      keys.ctypes.data_as(C.POINTER(C.c_uint32)), cap, C.byref(n)), "collect_poly")
+        return [int(k) for k in keys[: n.value]]
+
+    def collect_surrogate_collisions(self, item: int, transform, filter=None) -> list:
+        t = _f32(transform)
+        f = _Filter(filter)
+        cap = max(1, self.n_hazard_slots())
+        keys = np.zeros(cap, np.uint32)
+        n = C.c_uint32()
+        check(lib().jcde_collect_surrogate(self.h, int(item), _fp(t), f.ref,
+                                           keys.ctypes.data_as(C.POINTER(C.c_uint32)), cap, C.byref(n)),
+              "collect_surrogate")
+        return [int(k) for k in keys[: n.value]]
+
+    # --- batched queries -----------------------------------------------------------------------
+    def detect_batch(self, queries, filter=None, out=None, stream=None, mode: str = "both"):
+        """Verdicts of a query batch.
+
+        ``queries`` is either a numpy array of QUERY_DTYPE (host path: copies in, kernel, copies
+        out) or a CUDA torch uint8/int tensor holding packed 20-byte queries (device path, stream
+        ordered; ``out`` must then be a CUDA uint8 tensor).
+        """
+        f = _Filter(filter)
+        if isinstance(queries, np.ndarray):
+            q = np.ascontiguousarray(queries, dtype=QUERY_DTYPE)
+            res = np.zeros(len(q), np.uint8) if out is None else out
+            if mode != "both":
+                raise ValueError("host path supports mode='both' only")
+            check(lib().jcde_detect_batch_host(self.h, q.ctypes.data, len(q), f.ref, res.ctypes.data), "detect_batch")
+            return res
+        n = queries.numel() * queries.element_size() // QUERY_DTYPE.itemsize
+        if out is None:
+            import torch
+
+            out = torch.empty(n, dtype=torch.uint8, device=queries.device)
+        fn = {"both": lib().jcde_detect_batch, "surrogate": lib().jcde_detect_surrogate_batch,
+              "poly": lib().jcde_detect_poly_batch}[mode]
+        check(fn(self.h, queries.data_ptr(), n, f.ref, out.data_ptr(), _stream_handle(stream)), "detect_batch")
+        return out
+
+    def collect_batch(self, queries, filter=None, ids_cap: int | None = None, stream=None):
+        """Colliding hazard keys per query as (offsets, counts, ids) CUDA tensors (device path)."""
+        import torch
+
+        f = _Filter(filter)
+        if isinstance(queries, np.ndarray):
+            q = torch.from_numpy(np.ascontiguousarray(queries, dtype=QUERY_DTYPE).view(np.uint8)).cuda()
+        else:
+            q = queries
+        n = q.numel() * q.element_size() // QUERY_DTYPE.itemsize
+        dev = q.device
+        cap = ids_cap if ids_cap is not None else max(1024, 4 * n)
+        while True:
+            offsets = torch.empty(n, dtype=torch.int32, device=dev)
+            counts = torch.empty(n, dtype=torch.int32, device=dev)
+            ids = torch.empty(max(1, cap), dtype=torch.int32, device=dev)
+            total = torch.zeros(1, dtype=torch.int32, device=dev)
+            check(lib().jcde_collect_batch(self.h, q.data_ptr(), n, f.ref, offsets.data_ptr(), counts.data_ptr(),
+                                           ids.data_ptr(), cap, total.data_ptr(), _stream_handle(stream)),
+                  "collect_batch")
+            t = int(total.item())
+            if t <= cap:
+                return offsets, counts, ids[:t], t
+            cap = t
+
+    # --- snapshots -----------------------------------------------------------------------------
+    def save(self):
+        s = C.c_void_p()
+        check(lib().jcde_save(self.h, C.byref(s)), "save")
+        return _Snapshot(s)
+
+    def restore(self, snap) -> None:
+        check(lib().jcde_restore(self.h, snap.h), "restore")
+
+    # --- introspection -------------------------------------------------------------------------
+    def tree_dump(self) -> np.ndarray:
+        n = C.c_uint64()
+        check(lib().jcde_tree_dump(self.h, None, 0, C.byref(n)), "tree_dump")
+        out = np.zeros(n.value, np.uint32)
+        check(lib().jcde_tree_dump(self.h, out.ctypes.data_as(C.POINTER(C.c_uint32)), n.value, C.byref(n)), "tree_dump")
+        return out
+
+    def device_stats(self) -> dict:
+        a = (C.c_uint64 * 5)()
+        check(lib().jcde_device_stats(self.h, a), "device_stats")
+        return dict(nodes=a[0], entries=a[1], edges=a[2], hazard_vertices=a[3], item_vertices=a[4])
+
+    def kernel_launches(self) -> int:
+        return int(lib().jcde_kernel_launches(self.h))
+
+
+class _Snapshot:
+    def __init__(self, h):
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            try:
+                lib().jcde_snapshot_free(self.h)
+            except Exception:
+                pass
+            self.h = None
+
+
+def spolygon_new(xy):
+    """SPolygon::new (simple_polygon.rs:41-71): (xy_ccw, bbox, area, diameter, poi)."""
+    xy = _f32(xy).reshape(-1, 2)
+    xo = np.zeros_like(xy)
+    bbox = np.zeros(4, np.float32)
+    ad = np.zeros(2, np.float32)
+    poi = np.zeros(3, np.float32)
+    check(lib().jcde_spolygon_new(_fp(xy), len(xy), _fp(xo), _fp(bbox), _fp(ad), _fp(poi)), "spolygon_new")
+    return xo, bbox, ad[0], ad[1], poi
+
+
+def surrogate_poles(xy, area, poi, limits) -> np.ndarray:
+    """generate_surrogate_poles (pole.rs:12-47) of an internal shape: (k, 3) array, [0] = poi."""
+    xy, poi = _f32(xy).reshape(-1, 2), _f32(poi)
+    cfg = CDEConfig(n_pole_limits=tuple(limits)).to_c()
+    cap = 1024
+    out = np.zeros((cap, 3), np.float32)
+    n = C.c_uint32()
+    check(lib().jcde_surrogate_poles(_fp(xy), len(xy), np.float32(area), _fp(poi), C.byref(cfg), _fp(out), cap,
+                                     C.byref(n)), "surrogate_poles")
+    return out[: n.value].copy()
+
+
+class GpuEngine:
+    """Adapter of CDEngine to the workload generator's engine interface."""
+
+    def __init__(self, depth: int, cd_threshold: int, bbox):
+        self.eng = CDEngine(bbox, (), CDEConfig(quadtree_depth=depth, cd_threshold=cd_threshold))
+
+    def register_hazard(self, kind, dynamic, xy, poi, tag: int = 0) -> int:
+        return self.eng.register_hazard(Hazard(kind, xy, poi, dynamic, tag))
+
+    def deregister_hazard(self, key) -> None:
+        self.eng.deregister_hazard_by_key(key)
+
+    def add_item(self, xy, poi, poles, n_ff_poles, piers=None) -> int:
+        return self.eng.register_item(xy, poi, poles, piers)
+
+    def detect_batch(self, queries, ignored=None):
+        return self.eng.detect_batch(np.ascontiguousarray(queries, dtype=QUERY_DTYPE), filter=ignored)
+
+    def tree_dump(self):
+        return self.eng.tree_dump()
+
+
+class GpuBackend:
+    """Backend for jcde.workload: host preparation and engines from libjcde."""
+
+    name = "gpu"
+    spolygon_new = staticmethod(spolygon_new)
+    surrogate_poles = staticmethod(surrogate_poles)
+
+    @staticmethod
+    def new_engine(depth: int, cd_threshold: int, bbox):
+        return GpuEngine(depth, cd_threshold, bbox)

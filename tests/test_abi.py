@@ -1,0 +1,88 @@
+"""The C ABI: library loads, exports every declared entry point, rejects bad arguments.
+
+Only host-side entry points run here (no GPU is needed to create an engine, register hazards or
+prepare shapes); every query entry point is exercised by the GPU tests.
+"""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import REPO
+
+
+def declared_functions():
+    src = open(os.path.join(REPO, "include", "jcde.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(jcde_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_header_parses():
+    names = declared_functions()
+    assert "jcde_detect_batch" in names and "jcde_create" in names and len(names) >= 25
+
+
+def test_exports_every_declared_symbol(jcde_mod):
+    L = C.CDLL(os.path.join(REPO, "jagua-rs_gb300", "jcde", "libjcde.so"))
+    missing = [n for n in declared_functions() if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_ctypes_signatures_cover_header(jcde_mod):
+    from jcde import _ffi
+
+    assert set(declared_functions()) == set(_ffi.SIGNATURES), set(declared_functions()) ^ set(_ffi.SIGNATURES)
+
+
+def test_status_strings(jcde_mod):
+    L = jcde_mod.lib()
+    assert L.jcde_status_string(0) == b"ok"
+    assert L.jcde_status_string(-4) == b"not found"
+
+
+def test_bad_arguments(jcde_mod):
+    from jcde import _ffi
+
+    L = jcde_mod.lib()
+    cfg = _ffi.jcde_config()
+    L.jcde_default_config(C.byref(cfg))
+    h = C.c_void_p()
+    # empty box
+    assert L.jcde_create(C.byref(cfg), _ffi.jcde_rect(0, 0, 0, 1), None, 0, C.byref(h)) == _ffi.ERR_ARG
+    # depth beyond the 15 levels the kernels track
+    cfg.quadtree_depth = 16
+    assert L.jcde_create(C.byref(cfg), _ffi.jcde_rect(0, 0, 1, 1), None, 0, C.byref(h)) == _ffi.ERR_ARG
+    cfg.quadtree_depth = 5
+    assert L.jcde_create(C.byref(cfg), _ffi.jcde_rect(0, 0, 1, 1), None, 0, C.byref(h)) == _ffi.OK
+    # a hazard needs >= 3 vertices; unknown keys are reported, never abort
+    hz = _ffi.jcde_hazard()
+    hz.kind = 0
+    hz.n_vertices = 2
+    xy = np.zeros(4, np.float32)
+    hz.xy = xy.ctypes.data_as(C.POINTER(C.c_float))
+    k = C.c_uint32()
+    assert L.jcde_register_hazard(h, C.byref(hz), C.byref(k)) == _ffi.ERR_ARG
+    assert L.jcde_deregister_hazard(h, 7) == _ffi.ERR_NOT_FOUND
+    assert L.jcde_detect_batch(None, None, 0, None, None, None) == _ffi.ERR_ARG
+    L.jcde_destroy(h)
+
+
+def test_engine_default_config_matches_lbf(jcde_mod):
+    """lbf/src/config.rs:37-45."""
+    from jcde import _ffi
+
+    cfg = _ffi.jcde_config()
+    jcde_mod.lib().jcde_default_config(C.byref(cfg))
+    assert (cfg.quadtree_depth, cfg.cd_threshold, cfg.n_ff_poles, cfg.n_ff_piers) == (5, 16, 2, 0)
+    assert list(cfg.pole_limit_n) == [100, 20, 10]
+    assert [round(v, 2) for v in cfg.pole_limit_coverage] == [0.0, 0.75, 0.9]
+
+
+def test_python_engine_errors(jcde_mod):
+    eng = jcde_mod.CDEngine((0, 0, 10, 10))
+    with pytest.raises(KeyError):
+        eng.deregister_hazard_by_key(3)
+    with pytest.raises(KeyError):
+        eng.deregister_hazard_by_entity(0, 12345)
