@@ -214,11 +214,13 @@ static void init_launch_shape(jcde_engine* e) {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&e->n_sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&e->detect_blocks_per_sm, k_detect<3>, DETECT_WARPS * 32, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&e->detect_blocks_per_sm, k_poly, POLY_WARPS * 32, 0);
     if (e->detect_blocks_per_sm < 1) e->detect_blocks_per_sm = 1;
     if (e->n_sms < 1) e->n_sms = 1;
 }
 
+// mode 1: surrogate only; 2: polygon only; 3: surrogate pass, then the polygon pass on the
+// queries it left undecided (the order of lbf/benches/ci_bench.rs:111-119).
 static jcde_status launch_detect(jcde_engine* e, int mode, const jcde_query* dq, uint32_t n, const jcde_filter* f,
                                  uint8_t* dout, cudaStream_t s, RawShape raw) {
     jcde_status st = sync_device(e);
@@ -227,16 +229,20 @@ static jcde_status launch_detect(jcde_engine* e, int mode, const jcde_query* dq,
     View v = base_view(e);
     if ((st = apply_filter(e, f, s, v))) return st;
     if (n == 0) return JCDE_OK;
-    uint32_t want = (n + DETECT_WARPS - 1) / DETECT_WARPS;
-    uint32_t grid = std::min<uint32_t>(want, (uint32_t)(e->n_sms * e->detect_blocks_per_sm));
     const uint32_t* q = reinterpret_cast<const uint32_t*>(dq);
-    switch (mode) {
-        case 1: k_detect<1><<<grid, DETECT_WARPS * 32, 0, s>>>(v, q, n, dout, raw); break;
-        case 2: k_detect<2><<<grid, DETECT_WARPS * 32, 0, s>>>(v, q, n, dout, raw); break;
-        default: k_detect<3><<<grid, DETECT_WARPS * 32, 0, s>>>(v, q, n, dout, raw); break;
+    if (mode & 1) {
+        const uint32_t grid = (n + SURR_THREADS - 1) / SURR_THREADS;
+        k_surrogate<<<grid, SURR_THREADS, 0, s>>>(v, q, n, dout, mode == 1 ? (uint8_t)0 : PENDING);
+        CUDA_TRY(cudaGetLastError());
+        e->launches++;
     }
-    CUDA_TRY(cudaGetLastError());
-    e->launches++;
+    if (mode & 2) {
+        const uint32_t want = (n + POLY_WARPS - 1) / POLY_WARPS;
+        const uint32_t grid = std::min<uint32_t>(want, (uint32_t)(e->n_sms * e->detect_blocks_per_sm));
+        k_poly<<<grid, POLY_WARPS * 32, 0, s>>>(v, q, n, dout, raw, mode == 3);
+        CUDA_TRY(cudaGetLastError());
+        e->launches++;
+    }
     e->last_stream = s;
     e->have_last_stream = true;
     return JCDE_OK;

@@ -85,7 +85,8 @@ JHD int box_almost_relation(const Box& s, const Box& o) {
 // rect.rs:282-288
 JHD bool box_hits_pt(const Box& r, Pt p) { return p.x >= r.x0 && p.x <= r.x1 && p.y >= r.y0 && p.y <= r.y1; }
 // rect.rs:248-253
-JHD Pt box_mid(const Box& r) { return Pt{(r.x0 + r.x1) / 2.0f, (r.y0 + r.y1) / 2.0f}; }
+// x / 2 and x * 0.5 are the same correctly rounded value of the same real number
+JHD Pt box_mid(const Box& r) { return Pt{(r.x0 + r.x1) * 0.5f, (r.y0 + r.y1) * 0.5f}; }
 // rect.rs:259-263
 JHD float box_diameter(const Box& r) {
     float dx = r.x1 - r.x0;
@@ -109,6 +110,12 @@ JHD Box box_quadrant(const Box& r, int i) {
     Pt m = box_mid(r);
     Pt c = box_corner(r, i);
     return Box{fmn(c.x, m.x), fmn(c.y, m.y), fmx(c.x, m.x), fmx(c.y, m.y)};
+}
+// The same four boxes given the midpoint: the midpoint of a valid box lies between its bounds, so
+// from_diagonal_corners(corner_i, mid) reduces to picking bounds (q0 = ++, q1 = -+, q2 = --, q3 = +-).
+JHD Box quad_box(const Box& r, Pt m, int i) {
+    return Box{(i == 0 || i == 3) ? m.x : r.x0, (i == 0 || i == 1) ? m.y : r.y0,
+               (i == 0 || i == 3) ? r.x1 : m.x, (i == 0 || i == 1) ? r.y1 : m.y};
 }
 
 // rect.rs:301-345 — Rect collides with Edge
@@ -164,18 +171,21 @@ JHD int seg_hit_half(const Seg& e1, const Seg& e2) {
 JHD uint32_t seg_quadrant_mask(const Seg& e, const Box& r) {
     float ex0 = fmn(e.s.x, e.e.x), ex1 = fmx(e.s.x, e.e.x);
     float ey0 = fmn(e.s.y, e.e.y), ey1 = fmx(e.s.y, e.e.y);
-    uint32_t hit = 0, undet = 0;
-JCDE_UNROLL
-    for (int i = 0; i < 4; i++) {
-        Box q = box_quadrant(r, i);
-        bool no = fmx(ex0, q.x0) > fmn(ex1, q.x1) || fmx(ey0, q.y0) > fmn(ey1, q.y1);
-        if (!no) {
-            if (box_hits_pt(q, e.s) || box_hits_pt(q, e.e)) hit |= 1u << i;
-            else undet |= 1u << i;
-        }
-    }
+    const Pt c = box_mid(r);
+    // per-quadrant overlap tests of qt_traits.rs:29-31; quadrants share their x (or y) extents in
+    // pairs, so each distinct expression is evaluated once
+    const bool xr = !(fmx(ex0, c.x) > fmn(ex1, r.x1)), xl = !(fmx(ex0, r.x0) > fmn(ex1, c.x));
+    const bool yt = !(fmx(ey0, c.y) > fmn(ey1, r.y1)), yb = !(fmx(ey0, r.y0) > fmn(ey1, c.y));
+    const uint32_t ov = (xr && yt ? 1u : 0u) | (xl && yt ? 2u : 0u) | (xl && yb ? 4u : 0u) | (xr && yb ? 8u : 0u);
+    // end points inside quadrants (rect.rs:282-288 per quadrant box)
+    auto pt_mask = [&](Pt p) -> uint32_t {
+        const bool R = p.x >= c.x && p.x <= r.x1, L = p.x >= r.x0 && p.x <= c.x;
+        const bool T = p.y >= c.y && p.y <= r.y1, B = p.y >= r.y0 && p.y <= c.y;
+        return (R && T ? 1u : 0u) | (L && T ? 2u : 0u) | (L && B ? 4u : 0u) | (R && B ? 8u : 0u);
+    };
+    uint32_t hit = ov & (pt_mask(e.s) | pt_mask(e.e));
+    uint32_t undet = ov & ~hit;
     if (!undet) return hit;
-    Pt c = box_mid(r);
     // sides (rect.rs:164-184): top c0->c1, left c1->c2, bottom c2->c3, right c3->c0; bisectors
     // (qt_traits.rs:123-130).  half_intersect (qt_traits.rs:110-140) runs only while a quadrant it
     // could set is undetermined, and sets the quadrants of the half of the side that was hit.
@@ -236,11 +246,16 @@ JHD float disk_sep_dist(const Disk& c, Pt p) {
     float d = sqrtf(dx * dx + dy * dy);
     return d <= c.r ? c.r - d : d - c.r;
 }
-JHD uint32_t disk_quadrant_mask(const Disk& c, const Box& r) {  // qt_traits.rs:9-13 default
-    uint32_t m = 0;
-JCDE_UNROLL
-    for (int i = 0; i < 4; i++) m |= disk_hits_box(c, box_quadrant(r, i)) ? (1u << i) : 0u;
-    return m;
+// qt_traits.rs:9-13 default: Circle collides with each quadrant box (circle.rs:512-525); the
+// nearest-point terms are shared by the quadrants that share an extent
+JHD uint32_t disk_quadrant_mask(const Disk& c, const Box& r) {
+    const Pt m = box_mid(r);
+    const float nxr = fmx(m.x, fmn(c.c.x, r.x1)) - c.c.x, nxl = fmx(r.x0, fmn(c.c.x, m.x)) - c.c.x;
+    const float nyt = fmx(m.y, fmn(c.c.y, r.y1)) - c.c.y, nyb = fmx(r.y0, fmn(c.c.y, m.y)) - c.c.y;
+    const float dxr = nxr * nxr, dxl = nxl * nxl, dyt = nyt * nyt, dyb = nyb * nyb;
+    const float rr = c.r * c.r;
+    return (dxr + dyt <= rr ? 1u : 0u) | (dxl + dyt <= rr ? 2u : 0u) | (dxl + dyb <= rr ? 4u : 0u) |
+           (dxr + dyb <= rr ? 8u : 0u);
 }
 
 // point.rs:259-264 with the rot_transl_m matrix [[c, -s, tx], [s, c, ty]] (transformation.rs:475-483)

@@ -6,10 +6,10 @@
 // is walked down from the virtual root (cd_engine.rs:160-173), then the partially present hazards of
 // the virtual root are tested for containment (cd_engine.rs:176-193).  Its answer is the OR of all
 // those tests, so the warp spreads them over lanes:
-//   * probes (poles, piers, item edges) — one per lane, each lane walks its own descent with a
-//     4-bit pending-children mask per level packed into one 64-bit register (no stack memory); a
-//     lane that hits raises a per-warp shared-memory flag and every other lane abandons its walk at
-//     its next node (early exit at node granularity);
+//   * probes (poles, piers, item edges) — each lane walks one probe's descent with a 4-bit
+//     pending-children mask per level packed into one 64-bit register (no stack memory).  Probes
+//     are handed to lanes dynamically (ballot rank) as their previous walk ends, each loop
+//     iteration is one node visit per lane, and a hit anywhere ends the query at once;
 //   * containment — lanes evaluate the FPA bounding-box relation of one hazard each, then the
 //     warp runs each needed ray-cast point-in-polygon test cooperatively (edges over lanes,
 //     crossing counts by ballot + popc).
@@ -116,43 +116,53 @@ __device__ __forceinline__ int walk_next(const View& v, uint64_t& pend, int& dep
     return -1;
 }
 
-// QTNode::collides (qt_node.rs:99-147) for one probe from node `start`.
+// One lane's (or thread's) walk state for the step-wise traversals of k_surrogate and k_poly.
+struct Walk {
+    int node;        // node to visit next; -1 = idle (needs a probe), -2 = no probe left
+    int depth, parent;
+    uint64_t pend;   // 4 pending-children bits per level below the start node
+};
+
+// Leaf test of QTNode::collides (qt_node.rs:126-142): unfiltered Partial hazards, ff box first.
+// `stop` (shared memory, may be null) is raised by the lane that finds a hit; the other lanes of
+// the warp leave their leaf loops at the next check instead of finishing them.
 template <class P>
-__device__ bool detect_walk(const View& v, const P& p, int node, volatile int* flag) {
-    uint64_t pend = 0;
-    int depth = 0, parent = -1;
-    while (node >= 0) {
-        if (*flag) return false;
-        const uint32_t st = __ldg(&v.strength[node]);
-        if (st == PRES_ENTIRE) {
-            *flag = 1;
+__device__ __forceinline__ bool leaf_hits(const View& v, const P& p, const DNode& nd, volatile int* stop) {
+    for (uint32_t k = 0; k < nd.hz_cnt; k++) {
+        if (stop && *stop) return false;
+        DEntry e = ld_entry(v, nd.hz_off + k);
+        if (e.presence != PRES_PARTIAL || filtered(v, e.hkey)) continue;
+        if (!p_hits_box(p, e.ff)) continue;   // qt_partial_hazard.rs:67-71
+        for (uint32_t j = 0; j < e.edge_cnt; j++) {
+            if (p_hits_seg(p, ld_edge(v, e.edge_off + j))) {
+                if (stop) *stop = 1;
+                return true;
+            }
+            if (stop && (j & 7) == 7 && *stop) return false;
+        }
+    }
+    return false;
+}
+
+// Visit w.node for probe p (qt_node.rs:104-146) and advance the walk.  Returns true on a hit.
+template <class P>
+__device__ __forceinline__ bool walk_step(const View& v, const P& p, Walk& w, volatile int* stop) {
+    const uint32_t st = __ldg(&v.strength[w.node]);
+    if (st == PRES_ENTIRE) return true;
+    if (st == PRES_PARTIAL) {
+        DNode nd = ld_node(v, w.node);
+        if (nd.child >= 0) {
+            const uint32_t m = p_quad_mask(p, nd.box);
+            if (m) {
+                w.pend = (w.pend & ~(0xFull << (4 * w.depth))) | ((uint64_t)m << (4 * w.depth));
+                w.parent = w.node;
+                w.depth++;
+            }
+        } else if (leaf_hits(v, p, nd, stop)) {
             return true;
         }
-        if (st == PRES_PARTIAL) {
-            DNode nd = ld_node(v, node);
-            if (nd.child >= 0) {
-                uint32_t m = p_quad_mask(p, nd.box);
-                if (m) {
-                    pend = (pend & ~(0xFull << (4 * depth))) | ((uint64_t)m << (4 * depth));
-                    parent = node;
-                    depth++;
-                }
-            } else {
-                for (uint32_t k = 0; k < nd.hz_cnt; k++) {
-                    DEntry e = ld_entry(v, nd.hz_off + k);
-                    if (e.presence != PRES_PARTIAL || filtered(v, e.hkey)) continue;
-                    if (!p_hits_box(p, e.ff)) continue;   // qt_partial_hazard.rs:67-71
-                    for (uint32_t j = 0; j < e.edge_cnt; j++)
-                        if (p_hits_seg(p, ld_edge(v, e.edge_off + j))) {
-                            *flag = 1;
-                            return true;
-                        }
-                    if (*flag) return false;
-                }
-            }
-        }
-        node = walk_next(v, pend, depth, parent);
     }
+    w.node = walk_next(v, w.pend, w.depth, w.parent);
     return false;
 }
 
@@ -312,19 +322,56 @@ __device__ __forceinline__ QueryHead load_query(const uint32_t* __restrict__ q, 
 
 constexpr int MODE_SURROGATE = 1;
 constexpr int MODE_POLY = 2;
-constexpr int DETECT_WARPS = 8;
+constexpr int POLY_WARPS = 8;
+constexpr int SURR_THREADS = 256;
+constexpr uint8_t PENDING = 0xFFu;   // verdict slot of a query the surrogate pass left undecided
 
-// Detect: verdict per query (JCDE_FREE / JCDE_COLLIDES / JCDE_INVALID).
-template <int MODE>
-__global__ void __launch_bounds__(DETECT_WARPS * 32) k_detect(View v, const uint32_t* __restrict__ q, uint32_t n,
-                                                              uint8_t* __restrict__ out, RawShape raw) {
-    __shared__ int flags[DETECT_WARPS];
+// Surrogate pass — CDEngine::detect_surrogate_collision (cd_engine.rs:204-223), one thread per
+// query: the fail-fast poles, then the piers, each walked down from the root in the reference's
+// order, stopping at the first hit.  A hit writes JCDE_COLLIDES; a miss writes `miss` (JCDE_FREE
+// for a surrogate-only batch, PENDING when the polygon pass follows).
+__global__ void __launch_bounds__(SURR_THREADS) k_surrogate(View v, const uint32_t* __restrict__ q, uint32_t n,
+                                                            uint8_t* __restrict__ out, uint8_t miss) {
+    const uint32_t stride = gridDim.x * SURR_THREADS;
+    for (uint32_t qi = blockIdx.x * SURR_THREADS + threadIdx.x; qi < n; qi += stride) {
+        const uint32_t* w5 = q + (size_t)qi * 5;
+        const uint32_t item = __ldg(&w5[0]);
+        const float c = __uint_as_float(__ldg(&w5[1])), s = __uint_as_float(__ldg(&w5[2]));
+        const float tx = __uint_as_float(__ldg(&w5[3])), ty = __uint_as_float(__ldg(&w5[4]));
+        if (item >= v.n_items) {
+            out[qi] = 2;
+            continue;
+        }
+        const DItem it = v.items[item];
+        bool hit = false;
+        for (uint32_t p = 0; p < it.n_ff_poles && !hit; p++) {
+            const float4 pl = __ldg(&v.poles[it.pole_off + p]);
+            const Disk d{xform(Pt{pl.x, pl.y}, c, s, tx, ty), pl.z};
+            Walk w{0, 0, -1, 0ull};
+            while (w.node >= 0 && !hit) hit = walk_step(v, d, w, nullptr);
+        }
+        for (uint32_t p = 0; p < it.n_piers && !hit; p++) {
+            const float4 pr = __ldg(&v.piers[it.pier_off + p]);
+            const Seg sg{xform(Pt{pr.x, pr.y}, c, s, tx, ty), xform(Pt{pr.z, pr.w}, c, s, tx, ty)};
+            Walk w{0, 0, -1, 0ull};
+            while (w.node >= 0 && !hit) hit = walk_step(v, sg, w, nullptr);
+        }
+        out[qi] = hit ? (uint8_t)1 : miss;
+    }
+}
+
+// Polygon pass — CDEngine::detect_poly_collision (cd_engine.rs:160-197), one warp per query.
+// With `only_pending`, queries whose slot is not PENDING were decided by the surrogate pass and
+// are skipped.  Writes JCDE_FREE / JCDE_COLLIDES.
+__global__ void __launch_bounds__(POLY_WARPS * 32) k_poly(View v, const uint32_t* __restrict__ q, uint32_t n,
+                                                          uint8_t* __restrict__ out, RawShape raw, bool only_pending) {
+    __shared__ int stops[POLY_WARPS];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    volatile int* flag = &flags[warp];
-    const uint32_t stride = gridDim.x * DETECT_WARPS;
-    for (uint32_t qi = blockIdx.x * DETECT_WARPS + warp; qi < n; qi += stride) {
+    volatile int* stop = &stops[warp];
+    const uint32_t stride = gridDim.x * POLY_WARPS;
+    for (uint32_t qi = blockIdx.x * POLY_WARPS + warp; qi < n; qi += stride) {
+        if (only_pending && out[qi] != PENDING) continue;
         QShape sh;
-        DItem it{};
         Pt spoi;
         if (raw.verts) {
             sh = QShape{raw.verts, raw.nv, 1.0f, 0.0f, 0.0f, 0.0f, true};
@@ -335,44 +382,46 @@ __global__ void __launch_bounds__(DETECT_WARPS * 32) k_detect(View v, const uint
                 if (lane == 0) out[qi] = 2;
                 continue;
             }
-            it = v.items[qh.item];
+            const DItem it = v.items[qh.item];
             sh = QShape{v.iverts + it.v_off, it.v_cnt, qh.c, qh.s, qh.tx, qh.ty, false};
             spoi = xform(Pt{it.poi_x, it.poi_y}, qh.c, qh.s, qh.tx, qh.ty);
         }
-        if (lane == 0) *flag = 0;
+        if (lane == 0) *stop = 0;
         __syncwarp();
-        bool hit = false;
-        Box sb{0, 0, 0, 0};
-        int vr = 0;
-        if (MODE & MODE_POLY) {
-            sb = warp_bbox(sh, lane);
-            // detect_poly_collision: a shape not surrounded by the CDE box collides (cd_engine.rs:161-163)
-            hit = !box_surrounds(v.cde, sb);
-            if (!hit) vr = virtual_root(v, sb);
-        }
-        const uint32_t n_pole = (MODE & MODE_SURROGATE) ? it.n_ff_poles : 0u;
-        const uint32_t n_pier = (MODE & MODE_SURROGATE) ? it.n_piers : 0u;
-        const uint32_t n_edge = (MODE & MODE_POLY) ? sh.nv : 0u;
-        const uint32_t np = n_pole + n_pier + n_edge;
-        for (uint32_t base = 0; !hit && base < np; base += 32) {
-            const uint32_t p = base + lane;
-            bool h = false;
-            if (p < np) {
-                if (p < n_pole) {
-                    float4 pl = __ldg(&v.poles[it.pole_off + p]);
-                    Disk d{xform(Pt{pl.x, pl.y}, sh.c, sh.s, sh.tx, sh.ty), pl.z};
-                    h = detect_walk(v, d, 0, flag);
-                } else if (p < n_pole + n_pier) {
-                    float4 pr = __ldg(&v.piers[it.pier_off + (p - n_pole)]);
-                    Seg sg{xform(Pt{pr.x, pr.y}, sh.c, sh.s, sh.tx, sh.ty), xform(Pt{pr.z, pr.w}, sh.c, sh.s, sh.tx, sh.ty)};
-                    h = detect_walk(v, sg, 0, flag);
+        const Box sb = warp_bbox(sh, lane);
+        // a shape not surrounded by the CDE box collides (cd_engine.rs:161-163)
+        bool hit = !box_surrounds(v.cde, sb);
+        const int vr = hit ? 0 : virtual_root(v, sb);
+        // Edges are handed out dynamically: a lane whose walk is over takes the next unassigned
+        // edge (ballot rank), so no lane waits for the slowest walk of a fixed round.  Every loop
+        // iteration is one node visit per active lane; a hit anywhere ends the query.
+        const uint32_t lt = (1u << lane) - 1u;
+        uint32_t next = 0;
+        Walk w{-1, 0, -1, 0ull};
+        Seg e{};
+        while (!hit) {
+            const bool want = w.node == -1;
+            const uint32_t need = __ballot_sync(FULL, want);
+            if (want) {
+                const uint32_t p = next + __popc(need & lt);
+                if (p < sh.nv) {
+                    w = Walk{vr, 0, -1, 0ull};
+                    e = sh.edge(p);
                 } else {
-                    h = detect_walk(v, sh.edge(p - n_pole - n_pier), vr, flag);
+                    w.node = -2;
                 }
+            }
+            next += __popc(need);
+            const bool active = w.node >= 0;
+            if (!__any_sync(FULL, active)) break;
+            bool h = false;
+            if (active) {
+                h = walk_step(v, e, w, stop);
+                if (!h && w.node < 0) w.node = -1;
             }
             hit = __any_sync(FULL, h);
         }
-        if ((MODE & MODE_POLY) && !hit) {
+        if (!hit) {
             // containment of the shape in (or of) the partially present hazards of the virtual root
             DNode vn = ld_node(v, vr);
             for (uint32_t base = 0; !hit && base < vn.hz_cnt; base += 32) {
@@ -381,10 +430,10 @@ __global__ void __launch_bounds__(DETECT_WARPS * 32) k_detect(View v, const uint
                 bool res = false;
                 uint32_t hk = 0;
                 if (k < vn.hz_cnt) {
-                    DEntry e = ld_entry(v, vn.hz_off + k);
+                    DEntry en = ld_entry(v, vn.hz_off + k);
                     // an Entire entry here is an ignored one (qt_node.rs:104), and is skipped
-                    if (e.presence == PRES_PARTIAL && !filtered(v, e.hkey)) {
-                        hk = e.hkey;
+                    if (en.presence == PRES_PARTIAL && !filtered(v, en.hkey)) {
+                        hk = en.hkey;
                         const float4* hp = reinterpret_cast<const float4*>(v.haz + hk);
                         float4 a = __ldg(hp), b = __ldg(hp + 1);
                         int rel = box_almost_relation(Box{a.x, a.y, a.z, a.w}, sb);
