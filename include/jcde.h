@@ -140,6 +140,24 @@ jcde_status jcde_collect_batch(jcde_engine* e, const jcde_query* d_queries, uint
                                const jcde_filter* filter, uint32_t* d_offsets, uint32_t* d_counts,
                                uint32_t* d_ids, uint32_t ids_cap, uint32_t* d_total, void* stream);
 
+/* --- filtered detect that allocates nothing -------------------------------------------------- */
+/* No counterpart in the reference.  Same verdicts as jcde_detect_batch (device buffers, stream
+ * ordered), for callers that may not allocate device memory during a query: jcde_detect_batch
+ * allocates a device bitmask and a per-node table the first time it sees a filter, and cudaMalloc
+ * synchronizes the whole device and needs free memory — which a caller whose GPU memory is all
+ * owned by its own pool, or that runs queries on a latency-critical stream next to other work,
+ * cannot accept.  This entry point keeps the filter's keys, bitmask and per-node table in one static
+ * device array of JCDE_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until the
+ * process exits; it returns JCDE_ERR_CAPACITY when keys + bitmask + table exceed it.  Every call
+ * shares that array and leaves its contents behind, so calls that overlap on the GPU (another
+ * stream, another thread) race on it.  The engine's device copy must be current: after a
+ * register / deregister / restore / register_item, run any other query first (jcde_detect_batch
+ * with n = 0 suffices), else JCDE_ERR_STATE.  The first call on a device looks up the array's
+ * device address with that device current; make that first call before any stream capture. */
+#define JCDE_NOALLOC_SCRATCH_BYTES 1048576u
+jcde_status jcde_detect_batch_noalloc(jcde_engine* e, const jcde_query* d_queries, uint32_t n,
+                                      const jcde_filter* filter, uint8_t* d_verdicts, void* stream);
+
 /* --- single queries with the reference's signatures (host buffers, synchronous) -------------- */
 /* detect_poly_collision (cd_engine.rs:160-197) of an already transformed shape with its poi. */
 jcde_status jcde_detect_poly(jcde_engine* e, const float* xy, uint32_t n_vertices, const float poi[3],

@@ -640,3 +640,90 @@ jcde_status jcde_device_stats(jcde_engine* e, uint64_t* out5) {
 uint64_t jcde_kernel_launches(const jcde_engine* e) { return e ? e->launches : 0; }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------------------
+// Filtered detect that allocates nothing (jcde_detect_batch_noalloc).
+//
+// The regular filtered path keeps one device bitmask and one per-node strength array per distinct
+// filter, allocated on first use.  This variant keeps those in one static device array instead,
+// so a call never allocates device memory.  Every GPU that loads the library holds the array until
+// the process exits, every call shares it (it keeps the last call's contents), and calls that
+// overlap on the GPU race on it.
+// ---------------------------------------------------------------------------------------------
+static __device__ __align__(256) unsigned char g_noalloc_scratch[JCDE_NOALLOC_SCRATCH_BYTES];
+
+static std::mutex g_noalloc_mu;
+static void* g_noalloc_addr[256] = {};   // device address of g_noalloc_scratch, per device ordinal
+
+// The host name g_noalloc_scratch is only a stand-in; its device address is looked up once per
+// device, with that device current, on the first call made on it.
+static jcde_status noalloc_scratch_addr(void** out) {
+    int dev = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 256) return JCDE_ERR_STATE;
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || p == nullptr) return JCDE_ERR_CUDA;
+        g_noalloc_addr[dev] = p;
+    }
+    *out = g_noalloc_addr[dev];
+    return JCDE_OK;
+}
+
+// Ignored keys -> bitmask over hazard keys; the mask is cleared first (the array keeps old contents).
+__global__ void k_mask_from_keys(const uint32_t* __restrict__ keys, uint32_t n_keys, uint32_t n_slots,
+                                 uint32_t* __restrict__ mask, uint32_t words) {
+    for (uint32_t w = threadIdx.x; w < words; w += blockDim.x) mask[w] = 0u;
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < n_keys; i += blockDim.x) {
+        const uint32_t k = keys[i];
+        if (k < n_slots) atomicOr(&mask[k >> 5], 1u << (k & 31));
+    }
+}
+
+static inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+extern "C" jcde_status jcde_detect_batch_noalloc(jcde_engine* e, const jcde_query* dq, uint32_t n,
+                                                  const jcde_filter* f, uint8_t* dout, void* stream) {
+    if (!e || (n && (!dq || !dout))) return JCDE_ERR_ARG;
+    const uint32_t n_keys = f ? f->n_ignored : 0u;
+    if (n_keys && !f->ignored) return JCDE_ERR_ARG;
+    // bringing the device mirror up to date may allocate: it must already be current
+    if (e->tree_version != e->tree.version() || e->items_dirty) return JCDE_ERR_STATE;
+    const uint32_t words = mask_words(e);
+    const size_t keys_b = align256((size_t)n_keys * 4), mask_b = align256((size_t)words * 4);
+    const size_t str_b = align256(e->n_nodes);
+    if (keys_b + mask_b + str_b > JCDE_NOALLOC_SCRATCH_BYTES) return JCDE_ERR_CAPACITY;
+    void* base = nullptr;
+    jcde_status st = noalloc_scratch_addr(&base);
+    if (st) return st;
+    init_launch_shape(e);
+    cudaStream_t s = (cudaStream_t)stream;
+    unsigned char* b = static_cast<unsigned char*>(base);
+    uint32_t* keys = reinterpret_cast<uint32_t*>(b);
+    uint32_t* mask = reinterpret_cast<uint32_t*>(b + keys_b);
+    uint8_t* strength = b + keys_b + mask_b;
+    if (n_keys) CUDA_TRY(cudaMemcpyAsync(keys, f->ignored, (size_t)n_keys * 4, cudaMemcpyHostToDevice, s));
+    k_mask_from_keys<<<1, 256, 0, s>>>(keys, n_keys, e->tree.n_slots(), mask, words);
+    CUDA_TRY(cudaGetLastError());
+    View v = base_view(e);
+    v.mask = mask;
+    k_strength<<<(e->n_nodes + 255) / 256, 256, 0, s>>>(v, e->n_nodes, strength);
+    CUDA_TRY(cudaGetLastError());
+    v.strength = strength;
+    e->launches += 2;
+    if (n) {
+        const uint32_t* q = reinterpret_cast<const uint32_t*>(dq);
+        k_surrogate<<<(n + SURR_THREADS - 1) / SURR_THREADS, SURR_THREADS, 0, s>>>(v, q, n, dout, PENDING);
+        CUDA_TRY(cudaGetLastError());
+        const uint32_t want = (n + POLY_WARPS - 1) / POLY_WARPS;
+        const uint32_t grid = std::min<uint32_t>(want, (uint32_t)(e->n_sms * e->detect_blocks_per_sm));
+        k_poly<<<grid, POLY_WARPS * 32, 0, s>>>(v, q, n, dout, RawShape{nullptr, 0, 0, 0, 0}, true);
+        CUDA_TRY(cudaGetLastError());
+        e->launches += 2;
+    }
+    e->last_stream = s;
+    e->have_last_stream = true;
+    return JCDE_OK;
+}

@@ -72,6 +72,7 @@ SIGNATURES = {
     "jcde_detect_poly_batch": (C.c_int32, [P, P, C.c_uint32, C.POINTER(jcde_filter), P, P]),
     "jcde_detect_batch_host": (C.c_int32, [P, P, C.c_uint32, C.POINTER(jcde_filter), P]),
     "jcde_collect_batch": (C.c_int32, [P, P, C.c_uint32, C.POINTER(jcde_filter), P, P, P, C.c_uint32, P, P]),
+    "jcde_detect_batch_noalloc": (C.c_int32, [P, P, C.c_uint32, C.POINTER(jcde_filter), P, P]),
     "jcde_detect_poly": (C.c_int32, [P, f32p, C.c_uint32, f32p, C.POINTER(jcde_filter), u8p]),
     "jcde_detect_surrogate": (C.c_int32, [P, C.c_uint32, f32p, C.POINTER(jcde_filter), u8p]),
     "jcde_collect_poly": (C.c_int32, [P, f32p, C.c_uint32, f32p, C.POINTER(jcde_filter), u32p, C.c_uint32, u32p]),
