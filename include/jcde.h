@@ -15,7 +15,9 @@
  *     is what the reference's CDE consumes (`&Transformation`); sin/cos are the caller's;
  *   - `stream` arguments are cudaStream_t values passed as void* (NULL = legacy default stream);
  *     "device" pointers must be CUDA device (or managed) memory, "host" pointers plain host memory;
- *   - mutations (register / deregister / restore) must not overlap queries on the same engine.
+ *   - mutations (register / deregister / restore) must not overlap queries on the same engine, and
+ *     query batches of one engine must not overlap each other on the GPU (they share the engine's
+ *     scratch buffers): issue them on one stream, or synchronise between streams.
  */
 #ifndef JCDE_H
 #define JCDE_H

@@ -75,6 +75,7 @@ struct jcde_engine {
     std::list<FilterSlot> filters;
     // staging for host entry points and single queries
     DevBuf d_q, d_out, d_raw, d_coll;
+    DevBuf d_hist, d_order;   // spatial ordering of a query batch
     cudaStream_t last_stream = nullptr;
     bool have_last_stream = false;
     cudaStream_t own[2] = {nullptr, nullptr};
@@ -214,15 +215,71 @@ static void init_launch_shape(jcde_engine* e) {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&e->n_sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&e->detect_blocks_per_sm, k_poly, POLY_WARPS * 32, 0);
+    if (e->cfg.quadtree_depth <= 8)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&e->detect_blocks_per_sm, k_poly<uint32_t>, POLY_WARPS * 32, 0);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&e->detect_blocks_per_sm, k_poly<uint64_t>, POLY_WARPS * 32, 0);
     if (e->detect_blocks_per_sm < 1) e->detect_blocks_per_sm = 1;
     if (e->n_sms < 1) e->n_sms = 1;
+}
+
+#ifndef JCDE_SPATIAL_ORDER
+#define JCDE_SPATIAL_ORDER 1
+#endif
+constexpr uint32_t ORDER_MIN_BATCH = 4096;   // below this a batch is visited in its own order
+
+// Visit order of a batch: cell-by-cell over the CDE box (k_bucket_*), or nullptr for index order.
+// `slot` selects one of two histogram/order buffer pairs, so that the two streams of the host
+// entry point's pipeline never share one; `slot_cap` is the largest batch a slot must hold.
+static const uint32_t* spatial_order(jcde_engine* e, const uint32_t* q, uint32_t n, cudaStream_t s, int slot,
+                                     uint32_t slot_cap) {
+    if (!JCDE_SPATIAL_ORDER || n < ORDER_MIN_BATCH) return nullptr;
+    const size_t per_slot = std::max<size_t>(n, slot_cap);
+    if (!e->d_hist.ensure(2 * N_BUCKETS * 4)) return nullptr;
+    if (e->d_order.cap < 2 * per_slot * 4) {
+        // growing the buffer frees the old one, which queued batches may still read
+        if (e->have_last_stream && cudaStreamSynchronize(e->last_stream) != cudaSuccess) return nullptr;
+        if (!e->d_order.ensure(2 * per_slot * 4)) return nullptr;
+    }
+    uint32_t* hist = e->d_hist.as<uint32_t>() + (size_t)slot * N_BUCKETS;
+    uint32_t* order = e->d_order.as<uint32_t>() + (size_t)slot * (e->d_order.cap / 8);
+    if (cudaMemsetAsync(hist, 0, N_BUCKETS * 4, s) != cudaSuccess) return nullptr;
+    const Box b = e->tree.bbox();
+    const uint32_t grid = std::min<uint32_t>((n + 255) / 256, (uint32_t)e->n_sms * 8);
+    k_bucket_count<<<grid, 256, 0, s>>>(q, n, b, hist);
+    k_bucket_scan<<<1, 1024, 0, s>>>(hist);
+    k_bucket_scatter<<<grid, 256, 0, s>>>(q, n, b, hist, order);
+    e->launches += 3;
+    return order;
+}
+
+// The surrogate pass and/or the polygon pass; the walk's pending masks are 32-bit for trees of
+// depth <= 8 and 64-bit above.
+template <typename PendT>
+static void launch_passes_t(jcde_engine* e, const View& v, const uint32_t* q, uint32_t n, uint8_t* dout,
+                            cudaStream_t s, RawShape raw, int mode, const uint32_t* order) {
+    if (mode & 1) {
+        const uint32_t grid = (n + SURR_THREADS - 1) / SURR_THREADS;
+        k_surrogate<PendT><<<grid, SURR_THREADS, 0, s>>>(v, q, n, dout, mode == 1 ? (uint8_t)0 : PENDING, order);
+        e->launches++;
+    }
+    if (mode & 2) {
+        const uint32_t want = (n + POLY_WARPS - 1) / POLY_WARPS;
+        const uint32_t grid = std::min<uint32_t>(want, (uint32_t)(e->n_sms * e->detect_blocks_per_sm));
+        k_poly<PendT><<<grid, POLY_WARPS * 32, 0, s>>>(v, q, n, dout, raw, mode == 3, order);
+        e->launches++;
+    }
+}
+static void launch_passes(jcde_engine* e, const View& v, const uint32_t* q, uint32_t n, uint8_t* dout,
+                          cudaStream_t s, RawShape raw, int mode, const uint32_t* order = nullptr) {
+    if (e->cfg.quadtree_depth <= 8) launch_passes_t<uint32_t>(e, v, q, n, dout, s, raw, mode, order);
+    else launch_passes_t<uint64_t>(e, v, q, n, dout, s, raw, mode, order);
 }
 
 // mode 1: surrogate only; 2: polygon only; 3: surrogate pass, then the polygon pass on the
 // queries it left undecided (the order of lbf/benches/ci_bench.rs:111-119).
 static jcde_status launch_detect(jcde_engine* e, int mode, const jcde_query* dq, uint32_t n, const jcde_filter* f,
-                                 uint8_t* dout, cudaStream_t s, RawShape raw) {
+                                 uint8_t* dout, cudaStream_t s, RawShape raw, int slot = 0, uint32_t slot_cap = 0) {
     jcde_status st = sync_device(e);
     if (st) return st;
     init_launch_shape(e);
@@ -230,19 +287,9 @@ static jcde_status launch_detect(jcde_engine* e, int mode, const jcde_query* dq,
     if ((st = apply_filter(e, f, s, v))) return st;
     if (n == 0) return JCDE_OK;
     const uint32_t* q = reinterpret_cast<const uint32_t*>(dq);
-    if (mode & 1) {
-        const uint32_t grid = (n + SURR_THREADS - 1) / SURR_THREADS;
-        k_surrogate<<<grid, SURR_THREADS, 0, s>>>(v, q, n, dout, mode == 1 ? (uint8_t)0 : PENDING);
-        CUDA_TRY(cudaGetLastError());
-        e->launches++;
-    }
-    if (mode & 2) {
-        const uint32_t want = (n + POLY_WARPS - 1) / POLY_WARPS;
-        const uint32_t grid = std::min<uint32_t>(want, (uint32_t)(e->n_sms * e->detect_blocks_per_sm));
-        k_poly<<<grid, POLY_WARPS * 32, 0, s>>>(v, q, n, dout, raw, mode == 3);
-        CUDA_TRY(cudaGetLastError());
-        e->launches++;
-    }
+    const uint32_t* order = raw.verts ? nullptr : spatial_order(e, q, n, s, slot, slot_cap);
+    launch_passes(e, v, q, n, dout, s, raw, mode, order);
+    CUDA_TRY(cudaGetLastError());
     e->last_stream = s;
     e->have_last_stream = true;
     return JCDE_OK;
@@ -454,7 +501,8 @@ jcde_status jcde_detect_batch_host(jcde_engine* e, const jcde_query* hq, uint32_
         if (a >= b) break;
         cudaStream_t s = e->own[c & 1];
         CUDA_TRY(cudaMemcpyAsync(dq + a, hq + a, (size_t)(b - a) * sizeof(jcde_query), cudaMemcpyHostToDevice, s));
-        if ((st = launch_detect(e, 3, dq + a, b - a, f, dout + a, s, RawShape{nullptr, 0, 0, 0, 0}))) return st;
+        if ((st = launch_detect(e, 3, dq + a, b - a, f, dout + a, s, RawShape{nullptr, 0, 0, 0, 0}, (int)(c & 1), chunk)))
+            return st;
         CUDA_TRY(cudaMemcpyAsync(hout + a, dout + a, b - a, cudaMemcpyDeviceToHost, s));
     }
     CUDA_TRY(cudaStreamSynchronize(e->own[0]));
@@ -714,14 +762,8 @@ extern "C" jcde_status jcde_detect_batch_noalloc(jcde_engine* e, const jcde_quer
     v.strength = strength;
     e->launches += 2;
     if (n) {
-        const uint32_t* q = reinterpret_cast<const uint32_t*>(dq);
-        k_surrogate<<<(n + SURR_THREADS - 1) / SURR_THREADS, SURR_THREADS, 0, s>>>(v, q, n, dout, PENDING);
+        launch_passes(e, v, reinterpret_cast<const uint32_t*>(dq), n, dout, s, RawShape{nullptr, 0, 0, 0, 0}, 3);
         CUDA_TRY(cudaGetLastError());
-        const uint32_t want = (n + POLY_WARPS - 1) / POLY_WARPS;
-        const uint32_t grid = std::min<uint32_t>(want, (uint32_t)(e->n_sms * e->detect_blocks_per_sm));
-        k_poly<<<grid, POLY_WARPS * 32, 0, s>>>(v, q, n, dout, RawShape{nullptr, 0, 0, 0, 0}, true);
-        CUDA_TRY(cudaGetLastError());
-        e->launches += 2;
     }
     e->last_stream = s;
     e->have_last_stream = true;

@@ -100,28 +100,45 @@ __device__ __forceinline__ bool p_hits_seg(const Seg& s, const Seg& e) { return 
 __device__ __forceinline__ uint32_t p_quad_mask(const Disk& d, const Box& b) { return disk_quadrant_mask(d, b); }
 __device__ __forceinline__ uint32_t p_quad_mask(const Seg& s, const Box& b) { return seg_quadrant_mask(s, b); }
 
-// Advance the pending-children walk: returns the next node or -1 when the walk is finished.
-__device__ __forceinline__ int walk_next(const View& v, uint64_t& pend, int& depth, int& parent) {
-    while (depth > 0) {
-        const int sh = 4 * (depth - 1);
-        uint32_t m = (uint32_t)(pend >> sh) & 0xFu;
+// Breadth-first flattening stores the children of every node as one quartet, and quartets fill
+// indices 1, 5, 9, ... in order, so the quartet holding node i >= 1 starts at quartet_base(i).
+__device__ __forceinline__ int quartet_base(int i) { return 1 + ((i - 1) & ~3); }
+
+// One lane's (or thread's) walk of the quadtree below a start node.  `pend` keeps 4 pending-child
+// bits per level below the start (32 bits cover 8 levels, 64 bits 16); `qb` is the quartet of
+// the deepest pending level, so moving to a sibling costs no memory access.
+template <typename PendT>
+struct WalkT {
+    int node;    // node to visit next; -1 = idle (needs a probe), -2 = no probe left
+    int depth;   // levels with pending children below the start node
+    int qb;      // quartet base of level depth-1
+    PendT pend;
+};
+
+// Next node of the walk in depth-first order, or -1 when the walk is finished.
+template <typename PendT>
+__device__ __forceinline__ int walk_next(const View& v, WalkT<PendT>& w) {
+    while (w.depth > 0) {
+        const int sh = 4 * (w.depth - 1);
+        const uint32_t m = (uint32_t)(w.pend >> sh) & 0xFu;
         if (m) {
-            int i = __ffs(m) - 1;
-            pend &= ~(1ull << (sh + i));
-            return ld_node_links(v, parent).x + i;
+            const int i = __ffs(m) - 1;
+            w.pend &= ~((PendT)1 << (sh + i));
+            return w.qb + i;
         }
-        depth--;
-        parent = ld_node_links(v, parent).y;
+        if (--w.depth > 0) w.qb = quartet_base(__ldg(&v.nodes[w.qb].parent));
     }
     return -1;
 }
 
-// One lane's (or thread's) walk state for the step-wise traversals of k_surrogate and k_poly.
-struct Walk {
-    int node;        // node to visit next; -1 = idle (needs a probe), -2 = no probe left
-    int depth, parent;
-    uint64_t pend;   // 4 pending-children bits per level below the start node
-};
+// Children mask m of node nd is pending below the current level (its slot is empty: every deeper
+// slot is consumed before the walk moves on at a level).
+template <typename PendT>
+__device__ __forceinline__ void walk_push(WalkT<PendT>& w, uint32_t m, int child) {
+    w.pend |= (PendT)m << (4 * w.depth);
+    w.qb = child;
+    w.depth++;
+}
 
 // Leaf test of QTNode::collides (qt_node.rs:126-142): unfiltered Partial hazards, ff box first.
 // `stop` (shared memory, may be null) is raised by the lane that finds a hit; the other lanes of
@@ -145,24 +162,20 @@ __device__ __forceinline__ bool leaf_hits(const View& v, const P& p, const DNode
 }
 
 // Visit w.node for probe p (qt_node.rs:104-146) and advance the walk.  Returns true on a hit.
-template <class P>
-__device__ __forceinline__ bool walk_step(const View& v, const P& p, Walk& w, volatile int* stop) {
+template <class P, typename PendT>
+__device__ __forceinline__ bool walk_step(const View& v, const P& p, WalkT<PendT>& w, volatile int* stop) {
     const uint32_t st = __ldg(&v.strength[w.node]);
     if (st == PRES_ENTIRE) return true;
     if (st == PRES_PARTIAL) {
         DNode nd = ld_node(v, w.node);
         if (nd.child >= 0) {
             const uint32_t m = p_quad_mask(p, nd.box);
-            if (m) {
-                w.pend = (w.pend & ~(0xFull << (4 * w.depth))) | ((uint64_t)m << (4 * w.depth));
-                w.parent = w.node;
-                w.depth++;
-            }
+            if (m) walk_push(w, m, nd.child);
         } else if (leaf_hits(v, p, nd, stop)) {
             return true;
         }
     }
-    w.node = walk_next(v, w.pend, w.depth, w.parent);
+    w.node = walk_next(v, w);
     return false;
 }
 
@@ -173,19 +186,14 @@ __device__ __forceinline__ bool bit_get(const uint32_t* bits, uint32_t k) {
 
 // QTNode::collect_collisions (qt_node.rs:151-191) for one probe from node `start`.
 template <class P>
-__device__ void collect_walk(const View& v, const P& p, int node, uint32_t* bits) {
-    uint64_t pend = 0;
-    int depth = 0, parent = -1;
-    while (node >= 0) {
-        DNode nd = ld_node(v, node);
-        const bool now = __ldg(&v.nedges[node]) <= v.cd_threshold;
+__device__ void collect_walk(const View& v, const P& p, int start, uint32_t* bits) {
+    WalkT<uint64_t> w{start, 0, 0, 0ull};
+    while (w.node >= 0) {
+        DNode nd = ld_node(v, w.node);
+        const bool now = __ldg(&v.nedges[w.node]) <= v.cd_threshold;
         if (nd.child >= 0 && !now) {
-            uint32_t m = p_quad_mask(p, nd.box);
-            if (m) {
-                pend = (pend & ~(0xFull << (4 * depth))) | ((uint64_t)m << (4 * depth));
-                parent = node;
-                depth++;
-            }
+            const uint32_t m = p_quad_mask(p, nd.box);
+            if (m) walk_push(w, m, nd.child);
         } else {
             for (uint32_t k = 0; k < nd.hz_cnt; k++) {
                 DEntry e = ld_entry(v, nd.hz_off + k);
@@ -201,7 +209,7 @@ __device__ void collect_walk(const View& v, const P& p, int node, uint32_t* bits
                 }
             }
         }
-        node = walk_next(v, pend, depth, parent);
+        w.node = walk_next(v, w);
     }
 }
 
@@ -330,10 +338,13 @@ constexpr uint8_t PENDING = 0xFFu;   // verdict slot of a query the surrogate pa
 // query: the fail-fast poles, then the piers, each walked down from the root in the reference's
 // order, stopping at the first hit.  A hit writes JCDE_COLLIDES; a miss writes `miss` (JCDE_FREE
 // for a surrogate-only batch, PENDING when the polygon pass follows).
+template <typename PendT>
 __global__ void __launch_bounds__(SURR_THREADS) k_surrogate(View v, const uint32_t* __restrict__ q, uint32_t n,
-                                                            uint8_t* __restrict__ out, uint8_t miss) {
+                                                            uint8_t* __restrict__ out, uint8_t miss,
+                                                            const uint32_t* __restrict__ order) {
     const uint32_t stride = gridDim.x * SURR_THREADS;
-    for (uint32_t qi = blockIdx.x * SURR_THREADS + threadIdx.x; qi < n; qi += stride) {
+    for (uint32_t i = blockIdx.x * SURR_THREADS + threadIdx.x; i < n; i += stride) {
+        const uint32_t qi = order ? __ldg(&order[i]) : i;
         const uint32_t* w5 = q + (size_t)qi * 5;
         const uint32_t item = __ldg(&w5[0]);
         const float c = __uint_as_float(__ldg(&w5[1])), s = __uint_as_float(__ldg(&w5[2]));
@@ -347,13 +358,13 @@ __global__ void __launch_bounds__(SURR_THREADS) k_surrogate(View v, const uint32
         for (uint32_t p = 0; p < it.n_ff_poles && !hit; p++) {
             const float4 pl = __ldg(&v.poles[it.pole_off + p]);
             const Disk d{xform(Pt{pl.x, pl.y}, c, s, tx, ty), pl.z};
-            Walk w{0, 0, -1, 0ull};
+            WalkT<PendT> w{0, 0, 0, (PendT)0};
             while (w.node >= 0 && !hit) hit = walk_step(v, d, w, nullptr);
         }
         for (uint32_t p = 0; p < it.n_piers && !hit; p++) {
             const float4 pr = __ldg(&v.piers[it.pier_off + p]);
             const Seg sg{xform(Pt{pr.x, pr.y}, c, s, tx, ty), xform(Pt{pr.z, pr.w}, c, s, tx, ty)};
-            Walk w{0, 0, -1, 0ull};
+            WalkT<PendT> w{0, 0, 0, (PendT)0};
             while (w.node >= 0 && !hit) hit = walk_step(v, sg, w, nullptr);
         }
         out[qi] = hit ? (uint8_t)1 : miss;
@@ -363,13 +374,19 @@ __global__ void __launch_bounds__(SURR_THREADS) k_surrogate(View v, const uint32
 // Polygon pass — CDEngine::detect_poly_collision (cd_engine.rs:160-197), one warp per query.
 // With `only_pending`, queries whose slot is not PENDING were decided by the surrogate pass and
 // are skipped.  Writes JCDE_FREE / JCDE_COLLIDES.
-__global__ void __launch_bounds__(POLY_WARPS * 32) k_poly(View v, const uint32_t* __restrict__ q, uint32_t n,
-                                                          uint8_t* __restrict__ out, RawShape raw, bool only_pending) {
+#ifndef JCDE_POLY_MIN_BLOCKS
+#define JCDE_POLY_MIN_BLOCKS 1
+#endif
+template <typename PendT>
+__global__ void __launch_bounds__(POLY_WARPS * 32, JCDE_POLY_MIN_BLOCKS)
+    k_poly(View v, const uint32_t* __restrict__ q, uint32_t n, uint8_t* __restrict__ out, RawShape raw,
+           bool only_pending, const uint32_t* __restrict__ order) {
     __shared__ int stops[POLY_WARPS];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     volatile int* stop = &stops[warp];
     const uint32_t stride = gridDim.x * POLY_WARPS;
-    for (uint32_t qi = blockIdx.x * POLY_WARPS + warp; qi < n; qi += stride) {
+    for (uint32_t i = blockIdx.x * POLY_WARPS + warp; i < n; i += stride) {
+        const uint32_t qi = order ? __ldg(&order[i]) : i;
         if (only_pending && out[qi] != PENDING) continue;
         QShape sh;
         Pt spoi;
@@ -397,7 +414,7 @@ __global__ void __launch_bounds__(POLY_WARPS * 32) k_poly(View v, const uint32_t
         // iteration is one node visit per active lane; a hit anywhere ends the query.
         const uint32_t lt = (1u << lane) - 1u;
         uint32_t next = 0;
-        Walk w{-1, 0, -1, 0ull};
+        WalkT<PendT> w{-1, 0, 0, (PendT)0};
         Seg e{};
         while (!hit) {
             const bool want = w.node == -1;
@@ -405,7 +422,7 @@ __global__ void __launch_bounds__(POLY_WARPS * 32) k_poly(View v, const uint32_t
             if (want) {
                 const uint32_t p = next + __popc(need & lt);
                 if (p < sh.nv) {
-                    w = Walk{vr, 0, -1, 0ull};
+                    w = WalkT<PendT>{vr, 0, 0, (PendT)0};
                     e = sh.edge(p);
                 } else {
                     w.node = -2;
@@ -585,6 +602,65 @@ __global__ void __launch_bounds__(COLLECT_WARPS * 32) k_collect(View v, const ui
         }
         __syncwarp();
     }
+}
+
+// Spatial ordering of a batch: queries are counted into a BUCKET_GRID x BUCKET_GRID grid over the
+// CDE box by translation (Morton order of the cells), and the passes visit them cell by cell, so
+// the threads of a warp walk neighbouring parts of the quadtree.  Only the visiting order changes;
+// every query still writes its own verdict slot.
+constexpr uint32_t BUCKET_BITS = 6;
+constexpr uint32_t BUCKET_GRID = 1u << BUCKET_BITS;
+constexpr uint32_t N_BUCKETS = BUCKET_GRID * BUCKET_GRID;
+
+__device__ __forceinline__ uint32_t spread_bits(uint32_t x) {   // 6 bits -> even positions
+    x &= 0x3Fu;
+    x = (x | (x << 4)) & 0x30Fu;
+    x = (x | (x << 2)) & 0x333u;
+    x = (x | (x << 1)) & 0x555u;
+    return x;
+}
+__device__ __forceinline__ uint32_t bucket_of(const uint32_t* __restrict__ q, uint32_t qi, const Box& b) {
+    const float tx = __uint_as_float(__ldg(&q[(size_t)qi * 5 + 3]));
+    const float ty = __uint_as_float(__ldg(&q[(size_t)qi * 5 + 4]));
+    const float g = (float)BUCKET_GRID;
+    const float fx = fmaxf(0.0f, fminf((tx - b.x0) / (b.x1 - b.x0) * g, g - 1.0f));
+    const float fy = fmaxf(0.0f, fminf((ty - b.y0) / (b.y1 - b.y0) * g, g - 1.0f));
+    return spread_bits((uint32_t)fx) | (spread_bits((uint32_t)fy) << 1);
+}
+__global__ void k_bucket_count(const uint32_t* __restrict__ q, uint32_t n, Box b, uint32_t* __restrict__ hist) {
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) atomicAdd(&hist[bucket_of(q, i, b)], 1u);
+}
+// exclusive scan of N_BUCKETS counts in place (one block of 1024 threads, 4 counts each)
+__global__ void __launch_bounds__(1024) k_bucket_scan(uint32_t* __restrict__ hist) {
+    __shared__ uint32_t warp_sums[32];
+    const uint32_t t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    uint32_t c[4], s = 0;
+    for (int k = 0; k < 4; k++) { c[k] = hist[t * 4 + k]; s += c[k]; }
+    uint32_t incl = s;
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(FULL, incl, o);
+        if (lane >= (uint32_t)o) incl += y;
+    }
+    if (lane == 31) warp_sums[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = warp_sums[lane], wi = w;
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(FULL, wi, o);
+            if (lane >= (uint32_t)o) wi += y;
+        }
+        warp_sums[lane] = wi - w;
+    }
+    __syncthreads();
+    uint32_t run = warp_sums[warp] + incl - s;
+    for (int k = 0; k < 4; k++) { hist[t * 4 + k] = run; run += c[k]; }
+}
+__global__ void k_bucket_scatter(const uint32_t* __restrict__ q, uint32_t n, Box b, uint32_t* __restrict__ offs,
+                                 uint32_t* __restrict__ order) {
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        order[atomicAdd(&offs[bucket_of(q, i, b)], 1u)] = i;
 }
 
 // Strongest presence per node under a filter (QTHazardVec::strongest, qt_hazard_vec.rs:60-63).
