@@ -375,13 +375,16 @@ __global__ void __launch_bounds__(SURR_THREADS) k_surrogate(View v, const uint32
 // With `only_pending`, queries whose slot is not PENDING were decided by the surrogate pass and
 // are skipped.  Writes JCDE_FREE / JCDE_COLLIDES.
 #ifndef JCDE_POLY_MIN_BLOCKS
-#define JCDE_POLY_MIN_BLOCKS 1
+#define JCDE_POLY_MIN_BLOCKS 4   // 64 registers: four 256-thread blocks per SM
 #endif
+constexpr uint32_t POLY_MAXV = 256;   // items with more vertices transform edges on the fly
 template <typename PendT>
 __global__ void __launch_bounds__(POLY_WARPS * 32, JCDE_POLY_MIN_BLOCKS)
     k_poly(View v, const uint32_t* __restrict__ q, uint32_t n, uint8_t* __restrict__ out, RawShape raw,
            bool only_pending, const uint32_t* __restrict__ order) {
     __shared__ int stops[POLY_WARPS];
+    __shared__ float2 tverts[POLY_WARPS][POLY_MAXV];   // transformed item vertices
+    __shared__ uint32_t jobs[POLY_WARPS][POLY_MAXV];   // edge index | children mask below the virtual root << 16
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     volatile int* stop = &stops[warp];
     const uint32_t stride = gridDim.x * POLY_WARPS;
@@ -404,15 +407,73 @@ __global__ void __launch_bounds__(POLY_WARPS * 32, JCDE_POLY_MIN_BLOCKS)
             spoi = xform(Pt{it.poi_x, it.poi_y}, qh.c, qh.s, qh.tx, qh.ty);
         }
         if (lane == 0) *stop = 0;
+        // the transformed vertices are kept in shared memory (items up to POLY_MAXV vertices)
+        const bool cached = sh.nv <= POLY_MAXV;
+        float2* tv = tverts[warp];
+        Box sb;
+        {
+            float x0 = FLT_MAX, y0 = FLT_MAX, x1 = -FLT_MAX, y1 = -FLT_MAX;
+            for (uint32_t k = lane; k < sh.nv; k += 32) {
+                const Pt p = sh.vtx(k);
+                if (cached) tv[k] = make_float2(p.x, p.y);
+                x0 = fminf(x0, p.x);
+                y0 = fminf(y0, p.y);
+                x1 = fmaxf(x1, p.x);
+                y1 = fmaxf(y1, p.y);
+            }
+            JCDE_UNROLL
+            for (int o = 16; o; o >>= 1) {
+                x0 = fminf(x0, __shfl_xor_sync(FULL, x0, o));
+                y0 = fminf(y0, __shfl_xor_sync(FULL, y0, o));
+                x1 = fmaxf(x1, __shfl_xor_sync(FULL, x1, o));
+                y1 = fmaxf(y1, __shfl_xor_sync(FULL, y1, o));
+            }
+            sb = Box{x0, y0, x1, y1};   // SPolygon::generate_bounding_box (simple_polygon.rs:122-133)
+        }
         __syncwarp();
-        const Box sb = warp_bbox(sh, lane);
+        auto edge_of = [&](uint32_t k) -> Seg {
+            if (!cached) return sh.edge(k);
+            const float2 a = tv[k], b = tv[k + 1 == sh.nv ? 0 : k + 1];
+            return Seg{Pt{a.x, a.y}, Pt{b.x, b.y}};
+        };
         // a shape not surrounded by the CDE box collides (cd_engine.rs:161-163)
         bool hit = !box_surrounds(v.cde, sb);
         const int vr = hit ? 0 : virtual_root(v, sb);
-        // Edges are handed out dynamically: a lane whose walk is over takes the next unassigned
-        // edge (ballot rank), so no lane waits for the slowest walk of a fixed round.  Every loop
-        // iteration is one node visit per active lane; a hit anywhere ends the query.
         const uint32_t lt = (1u << lane) - 1u;
+        // Every edge's walk starts with a visit of the virtual root.  When the root of the walk is a
+        // Partial internal node, that first visit is done here for all edges at once (uniform work,
+        // 32 edges per round): edges whose quadrant mask is empty are dropped and the others are
+        // listed with their mask, so the walks below start one level down.
+        uint32_t n_jobs = sh.nv;   // without the list, job k is edge k starting at the virtual root
+        bool listed = false;
+        int vr_child = -1;
+        if (!hit) {
+            const uint32_t st = __ldg(&v.strength[vr]);
+            if (st == PRES_ENTIRE) {
+                hit = true;
+            } else if (st == PRES_NONE) {
+                n_jobs = 0;   // nothing to hit below; containment still runs
+            } else {
+                const DNode vn = ld_node(v, vr);
+                if (vn.child >= 0 && cached) {
+                    listed = true;
+                    vr_child = vn.child;
+                    uint32_t cnt = 0;
+                    for (uint32_t base = 0; base < sh.nv; base += 32) {
+                        const uint32_t k = base + lane;
+                        const uint32_t m = k < sh.nv ? seg_quadrant_mask(edge_of(k), vn.box) : 0u;
+                        const uint32_t bal = __ballot_sync(FULL, m != 0);
+                        if (m) jobs[warp][cnt + __popc(bal & lt)] = k | (m << 16);
+                        cnt += __popc(bal);
+                    }
+                    n_jobs = cnt;
+                    __syncwarp();
+                }
+            }
+        }
+        // Jobs are handed out dynamically: a lane whose walk is over takes the next unassigned job
+        // (ballot rank), so no lane waits for the slowest walk of a fixed round.  Every loop
+        // iteration is one node visit per active lane; a hit anywhere ends the query.
         uint32_t next = 0;
         WalkT<PendT> w{-1, 0, 0, (PendT)0};
         Seg e{};
@@ -421,9 +482,16 @@ __global__ void __launch_bounds__(POLY_WARPS * 32, JCDE_POLY_MIN_BLOCKS)
             const uint32_t need = __ballot_sync(FULL, want);
             if (want) {
                 const uint32_t p = next + __popc(need & lt);
-                if (p < sh.nv) {
-                    w = WalkT<PendT>{vr, 0, 0, (PendT)0};
-                    e = sh.edge(p);
+                if (p < n_jobs) {
+                    if (listed) {
+                        const uint32_t job = jobs[warp][p];
+                        e = edge_of(job & 0xFFFFu);
+                        w = WalkT<PendT>{-1, 1, vr_child, (PendT)(job >> 16)};
+                        w.node = walk_next(v, w);
+                    } else {
+                        e = edge_of(p);
+                        w = WalkT<PendT>{vr, 0, 0, (PendT)0};
+                    }
                 } else {
                     w.node = -2;
                 }
