@@ -84,7 +84,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "20"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
         except Exception:
@@ -156,39 +156,58 @@ def oracle_engine_for(lay):
     return W.replay(O.OracleBackend, lay)
 
 
-def bytes_per_query(counts: np.ndarray, n: int, lay, q) -> float:
-    """Algorithmic bytes per query: 20 B query + 1 B verdict, 8 B per item vertex, 12 B per ff pole,
-    16 B per quadtree node visited, 8 B per node-hazard entry scanned, 16 B per hazard edge tested,
-    16 B per point-in-polygon edge (counted by the oracle on the same queries)."""
-    nv = np.array([len(it.xy) for it in lay.items], np.float64)[q["item"]].mean()
-    nff = np.array([it.n_ff_poles for it in lay.items], np.float64)[q["item"]].mean()
-    c = counts.astype(np.float64) / n
-    return 21.0 + 8.0 * nv + 12.0 * nff + 16.0 * c[0] + 8.0 * c[1] + 16.0 * c[2] + 16.0 * c[3]
+def item_stats(lay, q):
+    nv = np.array([len(it.xy) for it in lay.items], np.float64)[q["item"]].mean() if len(q) else 0.0
+    nff = np.array([it.n_ff_poles for it in lay.items], np.float64)[q["item"]].mean() if len(q) else 0.0
+    return nv, nff
+
+
+def tree_bytes(counts: np.ndarray, n: int) -> float:
+    """16 B per quadtree node visited, 8 B per node-hazard entry scanned, 16 B per hazard edge
+    tested, 16 B per point-in-polygon edge (per query, counted by the oracle)."""
+    c = counts.astype(np.float64) / max(1, n)
+    return 16.0 * c[0] + 8.0 * c[1] + 16.0 * c[2] + 16.0 * c[3]
 
 
 def cpu_baseline(lay, queries, n_sample: int, repeats: int = 3):
+    """The oracle on all host cores over the first n_sample queries (best of `repeats`), plus the
+    algorithmic work of each pass on that sample (the roofline numerators)."""
     oeng = oracle_engine_for(lay)
     q = queries[:n_sample]
     cores = host_cores()
-    counts = np.zeros(4, np.uint64)
-    oeng.detect_batch(q, ignored=lay.filter_keys, n_threads=cores, counts=counts)   # warm-up + work counts
+    oeng.detect_batch(q, ignored=lay.filter_keys, n_threads=cores)   # warm-up
     best = float("inf")
     verdicts = None
     for _ in range(repeats):
         t = time.perf_counter()
         verdicts = oeng.detect_batch(q, ignored=lay.filter_keys, n_threads=cores)
         best = min(best, time.perf_counter() - t)
+    # per-pass work: surrogate on every query, polygon on those the surrogate leaves undecided
+    c_s = np.zeros(4, np.uint64)
+    surr = oeng.detect_batch(q, ignored=lay.filter_keys, n_threads=cores, counts=c_s, mode=1)
+    pend = q[surr == 0]
+    c_p = np.zeros(4, np.uint64)
+    oeng.detect_batch(pend, ignored=lay.filter_keys, n_threads=cores, counts=c_p, mode=2)
+    nv_all, nff = item_stats(lay, q)
+    nv_pend, _ = item_stats(lay, pend)
+    work = {
+        # bytes per query of the batch: query in + verdict out + poles + tree walk
+        "k_surrogate": 21.0 + 12.0 * nff + tree_bytes(c_s, len(q)),
+        # bytes per undecided query: query in + verdict out + item vertices + tree walk + PIP
+        "k_poly_per_pending": 21.0 + 8.0 * nv_pend + tree_bytes(c_p, len(pend)),
+        "pending_fraction": len(pend) / len(q),
+    }
     return {"value": n_sample / best, "unit": "queries/s", "cores": cores, "kind": "port",
-            "sample": f"first {n_sample} queries of the batch, best of {repeats}"}, counts, verdicts
+            "sample": f"first {n_sample} queries of the batch, best of {repeats}"}, work, verdicts
 
 
-def read_traffic(n_queries: int):
-    """DRAM bytes per launch of k_detect from the committed ncu summary, scaled to n_queries."""
-    path = os.path.join(REPO, "profiles", "k_detect_star.txt")
+def read_traffic(kernel: str):
+    """DRAM bytes per launch of `kernel` on this workload, from the committed ncu summary."""
+    path = os.path.join(REPO, "profiles", f"{kernel}_star_1m.txt")
     try:
         for line in open(path):
-            if line.startswith("dram_bytes_per_query"):
-                return float(line.split("=")[1]) * n_queries
+            if line.startswith("dram_bytes_per_launch"):
+                return float(line.split("=")[1])
     except OSError:
         pass
     return None
@@ -266,19 +285,29 @@ def run_gpu(args):
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    with ClockSampler(local) as clk:
-        profiler_range(True)
-        t0 = time.perf_counter()
-        for i in range(args.steps):
-            flush.zero_()
-            ev[i][0].record(stream)
-            eng.detect_batch(dq, filter=filt, out=out, stream=stream)
-            ev[i][1].record(stream)
-        torch.cuda.synchronize()
-        wall = time.perf_counter() - t0
-        profiler_range(False)
+    clk = ClockSampler(local)
+    clk.__enter__()   # sampled through the device loop, its profiled twin and the e2e loop
+    profiler_range(True)
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        flush.zero_()
+        ev[i][0].record(stream)
+        eng.detect_batch(dq, filter=filt, out=out, stream=stream)
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    profiler_range(False)
     launches = eng.kernel_launches() - launches0
     step_ms = [a.elapsed_time(b) for a, b in ev]
+    # per-kernel event times of the same steps (a second, profiled run of the timed loop)
+    eng.profile(True)
+    eng.profile_read(reset=True)
+    for i in range(args.steps):
+        flush.zero_()
+        eng.detect_batch(dq, filter=filt, out=out, stream=stream)
+    torch.cuda.synchronize()
+    kprof = eng.profile_read(reset=True)
+    eng.profile(False)
     dev_s = sum(step_ms) / 1e3
     if world > 1:
         t = torch.tensor([dev_s], device="cuda")
@@ -290,8 +319,6 @@ def run_gpu(args):
     # e2e: host buffers through the C ABI, copies inside the timed region
     hq = torch.from_numpy(q.view(np.uint8).copy()).pin_memory()
     hout = torch.empty(N_QUERIES, dtype=torch.uint8).pin_memory()
-    import ctypes as C
-
     from jcde._ffi import lib
 
     fobj = jcde.engine._Filter(filt)
@@ -305,6 +332,7 @@ def run_gpu(args):
         st = lib().jcde_detect_batch_host(eng.h, hq.data_ptr(), N_QUERIES, fobj.ref, hout.data_ptr())
         e2e_times.append(time.perf_counter() - t)
         assert st == 0
+    clk.__exit__(None, None, None)
     e2e_s = sum(e2e_times)
     if world > 1:
         t = torch.tensor([e2e_s], device="cuda")
@@ -319,18 +347,27 @@ def run_gpu(args):
         return 0
 
     # CPU baseline + algorithmic bytes per query (oracle on a bounded sample of the same queries)
-    cpu, counts, cpu_verdicts = cpu_baseline(lay, q, n_sample=args.cpu_sample)
+    cpu, work, cpu_verdicts = cpu_baseline(lay, q, n_sample=args.cpu_sample)
     sample_ok = bool(np.array_equal(cpu_verdicts, verdicts[: args.cpu_sample]))
-    bpq = bytes_per_query(counts, args.cpu_sample, lay, q[: args.cpu_sample])
-    avg_launch_s = dev_s / args.steps
-    achieved = bpq * N_QUERIES / avg_launch_s / 1e9
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json")))
     except Exception:
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
-    traffic = read_traffic(N_QUERIES)
+    kernels = {}
+    for name, kind, bytes_per_launch in (
+        ("k_surrogate", "surrogate", work["k_surrogate"] * N_QUERIES),
+        ("k_poly", "poly", work["k_poly_per_pending"] * work["pending_fraction"] * N_QUERIES),
+    ):
+        ms, cnt = kprof[kind]
+        avg_s = ms / 1e3 / max(1, cnt)
+        kernels[name] = {"avg_ms": 1e3 * avg_s, "launches": cnt, "bytes_per_launch": bytes_per_launch,
+                         "achieved_gbs": bytes_per_launch / avg_s / 1e9 if avg_s > 0 else None}
+    dom = max(kernels, key=lambda k: kernels[k]["avg_ms"])
+    achieved = kernels[dom]["achieved_gbs"]
+    traffic = read_traffic(dom)
+    order_ms, order_n = kprof["order"]
     clocks = clk.summary()
     line = {
         "metric": "collision queries/s", "value": value, "unit": "queries/s", "n_gpus": world,
@@ -340,8 +377,9 @@ def run_gpu(args):
                    "cd_threshold": lay.cd_threshold, "l2": "flushed between steps (256 MB write)",
                    "parallelism": f"{world} rank(s), queries per rank, layout replicated"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback",
-                     "bytes_per_query": bpq, "kernel": "k_detect<3>"},
+                     "traffic": traffic, "kernel": dom,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if peaks else "fallback 6.8 TB/s",
+                     "kernels": kernels, "ordering_ms_per_step": order_ms / max(1, order_n)},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": N_QUERIES * 20,
                 "d2h_bytes_per_step": N_QUERIES, "same_verdicts": e2e_same},
@@ -360,7 +398,7 @@ def run_gpu(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="jcde", choices=["jcde", "reference"])
     ap.add_argument("--cpu-sample", type=int, default=1 << 17)

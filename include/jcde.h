@@ -195,6 +195,17 @@ jcde_status jcde_tree_dump(const jcde_engine* e, uint32_t* out, uint64_t cap, ui
 jcde_status jcde_device_stats(jcde_engine* e, uint64_t* out5);
 /* number of kernels this engine has launched since creation (bench accounting) */
 uint64_t jcde_kernel_launches(const jcde_engine* e);
+/* Kernel timing (no counterpart in the reference): when enabled, every launch is bracketed by CUDA
+ * events on its stream; jcde_profile_read synchronises on them and returns, per kind, the summed
+ * milliseconds and launch counts (arrays of JCDE_PROF_KINDS), optionally resetting the totals. */
+#define JCDE_PROF_SURROGATE 0   /* surrogate pass (detect) */
+#define JCDE_PROF_POLY 1        /* polygon pass (detect) */
+#define JCDE_PROF_COLLECT 2     /* collect kernel */
+#define JCDE_PROF_ORDER 3       /* spatial ordering of a batch (3 small kernels) */
+#define JCDE_PROF_FILTER 4      /* per-node presence under a new filter */
+#define JCDE_PROF_KINDS 5
+jcde_status jcde_profile_enable(jcde_engine* e, int enable);
+jcde_status jcde_profile_read(jcde_engine* e, double* ms, uint64_t* count, int reset);
 
 #ifdef __cplusplus
 }

@@ -82,11 +82,23 @@ struct jcde_engine {
     int n_sms = 0;
     int detect_blocks_per_sm = 0, collect_blocks_per_sm = 0;
     uint64_t launches = 0;
+    // optional per-kernel timing (jcde_profile_enable): CUDA events around each launch
+    bool prof = false;
+    struct ProfMark { cudaEvent_t a, b; int kind; };
+    std::vector<ProfMark> prof_open;
+    std::vector<cudaEvent_t> prof_pool;
+    double prof_ms[JCDE_PROF_KINDS] = {};
+    uint64_t prof_n[JCDE_PROF_KINDS] = {};
 
     jcde_engine(const jcde_config& c, Box bbox) : cfg(c), tree(c.quadtree_depth, c.cd_threshold, bbox) {}
     ~jcde_engine() {
         for (auto& s : own)
             if (s) cudaStreamDestroy(s);
+        for (auto& m : prof_open) {
+            cudaEventDestroy(m.a);
+            cudaEventDestroy(m.b);
+        }
+        for (auto ev : prof_pool) cudaEventDestroy(ev);
     }
 };
 
@@ -94,6 +106,32 @@ struct jcde_engine {
     do {                                              \
         if ((x) != cudaSuccess) return JCDE_ERR_CUDA; \
     } while (0)
+
+// Kernel timing: prof_begin/prof_end bracket one launch (or a group of launches of one kind) with a
+// pair of events on the launch stream; jcde_profile_read folds finished pairs into totals.
+static cudaEvent_t prof_event(jcde_engine* e) {
+    if (!e->prof_pool.empty()) {
+        cudaEvent_t ev = e->prof_pool.back();
+        e->prof_pool.pop_back();
+        return ev;
+    }
+    cudaEvent_t ev = nullptr;
+    if (cudaEventCreate(&ev) != cudaSuccess) return nullptr;
+    return ev;
+}
+static cudaEvent_t prof_begin(jcde_engine* e, cudaStream_t s) {
+    if (!e->prof) return nullptr;
+    cudaEvent_t a = prof_event(e);
+    if (a) cudaEventRecord(a, s);
+    return a;
+}
+static void prof_end(jcde_engine* e, cudaStream_t s, cudaEvent_t a, int kind) {
+    if (!e->prof || !a) return;
+    cudaEvent_t b = prof_event(e);
+    if (!b) return;
+    cudaEventRecord(b, s);
+    e->prof_open.push_back({a, b, kind});
+}
 
 static jcde_status upload(DevBuf& b, const void* src, size_t bytes) {
     if (!b.ensure(std::max<size_t>(bytes, 16))) return JCDE_ERR_CUDA;
@@ -201,7 +239,9 @@ static jcde_status apply_filter(jcde_engine* e, const jcde_filter* f, cudaStream
     v.mask = slot->d_mask.as<uint32_t>();
     if (slot->version != e->tree.version()) {
         if (!slot->d_strength.ensure(std::max<uint32_t>(e->n_nodes, 16))) return JCDE_ERR_CUDA;
+        cudaEvent_t pa = prof_begin(e, s);
         k_strength<<<(e->n_nodes + 255) / 256, 256, 0, s>>>(v, e->n_nodes, slot->d_strength.as<uint8_t>());
+        prof_end(e, s, pa, JCDE_PROF_FILTER);
         CUDA_TRY(cudaGetLastError());
         e->launches++;
         slot->version = e->tree.version();
@@ -246,9 +286,11 @@ static const uint32_t* spatial_order(jcde_engine* e, const uint32_t* q, uint32_t
     if (cudaMemsetAsync(hist, 0, N_BUCKETS * 4, s) != cudaSuccess) return nullptr;
     const Box b = e->tree.bbox();
     const uint32_t grid = std::min<uint32_t>((n + 255) / 256, (uint32_t)e->n_sms * 8);
+    cudaEvent_t pa = prof_begin(e, s);
     k_bucket_count<<<grid, 256, 0, s>>>(q, n, b, hist);
     k_bucket_scan<<<1, 1024, 0, s>>>(hist);
     k_bucket_scatter<<<grid, 256, 0, s>>>(q, n, b, hist, order);
+    prof_end(e, s, pa, JCDE_PROF_ORDER);
     e->launches += 3;
     return order;
 }
@@ -260,13 +302,17 @@ static void launch_passes_t(jcde_engine* e, const View& v, const uint32_t* q, ui
                             cudaStream_t s, RawShape raw, int mode, const uint32_t* order) {
     if (mode & 1) {
         const uint32_t grid = (n + SURR_THREADS - 1) / SURR_THREADS;
+        cudaEvent_t pa = prof_begin(e, s);
         k_surrogate<PendT><<<grid, SURR_THREADS, 0, s>>>(v, q, n, dout, mode == 1 ? (uint8_t)0 : PENDING, order);
+        prof_end(e, s, pa, JCDE_PROF_SURROGATE);
         e->launches++;
     }
     if (mode & 2) {
         const uint32_t want = (n + POLY_WARPS - 1) / POLY_WARPS;
         const uint32_t grid = std::min<uint32_t>(want, (uint32_t)(e->n_sms * e->detect_blocks_per_sm));
+        cudaEvent_t pa = prof_begin(e, s);
         k_poly<PendT><<<grid, POLY_WARPS * 32, 0, s>>>(v, q, n, dout, raw, mode == 3, order);
+        prof_end(e, s, pa, JCDE_PROF_POLY);
         e->launches++;
     }
 }
@@ -320,12 +366,14 @@ static jcde_status launch_collect(jcde_engine* e, int mode, const jcde_query* dq
     uint32_t want = (n + COLLECT_WARPS - 1) / COLLECT_WARPS;
     uint32_t grid = std::min<uint32_t>(want, (uint32_t)(e->n_sms * per_sm));
     const uint32_t* q = reinterpret_cast<const uint32_t*>(dq);
+    cudaEvent_t pa = prof_begin(e, s);
     switch (mode) {
         case 1: k_collect<1><<<grid, COLLECT_WARPS * 32, smem, s>>>(v, q, n, words, d_off, d_cnt, d_ids, cap, d_total, raw); break;
         case 2: k_collect<2><<<grid, COLLECT_WARPS * 32, smem, s>>>(v, q, n, words, d_off, d_cnt, d_ids, cap, d_total, raw); break;
         default: k_collect<3><<<grid, COLLECT_WARPS * 32, smem, s>>>(v, q, n, words, d_off, d_cnt, d_ids, cap, d_total, raw); break;
     }
     CUDA_TRY(cudaGetLastError());
+    prof_end(e, s, pa, JCDE_PROF_COLLECT);
     e->launches++;
     e->last_stream = s;
     e->have_last_stream = true;
@@ -686,6 +734,35 @@ jcde_status jcde_device_stats(jcde_engine* e, uint64_t* out5) {
 }
 
 uint64_t jcde_kernel_launches(const jcde_engine* e) { return e ? e->launches : 0; }
+
+jcde_status jcde_profile_enable(jcde_engine* e, int enable) {
+    if (!e) return JCDE_ERR_ARG;
+    e->prof = enable != 0;
+    return JCDE_OK;
+}
+
+jcde_status jcde_profile_read(jcde_engine* e, double* ms, uint64_t* count, int reset) {
+    if (!e || !ms || !count) return JCDE_ERR_ARG;
+    for (auto& m : e->prof_open) {
+        float t = 0.0f;
+        CUDA_TRY(cudaEventSynchronize(m.b));
+        CUDA_TRY(cudaEventElapsedTime(&t, m.a, m.b));
+        e->prof_ms[m.kind] += t;
+        e->prof_n[m.kind] += 1;
+        e->prof_pool.push_back(m.a);
+        e->prof_pool.push_back(m.b);
+    }
+    e->prof_open.clear();
+    for (int k = 0; k < JCDE_PROF_KINDS; k++) {
+        ms[k] = e->prof_ms[k];
+        count[k] = e->prof_n[k];
+        if (reset) {
+            e->prof_ms[k] = 0.0;
+            e->prof_n[k] = 0;
+        }
+    }
+    return JCDE_OK;
+}
 
 }  // extern "C"
 

@@ -85,6 +85,8 @@ SIGNATURES = {
     "jcde_tree_dump": (C.c_int32, [P, u32p, C.c_uint64, u64p]),
     "jcde_device_stats": (C.c_int32, [P, u64p]),
     "jcde_kernel_launches": (C.c_uint64, [P]),
+    "jcde_profile_enable": (C.c_int32, [P, C.c_int]),
+    "jcde_profile_read": (C.c_int32, [P, C.POINTER(C.c_double), u64p, C.c_int]),
 }
 
 _lib = None

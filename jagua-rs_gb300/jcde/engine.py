@@ -287,6 +287,19 @@ class CDEngine:
     def kernel_launches(self) -> int:
         return int(lib().jcde_kernel_launches(self.h))
 
+    PROFILE_KINDS = ("surrogate", "poly", "collect", "order", "filter")
+
+    def profile(self, enable: bool = True) -> None:
+        """Bracket every kernel launch with CUDA events (jcde_profile_enable)."""
+        check(lib().jcde_profile_enable(self.h, int(enable)), "profile_enable")
+
+    def profile_read(self, reset: bool = True) -> dict:
+        """{kind: (total_ms, launches)} of the profiled launches since the last reset."""
+        ms = (C.c_double * len(self.PROFILE_KINDS))()
+        n = (C.c_uint64 * len(self.PROFILE_KINDS))()
+        check(lib().jcde_profile_read(self.h, ms, n, int(reset)), "profile_read")
+        return {k: (ms[i], int(n[i])) for i, k in enumerate(self.PROFILE_KINDS)}
+
 
 class _Snapshot:
     def __init__(self, h):
