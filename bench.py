@@ -332,6 +332,31 @@ def run_gpu(args):
         st = lib().jcde_detect_batch_host(eng.h, hq.data_ptr(), N_QUERIES, fobj.ref, hout.data_ptr())
         e2e_times.append(time.perf_counter() - t)
         assert st == 0
+    # collect mode on the same batch (cd_engine.rs:261-310): all colliding hazard keys per query
+    cap = 4 * N_QUERIES
+    c_off = torch.empty(N_QUERIES, dtype=torch.int32, device="cuda")
+    c_cnt = torch.empty(N_QUERIES, dtype=torch.int32, device="cuda")
+    c_ids = torch.empty(cap, dtype=torch.int32, device="cuda")
+    c_tot = torch.zeros(1, dtype=torch.int32, device="cuda")
+
+    def collect_once():
+        st = lib().jcde_collect_batch(eng.h, dq.data_ptr(), N_QUERIES, fobj.ref, c_off.data_ptr(), c_cnt.data_ptr(),
+                                      c_ids.data_ptr(), cap, c_tot.data_ptr(), stream.cuda_stream)
+        assert st == 0
+
+    for _ in range(args.warmup):
+        collect_once()
+    c_ms = []
+    for i in range(args.steps):
+        flush.zero_()
+        a_ev, b_ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a_ev.record(stream)
+        collect_once()
+        b_ev.record(stream)
+        c_ms.append((a_ev, b_ev))
+    torch.cuda.synchronize()
+    collect_s = sum(a.elapsed_time(b) for a, b in c_ms) / 1e3
+    collect_total = int(c_tot.item())
     clk.__exit__(None, None, None)
     e2e_s = sum(e2e_times)
     if world > 1:
@@ -349,6 +374,12 @@ def run_gpu(args):
     # CPU baseline + algorithmic bytes per query (oracle on a bounded sample of the same queries)
     cpu, work, cpu_verdicts = cpu_baseline(lay, q, n_sample=args.cpu_sample)
     sample_ok = bool(np.array_equal(cpu_verdicts, verdicts[: args.cpu_sample]))
+    # collect parity on a small sample: sorted key sets per query against the oracle
+    n_cs = min(8192, args.cpu_sample)
+    ocnt, oids = oracle_engine_for(lay).collect_batch(q[:n_cs], ignored=lay.filter_keys, n_threads=host_cores())
+    g_off, g_cnt, g_ids = c_off.cpu().numpy(), c_cnt.cpu().numpy(), c_ids.cpu().numpy()
+    o_off = np.concatenate([[0], np.cumsum(ocnt.astype(np.int64))])
+    collect_ok = all(np.array_equal(g_ids[g_off[i]:g_off[i] + g_cnt[i]], oids[o_off[i]:o_off[i + 1]]) for i in range(n_cs))
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json")))
@@ -383,6 +414,9 @@ def run_gpu(args):
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": N_QUERIES * 20,
                 "d2h_bytes_per_step": N_QUERIES, "same_verdicts": e2e_same},
+        "collect": {"value": N_QUERIES * args.steps / collect_s, "unit": "queries/s", "kernel": "k_collect",
+                    "ms_per_step": 1e3 * collect_s / args.steps, "keys_per_query": collect_total / N_QUERIES,
+                    "parity_sample": {"queries": n_cs, "bit_exact": bool(collect_ok)}},
         "gpu_launches": launches,
         "clocks": clocks,
         "wall_s_timed": wall,
@@ -395,6 +429,72 @@ def run_gpu(args):
     return 0
 
 
+def run_multi(args):
+    """configs[2]: 64 independent bin layouts, log-uniform 4,096-262,144 queries each, answered by
+    one launch sequence (CUDA graph) versus 64 per-layout jcde_detect_batch calls."""
+    import torch
+
+    import jcde
+    from jcde import workload as W
+
+    jcde.lib()
+    t = time.time()
+    lays = W.multi_layouts(jcde.GpuBackend)
+    log(f"[bench] {len(lays)} layouts, {sum(len(l.hazards) for l, _ in lays)} hazards ({time.time() - t:.1f}s)")
+    engines = [e.eng for _, e in lays]
+    q, offs = W.multi_queries(lays)
+    n = int(offs[-1])
+    dq = torch.from_numpy(q.view(np.uint8).copy()).cuda()
+    out_plain = torch.empty(n, dtype=torch.uint8, device="cuda")
+    out_multi = torch.empty(n, dtype=torch.uint8, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.Stream()
+    m = jcde.MultiEngine(engines)
+    qb = W.QUERY_DTYPE.itemsize
+
+    def plain():
+        for l, eng in enumerate(engines):
+            a, b = int(offs[l]), int(offs[l + 1])
+            eng.detect_batch(dq[a * qb:b * qb], out=out_plain[a:b], stream=stream)
+
+    def batched():
+        m.detect(dq, offs, out=out_multi, stream=stream, graph=True)
+
+    res = {}
+    with torch.cuda.stream(stream):
+        for name, fn in (("plain", plain), ("batched", batched)):
+            for _ in range(args.warmup):
+                fn()
+            stream.synchronize()
+            ms = []
+            for _ in range(args.steps):
+                flush.zero_()
+                a_ev, b_ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a_ev.record(stream)
+                fn()
+                b_ev.record(stream)
+                ms.append((a_ev, b_ev))
+            stream.synchronize()
+            res[name] = sum(a.elapsed_time(b) for a, b in ms) / args.steps
+    same = bool(torch.equal(out_plain, out_multi))
+    line = {
+        "metric": "multi-layout collision queries/s", "value": n / (res["batched"] / 1e3), "unit": "queries/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["batched"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"{len(lays)} star-container bins (32-128 v), 20-400 items each from 40 star types "
+                               f"(8-200 v), log-uniform 4,096-262,144 queries per bin ({n} total)",
+                   "batched": "one ordering + surrogate + polygon launch sequence, CUDA-graph replay",
+                   "plain": f"{len(lays)} jcde_detect_batch calls, one per layout",
+                   "l2": "flushed between steps (256 MB write)"},
+        "plain": {"value": n / (res["plain"] / 1e3), "ms_per_step": res["plain"]},
+        "speedup_vs_plain": res["plain"] / res["batched"],
+        "same_verdicts": same,
+        "impl": "jcde",
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -402,9 +502,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="jcde", choices=["jcde", "reference"])
     ap.add_argument("--cpu-sample", type=int, default=1 << 17)
+    ap.add_argument("--workload", default="star", choices=["star", "multi"],
+                    help="star: the headline single-layout batch; multi: 64 layouts in one launch sequence")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "multi":
+        return run_multi(args)
     return run_gpu(args)
 
 

@@ -160,6 +160,24 @@ jcde_status jcde_collect_batch(jcde_engine* e, const jcde_query* d_queries, uint
 jcde_status jcde_detect_batch_noalloc(jcde_engine* e, const jcde_query* d_queries, uint32_t n,
                                       const jcde_filter* filter, uint8_t* d_verdicts, void* stream);
 
+/* --- several layouts in one launch sequence (no counterpart in the reference) ------------------- */
+/* A jcde_multi groups engines (one per layout, e.g. the bins of a bin-packing problem, each a
+ * Layout with its own CDEngine, entities/layout.rs:14-21) so that one ordering + surrogate +
+ * polygon launch sequence answers all their batches: d_queries holds layout l's queries at
+ * [offsets[l], offsets[l+1]) (offsets: host array of n+1), filters is an array of n filters or
+ * NULL, d_verdicts one slot per query.  Verdicts equal those of jcde_detect_batch per engine.  The
+ * engines are borrowed; destroy the group before them.  The _graph variant captures the sequence
+ * into a CUDA graph on first use and replays it while the engines' device images, offsets, filters,
+ * buffers and stream stay the same (the stream must not be the legacy default stream). */
+typedef struct jcde_multi jcde_multi;
+jcde_status jcde_multi_create(jcde_engine* const* engines, uint32_t n, jcde_multi** out);
+void jcde_multi_destroy(jcde_multi* m);
+jcde_status jcde_multi_detect(jcde_multi* m, const jcde_query* d_queries, const uint32_t* offsets,
+                              const jcde_filter* filters, uint8_t* d_verdicts, void* stream);
+jcde_status jcde_multi_detect_graph(jcde_multi* m, const jcde_query* d_queries, const uint32_t* offsets,
+                                    const jcde_filter* filters, uint8_t* d_verdicts, void* stream);
+uint64_t jcde_multi_kernel_launches(const jcde_multi* m);
+
 /* --- single queries with the reference's signatures (host buffers, synchronous) -------------- */
 /* detect_poly_collision (cd_engine.rs:160-197) of an already transformed shape with its poi. */
 jcde_status jcde_detect_poly(jcde_engine* e, const float* xy, uint32_t n_vertices, const float poi[3],

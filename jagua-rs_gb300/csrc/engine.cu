@@ -256,9 +256,9 @@ static void init_launch_shape(jcde_engine* e) {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&e->n_sms, cudaDevAttrMultiProcessorCount, dev);
     if (e->cfg.quadtree_depth <= 8)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&e->detect_blocks_per_sm, k_poly<uint32_t>, POLY_WARPS * 32, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&e->detect_blocks_per_sm, k_poly<uint32_t, false>, POLY_WARPS * 32, 0);
     else
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&e->detect_blocks_per_sm, k_poly<uint64_t>, POLY_WARPS * 32, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&e->detect_blocks_per_sm, k_poly<uint64_t, false>, POLY_WARPS * 32, 0);
     if (e->detect_blocks_per_sm < 1) e->detect_blocks_per_sm = 1;
     if (e->n_sms < 1) e->n_sms = 1;
 }
@@ -303,7 +303,7 @@ static void launch_passes_t(jcde_engine* e, const View& v, const uint32_t* q, ui
     if (mode & 1) {
         const uint32_t grid = (n + SURR_THREADS - 1) / SURR_THREADS;
         cudaEvent_t pa = prof_begin(e, s);
-        k_surrogate<PendT><<<grid, SURR_THREADS, 0, s>>>(v, q, n, dout, mode == 1 ? (uint8_t)0 : PENDING, order);
+        k_surrogate<PendT, false><<<grid, SURR_THREADS, 0, s>>>(v, MultiSrc{}, q, n, dout, mode == 1 ? (uint8_t)0 : PENDING, order);
         prof_end(e, s, pa, JCDE_PROF_SURROGATE);
         e->launches++;
     }
@@ -311,7 +311,7 @@ static void launch_passes_t(jcde_engine* e, const View& v, const uint32_t* q, ui
         const uint32_t want = (n + POLY_WARPS - 1) / POLY_WARPS;
         const uint32_t grid = std::min<uint32_t>(want, (uint32_t)(e->n_sms * e->detect_blocks_per_sm));
         cudaEvent_t pa = prof_begin(e, s);
-        k_poly<PendT><<<grid, POLY_WARPS * 32, 0, s>>>(v, q, n, dout, raw, mode == 3, order);
+        k_poly<PendT, false><<<grid, POLY_WARPS * 32, 0, s>>>(v, MultiSrc{}, q, n, dout, raw, mode == 3, order);
         prof_end(e, s, pa, JCDE_PROF_POLY);
         e->launches++;
     }
@@ -846,3 +846,184 @@ extern "C" jcde_status jcde_detect_batch_noalloc(jcde_engine* e, const jcde_quer
     e->have_last_stream = true;
     return JCDE_OK;
 }
+
+// ---------------------------------------------------------------------------------------------
+// Several layouts queried together (jcde_multi_*): one ordering + surrogate + polygon launch
+// sequence covers every engine's batch; each query reads the View of its own layout.
+// ---------------------------------------------------------------------------------------------
+struct jcde_multi {
+    std::vector<jcde_engine*> engines;
+    std::vector<View> views;          // views / offsets of the current call
+    std::vector<uint32_t> offs;
+    std::vector<View> up_views;       // what d_views / d_offs hold
+    std::vector<uint32_t> up_offs;
+    DevBuf d_views, d_offs, d_hist, d_order;
+    bool wide = false;                // a tree deeper than 8 levels needs 64-bit walk masks
+    int n_sms = 1, poly_blocks = 1;
+    // graph replay
+    cudaGraphExec_t exec = nullptr;
+    const void* g_q = nullptr;
+    void* g_out = nullptr;
+    cudaStream_t g_stream = nullptr;
+    std::vector<View> g_views;
+    std::vector<uint32_t> g_offs;
+    uint64_t launches = 0;
+    ~jcde_multi() {
+        if (exec) cudaGraphExecDestroy(exec);
+    }
+};
+
+// Bring every engine's device copy up to date, resolve its filter, and upload views + offsets.
+static jcde_status multi_prepare(jcde_multi* m, const uint32_t* offsets, const jcde_filter* filters, cudaStream_t s) {
+    const uint32_t L = (uint32_t)m->engines.size();
+    m->views.resize(L);
+    m->offs.assign(offsets, offsets + L + 1);
+    for (uint32_t l = 0; l < L; l++) {
+        if (m->offs[l + 1] < m->offs[l]) return JCDE_ERR_ARG;
+        jcde_engine* e = m->engines[l];
+        jcde_status st = sync_device(e);
+        if (st) return st;
+        init_launch_shape(e);
+        View v = base_view(e);
+        if ((st = apply_filter(e, filters ? &filters[l] : nullptr, s, v))) return st;
+        m->views[l] = v;
+    }
+    const uint32_t total = m->offs[L];
+    if (m->d_views.cap < L * sizeof(View) || m->d_offs.cap < (L + 1) * 4) {
+        CUDA_TRY(cudaStreamSynchronize(s));
+        if (!m->d_views.ensure(L * sizeof(View)) || !m->d_offs.ensure((L + 1) * 4)) return JCDE_ERR_CUDA;
+        m->up_views.clear();
+    }
+    if (m->d_hist.cap < (size_t)L * N_BUCKETS * 4 || m->d_order.cap < std::max<size_t>(total, 1) * 4) {
+        CUDA_TRY(cudaStreamSynchronize(s));   // growing frees buffers that queued launches may read
+        if (!m->d_hist.ensure((size_t)L * N_BUCKETS * 4) || !m->d_order.ensure(std::max<size_t>(total, 1) * 4))
+            return JCDE_ERR_CUDA;
+        m->up_views.clear();
+    }
+    // upload only what changed; the device copies are read by queued launches, so wait for them first
+    const bool same = m->up_offs == m->offs && m->up_views.size() == L &&
+                      std::memcmp(m->up_views.data(), m->views.data(), L * sizeof(View)) == 0;
+    if (!same) {
+        CUDA_TRY(cudaStreamSynchronize(s));
+        CUDA_TRY(cudaMemcpy(m->d_views.p, m->views.data(), L * sizeof(View), cudaMemcpyHostToDevice));
+        CUDA_TRY(cudaMemcpy(m->d_offs.p, m->offs.data(), (L + 1) * 4, cudaMemcpyHostToDevice));
+        m->up_views = m->views;
+        m->up_offs = m->offs;
+    }
+    return JCDE_OK;
+}
+
+template <typename PendT>
+static void multi_launch_t(jcde_multi* m, const uint32_t* q, uint8_t* out, cudaStream_t s) {
+    const uint32_t L = (uint32_t)m->engines.size(), n = m->offs[L];
+    const MultiSrc ms{m->d_views.as<View>(), m->d_offs.as<uint32_t>(), L};
+    uint32_t* hist = m->d_hist.as<uint32_t>();
+    uint32_t* order = m->d_order.as<uint32_t>();
+    const uint32_t grid = std::min<uint32_t>((n + 255) / 256, (uint32_t)m->n_sms * 8);
+    cudaMemsetAsync(hist, 0, (size_t)L * N_BUCKETS * 4, s);
+    k_mbucket_count<<<grid, 256, 0, s>>>(q, n, ms, hist);
+    k_scan_counts<<<1, 1024, 0, s>>>(hist, L * N_BUCKETS);
+    k_mbucket_scatter<<<grid, 256, 0, s>>>(q, n, ms, hist, order);
+    k_surrogate<PendT, true><<<(n + SURR_THREADS - 1) / SURR_THREADS, SURR_THREADS, 0, s>>>(View{}, ms, q, n, out,
+                                                                                          PENDING, order);
+    const uint32_t pgrid = std::min<uint32_t>((n + POLY_WARPS - 1) / POLY_WARPS, (uint32_t)(m->n_sms * m->poly_blocks));
+    k_poly<PendT, true><<<pgrid, POLY_WARPS * 32, 0, s>>>(View{}, ms, q, n, out, RawShape{nullptr, 0, 0, 0, 0}, true,
+                                                          order);
+    m->launches += 5;
+}
+static void multi_launch(jcde_multi* m, const uint32_t* q, uint8_t* out, cudaStream_t s) {
+    if (m->wide) multi_launch_t<uint64_t>(m, q, out, s);
+    else multi_launch_t<uint32_t>(m, q, out, s);
+}
+
+extern "C" {
+
+jcde_status jcde_multi_create(jcde_engine* const* engines, uint32_t n, jcde_multi** out) {
+    if (!engines || !n || !out) return JCDE_ERR_ARG;
+    jcde_multi* m = new (std::nothrow) jcde_multi();
+    if (!m) return JCDE_ERR_CUDA;
+    for (uint32_t l = 0; l < n; l++) {
+        if (!engines[l]) {
+            delete m;
+            return JCDE_ERR_ARG;
+        }
+        m->engines.push_back(engines[l]);
+        m->wide = m->wide || engines[l]->cfg.quadtree_depth > 8;
+    }
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&m->n_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (m->wide) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m->poly_blocks, k_poly<uint64_t, true>, POLY_WARPS * 32, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m->poly_blocks, k_poly<uint32_t, true>, POLY_WARPS * 32, 0);
+    if (m->n_sms < 1) m->n_sms = 1;
+    if (m->poly_blocks < 1) m->poly_blocks = 1;
+    *out = m;
+    return JCDE_OK;
+}
+
+void jcde_multi_destroy(jcde_multi* m) { delete m; }
+
+jcde_status jcde_multi_detect(jcde_multi* m, const jcde_query* dq, const uint32_t* offsets, const jcde_filter* filters,
+                              uint8_t* dout, void* stream) {
+    if (!m || !offsets) return JCDE_ERR_ARG;
+    const uint32_t total = offsets[m->engines.size()];
+    if (total && (!dq || !dout)) return JCDE_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    jcde_status st = multi_prepare(m, offsets, filters, s);
+    if (st) return st;
+    if (total == 0) return JCDE_OK;
+    multi_launch(m, reinterpret_cast<const uint32_t*>(dq), dout, s);
+    CUDA_TRY(cudaGetLastError());
+    for (jcde_engine* e : m->engines) {
+        e->last_stream = s;
+        e->have_last_stream = true;
+    }
+    return JCDE_OK;
+}
+
+jcde_status jcde_multi_detect_graph(jcde_multi* m, const jcde_query* dq, const uint32_t* offsets,
+                                    const jcde_filter* filters, uint8_t* dout, void* stream) {
+    if (!m || !offsets || !stream) return JCDE_ERR_ARG;
+    const uint32_t total = offsets[m->engines.size()];
+    if (total == 0) return JCDE_OK;
+    if (!dq || !dout) return JCDE_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    jcde_status st = multi_prepare(m, offsets, filters, s);
+    if (st) return st;
+    const bool same = m->exec && m->g_q == dq && m->g_out == dout && m->g_stream == s && m->g_offs == m->offs &&
+                      m->g_views.size() == m->views.size() &&
+                      std::memcmp(m->g_views.data(), m->views.data(), m->views.size() * sizeof(View)) == 0;
+    if (!same) {
+        if (m->exec) {
+            cudaGraphExecDestroy(m->exec);
+            m->exec = nullptr;
+        }
+        cudaGraph_t g = nullptr;
+        CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        multi_launch(m, reinterpret_cast<const uint32_t*>(dq), dout, s);
+        cudaError_t ce = cudaStreamEndCapture(s, &g);
+        if (ce != cudaSuccess || !g) return JCDE_ERR_CUDA;
+        ce = cudaGraphInstantiate(&m->exec, g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess) {
+            m->exec = nullptr;
+            return JCDE_ERR_CUDA;
+        }
+        m->g_q = dq;
+        m->g_out = dout;
+        m->g_stream = s;
+        m->g_views = m->views;
+        m->g_offs = m->offs;
+    }
+    CUDA_TRY(cudaGraphLaunch(m->exec, s));
+    m->launches += 5;
+    for (jcde_engine* e : m->engines) {
+        e->last_stream = s;
+        e->have_last_stream = true;
+    }
+    return JCDE_OK;
+}
+
+uint64_t jcde_multi_kernel_launches(const jcde_multi* m) { return m ? m->launches : 0; }
+
+}  // extern "C"

@@ -338,36 +338,59 @@ constexpr uint8_t PENDING = 0xFFu;   // verdict slot of a query the surrogate pa
 // query: the fail-fast poles, then the piers, each walked down from the root in the reference's
 // order, stopping at the first hit.  A hit writes JCDE_COLLIDES; a miss writes `miss` (JCDE_FREE
 // for a surrogate-only batch, PENDING when the polygon pass follows).
+// Views of one or several layouts: a kernel reads the View of the layout a query belongs to.
+struct MultiSrc {
+    const View* __restrict__ views;     // one per layout
+    const uint32_t* __restrict__ offs;  // layout l owns queries [offs[l], offs[l+1])
+    uint32_t n_layouts;
+    __device__ __forceinline__ uint32_t layout_of(uint32_t qi) const {
+        uint32_t lo = 0, hi = n_layouts - 1;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi + 1) >> 1;
+            if (__ldg(&offs[mid]) <= qi) lo = mid;
+            else hi = mid - 1;
+        }
+        return lo;
+    }
+};
+
 template <typename PendT>
-__global__ void __launch_bounds__(SURR_THREADS) k_surrogate(View v, const uint32_t* __restrict__ q, uint32_t n,
-                                                            uint8_t* __restrict__ out, uint8_t miss,
+__device__ __forceinline__ void surrogate_query(const View& v, const uint32_t* __restrict__ q, uint32_t qi,
+                                                uint8_t* __restrict__ out, uint8_t miss) {
+    const uint32_t* w5 = q + (size_t)qi * 5;
+    const uint32_t item = __ldg(&w5[0]);
+    const float c = __uint_as_float(__ldg(&w5[1])), s = __uint_as_float(__ldg(&w5[2]));
+    const float tx = __uint_as_float(__ldg(&w5[3])), ty = __uint_as_float(__ldg(&w5[4]));
+    if (item >= v.n_items) {
+        out[qi] = 2;
+        return;
+    }
+    const DItem it = v.items[item];
+    bool hit = false;
+    for (uint32_t p = 0; p < it.n_ff_poles && !hit; p++) {
+        const float4 pl = __ldg(&v.poles[it.pole_off + p]);
+        const Disk d{xform(Pt{pl.x, pl.y}, c, s, tx, ty), pl.z};
+        WalkT<PendT> w{0, 0, 0, (PendT)0};
+        while (w.node >= 0 && !hit) hit = walk_step(v, d, w, nullptr);
+    }
+    for (uint32_t p = 0; p < it.n_piers && !hit; p++) {
+        const float4 pr = __ldg(&v.piers[it.pier_off + p]);
+        const Seg sg{xform(Pt{pr.x, pr.y}, c, s, tx, ty), xform(Pt{pr.z, pr.w}, c, s, tx, ty)};
+        WalkT<PendT> w{0, 0, 0, (PendT)0};
+        while (w.node >= 0 && !hit) hit = walk_step(v, sg, w, nullptr);
+    }
+    out[qi] = hit ? (uint8_t)1 : miss;
+}
+
+template <typename PendT, bool MULTI>
+__global__ void __launch_bounds__(SURR_THREADS) k_surrogate(View v, MultiSrc ms, const uint32_t* __restrict__ q,
+                                                            uint32_t n, uint8_t* __restrict__ out, uint8_t miss,
                                                             const uint32_t* __restrict__ order) {
     const uint32_t stride = gridDim.x * SURR_THREADS;
     for (uint32_t i = blockIdx.x * SURR_THREADS + threadIdx.x; i < n; i += stride) {
         const uint32_t qi = order ? __ldg(&order[i]) : i;
-        const uint32_t* w5 = q + (size_t)qi * 5;
-        const uint32_t item = __ldg(&w5[0]);
-        const float c = __uint_as_float(__ldg(&w5[1])), s = __uint_as_float(__ldg(&w5[2]));
-        const float tx = __uint_as_float(__ldg(&w5[3])), ty = __uint_as_float(__ldg(&w5[4]));
-        if (item >= v.n_items) {
-            out[qi] = 2;
-            continue;
-        }
-        const DItem it = v.items[item];
-        bool hit = false;
-        for (uint32_t p = 0; p < it.n_ff_poles && !hit; p++) {
-            const float4 pl = __ldg(&v.poles[it.pole_off + p]);
-            const Disk d{xform(Pt{pl.x, pl.y}, c, s, tx, ty), pl.z};
-            WalkT<PendT> w{0, 0, 0, (PendT)0};
-            while (w.node >= 0 && !hit) hit = walk_step(v, d, w, nullptr);
-        }
-        for (uint32_t p = 0; p < it.n_piers && !hit; p++) {
-            const float4 pr = __ldg(&v.piers[it.pier_off + p]);
-            const Seg sg{xform(Pt{pr.x, pr.y}, c, s, tx, ty), xform(Pt{pr.z, pr.w}, c, s, tx, ty)};
-            WalkT<PendT> w{0, 0, 0, (PendT)0};
-            while (w.node >= 0 && !hit) hit = walk_step(v, sg, w, nullptr);
-        }
-        out[qi] = hit ? (uint8_t)1 : miss;
+        if constexpr (MULTI) surrogate_query<PendT>(ms.views[ms.layout_of(qi)], q, qi, out, miss);
+        else surrogate_query<PendT>(v, q, qi, out, miss);
     }
 }
 
@@ -379,9 +402,165 @@ __global__ void __launch_bounds__(SURR_THREADS) k_surrogate(View v, const uint32
 #endif
 constexpr uint32_t POLY_MAXV = 256;   // items with more vertices transform edges on the fly
 template <typename PendT>
+__device__ __forceinline__ void poly_query(const View& v, const uint32_t* __restrict__ q, uint32_t qi,
+                                           uint8_t* __restrict__ out, const RawShape& raw, volatile int* stop,
+                                           float2* tv, uint32_t* jobsw, int lane) {
+    QShape sh;
+    Pt spoi;
+    if (raw.verts) {
+        sh = QShape{raw.verts, raw.nv, 1.0f, 0.0f, 0.0f, 0.0f, true};
+        spoi = Pt{raw.poi_x, raw.poi_y};
+    } else {
+        QueryHead qh = load_query(q, qi, lane);
+        if (qh.item >= v.n_items) {
+            if (lane == 0) out[qi] = 2;
+            return;
+        }
+        const DItem it = v.items[qh.item];
+        sh = QShape{v.iverts + it.v_off, it.v_cnt, qh.c, qh.s, qh.tx, qh.ty, false};
+        spoi = xform(Pt{it.poi_x, it.poi_y}, qh.c, qh.s, qh.tx, qh.ty);
+    }
+    if (lane == 0) *stop = 0;
+    // the transformed vertices are kept in shared memory (items up to POLY_MAXV vertices)
+    const bool cached = sh.nv <= POLY_MAXV;
+    Box sb;
+    {
+        float x0 = FLT_MAX, y0 = FLT_MAX, x1 = -FLT_MAX, y1 = -FLT_MAX;
+        for (uint32_t k = lane; k < sh.nv; k += 32) {
+            const Pt p = sh.vtx(k);
+            if (cached) tv[k] = make_float2(p.x, p.y);
+            x0 = fminf(x0, p.x);
+            y0 = fminf(y0, p.y);
+            x1 = fmaxf(x1, p.x);
+            y1 = fmaxf(y1, p.y);
+        }
+        JCDE_UNROLL
+        for (int o = 16; o; o >>= 1) {
+            x0 = fminf(x0, __shfl_xor_sync(FULL, x0, o));
+            y0 = fminf(y0, __shfl_xor_sync(FULL, y0, o));
+            x1 = fmaxf(x1, __shfl_xor_sync(FULL, x1, o));
+            y1 = fmaxf(y1, __shfl_xor_sync(FULL, y1, o));
+        }
+        sb = Box{x0, y0, x1, y1};   // SPolygon::generate_bounding_box (simple_polygon.rs:122-133)
+    }
+    __syncwarp();
+    auto edge_of = [&](uint32_t k) -> Seg {
+        if (!cached) return sh.edge(k);
+        const float2 a = tv[k], b = tv[k + 1 == sh.nv ? 0 : k + 1];
+        return Seg{Pt{a.x, a.y}, Pt{b.x, b.y}};
+    };
+    // a shape not surrounded by the CDE box collides (cd_engine.rs:161-163)
+    bool hit = !box_surrounds(v.cde, sb);
+    const int vr = hit ? 0 : virtual_root(v, sb);
+    const uint32_t lt = (1u << lane) - 1u;
+    // Every edge's walk starts with a visit of the virtual root.  When the root of the walk is a
+    // Partial internal node, that first visit is done here for all edges at once (uniform work,
+    // 32 edges per round): edges whose quadrant mask is empty are dropped and the others are
+    // listed with their mask, so the walks below start one level down.
+    uint32_t n_jobs = sh.nv;   // without the list, job k is edge k starting at the virtual root
+    bool listed = false;
+    int vr_child = -1;
+    if (!hit) {
+        const uint32_t st = __ldg(&v.strength[vr]);
+        if (st == PRES_ENTIRE) {
+            hit = true;
+        } else if (st == PRES_NONE) {
+            n_jobs = 0;   // nothing to hit below; containment still runs
+        } else {
+            const DNode vn = ld_node(v, vr);
+            if (vn.child >= 0 && cached) {
+                listed = true;
+                vr_child = vn.child;
+                uint32_t cnt = 0;
+                for (uint32_t base = 0; base < sh.nv; base += 32) {
+                    const uint32_t k = base + lane;
+                    const uint32_t m = k < sh.nv ? seg_quadrant_mask(edge_of(k), vn.box) : 0u;
+                    const uint32_t bal = __ballot_sync(FULL, m != 0);
+                    if (m) jobsw[cnt + __popc(bal & lt)] = k | (m << 16);
+                    cnt += __popc(bal);
+                }
+                n_jobs = cnt;
+                __syncwarp();
+            }
+        }
+    }
+    // Jobs are handed out dynamically: a lane whose walk is over takes the next unassigned job
+    // (ballot rank), so no lane waits for the slowest walk of a fixed round.  Every loop
+    // iteration is one node visit per active lane; a hit anywhere ends the query.
+    uint32_t next = 0;
+    WalkT<PendT> w{-1, 0, 0, (PendT)0};
+    Seg e{};
+    while (!hit) {
+        const bool want = w.node == -1;
+        const uint32_t need = __ballot_sync(FULL, want);
+        if (want) {
+            const uint32_t p = next + __popc(need & lt);
+            if (p < n_jobs) {
+                if (listed) {
+                    const uint32_t job = jobsw[p];
+                    e = edge_of(job & 0xFFFFu);
+                    w = WalkT<PendT>{-1, 1, vr_child, (PendT)(job >> 16)};
+                    w.node = walk_next(v, w);
+                } else {
+                    e = edge_of(p);
+                    w = WalkT<PendT>{vr, 0, 0, (PendT)0};
+                }
+            } else {
+                w.node = -2;
+            }
+        }
+        next += __popc(need);
+        const bool active = w.node >= 0;
+        if (!__any_sync(FULL, active)) break;
+        bool h = false;
+        if (active) {
+            h = walk_step(v, e, w, stop);
+            if (!h && w.node < 0) w.node = -1;
+        }
+        hit = __any_sync(FULL, h);
+    }
+    if (!hit) {
+        // containment of the shape in (or of) the partially present hazards of the virtual root
+        DNode vn = ld_node(v, vr);
+        for (uint32_t base = 0; !hit && base < vn.hz_cnt; base += 32) {
+            const uint32_t k = base + lane;
+            int need = 0;
+            bool res = false;
+            uint32_t hk = 0;
+            if (k < vn.hz_cnt) {
+                DEntry en = ld_entry(v, vn.hz_off + k);
+                // an Entire entry here is an ignored one (qt_node.rs:104), and is skipped
+                if (en.presence == PRES_PARTIAL && !filtered(v, en.hkey)) {
+                    hk = en.hkey;
+                    const float4* hp = reinterpret_cast<const float4*>(v.haz + hk);
+                    float4 a = __ldg(hp), b = __ldg(hp + 1);
+                    int rel = box_almost_relation(Box{a.x, a.y, a.z, a.w}, sb);
+                    if (rel == REL_SURROUNDING) need = 1;
+                    else if (rel == REL_ENCLOSED) need = 2;
+                    else res = (__float_as_uint(b.w) >> 31) != 0;   // not contained: exterior scope collides
+                }
+            }
+            if (__any_sync(FULL, res)) {
+                hit = true;
+                break;
+            }
+            uint32_t todo = __ballot_sync(FULL, need != 0);
+            while (todo && !hit) {
+                const int src = __ffs(todo) - 1;
+                todo &= todo - 1;
+                const int nd = __shfl_sync(FULL, need, src);
+                const uint32_t hkk = __shfl_sync(FULL, hk, src);
+                hit = warp_containment(v, sh, sb, spoi, hkk, nd, lane);
+            }
+        }
+    }
+    if (lane == 0) out[qi] = hit ? 1 : 0;
+}
+
+template <typename PendT, bool MULTI>
 __global__ void __launch_bounds__(POLY_WARPS * 32, JCDE_POLY_MIN_BLOCKS)
-    k_poly(View v, const uint32_t* __restrict__ q, uint32_t n, uint8_t* __restrict__ out, RawShape raw,
-           bool only_pending, const uint32_t* __restrict__ order) {
+    k_poly(View v, MultiSrc ms, const uint32_t* __restrict__ q, uint32_t n, uint8_t* __restrict__ out,
+           RawShape raw, bool only_pending, const uint32_t* __restrict__ order) {
     __shared__ int stops[POLY_WARPS];
     __shared__ float2 tverts[POLY_WARPS][POLY_MAXV];   // transformed item vertices
     __shared__ uint32_t jobs[POLY_WARPS][POLY_MAXV];   // edge index | children mask below the virtual root << 16
@@ -391,157 +570,10 @@ __global__ void __launch_bounds__(POLY_WARPS * 32, JCDE_POLY_MIN_BLOCKS)
     for (uint32_t i = blockIdx.x * POLY_WARPS + warp; i < n; i += stride) {
         const uint32_t qi = order ? __ldg(&order[i]) : i;
         if (only_pending && out[qi] != PENDING) continue;
-        QShape sh;
-        Pt spoi;
-        if (raw.verts) {
-            sh = QShape{raw.verts, raw.nv, 1.0f, 0.0f, 0.0f, 0.0f, true};
-            spoi = Pt{raw.poi_x, raw.poi_y};
-        } else {
-            QueryHead qh = load_query(q, qi, lane);
-            if (qh.item >= v.n_items) {
-                if (lane == 0) out[qi] = 2;
-                continue;
-            }
-            const DItem it = v.items[qh.item];
-            sh = QShape{v.iverts + it.v_off, it.v_cnt, qh.c, qh.s, qh.tx, qh.ty, false};
-            spoi = xform(Pt{it.poi_x, it.poi_y}, qh.c, qh.s, qh.tx, qh.ty);
-        }
-        if (lane == 0) *stop = 0;
-        // the transformed vertices are kept in shared memory (items up to POLY_MAXV vertices)
-        const bool cached = sh.nv <= POLY_MAXV;
-        float2* tv = tverts[warp];
-        Box sb;
-        {
-            float x0 = FLT_MAX, y0 = FLT_MAX, x1 = -FLT_MAX, y1 = -FLT_MAX;
-            for (uint32_t k = lane; k < sh.nv; k += 32) {
-                const Pt p = sh.vtx(k);
-                if (cached) tv[k] = make_float2(p.x, p.y);
-                x0 = fminf(x0, p.x);
-                y0 = fminf(y0, p.y);
-                x1 = fmaxf(x1, p.x);
-                y1 = fmaxf(y1, p.y);
-            }
-            JCDE_UNROLL
-            for (int o = 16; o; o >>= 1) {
-                x0 = fminf(x0, __shfl_xor_sync(FULL, x0, o));
-                y0 = fminf(y0, __shfl_xor_sync(FULL, y0, o));
-                x1 = fmaxf(x1, __shfl_xor_sync(FULL, x1, o));
-                y1 = fmaxf(y1, __shfl_xor_sync(FULL, y1, o));
-            }
-            sb = Box{x0, y0, x1, y1};   // SPolygon::generate_bounding_box (simple_polygon.rs:122-133)
-        }
-        __syncwarp();
-        auto edge_of = [&](uint32_t k) -> Seg {
-            if (!cached) return sh.edge(k);
-            const float2 a = tv[k], b = tv[k + 1 == sh.nv ? 0 : k + 1];
-            return Seg{Pt{a.x, a.y}, Pt{b.x, b.y}};
-        };
-        // a shape not surrounded by the CDE box collides (cd_engine.rs:161-163)
-        bool hit = !box_surrounds(v.cde, sb);
-        const int vr = hit ? 0 : virtual_root(v, sb);
-        const uint32_t lt = (1u << lane) - 1u;
-        // Every edge's walk starts with a visit of the virtual root.  When the root of the walk is a
-        // Partial internal node, that first visit is done here for all edges at once (uniform work,
-        // 32 edges per round): edges whose quadrant mask is empty are dropped and the others are
-        // listed with their mask, so the walks below start one level down.
-        uint32_t n_jobs = sh.nv;   // without the list, job k is edge k starting at the virtual root
-        bool listed = false;
-        int vr_child = -1;
-        if (!hit) {
-            const uint32_t st = __ldg(&v.strength[vr]);
-            if (st == PRES_ENTIRE) {
-                hit = true;
-            } else if (st == PRES_NONE) {
-                n_jobs = 0;   // nothing to hit below; containment still runs
-            } else {
-                const DNode vn = ld_node(v, vr);
-                if (vn.child >= 0 && cached) {
-                    listed = true;
-                    vr_child = vn.child;
-                    uint32_t cnt = 0;
-                    for (uint32_t base = 0; base < sh.nv; base += 32) {
-                        const uint32_t k = base + lane;
-                        const uint32_t m = k < sh.nv ? seg_quadrant_mask(edge_of(k), vn.box) : 0u;
-                        const uint32_t bal = __ballot_sync(FULL, m != 0);
-                        if (m) jobs[warp][cnt + __popc(bal & lt)] = k | (m << 16);
-                        cnt += __popc(bal);
-                    }
-                    n_jobs = cnt;
-                    __syncwarp();
-                }
-            }
-        }
-        // Jobs are handed out dynamically: a lane whose walk is over takes the next unassigned job
-        // (ballot rank), so no lane waits for the slowest walk of a fixed round.  Every loop
-        // iteration is one node visit per active lane; a hit anywhere ends the query.
-        uint32_t next = 0;
-        WalkT<PendT> w{-1, 0, 0, (PendT)0};
-        Seg e{};
-        while (!hit) {
-            const bool want = w.node == -1;
-            const uint32_t need = __ballot_sync(FULL, want);
-            if (want) {
-                const uint32_t p = next + __popc(need & lt);
-                if (p < n_jobs) {
-                    if (listed) {
-                        const uint32_t job = jobs[warp][p];
-                        e = edge_of(job & 0xFFFFu);
-                        w = WalkT<PendT>{-1, 1, vr_child, (PendT)(job >> 16)};
-                        w.node = walk_next(v, w);
-                    } else {
-                        e = edge_of(p);
-                        w = WalkT<PendT>{vr, 0, 0, (PendT)0};
-                    }
-                } else {
-                    w.node = -2;
-                }
-            }
-            next += __popc(need);
-            const bool active = w.node >= 0;
-            if (!__any_sync(FULL, active)) break;
-            bool h = false;
-            if (active) {
-                h = walk_step(v, e, w, stop);
-                if (!h && w.node < 0) w.node = -1;
-            }
-            hit = __any_sync(FULL, h);
-        }
-        if (!hit) {
-            // containment of the shape in (or of) the partially present hazards of the virtual root
-            DNode vn = ld_node(v, vr);
-            for (uint32_t base = 0; !hit && base < vn.hz_cnt; base += 32) {
-                const uint32_t k = base + lane;
-                int need = 0;
-                bool res = false;
-                uint32_t hk = 0;
-                if (k < vn.hz_cnt) {
-                    DEntry en = ld_entry(v, vn.hz_off + k);
-                    // an Entire entry here is an ignored one (qt_node.rs:104), and is skipped
-                    if (en.presence == PRES_PARTIAL && !filtered(v, en.hkey)) {
-                        hk = en.hkey;
-                        const float4* hp = reinterpret_cast<const float4*>(v.haz + hk);
-                        float4 a = __ldg(hp), b = __ldg(hp + 1);
-                        int rel = box_almost_relation(Box{a.x, a.y, a.z, a.w}, sb);
-                        if (rel == REL_SURROUNDING) need = 1;
-                        else if (rel == REL_ENCLOSED) need = 2;
-                        else res = (__float_as_uint(b.w) >> 31) != 0;   // not contained: exterior scope collides
-                    }
-                }
-                if (__any_sync(FULL, res)) {
-                    hit = true;
-                    break;
-                }
-                uint32_t todo = __ballot_sync(FULL, need != 0);
-                while (todo && !hit) {
-                    const int src = __ffs(todo) - 1;
-                    todo &= todo - 1;
-                    const int nd = __shfl_sync(FULL, need, src);
-                    const uint32_t hkk = __shfl_sync(FULL, hk, src);
-                    hit = warp_containment(v, sh, sb, spoi, hkk, nd, lane);
-                }
-            }
-        }
-        if (lane == 0) out[qi] = hit ? 1 : 0;
+        if constexpr (MULTI)
+            poly_query<PendT>(ms.views[ms.layout_of(qi)], q, qi, out, raw, stop, tverts[warp], jobs[warp], lane);
+        else
+            poly_query<PendT>(v, q, qi, out, raw, stop, tverts[warp], jobs[warp], lane);
     }
 }
 
@@ -729,6 +761,53 @@ __global__ void k_bucket_scatter(const uint32_t* __restrict__ q, uint32_t n, Box
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
         order[atomicAdd(&offs[bucket_of(q, i, b)], 1u)] = i;
+}
+
+// Several layouts in one batch: the bucket key is (layout, Morton cell of the layout's CDE box).
+__global__ void k_mbucket_count(const uint32_t* __restrict__ q, uint32_t n, MultiSrc ms, uint32_t* __restrict__ hist) {
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const uint32_t l = ms.layout_of(i);
+        atomicAdd(&hist[l * N_BUCKETS + bucket_of(q, i, ms.views[l].cde)], 1u);
+    }
+}
+__global__ void k_mbucket_scatter(const uint32_t* __restrict__ q, uint32_t n, MultiSrc ms, uint32_t* __restrict__ offs,
+                                  uint32_t* __restrict__ order) {
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const uint32_t l = ms.layout_of(i);
+        order[atomicAdd(&offs[l * N_BUCKETS + bucket_of(q, i, ms.views[l].cde)], 1u)] = i;
+    }
+}
+// exclusive scan of `total` counts in place, one block of 1024 threads, a contiguous run per thread
+__global__ void __launch_bounds__(1024) k_scan_counts(uint32_t* __restrict__ c, uint32_t total) {
+    __shared__ uint32_t warp_sums[32];
+    const uint32_t t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const uint32_t per = (total + 1023) / 1024, a = min(total, t * per), b = min(total, a + per);
+    uint32_t s = 0;
+    for (uint32_t k = a; k < b; k++) s += c[k];
+    uint32_t incl = s;
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(FULL, incl, o);
+        if (lane >= (uint32_t)o) incl += y;
+    }
+    if (lane == 31) warp_sums[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = warp_sums[lane], wi = w;
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(FULL, wi, o);
+            if (lane >= (uint32_t)o) wi += y;
+        }
+        warp_sums[lane] = wi - w;
+    }
+    __syncthreads();
+    uint32_t run = warp_sums[warp] + incl - s;
+    for (uint32_t k = a; k < b; k++) {
+        const uint32_t v = c[k];
+        c[k] = run;
+        run += v;
+    }
 }
 
 // Strongest presence per node under a filter (QTHazardVec::strongest, qt_hazard_vec.rs:60-63).

@@ -5,7 +5,7 @@ GPU memory and detect / collect queries run as hand-written sm_103a kernels behi
 ``include/jcde.h``.  This package is the Python host side over that ABI.
 """
 from ._ffi import JcdeError, build, lib
-from .engine import CDEConfig, CDEngine, GpuBackend, GpuEngine, Hazard, spolygon_new, surrogate_poles
+from .engine import CDEConfig, CDEngine, GpuBackend, GpuEngine, Hazard, MultiEngine, spolygon_new, surrogate_poles
 from .workload import QUERY_DTYPE
 
 __all__ = [
@@ -14,6 +14,7 @@ __all__ = [
     "GpuBackend",
     "GpuEngine",
     "Hazard",
+    "MultiEngine",
     "JcdeError",
     "QUERY_DTYPE",
     "build",

@@ -86,6 +86,11 @@ SIGNATURES = {
     "jcde_device_stats": (C.c_int32, [P, u64p]),
     "jcde_kernel_launches": (C.c_uint64, [P]),
     "jcde_profile_enable": (C.c_int32, [P, C.c_int]),
+    "jcde_multi_create": (C.c_int32, [C.POINTER(P), C.c_uint32, C.POINTER(P)]),
+    "jcde_multi_destroy": (None, [P]),
+    "jcde_multi_detect": (C.c_int32, [P, P, u32p, C.POINTER(jcde_filter), P, P]),
+    "jcde_multi_detect_graph": (C.c_int32, [P, P, u32p, C.POINTER(jcde_filter), P, P]),
+    "jcde_multi_kernel_launches": (C.c_uint64, [P]),
     "jcde_profile_read": (C.c_int32, [P, C.POINTER(C.c_double), u64p, C.c_int]),
 }
 

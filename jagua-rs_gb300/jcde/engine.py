@@ -369,3 +369,48 @@ class GpuBackend:
     @staticmethod
     def new_engine(depth: int, cd_threshold: int, bbox):
         return GpuEngine(depth, cd_threshold, bbox)
+
+
+class MultiEngine:
+    """Several engines (layouts) answered by one launch sequence (jcde_multi_*)."""
+
+    def __init__(self, engines):
+        self.engines = list(engines)   # keep the engines alive as long as the group
+        arr = (C.c_void_p * len(self.engines))(*[e.h.value if hasattr(e.h, "value") else e.h for e in self.engines])
+        h = C.c_void_p()
+        check(lib().jcde_multi_create(arr, len(self.engines), C.byref(h)), "jcde_multi_create")
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            try:
+                lib().jcde_multi_destroy(self.h)
+            except Exception:
+                pass
+            self.h = None
+
+    def _filters(self, filters):
+        if filters is None:
+            return None, []
+        fs = [_Filter(f) for f in filters]
+        arr = (jcde_filter * len(fs))(*[f.c for f in fs])
+        return arr, fs
+
+    def detect(self, queries, offsets, filters=None, out=None, stream=None, graph: bool = False):
+        """Verdicts of all layouts' queries; `queries` is a CUDA uint8 tensor of packed queries with
+        layout l's at [offsets[l], offsets[l+1])."""
+        import torch
+
+        offs = np.ascontiguousarray(offsets, dtype=np.uint32)
+        n = int(offs[-1])
+        if out is None:
+            out = torch.empty(n, dtype=torch.uint8, device=queries.device)
+        farr, keep = self._filters(filters)
+        fn = lib().jcde_multi_detect_graph if graph else lib().jcde_multi_detect
+        sh = _stream_handle(stream)
+        check(fn(self.h, queries.data_ptr(), offs.ctypes.data_as(C.POINTER(C.c_uint32)), farr, out.data_ptr(), sh),
+              "multi_detect")
+        return out
+
+    def kernel_launches(self) -> int:
+        return int(lib().jcde_multi_kernel_launches(self.h))

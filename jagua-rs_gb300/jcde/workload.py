@@ -359,3 +359,42 @@ def star_container_layout(backend, seed=0xC1, n_types=40, v_range=(8, 200), r_ra
 
 def queries_for(lay: Layout, n: int, seed: int, sid: int = 3) -> np.ndarray:
     return make_queries(Stream(seed, sid), n, len(lay.items), lay.cde_bbox)
+
+
+def multi_layouts(backend, seed=0xC2, n_layouts=64, n_types=40, v_range=(8, 200), r_range=(20.0, 60.0),
+                  items_range=(20, 400), container_v=(32, 128), radius_per_sqrt_item=70.0, depth=DEFAULT_DEPTH,
+                  cd_threshold=DEFAULT_CD_THRESHOLD, chunk=256, max_attempts=1 << 14, item_pool=None):
+    """Independent bin layouts (the batched multi-layout workload): star containers of 32-128
+    vertices, each holding a log-uniform 20-400 items drawn from one shared pool of star item types
+    (8-200 vertices).  Returns [(layout, engine)]."""
+    st = Stream(seed, 1)
+    if item_pool is None:
+        item_pool = []
+        for _ in range(n_types):
+            nv = int(st.randint(v_range[0], v_range[1], 1)[0])
+            item_pool.append(import_item(backend, star_polygon(st, nv, *r_range)))
+    sl = Stream(seed, 2)
+    out = []
+    for l in range(n_layouts):
+        n_items = int(round(math.exp(math.log(items_range[0]) + sl.f64(1)[0] *
+                                     (math.log(items_range[1]) - math.log(items_range[0])))))
+        nv = int(sl.randint(container_v[0], container_v[1], 1)[0])
+        R = radius_per_sqrt_item * math.sqrt(n_items)
+        outer = import_static(backend, star_polygon(sl, nv, R, R), EXTERIOR)
+        lay = Layout(f"bin{l}", depth, cd_threshold, inflate_to_square(bbox_of(outer.xy)), items=item_pool)
+        lay.hazards.append(outer)
+        eng = _new_layout_engine(backend, lay)
+        _place_items(backend, lay, eng, seed * 1000 + l, n_items, chunk, max_attempts)
+        out.append((lay, eng))
+    return out
+
+
+def multi_queries(layouts, seed=0xC2, q_range=(4096, 262144)):
+    """Per-layout uniform query batches with log-uniform sizes; returns (queries, offsets)."""
+    sq = Stream(seed, 3)
+    parts, offs = [], [0]
+    for l, (lay, _) in enumerate(layouts):
+        n = int(round(math.exp(math.log(q_range[0]) + sq.f64(1)[0] * (math.log(q_range[1]) - math.log(q_range[0])))))
+        parts.append(make_queries(Stream(seed, 100 + l), n, len(lay.items), lay.cde_bbox))
+        offs.append(offs[-1] + n)
+    return np.concatenate(parts), np.array(offs, dtype=np.uint32)
