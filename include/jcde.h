@@ -192,6 +192,33 @@ jcde_status jcde_collect_poly(jcde_engine* e, const float* xy, uint32_t n_vertic
 jcde_status jcde_collect_surrogate(jcde_engine* e, uint32_t item, const float transform[4],
                                    const jcde_filter* filter, uint32_t* keys, uint32_t cap, uint32_t* n_out);
 
+/* --- differentiable pole-overlap proxy (no counterpart in the reference) -------------------- */
+/* For a candidate (theta, tx, ty) of an item with surrogate poles p_i (all of them, poles[0] = poi;
+ * fail_fast/sp_surrogate.rs:19) placed at c_i = R(theta) p_i + t, and the poles (c_j, r_j) given to the
+ * hazards with jcde_set_hazard_poles (a placed item's are its item's poles under its placement,
+ * as SPolygon::transform moves the surrogate, simple_polygon.rs:214-216):
+ *     P = sum_ij max(0, r_i + r_j - |c_i - c_j|)^2,   grad = dP/d(theta, tx, ty)
+ * in float32.  Hazards ignored by the filter contribute nothing.  Params are 3 floats per candidate
+ * (theta, tx, ty); grad is 3 floats per candidate in the same order. */
+jcde_status jcde_set_hazard_poles(jcde_engine* e, uint32_t key, const float* poles_xyr, uint32_t n);
+jcde_status jcde_proxy_batch(jcde_engine* e, const float* d_params, const uint32_t* d_items, uint32_t n,
+                             const jcde_filter* filter, float* d_value, float* d_grad, void* stream);
+/* `steps` descent steps per candidate on P: a step tries t - eta*step_t*dP/dt and
+ * theta - eta*step_th/max|p_i|^2*dP/dtheta, keeps it if P drops (eta x1.5, at most 4) and halves eta
+ * otherwise (eta starts at 1), stopping once P = 0.  `clearance` grows every hazard pole's radius
+ * during the descent (poles under-cover a shape, so separating them by a clearance frees more
+ * placements; 0 descends on P itself).  Params are updated in place, d_queries receives
+ * the final placements as query records (cos, sin of the final theta) ready for jcde_detect_batch,
+ * d_value the final P. */
+jcde_status jcde_separate_batch(jcde_engine* e, float* d_params, const uint32_t* d_items, uint32_t n,
+                                uint32_t steps, float step_t, float step_th, float clearance,
+                                const jcde_filter* filter, jcde_query* d_queries, float* d_value, void* stream);
+/* Random-resampling baseline: k Gaussian perturbations (sigma_t in translation, sigma_th in
+ * rotation) of each candidate, as query records d_queries[i * k + j]. */
+jcde_status jcde_resample_batch(jcde_engine* e, const float* d_params, const uint32_t* d_items, uint32_t n,
+                                uint32_t k, float sigma_t, float sigma_th, uint32_t seed, jcde_query* d_queries,
+                                void* stream);
+
 /* --- snapshots: CDEngine::save / restore (cd_engine.rs:98-149) ------------------------------- */
 jcde_status jcde_save(const jcde_engine* e, jcde_snapshot** out);
 jcde_status jcde_restore(jcde_engine* e, const jcde_snapshot* s);
@@ -221,7 +248,8 @@ uint64_t jcde_kernel_launches(const jcde_engine* e);
 #define JCDE_PROF_COLLECT 2     /* collect kernel */
 #define JCDE_PROF_ORDER 3       /* spatial ordering of a batch (3 small kernels) */
 #define JCDE_PROF_FILTER 4      /* per-node presence under a new filter */
-#define JCDE_PROF_KINDS 5
+#define JCDE_PROF_PROXY 5       /* gradient-descent separation on the pole-overlap proxy */
+#define JCDE_PROF_KINDS 6
 jcde_status jcde_profile_enable(jcde_engine* e, int enable);
 jcde_status jcde_profile_read(jcde_engine* e, double* ms, uint64_t* count, int reset);
 

@@ -76,6 +76,12 @@ struct jcde_engine {
     // staging for host entry points and single queries
     DevBuf d_q, d_out, d_raw, d_coll;
     DevBuf d_hist, d_order;   // spatial ordering of a query batch
+    // hazard poles binned in a uniform grid (overlap proxy)
+    uint64_t pole_version = ~0ull;
+    DevBuf d_hpoles, d_hpstart;
+    float hp_x0 = 0, hp_y0 = 0, hp_inv_cs = 0, hp_rmax = 0;
+    int32_t hp_g = 1;
+    uint32_t n_hpoles = 0;
     cudaStream_t last_stream = nullptr;
     bool have_last_stream = false;
     cudaStream_t own[2] = {nullptr, nullptr};
@@ -141,7 +147,8 @@ static jcde_status upload(DevBuf& b, const void* src, size_t bytes) {
 
 // Bring the device mirror up to date with the host quadtree and item table.
 static jcde_status sync_device(jcde_engine* e) {
-    if (e->tree_version == e->tree.version() && !e->items_dirty) return JCDE_OK;
+    if (e->tree_version == e->tree.version() && !e->items_dirty && e->pole_version == e->tree.pole_version())
+        return JCDE_OK;
     // queries already queued on the caller's stream may still read the old image
     if (e->have_last_stream) CUDA_TRY(cudaStreamSynchronize(e->last_stream));
     if (e->tree_version != e->tree.version()) {
@@ -170,6 +177,61 @@ static jcde_status sync_device(jcde_engine* e) {
         if ((st = upload(e->d_hverts, e->hverts.data(), e->hverts.size() * sizeof(float2)))) return st;
         e->n_nodes = (uint32_t)e->flat.nodes.size();
         e->tree_version = e->tree.version();
+    }
+    if (e->pole_version != e->tree.pole_version()) {
+        // bin every live hazard pole into each grid cell its bounding box overlaps; a pair of poles
+        // is then examined in one cell only, the one holding the low corner of their boxes' overlap
+        const auto& hs = e->tree.hazards();
+        const Box b = e->tree.bbox();
+        std::vector<float> diam;
+        float rmax = 0.0f;
+        for (const HazardRec& h : hs)
+            if (h.alive)
+                for (const Disk& d : h.poles) {
+                    diam.push_back(2.0f * d.r);
+                    rmax = fmaxf(rmax, d.r);
+                }
+        const uint32_t np = (uint32_t)diam.size();
+        const float ext = fmaxf(b.x1 - b.x0, b.y1 - b.y0);
+        float typical = 0.0f;
+        if (np) {   // cells about the size of a typical pole
+            std::nth_element(diam.begin(), diam.begin() + diam.size() * 3 / 4, diam.end());
+            typical = diam[diam.size() * 3 / 4];
+        }
+        const float cs = fmaxf(fmaxf(typical, ext / 1024.0f), 1e-6f);
+        const int32_t g = std::max<int32_t>(1, std::min<int32_t>(1024, (int32_t)ceilf(ext / cs)));
+        const float inv = (float)g / fmaxf(ext, 1e-6f);
+        auto cix = [&](float x, float o) { return std::max(0, std::min(g - 1, (int)floorf((x - o) * inv))); };
+        std::vector<uint32_t> start((size_t)g * g + 1, 0u);
+        auto for_cells = [&](const Disk& d, auto&& fn) {
+            const int x0 = cix(d.c.x - d.r, b.x0), x1 = cix(d.c.x + d.r, b.x0);
+            const int y0 = cix(d.c.y - d.r, b.y0), y1 = cix(d.c.y + d.r, b.y0);
+            for (int iy = y0; iy <= y1; iy++)
+                for (int ix = x0; ix <= x1; ix++) fn((uint32_t)iy * (uint32_t)g + (uint32_t)ix);
+        };
+        for (const HazardRec& h : hs)
+            if (h.alive)
+                for (const Disk& d : h.poles) for_cells(d, [&](uint32_t c) { start[c + 1]++; });
+        for (size_t c = 1; c < start.size(); c++) start[c] += start[c - 1];
+        std::vector<float4> hp(std::max<uint32_t>(start.back(), 1));
+        std::vector<uint32_t> fill(start.begin(), start.end() - 1);
+        for (uint32_t k = 0; k < hs.size(); k++)
+            if (hs[k].alive)
+                for (const Disk& d : hs[k].poles) {
+                    float kf;
+                    std::memcpy(&kf, &k, 4);
+                    for_cells(d, [&](uint32_t c) { hp[fill[c]++] = make_float4(d.c.x, d.c.y, d.r, kf); });
+                }
+        jcde_status st;
+        if ((st = upload(e->d_hpoles, hp.data(), hp.size() * sizeof(float4)))) return st;
+        if ((st = upload(e->d_hpstart, start.data(), start.size() * 4))) return st;
+        e->hp_x0 = b.x0;
+        e->hp_y0 = b.y0;
+        e->hp_inv_cs = inv;
+        e->hp_rmax = rmax;
+        e->hp_g = g;
+        e->n_hpoles = np;
+        e->pole_version = e->tree.pole_version();
     }
     if (e->items_dirty) {
         jcde_status st;
@@ -201,6 +263,13 @@ static View base_view(const jcde_engine* e) {
     v.n_slots = e->tree.n_slots();
     v.cd_threshold = e->cfg.cd_threshold;
     v.exterior = e->tree.exterior_key();
+    v.hpoles = e->d_hpoles.as<float4>();
+    v.hp_start = e->d_hpstart.as<uint32_t>();
+    v.hp_x0 = e->hp_x0;
+    v.hp_y0 = e->hp_y0;
+    v.hp_inv_cs = e->hp_inv_cs;
+    v.hp_rmax = e->hp_rmax;
+    v.hp_g = e->hp_g;
     return v;
 }
 
@@ -500,6 +569,14 @@ jcde_status jcde_register_item(jcde_engine* e, const float* xy, uint32_t nv, con
     it.n_piers = n_piers;
     it.poi_x = poi[0];
     it.poi_y = poi[1];
+    it.n_poles = n_poles;
+    it.pole_r2max = 0.0f;
+    it.pole_bound = 0.0f;
+    for (uint32_t i = 0; i < n_poles; i++) {
+        const float d2 = poles[3 * i] * poles[3 * i] + poles[3 * i + 1] * poles[3 * i + 1];
+        it.pole_r2max = std::max(it.pole_r2max, d2);
+        it.pole_bound = std::max(it.pole_bound, sqrtf(d2) + poles[3 * i + 2]);
+    }
     for (uint32_t i = 0; i < nv; i++) e->iverts.push_back(make_float2(xy[2 * i], xy[2 * i + 1]));
     for (uint32_t i = 0; i < n_poles; i++) e->poles.push_back(make_float4(poles[3 * i], poles[3 * i + 1], poles[3 * i + 2], 0.0f));
     for (uint32_t i = 0; i < n_piers; i++)
@@ -815,7 +892,8 @@ extern "C" jcde_status jcde_detect_batch_noalloc(jcde_engine* e, const jcde_quer
     const uint32_t n_keys = f ? f->n_ignored : 0u;
     if (n_keys && !f->ignored) return JCDE_ERR_ARG;
     // bringing the device mirror up to date may allocate: it must already be current
-    if (e->tree_version != e->tree.version() || e->items_dirty) return JCDE_ERR_STATE;
+    if (e->tree_version != e->tree.version() || e->items_dirty || e->pole_version != e->tree.pole_version())
+        return JCDE_ERR_STATE;
     const uint32_t words = mask_words(e);
     const size_t keys_b = align256((size_t)n_keys * 4), mask_b = align256((size_t)words * 4);
     const size_t str_b = align256(e->n_nodes);
@@ -1025,5 +1103,81 @@ jcde_status jcde_multi_detect_graph(jcde_multi* m, const jcde_query* dq, const u
 }
 
 uint64_t jcde_multi_kernel_launches(const jcde_multi* m) { return m ? m->launches : 0; }
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------------------------
+// Pole-overlap proxy: hazard poles, forward/adjoint batch, gradient-descent separation, and the
+// random-resampling baseline (no counterpart in the reference).
+// ---------------------------------------------------------------------------------------------
+extern "C" {
+
+jcde_status jcde_set_hazard_poles(jcde_engine* e, uint32_t key, const float* xyr, uint32_t n) {
+    if (!e || (n && !xyr)) return JCDE_ERR_ARG;
+    std::vector<Disk> p(n);
+    for (uint32_t i = 0; i < n; i++) p[i] = Disk{Pt{xyr[3 * i], xyr[3 * i + 1]}, xyr[3 * i + 2]};
+    return e->tree.set_poles(key, std::move(p)) ? JCDE_OK : JCDE_ERR_NOT_FOUND;
+}
+
+static jcde_status proxy_prepare(jcde_engine* e, const jcde_filter* f, cudaStream_t s, View& v) {
+    jcde_status st = sync_device(e);
+    if (st) return st;
+    init_launch_shape(e);
+    v = base_view(e);
+    return apply_filter(e, f, s, v);
+}
+
+jcde_status jcde_proxy_batch(jcde_engine* e, const float* d_params, const uint32_t* d_items, uint32_t n,
+                             const jcde_filter* f, float* d_value, float* d_grad, void* stream) {
+    if (!e || (n && (!d_params || !d_items || !d_value || !d_grad))) return JCDE_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    View v;
+    jcde_status st = proxy_prepare(e, f, s, v);
+    if (st || n == 0) return st;
+    const uint32_t grid = std::min<uint32_t>((n + PROXY_WARPS - 1) / PROXY_WARPS, (uint32_t)e->n_sms * 8);
+    k_proxy<<<grid, PROXY_WARPS * 32, 0, s>>>(v, d_params, d_items, n, d_value, d_grad);
+    CUDA_TRY(cudaGetLastError());
+    e->launches++;
+    e->last_stream = s;
+    e->have_last_stream = true;
+    return JCDE_OK;
+}
+
+jcde_status jcde_separate_batch(jcde_engine* e, float* d_params, const uint32_t* d_items, uint32_t n, uint32_t steps,
+                                float step_t, float step_th, float clearance, const jcde_filter* f,
+                                jcde_query* d_queries, float* d_value, void* stream) {
+    if (!e || (n && (!d_params || !d_items || !d_queries || !d_value))) return JCDE_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    View v;
+    jcde_status st = proxy_prepare(e, f, s, v);
+    if (st || n == 0) return st;
+    const uint32_t per_block = PROXY_WARPS * (32 / JCDE_SEP_LANES);
+    const uint32_t grid = std::min<uint32_t>((n + per_block - 1) / per_block, (uint32_t)e->n_sms * 8);
+    cudaEvent_t pa = prof_begin(e, s);
+    k_separate<<<grid, PROXY_WARPS * 32, 0, s>>>(v, d_params, d_items, n, steps, step_t, step_th, clearance,
+                                                reinterpret_cast<uint32_t*>(d_queries), d_value);
+    prof_end(e, s, pa, JCDE_PROF_PROXY);
+    CUDA_TRY(cudaGetLastError());
+    e->launches++;
+    e->last_stream = s;
+    e->have_last_stream = true;
+    return JCDE_OK;
+}
+
+jcde_status jcde_resample_batch(jcde_engine* e, const float* d_params, const uint32_t* d_items, uint32_t n,
+                                uint32_t k, float sigma_t, float sigma_th, uint32_t seed, jcde_query* d_queries,
+                                void* stream) {
+    if (!e || !k || (n && (!d_params || !d_items || !d_queries))) return JCDE_ERR_ARG;
+    if (n == 0) return JCDE_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    init_launch_shape(e);
+    const uint64_t total = (uint64_t)n * k;
+    const uint32_t grid = (uint32_t)std::min<uint64_t>((total + 255) / 256, (uint64_t)e->n_sms * 16);
+    k_resample<<<grid, 256, 0, s>>>(d_params, d_items, n, k, sigma_t, sigma_th, seed,
+                                    reinterpret_cast<uint32_t*>(d_queries));
+    CUDA_TRY(cudaGetLastError());
+    e->launches++;
+    return JCDE_OK;
+}
 
 }  // extern "C"

@@ -44,6 +44,11 @@ struct View {
     Box cde;
     uint32_t n_items, n_slots, cd_threshold;
     int32_t exterior;
+    // hazard poles binned in a uniform grid over the CDE box (overlap proxy)
+    const float4* __restrict__ hpoles;      // x, y, r, hazard key (bits)
+    const uint32_t* __restrict__ hp_start;  // cell c holds hpoles[hp_start[c], hp_start[c+1])
+    float hp_x0, hp_y0, hp_inv_cs, hp_rmax;
+    int32_t hp_g;
 };
 
 // A raw (already transformed) query shape for the single-polygon entry points.
@@ -807,6 +812,312 @@ __global__ void __launch_bounds__(1024) k_scan_counts(uint32_t* __restrict__ c, 
         const uint32_t v = c[k];
         c[k] = run;
         run += v;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Differentiable pole-overlap proxy (no counterpart in the reference).  For a candidate placement
+// (theta, tx, ty) of an item, with the item's surrogate poles p_i (circle.rs:95-107 as circles,
+// sp_surrogate.rs:19) placed at c_i = R(theta) p_i + t and the hazards' poles (c_j, r_j):
+//     P = sum_ij max(0, r_i + r_j - |c_i - c_j|)^2
+//     dP/dt = sum -2 pen_ij (c_i - c_j) / |c_i - c_j|
+//     dP/dtheta = sum -2 pen_ij (c_i - c_j) . R'(theta) p_i / |c_i - c_j|,  R'(theta) p = (-ry, rx)
+// with (rx, ry) = R(theta) p.  Differences are formed as (t - c_j) + R p to keep float32 precision.
+// One warp per candidate, lanes over the item's poles, FP32 accumulation, warp-reduced.
+// ---------------------------------------------------------------------------------------------
+struct ProxyOut {
+    float p, gx, gy, gth;
+};
+
+// Neumaier-compensated float32 accumulation (sum + running correction)
+struct KSum {
+    float s = 0.0f, c = 0.0f;
+    __device__ __forceinline__ void add(float x) {
+        const float t = s + x;
+        c += fabsf(s) >= fabsf(x) ? (s - t) + x : (x - t) + s;
+        s = t;
+    }
+    __device__ __forceinline__ float get() const { return s + c; }
+};
+
+__device__ __forceinline__ int pole_cell(float x, float o, float inv, int g) {
+    return max(0, min(g - 1, (int)floorf((x - o) * inv)));
+}
+
+// `lane` counts within a group of `nsub` lanes (32 or 16) whose member mask is `mask`; hazard pole
+// radii are grown by `clear` (0 for the proxy itself).
+__device__ __forceinline__ ProxyOut proxy_eval(const View& v, const DItem& it, float c, float s, float tx, float ty,
+                                               int lane, int nsub, uint32_t mask, float clear) {
+    KSum p, gx, gy, gth;
+    const int g = v.hp_g;
+    for (uint32_t k = lane; k < it.n_poles; k += nsub) {
+        const float4 pl = __ldg(&v.poles[it.pole_off + k]);
+        const float rx = c * pl.x - s * pl.y, ry = s * pl.x + c * pl.y;
+        const float cx = rx + tx, cy = ry + ty;
+        const float rc = pl.z + clear;   // reach: a hazard pole's box grown by `clear` must overlap this one
+        const float bx0 = cx - rc, by0 = cy - rc, bx1 = cx + rc, by1 = cy + rc;
+        const int ix0 = pole_cell(bx0, v.hp_x0, v.hp_inv_cs, g), ix1 = pole_cell(bx1, v.hp_x0, v.hp_inv_cs, g);
+        const int iy0 = pole_cell(by0, v.hp_y0, v.hp_inv_cs, g), iy1 = pole_cell(by1, v.hp_y0, v.hp_inv_cs, g);
+        for (int iy = iy0; iy <= iy1; iy++)
+            for (int ix = ix0; ix <= ix1; ix++) {
+                const uint32_t cell = (uint32_t)iy * (uint32_t)g + (uint32_t)ix;
+                const uint32_t a = __ldg(&v.hp_start[cell]), b = __ldg(&v.hp_start[cell + 1]);
+                for (uint32_t j = a; j < b; j++) {
+                    const float4 h = __ldg(&v.hpoles[j]);
+                    // the pair belongs to the cell of the low corner of the two boxes' overlap
+                    const float mx = fmaxf(bx0, h.x - h.z), my = fmaxf(by0, h.y - h.z);
+                    if (mx > fminf(bx1, h.x + h.z) || my > fminf(by1, h.y + h.z)) continue;
+                    // (the item box carries the clearance, so every grown overlap is still found, and
+                    // the low corner lies in a cell both boxes reach: each pair is counted once)
+                    if (pole_cell(mx, v.hp_x0, v.hp_inv_cs, g) != ix || pole_cell(my, v.hp_y0, v.hp_inv_cs, g) != iy)
+                        continue;
+                    if (filtered(v, __float_as_uint(h.w))) continue;
+                    const float dx = (tx - h.x) + rx, dy = (ty - h.y) + ry;
+                    const float d2 = dx * dx + dy * dy;
+                    const float rr = pl.z + h.z + clear;
+                    if (d2 >= rr * rr) continue;
+                    const float d = sqrtf(d2), pen = rr - d;
+                    p.add(pen * pen);
+                    if (d > 0.0f) {
+                        const float f = -2.0f * pen / d;
+                        gx.add(f * dx);
+                        gy.add(f * dy);
+                        gth.add(f * (dy * rx - dx * ry));
+                    }
+                }
+            }
+    }
+    ProxyOut o{p.get(), gx.get(), gy.get(), gth.get()};
+    for (int sh = nsub >> 1; sh; sh >>= 1) {
+        o.p += __shfl_xor_sync(mask, o.p, sh);
+        o.gx += __shfl_xor_sync(mask, o.gx, sh);
+        o.gy += __shfl_xor_sync(mask, o.gy, sh);
+        o.gth += __shfl_xor_sync(mask, o.gth, sh);
+    }
+    return o;
+}
+
+constexpr int PROXY_WARPS = 8;
+
+// Forward + adjoint for a batch: params are (theta, tx, ty) per candidate.
+__global__ void __launch_bounds__(PROXY_WARPS * 32) k_proxy(View v, const float* __restrict__ params,
+                                                            const uint32_t* __restrict__ items, uint32_t n,
+                                                            float* __restrict__ value, float* __restrict__ grad) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (uint32_t i = blockIdx.x * PROXY_WARPS + warp; i < n; i += gridDim.x * PROXY_WARPS) {
+        const uint32_t item = __ldg(&items[i]);
+        if (item >= v.n_items) {
+            if (lane == 0) value[i] = -1.0f;
+            continue;
+        }
+        const DItem it = v.items[item];
+        float s, c;
+        sincosf(__ldg(&params[3 * i]), &s, &c);
+        const ProxyOut o = proxy_eval(v, it, c, s, __ldg(&params[3 * i + 1]), __ldg(&params[3 * i + 2]), lane, 32, FULL, 0.0f);
+        if (lane == 0) {
+            value[i] = o.p;
+            grad[3 * i] = o.gth;
+            grad[3 * i + 1] = o.gx;
+            grad[3 * i + 2] = o.gy;
+        }
+    }
+}
+
+// Gradient-descent separation: `steps` descent steps on the proxy per candidate (state in
+// registers).  Each step tries x - eta * D grad (D scales translation by step_t and rotation by
+// step_th / max|p_i|^2); the trial is kept when it lowers the proxy (eta grows x1.5, up to 4) and
+// dropped otherwise (eta halves), so the proxy never increases.  Stops when the proxy reaches 0.
+// Writes the final params and the query record (item, cos, sin, tx, ty) for the exact verdict.
+#ifndef JCDE_SEP_LANES
+#define JCDE_SEP_LANES 32       // lanes per candidate in k_separate (measured faster than 8 or 16)
+#endif
+#ifndef JCDE_SEP_MARGIN
+#define JCDE_SEP_MARGIN 0.25f   // motion (in item bounds) allowed before a candidate's list is gathered again
+#endif
+constexpr uint32_t SEP_LOCAL = 96;   // hazard poles kept per candidate for its descent
+
+// The hazard poles a candidate at (cx, cy) can meet while it moves less than `margin`: every
+// pole box overlapping the square of half-size `reach` around it, gathered once from the grid (a
+// pole is taken from the cell holding the low corner of its box's overlap with the square).
+// Radii are stored grown by `clear`.  Returns the count, or SEP_LOCAL + 1 when they do not fit.
+__device__ __forceinline__ uint32_t gather_poles(const View& v, float cx, float cy, float reach, float clear,
+                                                 float4* list, int lane, int nsub, uint32_t mask) {
+    const int g = v.hp_g;
+    const float gx0 = cx - reach, gy0 = cy - reach, gx1 = cx + reach, gy1 = cy + reach;
+    const int ix0 = pole_cell(gx0, v.hp_x0, v.hp_inv_cs, g), ix1 = pole_cell(gx1, v.hp_x0, v.hp_inv_cs, g);
+    const int iy0 = pole_cell(gy0, v.hp_y0, v.hp_inv_cs, g), iy1 = pole_cell(gy1, v.hp_y0, v.hp_inv_cs, g);
+    const int nx = ix1 - ix0 + 1, ncell = nx * (iy1 - iy0 + 1);
+    uint32_t cnt = 0;
+    for (int base = 0; base < ncell; base += nsub) {
+        const int ci = base + lane;
+        uint32_t a = 0, b = 0;
+        int ix = 0, iy = 0;
+        if (ci < ncell) {
+            ix = ix0 + ci % nx;
+            iy = iy0 + ci / nx;
+            const uint32_t cell = (uint32_t)iy * (uint32_t)g + (uint32_t)ix;
+            a = __ldg(&v.hp_start[cell]);
+            b = __ldg(&v.hp_start[cell + 1]);
+        }
+        for (uint32_t j = a;; j++) {   // lanes walk their own cells; appends are ballot-compacted
+            const bool live = j < b;
+            bool take = false;
+            float4 h = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (live) {
+                h = __ldg(&v.hpoles[j]);
+                const float mx = fmaxf(gx0, h.x - h.z), my = fmaxf(gy0, h.y - h.z);
+                take = mx <= fminf(gx1, h.x + h.z) && my <= fminf(gy1, h.y + h.z) &&
+                       pole_cell(mx, v.hp_x0, v.hp_inv_cs, g) == ix && pole_cell(my, v.hp_y0, v.hp_inv_cs, g) == iy &&
+                       !filtered(v, __float_as_uint(h.w));
+            }
+            const uint32_t bal = __ballot_sync(mask, take);
+            if (take) {
+                const uint32_t pos = cnt + __popc(bal & mask & ((1u << (threadIdx.x & 31)) - 1u));
+                if (pos < SEP_LOCAL) list[pos] = make_float4(h.x, h.y, h.z + clear, 0.0f);
+            }
+            cnt += __popc(bal & mask);
+            if (!__any_sync(mask, live)) break;
+        }
+    }
+    __syncwarp(mask);
+    return cnt <= SEP_LOCAL ? cnt : SEP_LOCAL + 1;
+}
+
+// The proxy against a gathered list (radii already grown): lanes over the item's poles.
+__device__ __forceinline__ ProxyOut proxy_local(const View& v, const DItem& it, float c, float s, float tx, float ty,
+                                                const float4* list, uint32_t m, int lane, int nsub, uint32_t mask) {
+    KSum p, gx, gy, gth;
+    for (uint32_t k = lane; k < it.n_poles; k += nsub) {
+        const float4 pl = __ldg(&v.poles[it.pole_off + k]);
+        const float rx = c * pl.x - s * pl.y, ry = s * pl.x + c * pl.y;
+        for (uint32_t j = 0; j < m; j++) {
+            const float4 h = list[j];
+            const float dx = (tx - h.x) + rx, dy = (ty - h.y) + ry;
+            const float d2 = dx * dx + dy * dy;
+            const float rr = pl.z + h.z;
+            if (d2 >= rr * rr) continue;
+            const float d = sqrtf(d2), pen = rr - d;
+            p.add(pen * pen);
+            if (d > 0.0f) {
+                const float f = -2.0f * pen / d;
+                gx.add(f * dx);
+                gy.add(f * dy);
+                gth.add(f * (dy * rx - dx * ry));
+            }
+        }
+    }
+    ProxyOut o{p.get(), gx.get(), gy.get(), gth.get()};
+    for (int sh = nsub >> 1; sh; sh >>= 1) {
+        o.p += __shfl_xor_sync(mask, o.p, sh);
+        o.gx += __shfl_xor_sync(mask, o.gx, sh);
+        o.gy += __shfl_xor_sync(mask, o.gy, sh);
+        o.gth += __shfl_xor_sync(mask, o.gth, sh);
+    }
+    return o;
+}
+
+__global__ void __launch_bounds__(PROXY_WARPS * 32) k_separate(View v, float* __restrict__ params,
+                                                               const uint32_t* __restrict__ items, uint32_t n,
+                                                               uint32_t steps, float step_t, float step_th, float clear,
+                                                               uint32_t* __restrict__ qout, float* __restrict__ value) {
+    constexpr int L = JCDE_SEP_LANES, PER_WARP = 32 / L;
+    __shared__ float4 local[PROXY_WARPS * PER_WARP][SEP_LOCAL];
+    // PER_WARP candidates per warp, L lanes each
+    const int grp = (threadIdx.x & 31) / L, hl = threadIdx.x % L;
+    const uint32_t mask = (L == 32 ? FULL : ((1u << L) - 1u)) << (L * grp);
+    float4* list = local[(threadIdx.x >> 5) * PER_WARP + grp];
+    const uint32_t groups = gridDim.x * PROXY_WARPS * PER_WARP;
+    for (uint32_t i = (blockIdx.x * PROXY_WARPS + (threadIdx.x >> 5)) * PER_WARP + grp; i < n; i += groups) {
+        const uint32_t item = __ldg(&items[i]);
+        float th = params[3 * i], tx = params[3 * i + 1], ty = params[3 * i + 2];
+        float p = -1.0f;
+        if (item < v.n_items) {
+            const DItem it = v.items[item];
+            const float kth = step_th / fmaxf(it.pole_r2max, 1.0f);
+            const float margin = JCDE_SEP_MARGIN * it.pole_bound;   // motion allowed before gathering again
+            const float reach = it.pole_bound + clear + margin;
+            float ox = tx, oy = ty;
+            uint32_t m = gather_poles(v, ox, oy, reach, clear, list, hl, L, mask);
+            auto eval = [&](float c, float s, float x, float y) -> ProxyOut {
+                if (fabsf(x - ox) > margin || fabsf(y - oy) > margin) {
+                    ox = x;
+                    oy = y;
+                    m = gather_poles(v, ox, oy, reach, clear, list, hl, L, mask);
+                }
+                return m <= SEP_LOCAL ? proxy_local(v, it, c, s, x, y, list, m, hl, L, mask)
+                                      : proxy_eval(v, it, c, s, x, y, hl, L, mask, clear);
+            };
+            float s, c;
+            sincosf(th, &s, &c);
+            ProxyOut cur = eval(c, s, tx, ty);
+            float eta = 1.0f;
+            for (uint32_t k = 0; k < steps && cur.p > 0.0f; k++) {
+                const float th2 = th - eta * kth * cur.gth;
+                const float tx2 = tx - eta * step_t * cur.gx, ty2 = ty - eta * step_t * cur.gy;
+                sincosf(th2, &s, &c);
+                const ProxyOut trial = eval(c, s, tx2, ty2);
+                if (trial.p < cur.p) {
+                    th = th2;
+                    tx = tx2;
+                    ty = ty2;
+                    cur = trial;
+                    eta = fminf(eta * 1.5f, 4.0f);
+                } else {
+                    eta *= 0.5f;
+                }
+            }
+            p = cur.p;
+        }
+        if (hl == 0) {
+            params[3 * i] = th;
+            params[3 * i + 1] = tx;
+            params[3 * i + 2] = ty;
+            value[i] = p;
+            float s, c;
+            sincosf(th, &s, &c);
+            uint32_t* r = qout + (size_t)i * 5;
+            r[0] = item;
+            r[1] = __float_as_uint(c);
+            r[2] = __float_as_uint(s);
+            r[3] = __float_as_uint(tx);
+            r[4] = __float_as_uint(ty);
+        }
+        __syncwarp(mask);
+    }
+}
+
+// Random-resampling baseline: `k` perturbed copies of each candidate (Gaussian in translation and
+// rotation, counter-based hash RNG), written as query records for the exact verdict.
+__device__ __forceinline__ uint32_t hash32(uint32_t x) {
+    x ^= x >> 16;
+    x *= 0x7feb352dU;
+    x ^= x >> 15;
+    x *= 0x846ca68bU;
+    x ^= x >> 16;
+    return x;
+}
+__device__ __forceinline__ float gauss(uint32_t a, uint32_t b) {   // Box-Muller from two hashes
+    const float u1 = ((hash32(a) >> 8) + 1u) * (1.0f / 16777217.0f);
+    const float u2 = (hash32(b) >> 8) * (1.0f / 16777216.0f);
+    return sqrtf(-2.0f * __logf(u1)) * __cosf(6.2831853f * u2);
+}
+__global__ void k_resample(const float* __restrict__ params, const uint32_t* __restrict__ items, uint32_t n, uint32_t k,
+                           float sigma_t, float sigma_th, uint32_t seed, uint32_t* __restrict__ qout) {
+    const uint64_t total = (uint64_t)n * k;
+    for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < total; j += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t i = (uint32_t)(j / k);
+        const uint32_t h = hash32((uint32_t)j * 4u + seed);
+        const float th = params[3 * i] + sigma_th * gauss(h, h ^ 0x9e3779b9u);
+        const float tx = params[3 * i + 1] + sigma_t * gauss(h + 1u, h ^ 0x85ebca6bu);
+        const float ty = params[3 * i + 2] + sigma_t * gauss(h + 2u, h ^ 0xc2b2ae35u);
+        float s, c;
+        sincosf(th, &s, &c);
+        uint32_t* r = qout + j * 5;
+        r[0] = items[i];
+        r[1] = __float_as_uint(c);
+        r[2] = __float_as_uint(s);
+        r[3] = __float_as_uint(tx);
+        r[4] = __float_as_uint(ty);
     }
 }
 

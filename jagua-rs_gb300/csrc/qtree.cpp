@@ -224,6 +224,7 @@ bool QuadTree::remove(uint32_t k) {
     dereg(0, k);
     haz_[k].alive = false;
     haz_[k].shape = Polygon{};
+    haz_[k].poles.clear();
     if ((int32_t)k == exterior_) exterior_ = -1;
     free_keys_.push_back(k);
     version_++;

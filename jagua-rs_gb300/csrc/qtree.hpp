@@ -30,6 +30,7 @@ struct HazardRec {
     bool alive = false;
     uint64_t tag = 0;   // caller's entity identity (placed-item key, zone index, ...)
     Polygon shape;
+    std::vector<Disk> poles;   // surrogate poles of the shape (SPolygon::surrogate), optional
 };
 
 struct NodeHaz {
@@ -70,6 +71,10 @@ struct alignas(16) DItem {
     uint32_t v_off, v_cnt, pole_off, n_ff_poles;
     uint32_t pier_off, n_piers;
     float poi_x, poi_y;
+    uint32_t n_poles;       // all surrogate poles (the proxy uses every pole, probes only the ff ones)
+    float pole_r2max;       // largest squared distance of a pole centre from the item origin
+    float pole_bound;       // radius around the item origin that holds every pole
+    uint32_t pad0;
 };
 
 struct FlatTree {
@@ -98,6 +103,14 @@ class QuadTree {
     void flatten(FlatTree& out) const;                 // breadth-first, quartets contiguous
     void dump(std::vector<uint32_t>& out) const;       // canonical form (tests)
     uint64_t version() const { return version_; }
+    // surrogate poles of a registered hazard (used by the overlap proxy); false for an unknown key
+    bool set_poles(uint32_t key, std::vector<Disk>&& poles) {
+        if (key >= haz_.size() || !haz_[key].alive) return false;
+        haz_[key].poles = std::move(poles);
+        pole_version_++;
+        return true;
+    }
+    uint64_t pole_version() const { return pole_version_ + version_; }
 
   private:
     int32_t alloc_quartet(int32_t parent);
@@ -115,6 +128,7 @@ class QuadTree {
     uint8_t cdt_;
     int32_t exterior_ = -1;
     uint64_t version_ = 0;
+    uint64_t pole_version_ = 0;
 };
 
 // simple_polygon.rs:255-292 — ray-cast point in polygon with the FPA vertex guard

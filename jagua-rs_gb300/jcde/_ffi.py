@@ -87,6 +87,10 @@ SIGNATURES = {
     "jcde_kernel_launches": (C.c_uint64, [P]),
     "jcde_profile_enable": (C.c_int32, [P, C.c_int]),
     "jcde_multi_create": (C.c_int32, [C.POINTER(P), C.c_uint32, C.POINTER(P)]),
+    "jcde_set_hazard_poles": (C.c_int32, [P, C.c_uint32, f32p, C.c_uint32]),
+    "jcde_proxy_batch": (C.c_int32, [P, P, P, C.c_uint32, C.POINTER(jcde_filter), P, P, P]),
+    "jcde_separate_batch": (C.c_int32, [P, P, P, C.c_uint32, C.c_uint32, C.c_float, C.c_float, C.c_float, C.POINTER(jcde_filter), P, P, P]),
+    "jcde_resample_batch": (C.c_int32, [P, P, P, C.c_uint32, C.c_uint32, C.c_float, C.c_float, C.c_uint32, P, P]),
     "jcde_multi_destroy": (None, [P]),
     "jcde_multi_detect": (C.c_int32, [P, P, u32p, C.POINTER(jcde_filter), P, P]),
     "jcde_multi_detect_graph": (C.c_int32, [P, P, u32p, C.POINTER(jcde_filter), P, P]),

@@ -262,6 +262,51 @@ class CDEngine:
                 return offsets, counts, ids[:t], t
             cap = t
 
+    # --- pole-overlap proxy ---------------------------------------------------------------------
+    def set_hazard_poles(self, key: int, poles) -> None:
+        """Surrogate poles (x, y, r) of hazard `key`, used by the overlap proxy."""
+        p = _f32(np.asarray(poles).reshape(-1, 3))
+        st = lib().jcde_set_hazard_poles(self.h, int(key), _fp(p) if len(p) else None, len(p))
+        if st == _ffi.ERR_NOT_FOUND:
+            raise KeyError(key)
+        check(st, "set_hazard_poles")
+
+    def proxy_batch(self, params, items, filter=None, stream=None):
+        """(value, grad) CUDA tensors of the proxy for (theta, tx, ty) params [n, 3] and items [n]."""
+        import torch
+
+        f = _Filter(filter)
+        n = items.numel()
+        val = torch.empty(n, dtype=torch.float32, device=params.device)
+        grad = torch.empty((n, 3), dtype=torch.float32, device=params.device)
+        check(lib().jcde_proxy_batch(self.h, params.data_ptr(), items.data_ptr(), n, f.ref, val.data_ptr(),
+                                     grad.data_ptr(), _stream_handle(stream)), "proxy_batch")
+        return val, grad
+
+    def separate_batch(self, params, items, steps=20, step_t=0.25, step_th=0.25, clearance=0.0, filter=None,
+                       stream=None):
+        """Gradient-descent separation in place on params [n, 3]; returns (packed queries, final P)."""
+        import torch
+
+        f = _Filter(filter)
+        n = items.numel()
+        q = torch.empty(n * QUERY_DTYPE.itemsize, dtype=torch.uint8, device=params.device)
+        val = torch.empty(n, dtype=torch.float32, device=params.device)
+        check(lib().jcde_separate_batch(self.h, params.data_ptr(), items.data_ptr(), n, steps, step_t, step_th,
+                                        clearance, f.ref, q.data_ptr(), val.data_ptr(), _stream_handle(stream)),
+              "separate_batch")
+        return q, val
+
+    def resample_batch(self, params, items, k=20, sigma_t=10.0, sigma_th=0.2, seed=1, stream=None):
+        """k random perturbations per candidate as packed queries [n * k]."""
+        import torch
+
+        n = items.numel()
+        q = torch.empty(n * k * QUERY_DTYPE.itemsize, dtype=torch.uint8, device=params.device)
+        check(lib().jcde_resample_batch(self.h, params.data_ptr(), items.data_ptr(), n, k, sigma_t, sigma_th, seed,
+                                        q.data_ptr(), _stream_handle(stream)), "resample_batch")
+        return q
+
     # --- snapshots -----------------------------------------------------------------------------
     def save(self):
         s = C.c_void_p()
@@ -287,7 +332,7 @@ class CDEngine:
     def kernel_launches(self) -> int:
         return int(lib().jcde_kernel_launches(self.h))
 
-    PROFILE_KINDS = ("surrogate", "poly", "collect", "order", "filter")
+    PROFILE_KINDS = ("surrogate", "poly", "collect", "order", "filter", "proxy")
 
     def profile(self, enable: bool = True) -> None:
         """Bracket every kernel launch with CUDA events (jcde_profile_enable)."""

@@ -398,3 +398,54 @@ def multi_queries(layouts, seed=0xC2, q_range=(4096, 262144)):
         parts.append(make_queries(Stream(seed, 100 + l), n, len(lay.items), lay.cde_bbox))
         offs.append(offs[-1] + n)
     return np.concatenate(parts), np.array(offs, dtype=np.uint32)
+
+
+def exterior_ring(xy, radius: float) -> np.ndarray:
+    """Circles just outside a counter-clockwise container, tangent to each edge from outside and
+    spaced one radius apart: the exterior hazard's stand-in for poles (the region outside a polygon
+    has no inscribed circles of its own)."""
+    xy = np.asarray(xy, dtype=np.float64)
+    out = []
+    for i in range(len(xy)):
+        a, b = xy[i], xy[(i + 1) % len(xy)]
+        d = b - a
+        L = float(np.hypot(d[0], d[1]))
+        if L == 0.0:
+            continue
+        nrm = np.array([d[1], -d[0]]) / L   # outward for counter-clockwise vertices
+        k = max(1, int(math.ceil(L / radius)))
+        for j in range(k):
+            c = a + d * ((j + 0.5) / k) + nrm * radius
+            out.append((c[0], c[1], radius))
+    return np.asarray(out, dtype=np.float32)
+
+
+def hazard_poles(backend, lay: Layout, pole_limits=DEFAULT_POLE_LIMITS, ring_radius=40.0) -> np.ndarray:
+    """Poles of every hazard, as rows (x, y, r, key bits) — the pole sets the overlap proxy measures
+    against.  A placed item's are its item's surrogate poles under its placement (SPolygon::transform
+    moves the surrogate with the shape, simple_polygon.rs:195-224); holes and zones get poles
+    generated on their own shapes; the exterior gets a ring of tangent circles outside the container."""
+    rows = []
+    for hz in lay.hazards:
+        if hz.kind == EXTERIOR:
+            poles = exterior_ring(hz.xy, ring_radius)
+        elif hz.placement is not None and hz.kind == PLACED_ITEM:
+            t, c, s, tx, ty = hz.placement
+            it = lay.items[t]
+            ctr = transform_points(it.poles[:, :2], c, s, tx, ty)
+            poles = np.concatenate([ctr, it.poles[:, 2:3]], axis=1)
+        else:
+            _, _, area, _, _ = backend.spolygon_new(hz.xy)
+            poles = backend.surrogate_poles(hz.xy, area, hz.poi, pole_limits)
+        key = np.full((len(poles), 1), hz.key, dtype=np.uint32).view(np.float32)
+        rows.append(np.concatenate([poles.astype(np.float32), key], axis=1))
+    return np.ascontiguousarray(np.concatenate(rows).astype(np.float32))
+
+
+def random_params(st: Stream, n: int, n_item_types: int, bbox):
+    """Uniform candidate placements as (theta, tx, ty) float32 rows + item types."""
+    items = st.randint(0, n_item_types - 1, n).astype(np.uint32)
+    th = (st.f64(n) * (2.0 * math.pi)).astype(np.float32)
+    tx = st.uniform_f32(bbox[0], bbox[2], n)
+    ty = st.uniform_f32(bbox[1], bbox[3], n)
+    return np.ascontiguousarray(np.stack([th, tx, ty], axis=1).astype(np.float32)), items

@@ -1302,3 +1302,53 @@ uint64_t or_tree_dump(void* ep, uint32_t* out, uint64_t cap) {
 uint32_t or_n_slots(void* ep) { return (uint32_t)((Engine*)ep)->hmap.size(); }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------------------------------
+// FP64 oracle of the pole-overlap proxy (test infrastructure): for each candidate (theta, tx, ty)
+// of item `items[i]` whose poles are item_poles[pole_off[item] .. pole_off[item+1]) (x, y, r),
+//   P = sum_ij max(0, r_i + r_j - |R(theta) p_i + t - c_j|)^2
+// over every hazard pole (x, y, r, key) whose key is not ignored, evaluated in double precision
+// from the float32 inputs, with its analytic gradient d/d(theta, tx, ty).
+// ------------------------------------------------------------------------------------------
+extern "C" void or_proxy_f64(uint64_t n, const double* params, const uint32_t* items, const uint32_t* pole_off,
+                             const float* item_poles, const float* hpoles, uint64_t n_hpoles,
+                             const uint32_t* ignored, uint32_t n_ignored, double* value, double* grad,
+                             int32_t n_threads) {
+    std::vector<uint8_t> ign;
+    for (uint32_t i = 0; i < n_ignored; i++) {
+        if (ignored[i] >= ign.size()) ign.resize(ignored[i] + 1, 0);
+        ign[ignored[i]] = 1;
+    }
+    run_threads(n, n_threads, [&](uint64_t a, uint64_t b, int) {
+        for (uint64_t i = a; i < b; i++) {
+            const double th = params[3 * i], tx = params[3 * i + 1], ty = params[3 * i + 2];
+            const double c = std::cos(th), s = std::sin(th);
+            double P = 0, gt = 0, gx = 0, gy = 0;
+            const uint32_t it = items[i];
+            for (uint32_t k = pole_off[it]; k < pole_off[it + 1]; k++) {
+                const double px = item_poles[3 * k], py = item_poles[3 * k + 1], r = item_poles[3 * k + 2];
+                const double rx = c * px - s * py, ry = s * px + c * py;
+                for (uint64_t j = 0; j < n_hpoles; j++) {
+                    uint32_t key;
+                    std::memcpy(&key, &hpoles[4 * j + 3], 4);
+                    if (key < ign.size() && ign[key]) continue;
+                    const double dx = (tx - (double)hpoles[4 * j]) + rx, dy = (ty - (double)hpoles[4 * j + 1]) + ry;
+                    const double d = std::sqrt(dx * dx + dy * dy);
+                    const double pen = r + (double)hpoles[4 * j + 2] - d;
+                    if (pen <= 0) continue;
+                    P += pen * pen;
+                    if (d > 0) {
+                        const double f = -2.0 * pen / d;
+                        gx += f * dx;
+                        gy += f * dy;
+                        gt += f * (dy * rx - dx * ry);
+                    }
+                }
+            }
+            value[i] = P;
+            grad[3 * i] = gt;
+            grad[3 * i + 1] = gx;
+            grad[3 * i + 2] = gy;
+        }
+    });
+}

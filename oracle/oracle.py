@@ -66,6 +66,8 @@ def lib():
             "or_edge_quadrants": (None, [f32p, f32p, u8p]),
             "or_tree_dump": (C.c_uint64, [P, u32p, C.c_uint64]),
             "or_n_slots": (C.c_uint32, [P]),
+            "or_proxy_f64": (None, [C.c_uint64, C.POINTER(C.c_double), u32p, u32p, f32p, f32p, C.c_uint64, u32p, C.c_uint32,
+                                     C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int32]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -258,3 +260,26 @@ def edge_quadrants(e, r):
     out = np.zeros(4, np.uint8)
     lib().or_edge_quadrants(_ptr(a, C.c_float), _ptr(b, C.c_float), _ptr(out, C.c_uint8))
     return [bool(v) for v in out]
+
+
+def proxy_f64(params, items, item_poles, hazard_poles, ignored=None, n_threads=0):
+    """FP64 pole-overlap proxy and gradient (theta, tx, ty) — the tolerance reference.
+
+    params [n, 3] (float32 values are taken exactly; float64 allowed for finite differences),
+    items [n], item_poles: list of (k, 3) arrays per item type,
+    hazard_poles [m, 4] float32 (x, y, r, key as uint32 bits)."""
+    params = np.ascontiguousarray(params, dtype=np.float64).reshape(-1, 3)
+    items = np.ascontiguousarray(items, dtype=np.uint32)
+    offs = np.zeros(len(item_poles) + 1, np.uint32)
+    offs[1:] = np.cumsum([len(p) for p in item_poles])
+    ip = np.ascontiguousarray(np.concatenate([np.asarray(p, np.float32).reshape(-1, 3) for p in item_poles]))
+    hp = np.ascontiguousarray(hazard_poles, dtype=np.float32).reshape(-1, 4)
+    ids, nf = _filter_arr(ignored)
+    val = np.zeros(len(params), np.float64)
+    grad = np.zeros((len(params), 3), np.float64)
+    lib().or_proxy_f64(len(params), params.ctypes.data_as(C.POINTER(C.c_double)), _ptr(items, C.c_uint32),
+                       _ptr(offs, C.c_uint32),
+                       _ptr(ip, C.c_float), _ptr(hp, C.c_float), len(hp), _ptr(ids, C.c_uint32), nf,
+                       val.ctypes.data_as(C.POINTER(C.c_double)), grad.ctypes.data_as(C.POINTER(C.c_double)),
+                       n_threads or (os.cpu_count() or 1))
+    return val, grad
