@@ -219,6 +219,81 @@ jcde_status jcde_resample_batch(jcde_engine* e, const float* d_params, const uin
                                 uint32_t k, float sigma_t, float sigma_th, uint32_t seed, jcde_query* d_queries,
                                 void* stream);
 
+/* --- LBF choice of a candidate batch (lbf/src/opt/search.rs:44-66, LBFLoss lbf/src/opt/loss.rs) -- */
+/* Among queries whose verdict is JCDE_FREE: the smallest cost x_max * 10 + y_max of the transformed
+ * shape's bounding box, lowest index among equal costs.  *d_best (device) receives
+ * (order-preserving cost bits << 32) | index, or all ones when no candidate is free. */
+jcde_status jcde_lbf_select(jcde_engine* e, const jcde_query* d_queries, const uint8_t* d_verdicts, uint32_t n,
+                            uint64_t* d_best, void* stream);
+
+/* --- Device-resident engine: register / deregister on the GPU ---------------------------------
+ * A copy of an engine's quadtree in device pools that single-warp kernels update in place,
+ * restating QTNode::register_hazard / deregister_hazard (quadtree/qt_node.rs:38-94) and
+ * QTHazard::constrict (quadtree/qt_hazard.rs:48-167) on the device.  Every call is stream-ordered
+ * and asynchronous (no host round trip), so a whole query -> choose -> register loop can be
+ * captured in one CUDA graph.  Keys follow the host engine's rule (a freed key is reused
+ * last-in first-out).  The resident copy shares the engine's items and staging buffers: it is
+ * created from the engine's current hazards, and while it is in use the engine's own query calls
+ * must not overlap it on the GPU.  Capacities are fixed at creation; exceeding one sets a sticky
+ * error (jcde_resident_status returns JCDE_ERR_CAPACITY) and further updates are skipped.  Destroy
+ * the resident copy before its engine; the engine's items must not change while it exists. */
+typedef struct jcde_resident jcde_resident;
+typedef struct jcde_resident_config {
+    uint32_t max_nodes;             /* 0: every node of a full tree of the engine's depth */
+    uint32_t max_entries;           /* hazard entries over all nodes (slabs, grown by doubling) */
+    uint32_t max_edges;             /* clipped edges over all Partial entries */
+    uint32_t max_hazard_vertices;   /* vertices of all hazards ever registered */
+    uint32_t max_keys;              /* hazard keys */
+    uint32_t max_tasks;             /* work stack of one update */
+} jcde_resident_config;
+void jcde_resident_default_config(jcde_resident_config* c);
+jcde_status jcde_resident_create(jcde_engine* e, const jcde_resident_config* cfg, jcde_resident** out);
+void jcde_resident_destroy(jcde_resident* r);
+/* Layout::place_item (entities/layout.rs:73-85): PlacedItem::new of item d_query->item under the
+ * query's transformation, then CDEngine::register_hazard (cd_engine.rs:59-70).  *d_key (device,
+ * may be null) receives the key, ~0 on failure. */
+jcde_status jcde_resident_register_placed(jcde_resident* r, const jcde_query* d_query, uint32_t* d_key, void* stream);
+/* CDEngine::deregister_hazard_by_key (cd_engine.rs:87-96) of the key at d_key (device); unknown keys are
+ * counted (status word 1) and ignored. */
+jcde_status jcde_resident_deregister(jcde_resident* r, const uint32_t* d_key, void* stream);
+/* jcde_detect_batch (surrogate pass, then polygon pass) against the resident tree, no filter. */
+jcde_status jcde_resident_detect_batch(jcde_resident* r, const jcde_query* d_queries, uint32_t n, uint8_t* d_out,
+                                       void* stream);
+/* Synchronises; out8 = error, unknown-key count, live hazards, key slots, node pool high-water mark,
+ * entry / edge / hazard-vertex pool use. */
+jcde_status jcde_resident_status(jcde_resident* r, uint32_t* out8);
+/* Synchronises; the canonical form of jcde_tree_dump for the resident tree. */
+jcde_status jcde_resident_tree_dump(jcde_resident* r, uint32_t* out, uint64_t cap, uint64_t* n_words);
+uint64_t jcde_resident_kernel_launches(const jcde_resident* r);
+
+/* --- LBF-style build on the device (lbf/src/opt/search.rs:17-106, restated) ----------------------
+ * Step s: item type t = draw s of stream (seed, 2) mod n_types; n_candidates placements of t with
+ * rotation ~ U[0, 2pi) and translation ~ U(sample_box) from stream (seed, 10000 + s) (draw n+i, 2n+i,
+ * 3n+i of candidate i); verdicts by the surrogate and polygon passes; the free candidate of least
+ * LBFLoss cost (lbf/src/opt/loss.rs:29-31, lowest index on ties) is registered; after every
+ * remove_every-th step the placed item at position (draw k of stream (seed, 4)) mod live of the
+ * placement list is deregistered (k = removals so far).  Streams: SplitMix64 counter-based draws,
+ * mix(key ^ mix(i)) with key = mix(seed * 0x100000001B3 + sid * 0x9E3779B97F4A7C15).
+ * No host round trip per step; steps_per_graph > 0 replays that many steps per CUDA graph launch. */
+typedef struct jcde_lbf_params {
+    uint64_t seed;
+    uint32_t n_candidates;
+    uint32_t n_types;              /* item types 0..n_types-1 of the engine */
+    uint32_t remove_every;         /* 0: no removals */
+    uint32_t max_steps;            /* log capacity; steps beyond it do nothing */
+    uint32_t verdict_log_steps;    /* keep the verdicts of the first steps (0: none) */
+    uint32_t reserved;
+    jcde_rect sample_box;
+} jcde_lbf_params;
+jcde_status jcde_lbf_begin(jcde_resident* r, const jcde_lbf_params* p);
+jcde_status jcde_lbf_steps(jcde_resident* r, uint32_t n_steps, uint32_t steps_per_graph, void* stream);
+/* Synchronises.  counts4 = steps done, placements, removals, placed items still live.  placements:
+ * 8 words each (step, key, candidate, item, cos, sin, tx, ty as float bits); removals: 2 words each
+ * (step, key); free_counts: free candidates per step; verdicts: step-major verdict log. */
+jcde_status jcde_lbf_read(jcde_resident* r, uint32_t* counts4, uint32_t* placements, uint32_t place_cap,
+                          uint32_t* removals, uint32_t removal_cap, uint32_t* free_counts, uint32_t free_cap,
+                          uint8_t* verdicts, uint64_t verdict_cap);
+
 /* --- snapshots: CDEngine::save / restore (cd_engine.rs:98-149) ------------------------------- */
 jcde_status jcde_save(const jcde_engine* e, jcde_snapshot** out);
 jcde_status jcde_restore(jcde_engine* e, const jcde_snapshot* s);

@@ -2,6 +2,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <list>
@@ -11,6 +13,7 @@
 
 #include "../../include/jcde.h"
 #include "kernels.cuh"
+#include "resident.cuh"
 #include "prep.hpp"
 #include "qtree.hpp"
 
@@ -340,6 +343,8 @@ constexpr uint32_t ORDER_MIN_BATCH = 4096;   // below this a batch is visited in
 // Visit order of a batch: cell-by-cell over the CDE box (k_bucket_*), or nullptr for index order.
 // `slot` selects one of two histogram/order buffer pairs, so that the two streams of the host
 // entry point's pipeline never share one; `slot_cap` is the largest batch a slot must hold.
+static const uint32_t* spatial_order_into(jcde_engine* e, const uint32_t* q, uint32_t n, cudaStream_t s,
+                                          uint32_t* hist, uint32_t* order);
 static const uint32_t* spatial_order(jcde_engine* e, const uint32_t* q, uint32_t n, cudaStream_t s, int slot,
                                      uint32_t slot_cap) {
     if (!JCDE_SPATIAL_ORDER || n < ORDER_MIN_BATCH) return nullptr;
@@ -352,6 +357,12 @@ static const uint32_t* spatial_order(jcde_engine* e, const uint32_t* q, uint32_t
     }
     uint32_t* hist = e->d_hist.as<uint32_t>() + (size_t)slot * N_BUCKETS;
     uint32_t* order = e->d_order.as<uint32_t>() + (size_t)slot * (e->d_order.cap / 8);
+    return spatial_order_into(e, q, n, s, hist, order);
+}
+
+// The ordering kernels over caller-owned buffers: hist of N_BUCKETS words, order of n words.
+static const uint32_t* spatial_order_into(jcde_engine* e, const uint32_t* q, uint32_t n, cudaStream_t s,
+                                          uint32_t* hist, uint32_t* order) {
     if (cudaMemsetAsync(hist, 0, N_BUCKETS * 4, s) != cudaSuccess) return nullptr;
     const Box b = e->tree.bbox();
     const uint32_t grid = std::min<uint32_t>((n + 255) / 256, (uint32_t)e->n_sms * 8);
@@ -1178,6 +1189,482 @@ jcde_status jcde_resample_batch(jcde_engine* e, const float* d_params, const uin
     CUDA_TRY(cudaGetLastError());
     e->launches++;
     return JCDE_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------------------------
+// LBF choice of a candidate batch (lbf/src/opt/search.rs:44-66): see k_lbf_select.
+// ---------------------------------------------------------------------------------------------
+extern "C" jcde_status jcde_lbf_select(jcde_engine* e, const jcde_query* d_queries, const uint8_t* d_verdicts,
+                                        uint32_t n, uint64_t* d_best, void* stream) {
+    if (!e || !d_best || (n && (!d_queries || !d_verdicts))) return JCDE_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    jcde_status st = sync_device(e);
+    if (st) return st;
+    init_launch_shape(e);
+    CUDA_TRY(cudaMemsetAsync(d_best, 0xFF, 8, s));
+    if (n == 0) return JCDE_OK;
+    const View v = base_view(e);
+    const uint32_t grid = std::min<uint32_t>((n + 7) / 8, (uint32_t)e->n_sms * 8);
+    k_lbf_select<<<grid, 256, 0, s>>>(v, reinterpret_cast<const uint32_t*>(d_queries), d_verdicts, n,
+                                      reinterpret_cast<unsigned long long*>(d_best), nullptr);
+    CUDA_TRY(cudaGetLastError());
+    e->launches++;
+    e->last_stream = s;
+    e->have_last_stream = true;
+    return JCDE_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Device-resident engine (resident.cuh): the quadtree lives in device pools that register /
+// deregister update on the GPU, and the LBF-style build that runs on it step by step.
+// ---------------------------------------------------------------------------------------------
+struct jcde_resident {
+    jcde_engine* e = nullptr;
+    RTree t{};
+    int32_t exterior = -1;
+    DevBuf d_nodes, d_ncap, d_level, d_strength, d_nedges, d_entries, d_edges, d_haz, d_hverts, d_alive, d_qfree,
+        d_kfree, d_tasks, d_ctl;
+    // LBF-style build
+    bool lbf_ready = false;
+    LbfParams lp{};
+    DevBuf d_lbf, d_cand, d_verd, d_place, d_remv, d_free, d_live, d_vlog;
+    DevBuf d_hist, d_order;   // spatial ordering of the resident's own query batches
+    cudaGraphExec_t exec = nullptr;
+    uint32_t exec_steps = 0;
+    cudaStream_t exec_stream = nullptr;
+    cudaStream_t own = nullptr;
+    cudaStream_t last = nullptr;
+    uint64_t launches = 0;
+    ~jcde_resident() {
+        if (last) cudaStreamSynchronize(last);
+        if (exec) cudaGraphExecDestroy(exec);
+        if (own) {
+            // the engine must not wait on a stream that no longer exists
+            if (e && e->have_last_stream && e->last_stream == own) {
+                e->have_last_stream = false;
+                e->last_stream = nullptr;
+            }
+            cudaStreamDestroy(own);
+        }
+    }
+};
+
+static View resident_view(const jcde_resident* r) {
+    View v = base_view(r->e);
+    v.nodes = r->t.nodes;
+    v.entries = r->t.entries;
+    v.edges = r->t.edges;
+    v.haz = r->t.haz;
+    v.hverts = r->t.hverts;
+    v.strength = r->t.strength;
+    v.nedges = r->t.nedges;
+    v.mask = nullptr;
+    v.n_slots = r->t.key_cap;
+    v.exterior = r->exterior;
+    return v;
+}
+
+static inline uint64_t host_mix64(uint64_t x) {
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+static inline uint64_t host_stream_key(uint64_t seed, uint64_t sid) {
+    return host_mix64(seed * 0x100000001B3ull + sid * 0x9E3779B97F4A7C15ull);
+}
+
+// The resident's ordering buffers hold a batch of n queries (growing them waits for queued work).
+static jcde_status ensure_order_buffers(jcde_resident* r, uint32_t n) {
+    if (!r->d_hist.ensure(N_BUCKETS * 4)) return JCDE_ERR_CUDA;
+    if (r->d_order.cap < (size_t)n * 4) {
+        if (r->last) CUDA_TRY(cudaStreamSynchronize(r->last));
+        if (!r->d_order.ensure((size_t)n * 4)) return JCDE_ERR_CUDA;
+    }
+    return JCDE_OK;
+}
+
+static void resident_detect(jcde_resident* r, const uint32_t* q, uint32_t n, uint8_t* dout, cudaStream_t s) {
+    jcde_engine* e = r->e;
+    const View v = resident_view(r);
+    const uint32_t* order = nullptr;
+    if (JCDE_SPATIAL_ORDER && n >= ORDER_MIN_BATCH)
+        order = spatial_order_into(e, q, n, s, r->d_hist.as<uint32_t>(), r->d_order.as<uint32_t>());
+    launch_passes(e, v, q, n, dout, s, RawShape{}, 3, order);
+    r->launches += (order ? 3 : 0) + 2;
+}
+
+// One step of the LBF-style build: 8 launches (generate, order x3, surrogate, polygon, select, commit).
+static void lbf_step(jcde_resident* r, cudaStream_t s) {
+    jcde_engine* e = r->e;
+    LbfDev* st = r->d_lbf.as<LbfDev>();
+    uint32_t* cand = r->d_cand.as<uint32_t>();
+    uint8_t* verd = r->d_verd.as<uint8_t>();
+    res_launch_lbf_gen(r->lp, st, cand, e->n_sms, s);
+    resident_detect(r, cand, r->lp.n_cand, verd, s);
+    const View v = resident_view(r);
+    const uint32_t grid = std::min<uint32_t>((r->lp.n_cand + 7) / 8, (uint32_t)e->n_sms * 8);
+    k_lbf_select<<<grid, 256, 0, s>>>(v, cand, verd, r->lp.n_cand, &st->best, &st->n_free);
+    LbfLogs logs{r->d_place.as<uint32_t>(), r->d_remv.as<uint32_t>(), r->d_free.as<uint32_t>(),
+                 r->d_live.as<uint32_t>(), r->lp.vlog_steps ? r->d_vlog.as<uint8_t>() : nullptr};
+    res_launch_lbf_commit(r->t, e->d_items.as<DItem>(), e->d_iverts.as<float2>(), (uint32_t)e->items.size(), r->lp,
+                          st, cand, verd, logs, s);
+    r->launches += 3;
+}
+
+extern "C" {
+
+void jcde_resident_default_config(jcde_resident_config* c) {
+    if (!c) return;
+    std::memset(c, 0, sizeof(*c));
+    c->max_entries = 1u << 21;
+    c->max_edges = 1u << 23;
+    c->max_hazard_vertices = 1u << 22;
+    c->max_keys = 1u << 20;
+    c->max_tasks = 1u << 16;
+}
+
+jcde_status jcde_resident_create(jcde_engine* e, const jcde_resident_config* cfg, jcde_resident** out) {
+    if (!e || !out) return JCDE_ERR_ARG;
+    *out = nullptr;
+    jcde_resident_config c;
+    jcde_resident_default_config(&c);
+    if (cfg) {
+        if (cfg->max_nodes) c.max_nodes = cfg->max_nodes;
+        if (cfg->max_entries) c.max_entries = cfg->max_entries;
+        if (cfg->max_edges) c.max_edges = cfg->max_edges;
+        if (cfg->max_hazard_vertices) c.max_hazard_vertices = cfg->max_hazard_vertices;
+        if (cfg->max_keys) c.max_keys = cfg->max_keys;
+        if (cfg->max_tasks) c.max_tasks = cfg->max_tasks;
+    }
+    if (!c.max_nodes) {   // every node of a full tree of the engine's depth, at most 2^22
+        uint64_t full = 0, lv = 1;
+        for (int d = 0; d <= e->cfg.quadtree_depth && full < (1u << 22); d++, lv *= 4) full += lv;
+        c.max_nodes = (uint32_t)std::min<uint64_t>(full, 1u << 22);
+    }
+    const auto& hs = e->tree.hazards();
+    if (c.max_keys < e->tree.n_slots() || c.max_nodes < 1) return JCDE_ERR_CAPACITY;
+    jcde_status st = sync_device(e);
+    if (st) return st;
+    init_launch_shape(e);
+    jcde_resident* r = new (std::nothrow) jcde_resident();
+    if (!r) return JCDE_ERR_CUDA;
+    r->e = e;
+    r->exterior = e->tree.exterior_key();
+    RTree& t = r->t;
+    const uint32_t nq = c.max_nodes / 4 + 1;
+    bool ok = r->d_nodes.ensure((size_t)c.max_nodes * sizeof(DNode)) && r->d_ncap.ensure((size_t)c.max_nodes * 4) &&
+              r->d_level.ensure(c.max_nodes) && r->d_strength.ensure(c.max_nodes) &&
+              r->d_nedges.ensure((size_t)c.max_nodes * 4) &&
+              r->d_entries.ensure((size_t)c.max_entries * sizeof(DEntry)) &&
+              r->d_edges.ensure((size_t)c.max_edges * sizeof(float4)) &&
+              r->d_haz.ensure((size_t)c.max_keys * sizeof(DHaz)) &&
+              r->d_hverts.ensure((size_t)c.max_hazard_vertices * sizeof(float2)) && r->d_alive.ensure(c.max_keys) &&
+              r->d_qfree.ensure((size_t)nq * 4) && r->d_kfree.ensure((size_t)c.max_keys * 4) &&
+              r->d_tasks.ensure((size_t)c.max_tasks * sizeof(RTask)) && r->d_ctl.ensure(sizeof(RCtl));
+    if (!ok || cudaStreamCreateWithFlags(&r->own, cudaStreamNonBlocking) != cudaSuccess) {
+        delete r;
+        return JCDE_ERR_CUDA;
+    }
+    t.nodes = r->d_nodes.as<DNode>();
+    t.ncap = r->d_ncap.as<uint32_t>();
+    t.level = r->d_level.as<uint8_t>();
+    t.strength = r->d_strength.as<uint8_t>();
+    t.nedges = r->d_nedges.as<uint32_t>();
+    t.entries = r->d_entries.as<DEntry>();
+    t.edges = r->d_edges.as<float4>();
+    t.haz = r->d_haz.as<DHaz>();
+    t.hverts = r->d_hverts.as<float2>();
+    t.alive = r->d_alive.as<uint8_t>();
+    t.qfree = r->d_qfree.as<int32_t>();
+    t.kfree = r->d_kfree.as<uint32_t>();
+    t.tasks = r->d_tasks.as<RTask>();
+    t.ctl = r->d_ctl.as<RCtl>();
+    t.node_cap = c.max_nodes;
+    t.entry_cap = c.max_entries;
+    t.edge_cap = c.max_edges;
+    t.hvert_cap = c.max_hazard_vertices;
+    t.key_cap = c.max_keys;
+    t.task_cap = c.max_tasks;
+    t.cde = e->tree.bbox();
+    t.depth = e->cfg.quadtree_depth;
+    // the engine's live hazards, each under its own key
+    std::vector<float2> verts;
+    std::vector<uint4> recs;
+    std::vector<float2> pois;
+    for (uint32_t k = 0; k < hs.size(); k++) {
+        if (!hs[k].alive) continue;
+        const Polygon& p = hs[k].shape;
+        recs.push_back(make_uint4(k, (uint32_t)hs[k].kind, (uint32_t)verts.size(), (uint32_t)p.v.size()));
+        pois.push_back(make_float2(p.poi.c.x, p.poi.c.y));
+        for (const Pt& v : p.v) verts.push_back(make_float2(v.x, v.y));
+    }
+    const std::vector<uint32_t>& fk = e->tree.free_keys();
+    DevBuf d_v, d_r, d_p, d_k;
+    cudaStream_t s = r->own;
+    ok = d_v.ensure(std::max<size_t>(verts.size(), 1) * sizeof(float2)) &&
+         d_r.ensure(std::max<size_t>(recs.size(), 1) * sizeof(uint4)) &&
+         d_p.ensure(std::max<size_t>(pois.size(), 1) * sizeof(float2)) && d_k.ensure(std::max<size_t>(fk.size(), 1) * 4);
+    if (!ok || cudaMemsetAsync(t.alive, 0, c.max_keys, s) != cudaSuccess ||
+        cudaMemsetAsync(t.ctl, 0, sizeof(RCtl), s) != cudaSuccess ||
+        (verts.size() && cudaMemcpyAsync(d_v.p, verts.data(), verts.size() * sizeof(float2), cudaMemcpyHostToDevice, s)) ||
+        (recs.size() && cudaMemcpyAsync(d_r.p, recs.data(), recs.size() * sizeof(uint4), cudaMemcpyHostToDevice, s)) ||
+        (pois.size() && cudaMemcpyAsync(d_p.p, pois.data(), pois.size() * sizeof(float2), cudaMemcpyHostToDevice, s)) ||
+        (fk.size() && cudaMemcpyAsync(d_k.p, fk.data(), fk.size() * 4, cudaMemcpyHostToDevice, s))) {
+        delete r;
+        return JCDE_ERR_CUDA;
+    }
+    res_launch_init(t, d_v.as<float2>(), d_r.as<uint4>(), d_p.as<float2>(), (uint32_t)recs.size(), e->tree.n_slots(),
+                    d_k.as<uint32_t>(), (uint32_t)fk.size(), s);
+    RCtl ctl{};
+    if (cudaGetLastError() != cudaSuccess || cudaMemcpyAsync(&ctl, t.ctl, sizeof(RCtl), cudaMemcpyDeviceToHost, s) ||
+        cudaStreamSynchronize(s) != cudaSuccess) {
+        delete r;
+        return JCDE_ERR_CUDA;
+    }
+    r->launches++;
+    if (ctl.error) {
+        delete r;
+        return JCDE_ERR_CAPACITY;
+    }
+    *out = r;
+    return JCDE_OK;
+}
+
+void jcde_resident_destroy(jcde_resident* r) { delete r; }
+
+jcde_status jcde_resident_register_placed(jcde_resident* r, const jcde_query* d_query, uint32_t* d_key, void* stream) {
+    if (!r || !d_query) return JCDE_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    jcde_engine* e = r->e;
+    res_launch_insert_placed(r->t, e->d_items.as<DItem>(), e->d_iverts.as<float2>(), (uint32_t)e->items.size(),
+                             reinterpret_cast<const uint32_t*>(d_query), d_key, s);
+    CUDA_TRY(cudaGetLastError());
+    r->launches++;
+    r->last = s;
+    return JCDE_OK;
+}
+
+jcde_status jcde_resident_deregister(jcde_resident* r, const uint32_t* d_key, void* stream) {
+    if (!r || !d_key) return JCDE_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    res_launch_remove(r->t, d_key, s);
+    CUDA_TRY(cudaGetLastError());
+    r->launches++;
+    r->last = s;
+    return JCDE_OK;
+}
+
+jcde_status jcde_resident_detect_batch(jcde_resident* r, const jcde_query* d_queries, uint32_t n, uint8_t* d_out,
+                                       void* stream) {
+    if (!r || (n && (!d_queries || !d_out))) return JCDE_ERR_ARG;
+    if (n == 0) return JCDE_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    jcde_status st = ensure_order_buffers(r, n);
+    if (st) return st;
+    resident_detect(r, reinterpret_cast<const uint32_t*>(d_queries), n, d_out, s);
+    CUDA_TRY(cudaGetLastError());
+    r->e->last_stream = s;
+    r->e->have_last_stream = true;
+    r->last = s;
+    return JCDE_OK;
+}
+
+jcde_status jcde_resident_status(jcde_resident* r, uint32_t* out8) {
+    if (!r || !out8) return JCDE_ERR_ARG;
+    if (r->last) CUDA_TRY(cudaStreamSynchronize(r->last));
+    RCtl c{};
+    CUDA_TRY(cudaMemcpy(&c, r->t.ctl, sizeof(RCtl), cudaMemcpyDeviceToHost));
+    const uint32_t v[8] = {c.error, c.not_found, c.n_live, c.n_slots, c.n_nodes, c.entry_top, c.edge_top, c.hvert_top};
+    std::memcpy(out8, v, sizeof(v));
+    return c.error ? JCDE_ERR_CAPACITY : JCDE_OK;
+}
+
+jcde_status jcde_resident_tree_dump(jcde_resident* r, uint32_t* out, uint64_t cap, uint64_t* n_words) {
+    if (!r || !n_words) return JCDE_ERR_ARG;
+    if (r->last) CUDA_TRY(cudaStreamSynchronize(r->last));
+    RCtl c{};
+    CUDA_TRY(cudaMemcpy(&c, r->t.ctl, sizeof(RCtl), cudaMemcpyDeviceToHost));
+    std::vector<DNode> nodes(c.n_nodes);
+    std::vector<uint8_t> level(c.n_nodes);
+    std::vector<uint32_t> nedges(c.n_nodes);
+    std::vector<DEntry> ents(c.entry_top);
+    std::vector<float4> edges(c.edge_top);
+    CUDA_TRY(cudaMemcpy(nodes.data(), r->t.nodes, nodes.size() * sizeof(DNode), cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(level.data(), r->t.level, level.size(), cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(nedges.data(), r->t.nedges, nedges.size() * 4, cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(ents.data(), r->t.entries, ents.size() * sizeof(DEntry), cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(edges.data(), r->t.edges, edges.size() * sizeof(float4), cudaMemcpyDeviceToHost));
+    // the canonical form of QuadTree::dump: depth-first, entries by key, edges sorted
+    std::vector<uint32_t> o;
+    auto fb = [](float f) {
+        uint32_t u;
+        std::memcpy(&u, &f, 4);
+        return u;
+    };
+    auto box = [&](const Box& b) {
+        o.push_back(fb(b.x0));
+        o.push_back(fb(b.y0));
+        o.push_back(fb(b.x1));
+        o.push_back(fb(b.y1));
+    };
+    std::vector<int32_t> stack{0};
+    while (!stack.empty()) {
+        const int32_t ni = stack.back();
+        stack.pop_back();
+        if (ni < 0 || (uint32_t)ni >= c.n_nodes) return JCDE_ERR_STATE;
+        const DNode& n = nodes[ni];
+        o.push_back(level[ni]);
+        o.push_back(n.child >= 0 ? 1u : 0u);
+        o.push_back(n.hz_cnt);
+        o.push_back(nedges[ni]);
+        box(n.box);
+        if (n.hz_off + (uint64_t)n.hz_cnt > ents.size()) return JCDE_ERR_STATE;
+        std::vector<const DEntry*> hs;
+        for (uint32_t k = 0; k < n.hz_cnt; k++) hs.push_back(&ents[n.hz_off + k]);
+        std::sort(hs.begin(), hs.end(), [](const DEntry* a, const DEntry* b) { return a->hkey < b->hkey; });
+        for (const DEntry* h : hs) {
+            o.push_back(h->hkey);
+            o.push_back(h->presence);
+            if (h->presence == PRES_PARTIAL) {
+                box(h->ff);
+                if (h->edge_off + (uint64_t)h->edge_cnt > edges.size()) return JCDE_ERR_STATE;
+                std::vector<std::array<uint32_t, 4>> es;
+                for (uint32_t j = 0; j < h->edge_cnt; j++) {
+                    const float4 f = edges[h->edge_off + j];
+                    es.push_back({fb(f.x), fb(f.y), fb(f.z), fb(f.w)});
+                }
+                std::sort(es.begin(), es.end());
+                o.push_back((uint32_t)es.size());
+                for (auto& e4 : es) o.insert(o.end(), e4.begin(), e4.end());
+            }
+        }
+        if (n.child >= 0)
+            for (int i = 3; i >= 0; i--) stack.push_back(n.child + i);
+    }
+    *n_words = o.size();
+    if (!out || cap < o.size()) return out ? JCDE_ERR_CAPACITY : JCDE_OK;
+    std::memcpy(out, o.data(), o.size() * 4);
+    return JCDE_OK;
+}
+
+uint64_t jcde_resident_kernel_launches(const jcde_resident* r) { return r ? r->launches : 0; }
+
+jcde_status jcde_lbf_begin(jcde_resident* r, const jcde_lbf_params* p) {
+    if (!r || !p || !p->n_candidates || !p->n_types || !p->max_steps) return JCDE_ERR_ARG;
+    if (p->n_types > r->e->items.size()) return JCDE_ERR_ARG;
+    const jcde_rect b = p->sample_box;
+    if (!(b.x_min < b.x_max && b.y_min < b.y_max)) return JCDE_ERR_ARG;
+    if (r->last) CUDA_TRY(cudaStreamSynchronize(r->last));
+    LbfParams& lp = r->lp;
+    lp = LbfParams{};
+    lp.seed = p->seed;
+    lp.key_types = host_stream_key(p->seed, 2);
+    lp.key_remove = host_stream_key(p->seed, 4);
+    lp.sid_base = 10000;
+    lp.n_cand = p->n_candidates;
+    lp.n_types = p->n_types;
+    lp.remove_every = p->remove_every;
+    lp.max_steps = p->max_steps;
+    lp.vlog_steps = std::min(p->verdict_log_steps, p->max_steps);
+    lp.x0 = b.x_min;
+    lp.y0 = b.y_min;
+    lp.x1 = b.x_max;
+    lp.y1 = b.y_max;
+    lp.x1_below = std::nextafter(b.x_max, b.x_min);
+    lp.y1_below = std::nextafter(b.y_max, b.y_min);
+    const size_t n = p->n_candidates, ms = p->max_steps;
+    const bool ok = r->d_lbf.ensure(sizeof(LbfDev)) && r->d_cand.ensure(n * 20) && r->d_verd.ensure(n) &&
+                    r->d_place.ensure(ms * 32) && r->d_remv.ensure(ms * 8) && r->d_free.ensure(ms * 4) &&
+                    r->d_live.ensure(ms * 4) && (!lp.vlog_steps || r->d_vlog.ensure((size_t)lp.vlog_steps * n));
+    if (!ok) return JCDE_ERR_CUDA;
+    CUDA_TRY(cudaMemset(r->d_lbf.p, 0, sizeof(LbfDev)));
+    if (r->exec) {
+        cudaGraphExecDestroy(r->exec);
+        r->exec = nullptr;
+    }
+    jcde_status st = ensure_order_buffers(r, p->n_candidates);
+    if (st) return st;
+    r->lbf_ready = true;
+    return JCDE_OK;
+}
+
+jcde_status jcde_lbf_steps(jcde_resident* r, uint32_t n_steps, uint32_t steps_per_graph, void* stream) {
+    if (!r || !r->lbf_ready) return JCDE_ERR_STATE;
+    cudaStream_t s = stream ? (cudaStream_t)stream : r->own;
+    jcde_engine* e = r->e;
+    const bool prof = e->prof;
+    e->prof = false;   // per-kernel events are not recorded inside graphs
+    uint32_t done = 0;
+    if (steps_per_graph > 0 && n_steps >= steps_per_graph) {
+        if (!r->exec || r->exec_steps != steps_per_graph || r->exec_stream != s) {
+            if (r->exec) {
+                cudaGraphExecDestroy(r->exec);
+                r->exec = nullptr;
+            }
+            cudaGraph_t g = nullptr;
+            if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+                e->prof = prof;
+                return JCDE_ERR_CUDA;
+            }
+            const uint64_t before = r->launches;
+            for (uint32_t i = 0; i < steps_per_graph; i++) lbf_step(r, s);
+            r->launches = before;
+            cudaError_t ce = cudaStreamEndCapture(s, &g);
+            if (ce == cudaSuccess && g) ce = cudaGraphInstantiate(&r->exec, g, 0);
+            if (g) cudaGraphDestroy(g);
+            if (ce != cudaSuccess) {
+                r->exec = nullptr;
+                e->prof = prof;
+                return JCDE_ERR_CUDA;
+            }
+            r->exec_steps = steps_per_graph;
+            r->exec_stream = s;
+        }
+        for (; done + steps_per_graph <= n_steps; done += steps_per_graph) {
+            if (cudaGraphLaunch(r->exec, s) != cudaSuccess) {
+                e->prof = prof;
+                return JCDE_ERR_CUDA;
+            }
+            r->launches += 8ull * steps_per_graph;
+        }
+    }
+    for (; done < n_steps; done++) lbf_step(r, s);
+    e->prof = prof;
+    CUDA_TRY(cudaGetLastError());
+    r->last = s;
+    e->last_stream = s;
+    e->have_last_stream = true;
+    return JCDE_OK;
+}
+
+jcde_status jcde_lbf_read(jcde_resident* r, uint32_t* counts4, uint32_t* placements, uint32_t place_cap,
+                          uint32_t* removals, uint32_t removal_cap, uint32_t* free_counts, uint32_t free_cap,
+                          uint8_t* verdicts, uint64_t verdict_cap) {
+    if (!r || !counts4) return JCDE_ERR_ARG;
+    if (!r->lbf_ready) return JCDE_ERR_STATE;
+    if (r->last) CUDA_TRY(cudaStreamSynchronize(r->last));
+    LbfDev d{};
+    CUDA_TRY(cudaMemcpy(&d, r->d_lbf.p, sizeof(LbfDev), cudaMemcpyDeviceToHost));
+    counts4[0] = d.step;
+    counts4[1] = d.n_placed;
+    counts4[2] = d.n_removed;
+    counts4[3] = d.n_live;
+    if (placements && place_cap)
+        CUDA_TRY(cudaMemcpy(placements, r->d_place.p, (size_t)std::min(place_cap, d.n_placed) * 32, cudaMemcpyDeviceToHost));
+    if (removals && removal_cap)
+        CUDA_TRY(cudaMemcpy(removals, r->d_remv.p, (size_t)std::min(removal_cap, d.n_removed) * 8, cudaMemcpyDeviceToHost));
+    if (free_counts && free_cap)
+        CUDA_TRY(cudaMemcpy(free_counts, r->d_free.p, (size_t)std::min(free_cap, d.step) * 4, cudaMemcpyDeviceToHost));
+    if (verdicts && verdict_cap && r->lp.vlog_steps) {
+        const uint64_t have = (uint64_t)std::min(d.step, r->lp.vlog_steps) * r->lp.n_cand;
+        CUDA_TRY(cudaMemcpy(verdicts, r->d_vlog.p, std::min(verdict_cap, have), cudaMemcpyDeviceToHost));
+    }
+    RCtl c{};
+    CUDA_TRY(cudaMemcpy(&c, r->t.ctl, sizeof(RCtl), cudaMemcpyDeviceToHost));
+    return c.error ? JCDE_ERR_CAPACITY : JCDE_OK;
 }
 
 }  // extern "C"

@@ -1121,6 +1121,34 @@ __global__ void k_resample(const float* __restrict__ params, const uint32_t* __r
     }
 }
 
+// LBF choice over a candidate batch (lbf/src/opt/search.rs:44-66 with LBFLoss, lbf/src/opt/loss.rs):
+// among candidates whose verdict is JCDE_FREE, the smallest cost x_max * 10 + y_max of the
+// transformed shape's bounding box, the lowest index among equal costs (the strict `<` of
+// search.rs:52 keeps the first best).  Costs are mapped to order-preserving integers and
+// packed with the index into one 64-bit atomicMin.
+__device__ __forceinline__ uint32_t orderable(float f) {
+    const uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__global__ void k_lbf_select(View v, const uint32_t* __restrict__ q, const uint8_t* __restrict__ verdicts, uint32_t n,
+                             unsigned long long* __restrict__ best, uint32_t* __restrict__ n_free) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t wpb = blockDim.x >> 5;
+    for (uint32_t qi = blockIdx.x * wpb + warp; qi < n; qi += gridDim.x * wpb) {
+        if (verdicts[qi] != 0) continue;
+        const QueryHead qh = load_query(q, qi, lane);
+        if (qh.item >= v.n_items) continue;
+        const DItem it = v.items[qh.item];
+        const QShape sh{v.iverts + it.v_off, it.v_cnt, qh.c, qh.s, qh.tx, qh.ty, false};
+        const Box b = warp_bbox(sh, lane);
+        const float cost = b.x1 * 10.0f + b.y1;   // LBFLoss::cost (loss.rs:29-31)
+        if (lane == 0) {
+            atomicMin(best, ((unsigned long long)orderable(cost) << 32) | qi);
+            if (n_free) atomicAdd(n_free, 1u);
+        }
+    }
+}
+
 // Strongest presence per node under a filter (QTHazardVec::strongest, qt_hazard_vec.rs:60-63).
 __global__ void k_strength(View v, uint32_t n_nodes, uint8_t* __restrict__ out) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;

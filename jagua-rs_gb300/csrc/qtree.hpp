@@ -95,6 +95,7 @@ class QuadTree {
         return key < haz_.size() && haz_[key].alive ? &haz_[key] : nullptr;
     }
     uint32_t n_slots() const { return (uint32_t)haz_.size(); }
+    const std::vector<uint32_t>& free_keys() const { return free_keys_; }   // next reused key last
     const std::vector<HazardRec>& hazards() const { return haz_; }
     int32_t exterior_key() const { return exterior_; }
     Box bbox() const { return nodes_[0].bbox; }

@@ -1,0 +1,123 @@
+// Device-resident quadtree: the CDE's register / deregister run on the GPU.
+//
+// The image the query kernels walk (kernels.cuh: nodes, per-node hazard entries, edge lists,
+// hazard table) lives in fixed-capacity pools in device memory and is updated in place by
+// single-warp kernels that restate QTNode::register_hazard / deregister_hazard
+// (collision_detection/quadtree/qt_node.rs:38-94) and QTHazard::constrict (qt_hazard.rs:48-167):
+//   * nodes form a pool in which every quartet of children is contiguous and starts at 1 + 4k,
+//     like the host tree's node pool; freed quartets are reused last-in first-out;
+//   * each node owns a slab of entries (an unordered set: a node's answer does not depend on the
+//     order of its hazards), doubled when full; removal swaps in the slab's last entry;
+//   * every Partial entry owns its clipped edge list in the edge pool (a quadrant that keeps all of
+//     its parent's edges shares the parent's list); edge lists are never moved;
+//   * the strongest presence and the active-edge count of every node are kept up to date.
+// Hazard keys follow the host registry: a freed key is reused last-in first-out (slotmap order).
+//
+// The same headers hold the device state of the LBF-style build (lbf/src/opt/search.rs:17-106):
+// candidate generation, the selection of the left-bottom-most free candidate, its registration and
+// the periodic removal of a random placed item, all on the device so that one CUDA graph replays
+// a whole step.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cfloat>
+#include <cmath>
+#include <cstdint>
+
+#include "geom.cuh"
+#include "qtree.hpp"
+
+namespace jcde {
+
+enum : uint32_t {
+    RES_OK = 0,
+    RES_ERR_NODES = 1,
+    RES_ERR_ENTRIES = 2,
+    RES_ERR_EDGES = 3,
+    RES_ERR_HVERTS = 4,
+    RES_ERR_KEYS = 5,
+    RES_ERR_TASKS = 6,
+};
+
+// Allocation state of the pools (device memory; loaded by the update kernels, written back at the end).
+struct RCtl {
+    uint32_t n_nodes;     // high-water mark of the node pool
+    uint32_t n_qfree;     // depth of the free-quartet stack
+    uint32_t entry_top;   // entry pool bump pointer
+    uint32_t edge_top;    // edge pool bump pointer
+    uint32_t hvert_top;   // hazard vertex pool bump pointer
+    uint32_t n_slots;     // hazard key high-water mark
+    uint32_t n_kfree;     // depth of the free-key stack
+    uint32_t error;       // first capacity failure (RES_ERR_*), sticky
+    uint32_t not_found;   // deregistrations of unknown keys, placements of unknown items
+    uint32_t last_key;    // key of the last registration (~0 when it failed)
+    uint32_t n_live;      // registered hazards
+    uint32_t pad[5];
+};
+
+struct RTask {
+    int32_t node;
+    uint32_t kind;
+    uint32_t pad[2];
+    DEntry e;
+};
+
+struct RTree {
+    DNode* nodes;
+    uint32_t* ncap;      // entry slab capacity per node
+    uint8_t* level;
+    uint8_t* strength;   // strongest presence per node (the query kernels' unfiltered strength)
+    uint32_t* nedges;    // active edges per node
+    DEntry* entries;
+    float4* edges;
+    DHaz* haz;
+    float2* hverts;
+    uint8_t* alive;
+    int32_t* qfree;
+    uint32_t* kfree;
+    RTask* tasks;
+    RCtl* ctl;
+    uint32_t node_cap, entry_cap, edge_cap, hvert_cap, key_cap, task_cap;
+    Box cde;
+    uint32_t depth;
+};
+
+// LBF-style build state (device memory).
+struct LbfDev {
+    uint32_t step;        // next step
+    uint32_t n_live;      // placed items not removed
+    uint32_t n_removed;   // removals so far (index of the next removal draw)
+    uint32_t n_placed;
+    unsigned long long best;   // (order-preserving cost bits << 32) | candidate, ~0 = none free
+    uint32_t n_free;           // free candidates of the current step
+    uint32_t pad[9];
+};
+
+struct LbfParams {
+    unsigned long long seed;   // candidate stream of step s: (seed, sid_base + s)
+    unsigned long long key_types, key_remove;   // stream keys of the type and removal draws
+    uint32_t sid_base, n_cand, n_types, remove_every, max_steps, vlog_steps;
+    float x0, y0, x1, y1;      // sampling box of the translations
+    float x1_below, y1_below;  // the largest float32 below x1 / y1 (draws stay inside the box)
+};
+
+struct LbfLogs {
+    uint32_t* placements;   // 8 words per placement: step, key, candidate, item, cos, sin, tx, ty (bits)
+    uint32_t* removals;     // 2 words per removal: step, key
+    uint32_t* free_counts;  // free candidates per step
+    uint32_t* live;         // keys of the placed items, in placement order
+    uint8_t* vlog;          // verdicts of the first vlog_steps steps (optional)
+};
+
+// Host-side launchers (resident.cu).  All launch one warp unless stated.
+void res_launch_init(const RTree& t, const float2* verts, const uint4* recs, const float2* pois, uint32_t n,
+                     uint32_t n_slots, const uint32_t* kfree, uint32_t n_kfree, cudaStream_t s);
+void res_launch_insert_placed(const RTree& t, const DItem* items, const float2* iverts, uint32_t n_items,
+                              const uint32_t* q, uint32_t* out_key, cudaStream_t s);
+void res_launch_remove(const RTree& t, const uint32_t* key, cudaStream_t s);
+void res_launch_lbf_gen(const LbfParams& p, LbfDev* st, uint32_t* q, int n_sms, cudaStream_t s);
+void res_launch_lbf_commit(const RTree& t, const DItem* items, const float2* iverts, uint32_t n_items,
+                           const LbfParams& p, LbfDev* st, const uint32_t* q, const uint8_t* verdicts,
+                           const LbfLogs& logs, cudaStream_t s);
+
+}  // namespace jcde

@@ -5,7 +5,8 @@ GPU memory and detect / collect queries run as hand-written sm_103a kernels behi
 ``include/jcde.h``.  This package is the Python host side over that ABI.
 """
 from ._ffi import JcdeError, build, lib
-from .engine import CDEConfig, CDEngine, GpuBackend, GpuEngine, Hazard, MultiEngine, spolygon_new, surrogate_poles
+from .engine import (CDEConfig, CDEngine, GpuBackend, GpuEngine, Hazard, MultiEngine, ResidentEngine, spolygon_new,
+                     surrogate_poles)
 from .workload import QUERY_DTYPE
 
 __all__ = [
@@ -15,6 +16,7 @@ __all__ = [
     "GpuEngine",
     "Hazard",
     "MultiEngine",
+    "ResidentEngine",
     "JcdeError",
     "QUERY_DTYPE",
     "build",

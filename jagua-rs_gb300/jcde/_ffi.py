@@ -22,6 +22,17 @@ class jcde_rect(C.Structure):
     _fields_ = [("x_min", C.c_float), ("y_min", C.c_float), ("x_max", C.c_float), ("y_max", C.c_float)]
 
 
+class jcde_resident_config(C.Structure):
+    _fields_ = [("max_nodes", C.c_uint32), ("max_entries", C.c_uint32), ("max_edges", C.c_uint32),
+                ("max_hazard_vertices", C.c_uint32), ("max_keys", C.c_uint32), ("max_tasks", C.c_uint32)]
+
+
+class jcde_lbf_params(C.Structure):
+    _fields_ = [("seed", C.c_uint64), ("n_candidates", C.c_uint32), ("n_types", C.c_uint32),
+                ("remove_every", C.c_uint32), ("max_steps", C.c_uint32), ("verdict_log_steps", C.c_uint32),
+                ("reserved", C.c_uint32), ("sample_box", jcde_rect)]
+
+
 class jcde_config(C.Structure):
     _fields_ = [
         ("quadtree_depth", C.c_uint8),
@@ -88,6 +99,19 @@ SIGNATURES = {
     "jcde_profile_enable": (C.c_int32, [P, C.c_int]),
     "jcde_multi_create": (C.c_int32, [C.POINTER(P), C.c_uint32, C.POINTER(P)]),
     "jcde_set_hazard_poles": (C.c_int32, [P, C.c_uint32, f32p, C.c_uint32]),
+    "jcde_resident_default_config": (None, [P]),
+    "jcde_resident_create": (C.c_int32, [P, P, P]),
+    "jcde_resident_destroy": (None, [P]),
+    "jcde_resident_register_placed": (C.c_int32, [P, P, P, P]),
+    "jcde_resident_deregister": (C.c_int32, [P, P, P]),
+    "jcde_resident_detect_batch": (C.c_int32, [P, P, C.c_uint32, P, P]),
+    "jcde_resident_status": (C.c_int32, [P, u32p]),
+    "jcde_resident_tree_dump": (C.c_int32, [P, u32p, C.c_uint64, C.POINTER(C.c_uint64)]),
+    "jcde_resident_kernel_launches": (C.c_uint64, [P]),
+    "jcde_lbf_begin": (C.c_int32, [P, P]),
+    "jcde_lbf_steps": (C.c_int32, [P, C.c_uint32, C.c_uint32, P]),
+    "jcde_lbf_read": (C.c_int32, [P, u32p, u32p, C.c_uint32, u32p, C.c_uint32, u32p, C.c_uint32, P, C.c_uint64]),
+    "jcde_lbf_select": (C.c_int32, [P, P, P, C.c_uint32, P, P]),
     "jcde_proxy_batch": (C.c_int32, [P, P, P, C.c_uint32, C.POINTER(jcde_filter), P, P, P]),
     "jcde_separate_batch": (C.c_int32, [P, P, P, C.c_uint32, C.c_uint32, C.c_float, C.c_float, C.c_float, C.POINTER(jcde_filter), P, P, P]),
     "jcde_resample_batch": (C.c_int32, [P, P, P, C.c_uint32, C.c_uint32, C.c_float, C.c_float, C.c_uint32, P, P]),

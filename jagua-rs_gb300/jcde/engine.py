@@ -16,7 +16,7 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _ffi
-from ._ffi import check, jcde_config, jcde_filter, jcde_hazard, jcde_rect, lib
+from ._ffi import check, jcde_config, jcde_filter, jcde_hazard, jcde_lbf_params, jcde_rect, jcde_resident_config, lib
 from .workload import QUERY_DTYPE
 
 PLACED_ITEM, EXTERIOR, HOLE, QUALITY_ZONE = 0, 1, 2, 3
@@ -459,3 +459,111 @@ class MultiEngine:
 
     def kernel_launches(self) -> int:
         return int(lib().jcde_multi_kernel_launches(self.h))
+
+
+
+class ResidentEngine:
+    """An engine's quadtree resident in device memory, updated by register / deregister kernels
+    (jcde_resident_*), plus the on-device LBF-style build that runs on it (jcde_lbf_*)."""
+
+    def __init__(self, engine: CDEngine, **capacities):
+        cfg = jcde_resident_config()
+        lib().jcde_resident_default_config(C.byref(cfg))
+        for k, v in capacities.items():
+            setattr(cfg, k, int(v))
+        h = C.c_void_p()
+        check(lib().jcde_resident_create(engine.h, C.byref(cfg), C.byref(h)), "resident_create")
+        self.h = h
+        self.engine = engine   # items and staging are shared with the engine
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            try:
+                lib().jcde_resident_destroy(self.h)
+            except Exception:
+                pass
+            self.h = None
+
+    def register_placed(self, query, key_out=None, stream=None) -> None:
+        """query: CUDA uint8 tensor holding one packed query; key_out: CUDA int32 tensor of 1 or None."""
+        check(lib().jcde_resident_register_placed(self.h, query.data_ptr(),
+                                                  None if key_out is None else key_out.data_ptr(),
+                                                  _stream_handle(stream)), "resident_register_placed")
+
+    def deregister(self, key, stream=None) -> None:
+        """key: CUDA int32 tensor of 1."""
+        check(lib().jcde_resident_deregister(self.h, key.data_ptr(), _stream_handle(stream)), "resident_deregister")
+
+    def detect_batch(self, queries, out=None, stream=None):
+        import torch
+
+        n = queries.numel() // QUERY_DTYPE.itemsize
+        if out is None:
+            out = torch.empty(n, dtype=torch.uint8, device=queries.device)
+        check(lib().jcde_resident_detect_batch(self.h, queries.data_ptr(), n, out.data_ptr(), _stream_handle(stream)),
+              "resident_detect_batch")
+        return out
+
+    def status(self) -> dict:
+        a = (C.c_uint32 * 8)()
+        st = lib().jcde_resident_status(self.h, a)
+        names = ("error", "not_found", "n_live", "n_slots", "n_nodes", "entries", "edges", "hazard_vertices")
+        d = dict(zip(names, (int(x) for x in a)))
+        d["status"] = int(st)
+        return d
+
+    def tree_dump(self) -> np.ndarray:
+        n = C.c_uint64()
+        check(lib().jcde_resident_tree_dump(self.h, None, 0, C.byref(n)), "resident_tree_dump")
+        out = np.zeros(n.value, dtype=np.uint32)
+        check(lib().jcde_resident_tree_dump(self.h, out.ctypes.data_as(C.POINTER(C.c_uint32)), n.value, C.byref(n)),
+              "resident_tree_dump")
+        return out
+
+    def kernel_launches(self) -> int:
+        return int(lib().jcde_resident_kernel_launches(self.h))
+
+    def lbf_begin(self, seed, n_candidates, n_types, remove_every, max_steps, sample_box, verdict_log_steps=0):
+        p = jcde_lbf_params()
+        p.seed = int(seed)
+        p.n_candidates = int(n_candidates)
+        p.n_types = int(n_types)
+        p.remove_every = int(remove_every)
+        p.max_steps = int(max_steps)
+        p.verdict_log_steps = int(verdict_log_steps)
+        b = np.asarray(sample_box, dtype=np.float32)
+        p.sample_box = jcde_rect(*[float(x) for x in b])
+        self._lbf = p
+        check(lib().jcde_lbf_begin(self.h, C.byref(p)), "lbf_begin")
+
+    def lbf_steps(self, n_steps, steps_per_graph=0, stream=None) -> None:
+        check(lib().jcde_lbf_steps(self.h, int(n_steps), int(steps_per_graph), _stream_handle(stream)), "lbf_steps")
+
+    def lbf_read(self) -> dict:
+        p = self._lbf
+        counts = np.zeros(4, dtype=np.uint32)
+        u32 = C.POINTER(C.c_uint32)
+        pl = np.zeros((p.max_steps, 8), dtype=np.uint32)
+        rm = np.zeros((p.max_steps, 2), dtype=np.uint32)
+        fc = np.zeros(p.max_steps, dtype=np.uint32)
+        vl = np.zeros(max(1, p.verdict_log_steps * p.n_candidates), dtype=np.uint8)
+        check(lib().jcde_lbf_read(self.h, counts.ctypes.data_as(u32), pl.ctypes.data_as(u32), p.max_steps,
+                                  rm.ctypes.data_as(u32), p.max_steps, fc.ctypes.data_as(u32), p.max_steps,
+                                  vl.ctypes.data, vl.size if p.verdict_log_steps else 0), "lbf_read")
+        steps, n_pl, n_rm = int(counts[0]), int(counts[1]), int(counts[2])
+        nv = min(steps, p.verdict_log_steps)
+        return {"steps": steps, "placements": pl[:n_pl], "removals": rm[:n_rm], "free_counts": fc[:steps],
+                "n_live": int(counts[3]), "verdicts": vl[: nv * p.n_candidates].reshape(nv, p.n_candidates)}
+
+
+def lbf_select(eng: "GpuEngine", q, verdicts) -> int:
+    """The LBF choice of a candidate batch on the device (jcde_lbf_select): index or -1."""
+    import torch
+
+    dq = torch.from_numpy(np.ascontiguousarray(q, dtype=QUERY_DTYPE).view(np.uint8).copy()).cuda()
+    dv = torch.from_numpy(np.ascontiguousarray(verdicts, dtype=np.uint8)).cuda()
+    best = torch.empty(1, dtype=torch.int64, device="cuda")
+    check(lib().jcde_lbf_select(eng.eng.h, dq.data_ptr(), dv.data_ptr(), len(q), best.data_ptr(),
+                                _stream_handle(None)), "lbf_select")
+    b = int(best.item()) & 0xFFFFFFFFFFFFFFFF
+    return -1 if b == 0xFFFFFFFFFFFFFFFF else int(b & 0xFFFFFFFF)

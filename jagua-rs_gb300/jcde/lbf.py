@@ -1,0 +1,169 @@
+"""LBF-style incremental build over the engine (the caller of the CDE in lbf/src/opt/search.rs).
+
+Each step draws an item type and a batch of candidate placements, asks the engine for their
+verdicts, commits the candidate with the lowest LBF cost among the free ones
+(LBFLoss::cost = x_max * 10 + y_max of the placed shape's bounding box, lbf/src/opt/loss.rs:29-31;
+ties keep the first, search.rs:52) by registering it as a hazard, and every `remove_every` steps
+deregisters a random placed item (as Layout::remove_item does, entities/layout.rs:88-100).
+
+Differences from lbf's search, chosen so that every engine sees the same candidates: the
+candidates of a step are drawn up front from a seeded stream (no sampling-box tightening between
+samples, search.rs:63-64, and no local-search phase, search.rs:80-101), uniformly over the strip.
+
+Two drivers share the definition: `run_host` (one engine call per step from Python: the oracle,
+or the GPU engine with host-side registration) and `run_device` (jcde_lbf_*: generation, verdicts,
+choice, registration and removal all on the GPU, no host round trip per step).  Both return the
+same log: placements (step, key, candidate, item, cos, sin, tx, ty as float32 bits), removals
+(step, key) and free-candidate counts per step.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import workload as W
+
+SEED = 0xC3
+TYPE_SID, REMOVE_SID, CAND_SID_BASE = 2, 4, 10_000   # stream ids of the driver's draws
+
+
+@dataclass
+class LbfSpec:
+    """The strip build: 60 star types of 8-120 vertices, a 20000 x 2000 strip, 16384 candidates per step."""
+
+    seed: int = SEED
+    n_types: int = 60
+    v_range: tuple = (8, 120)
+    r_range: tuple = (20.0, 60.0)
+    width: float = 20000.0
+    height: float = 2000.0
+    steps: int = 2000
+    n_cand: int = 16384
+    remove_every: int = 50
+    depth: int = W.DEFAULT_DEPTH
+    cd_threshold: int = W.DEFAULT_CD_THRESHOLD
+
+    @property
+    def box(self) -> np.ndarray:
+        return np.array([0.0, 0.0, self.width, self.height], np.float32)
+
+
+@dataclass
+class LbfLog:
+    placements: np.ndarray   # (n, 8) uint32
+    removals: np.ndarray     # (m, 2) uint32
+    free_counts: np.ndarray  # (steps,) uint32
+    verdicts: list = field(default_factory=list)   # per-step verdict arrays (host driver, if kept)
+
+    def same_as(self, other: "LbfLog") -> bool:
+        return (np.array_equal(self.placements, other.placements) and np.array_equal(self.removals, other.removals)
+                and np.array_equal(self.free_counts, other.free_counts))
+
+
+def lbf_cost(xy: np.ndarray) -> np.float32:
+    """LBFLoss::cost of a placed shape (loss.rs:29-31) in float32."""
+    return np.float32(np.float32(xy[:, 0].max()) * np.float32(10.0) + np.float32(xy[:, 1].max()))
+
+
+def select_host(items, q: np.ndarray, verdicts: np.ndarray) -> int:
+    """The LBF choice on the host: index of the free candidate of least cost, first on ties, or -1.
+
+    The transformation is TRANSFORM_FORMULA in float32 (workload.transform_points), vectorised over
+    the candidates; min/max and the argmin's first-occurrence rule are exact."""
+    free = np.flatnonzero(verdicts == 0)
+    if len(free) == 0:
+        return -1
+    costs = np.empty(len(free), dtype=np.float32)
+    item_ids = q["item"][free]
+    for t in np.unique(item_ids):
+        sel = np.flatnonzero(item_ids == t)
+        rows = q[free[sel]]
+        xy = np.asarray(items[int(t)].xy, dtype=np.float32)
+        c, s = rows["cos"][:, None], rows["sin"][:, None]
+        one = np.float32(1.0)
+        ox = (c * xy[None, :, 0] + (-s) * xy[None, :, 1]) + rows["tx"][:, None] * one
+        oy = (s * xy[None, :, 0] + c * xy[None, :, 1]) + rows["ty"][:, None] * one
+        costs[sel] = ox.max(axis=1) * np.float32(10.0) + oy.max(axis=1)
+    return int(free[int(np.argmin(costs))])
+
+
+def _select_host_scalar(items, q: np.ndarray, verdicts: np.ndarray) -> int:
+    best, best_cost = -1, None
+    for i in np.flatnonzero(verdicts == 0):
+        it = items[int(q["item"][i])]
+        cost = lbf_cost(W.transform_points(it.xy, q["cos"][i], q["sin"][i], q["tx"][i], q["ty"][i]))
+        if best_cost is None or cost < best_cost:
+            best, best_cost = int(i), cost
+    return best
+
+
+def setup(backend, spec: LbfSpec, item_pool=None):
+    """Items, the strip container (an Exterior hazard) and a fresh engine: (layout, engine)."""
+    st = W.Stream(spec.seed, 1)
+    items = item_pool
+    if items is None:
+        items = []
+        for _ in range(spec.n_types):
+            nv = int(st.randint(spec.v_range[0], spec.v_range[1], 1)[0])
+            items.append(W.import_item(backend, W.star_polygon(st, nv, *spec.r_range)))
+    outer = W.import_static(backend, W.rect_polygon(0.0, 0.0, spec.width, spec.height), W.EXTERIOR)
+    lay = W.Layout("lbf-strip", spec.depth, spec.cd_threshold, W.inflate_to_square(W.bbox_of(outer.xy)), items=items)
+    lay.hazards.append(outer)
+    return lay, W._new_layout_engine(backend, lay)
+
+
+def step_queries(spec: LbfSpec, step: int) -> np.ndarray:
+    t = int(W.Stream(spec.seed, TYPE_SID).u64(step + 1)[step] % np.uint64(spec.n_types))
+    q = W.make_queries(W.Stream(spec.seed, CAND_SID_BASE + step), spec.n_cand, 1, spec.box)
+    q["item"] = t
+    return q
+
+
+def run_host(lay, eng, spec: LbfSpec, steps: int | None = None, keep_verdicts: int = 0, on_step=None) -> LbfLog:
+    """The build with one engine call per step (oracle or GPU engine)."""
+    steps = spec.steps if steps is None else steps
+    s_rm = W.Stream(spec.seed, REMOVE_SID)
+    types = W.Stream(spec.seed, TYPE_SID).u64(steps) % np.uint64(spec.n_types)
+    placements, removals, free_counts, vkeep = [], [], [], []
+    live = []   # keys of placed items, in placement order
+    for step in range(steps):
+        q = W.make_queries(W.Stream(spec.seed, CAND_SID_BASE + step), spec.n_cand, 1, spec.box)
+        t = int(types[step])
+        q["item"] = t
+        verdicts = eng.detect_batch(q)
+        if step < keep_verdicts:
+            vkeep.append(np.asarray(verdicts).copy())
+        free_counts.append(int((verdicts == 0).sum()))
+        best = select_host(lay.items, q, verdicts)
+        if best >= 0:
+            hz = W.placed_hazard(lay.items[t], t, q["cos"][best], q["sin"][best], q["tx"][best], q["ty"][best])
+            key = eng.register_hazard(hz.kind, hz.dynamic, hz.xy, hz.poi, 1_000_000 + step)
+            live.append(key)
+            r = q[best]
+            placements.append([step, key, best, t] +
+                              [int(np.float32(r[f]).view(np.uint32)) for f in ("cos", "sin", "tx", "ty")])
+        if spec.remove_every and (step + 1) % spec.remove_every == 0 and live:
+            j = int(s_rm.randint(0, len(live) - 1, 1)[0])
+            key = live.pop(j)
+            eng.deregister_hazard(key)
+            removals.append([step, key])
+        if on_step is not None:
+            on_step(step, eng)
+    return LbfLog(np.array(placements, dtype=np.uint32).reshape(-1, 8), np.array(removals, dtype=np.uint32).reshape(-1, 2),
+                  np.array(free_counts, dtype=np.uint32), vkeep)
+
+
+def run_device(eng, spec: LbfSpec, steps: int | None = None, steps_per_graph: int = 0, keep_verdicts: int = 0,
+               resident=None):
+    """The build on the GPU (jcde_lbf_*) from the engine's current state; returns (log, resident)."""
+    from .engine import ResidentEngine
+
+    steps = spec.steps if steps is None else steps
+    cde = eng.eng if hasattr(eng, "eng") else eng
+    r = resident if resident is not None else ResidentEngine(cde)
+    r.lbf_begin(spec.seed, spec.n_cand, spec.n_types, spec.remove_every, steps, spec.box, keep_verdicts)
+    r.lbf_steps(steps, steps_per_graph)
+    d = r.lbf_read()
+    log = LbfLog(d["placements"], d["removals"], d["free_counts"], list(d["verdicts"]))
+    return log, r
