@@ -597,6 +597,123 @@ def run_proxy(args):
     return 0
 
 
+def run_lbf(args):
+    """configs[3]: LBF-style strip build on the device-resident engine.  2000 steps, each: 16384
+    candidates generated, judged (surrogate + polygon passes), the least-cost free one registered on
+    the device, and a random placed item deregistered every 50 steps.  A timed step is one whole build
+    from the strip's initial state.  Metric: candidate placements judged per second over the build."""
+    import torch
+
+    import jcde
+    from jcde import lbf
+
+    jcde.lib()
+    spec = lbf.LbfSpec()
+    lay, geng = lbf.setup(jcde.GpuBackend, spec)
+    r = jcde.ResidentEngine(geng.eng)
+    SPG = 25   # LBF steps per CUDA graph launch
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.Stream()   # a captured graph needs a stream other than the legacy default one
+    sh = stream.cuda_stream
+
+    def build(timed):
+        r.reset()
+        r.lbf_begin(spec.seed, spec.n_cand, spec.n_types, spec.remove_every, spec.steps, spec.box)
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        r.lbf_steps(spec.steps, SPG, stream=sh)
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b)
+
+    for _ in range(args.warmup):
+        build(False)
+    launches0 = r.kernel_launches()
+    clk = ClockSampler(0)
+    clk.__enter__()
+    profiler_range(True)
+    times = [build(True) for _ in range(args.steps)]
+    profiler_range(False)
+    launches = r.kernel_launches() - launches0
+    clk.__exit__()
+    ms = float(np.sum(times))
+    n_cand_total = spec.steps * spec.n_cand
+    value = n_cand_total * args.steps / (ms / 1e3)
+    d = r.lbf_read()
+    st = r.status()
+    # per-kernel shares from one eager, profiled build (events around every launch)
+    geng.eng.profile(True)
+    r.reset()
+    r.lbf_begin(spec.seed, spec.n_cand, spec.n_types, spec.remove_every, spec.steps, spec.box)
+    geng.eng.profile_read(reset=True)
+    r.lbf_steps(spec.steps, 0, stream=sh)
+    kp = geng.eng.profile_read(reset=True)
+    geng.eng.profile(False)
+    kinds = {k: {"ms_per_build": v[0], "launches": v[1]} for k, v in kp.items() if v[1]}
+    dominant = max(kinds, key=lambda k: kinds[k]["ms_per_build"])
+    # end to end through the public API: resident copy from the host engine, the build, the log read back
+    e2e_ms = []
+    h2d = d2h = 0
+    for _ in range(max(1, min(args.steps, 5))):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        h2d = r.reset()
+        log_e2e, _ = lbf.run_device(geng, spec, steps_per_graph=SPG, resident=r)
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+        d2h = (log_e2e.placements.nbytes + log_e2e.removals.nbytes + log_e2e.free_counts.nbytes + 16)
+    e2e_value = n_cand_total / (np.median(e2e_ms) / 1e3)
+    # the same build driven step by step from the host through the regular engine (host registration,
+    # a re-flattened tree upload per step): a bounded sample of its first steps
+    host_steps = 200
+    lay_h, geng_h = lbf.setup(jcde.GpuBackend, spec)
+    t0 = time.perf_counter()
+    hlog = lbf.run_host(lay_h, geng_h, spec, steps=host_steps)
+    host_s = time.perf_counter() - t0
+    host_ok = bool(np.array_equal(hlog.placements, d["placements"][: len(hlog.placements)]))
+    line = {
+        "metric": "LBF candidate placements judged per second (device-resident build)",
+        "value": value, "unit": "candidates/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"LBF strip build: {spec.n_types} star types ({spec.v_range[0]}-{spec.v_range[1]} "
+                               f"vertices), {spec.width:.0f} x {spec.height:.0f} strip, {spec.steps} steps x "
+                               f"{spec.n_cand} candidates, removal every {spec.remove_every} steps; one timed step = "
+                               "one whole build; register/deregister on the device; "
+                               f"{SPG} LBF steps per CUDA graph launch",
+                   "l2": "flushed between builds (256 MB write)"},
+        "lbf_steps_per_s": spec.steps * args.steps / (ms / 1e3),
+        "placed": int(len(d["placements"])), "removed": int(len(d["removals"])), "live": d["n_live"],
+        "pool_use": st,
+        "kernels_eager_build": kinds, "dominant": dominant,
+        "gpu_launches": int(launches),
+        "e2e": {"value": e2e_value, "unit": "candidates/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "ms_per_build": float(np.median(e2e_ms))},
+        "host_driven_gpu": {"value": host_steps * spec.n_cand / host_s, "unit": "candidates/s",
+                            "sample": f"first {host_steps} steps", "same_placements": host_ok},
+        "clocks": clk.summary(),
+        "impl": "jcde",
+    }
+    if not args.no_cpu:
+        from oracle import oracle as O
+
+        O.build()
+        cpu_steps = args.lbf_cpu_steps
+        lay_o, oeng = lbf.setup(O.OracleBackend, spec)
+        t0 = time.perf_counter()
+        olog = lbf.run_host(lay_o, oeng, spec, steps=cpu_steps)
+        cpu_s = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": cpu_steps * spec.n_cand / cpu_s, "unit": "candidates/s",
+                                "cores": host_cores(), "kind": "port",
+                                "sample": f"first {cpu_steps} of {spec.steps} steps, oracle detect on all cores, "
+                                          "numpy choice, oracle register",
+                                "same_placements": bool(np.array_equal(olog.placements,
+                                                                       d["placements"][: len(olog.placements)]))}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -604,9 +721,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="jcde", choices=["jcde", "reference"])
     ap.add_argument("--cpu-sample", type=int, default=1 << 17)
-    ap.add_argument("--workload", default="star", choices=["star", "multi", "proxy"],
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--lbf-cpu-steps", type=int, default=2000)
+    ap.add_argument("--workload", default="star", choices=["star", "multi", "proxy", "lbf"],
                     help="star: the headline single-layout batch; multi: 64 layouts in one launch sequence; "
-                         "proxy: gradient separation of colliding candidates vs random resampling")
+                         "proxy: gradient separation of colliding candidates vs random resampling; "
+                         "lbf: LBF-style build on the device-resident engine")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -614,6 +734,8 @@ def main():
         return run_multi(args)
     if args.workload == "proxy":
         return run_proxy(args)
+    if args.workload == "lbf":
+        return run_lbf(args)
     return run_gpu(args)
 
 

@@ -249,6 +249,9 @@ typedef struct jcde_resident_config {
 void jcde_resident_default_config(jcde_resident_config* c);
 jcde_status jcde_resident_create(jcde_engine* e, const jcde_resident_config* cfg, jcde_resident** out);
 void jcde_resident_destroy(jcde_resident* r);
+/* Back to a copy of the engine's current hazards (pools emptied, keys as the engine's); synchronises.
+ * *h2d_bytes (may be null) receives the bytes uploaded. */
+jcde_status jcde_resident_reset(jcde_resident* r, uint64_t* h2d_bytes);
 /* Layout::place_item (entities/layout.rs:73-85): PlacedItem::new of item d_query->item under the
  * query's transformation, then CDEngine::register_hazard (cd_engine.rs:59-70).  *d_key (device,
  * may be null) receives the key, ~0 on failure. */
@@ -324,7 +327,9 @@ uint64_t jcde_kernel_launches(const jcde_engine* e);
 #define JCDE_PROF_ORDER 3       /* spatial ordering of a batch (3 small kernels) */
 #define JCDE_PROF_FILTER 4      /* per-node presence under a new filter */
 #define JCDE_PROF_PROXY 5       /* gradient-descent separation on the pole-overlap proxy */
-#define JCDE_PROF_KINDS 6
+#define JCDE_PROF_UPDATE 6      /* device-resident register / deregister (LBF commit) */
+#define JCDE_PROF_LBF 7         /* LBF candidate generation and choice */
+#define JCDE_PROF_KINDS 8
 jcde_status jcde_profile_enable(jcde_engine* e, int enable);
 jcde_status jcde_profile_read(jcde_engine* e, double* ms, uint64_t* count, int reset);
 

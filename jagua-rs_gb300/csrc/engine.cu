@@ -376,14 +376,25 @@ static const uint32_t* spatial_order_into(jcde_engine* e, const uint32_t* q, uin
 }
 
 // The surrogate pass and/or the polygon pass; the walk's pending masks are 32-bit for trees of
-// depth <= 8 and 64-bit above.
+// depth <= 8 and 64-bit above.  Batches of at most JCDE_SURR_WARP_MAX queries take the
+// warp-per-query surrogate pass.
+#ifndef JCDE_SURR_WARP_MAX
+#define JCDE_SURR_WARP_MAX (1u << 17)
+#endif
 template <typename PendT>
 static void launch_passes_t(jcde_engine* e, const View& v, const uint32_t* q, uint32_t n, uint8_t* dout,
                             cudaStream_t s, RawShape raw, int mode, const uint32_t* order) {
     if (mode & 1) {
-        const uint32_t grid = (n + SURR_THREADS - 1) / SURR_THREADS;
+        const uint8_t miss = mode == 1 ? (uint8_t)0 : PENDING;
         cudaEvent_t pa = prof_begin(e, s);
-        k_surrogate<PendT, false><<<grid, SURR_THREADS, 0, s>>>(v, MultiSrc{}, q, n, dout, mode == 1 ? (uint8_t)0 : PENDING, order);
+        if (n <= JCDE_SURR_WARP_MAX) {   // too few queries to fill the GPU one thread each
+            const uint32_t wpb = SURR_THREADS / 32;
+            const uint32_t grid = std::min<uint32_t>((n + wpb - 1) / wpb, (uint32_t)e->n_sms * 8);
+            k_surrogate_warp<PendT><<<grid, SURR_THREADS, 0, s>>>(v, q, n, dout, miss, order);
+        } else {
+            const uint32_t grid = (n + SURR_THREADS - 1) / SURR_THREADS;
+            k_surrogate<PendT, false><<<grid, SURR_THREADS, 0, s>>>(v, MultiSrc{}, q, n, dout, miss, order);
+        }
         prof_end(e, s, pa, JCDE_PROF_SURROGATE);
         e->launches++;
     }
@@ -1237,6 +1248,7 @@ struct jcde_resident {
     cudaStream_t own = nullptr;
     cudaStream_t last = nullptr;
     uint64_t launches = 0;
+    uint64_t load_bytes = 0;   // host-to-device bytes of the last load of the engine's hazards
     ~jcde_resident() {
         if (last) cudaStreamSynchronize(last);
         if (exec) cudaGraphExecDestroy(exec);
@@ -1302,16 +1314,63 @@ static void lbf_step(jcde_resident* r, cudaStream_t s) {
     LbfDev* st = r->d_lbf.as<LbfDev>();
     uint32_t* cand = r->d_cand.as<uint32_t>();
     uint8_t* verd = r->d_verd.as<uint8_t>();
+    cudaEvent_t pa = prof_begin(e, s);
     res_launch_lbf_gen(r->lp, st, cand, e->n_sms, s);
+    prof_end(e, s, pa, JCDE_PROF_LBF);
     resident_detect(r, cand, r->lp.n_cand, verd, s);
     const View v = resident_view(r);
     const uint32_t grid = std::min<uint32_t>((r->lp.n_cand + 7) / 8, (uint32_t)e->n_sms * 8);
+    pa = prof_begin(e, s);
     k_lbf_select<<<grid, 256, 0, s>>>(v, cand, verd, r->lp.n_cand, &st->best, &st->n_free);
+    prof_end(e, s, pa, JCDE_PROF_LBF);
     LbfLogs logs{r->d_place.as<uint32_t>(), r->d_remv.as<uint32_t>(), r->d_free.as<uint32_t>(),
                  r->d_live.as<uint32_t>(), r->lp.vlog_steps ? r->d_vlog.as<uint8_t>() : nullptr};
+    pa = prof_begin(e, s);
     res_launch_lbf_commit(r->t, e->d_items.as<DItem>(), e->d_iverts.as<float2>(), (uint32_t)e->items.size(), r->lp,
                           st, cand, verd, logs, s);
+    prof_end(e, s, pa, JCDE_PROF_UPDATE);
     r->launches += 3;
+}
+
+// Loads the engine's live hazards, each under its own key, into empty pools (jcde_resident_create
+// and jcde_resident_reset).  Synchronises.
+static jcde_status resident_load(jcde_resident* r) {
+    jcde_engine* e = r->e;
+    const RTree& t = r->t;
+    const auto& hs = e->tree.hazards();
+    std::vector<float2> verts;
+    std::vector<uint4> recs;
+    std::vector<float2> pois;
+    for (uint32_t k = 0; k < hs.size(); k++) {
+        if (!hs[k].alive) continue;
+        const Polygon& p = hs[k].shape;
+        recs.push_back(make_uint4(k, (uint32_t)hs[k].kind, (uint32_t)verts.size(), (uint32_t)p.v.size()));
+        pois.push_back(make_float2(p.poi.c.x, p.poi.c.y));
+        for (const Pt& v : p.v) verts.push_back(make_float2(v.x, v.y));
+    }
+    const std::vector<uint32_t>& fk = e->tree.free_keys();
+    DevBuf d_v, d_r, d_p, d_k;
+    cudaStream_t s = r->own;
+    if (!d_v.ensure(std::max<size_t>(verts.size(), 1) * sizeof(float2)) ||
+        !d_r.ensure(std::max<size_t>(recs.size(), 1) * sizeof(uint4)) ||
+        !d_p.ensure(std::max<size_t>(pois.size(), 1) * sizeof(float2)) || !d_k.ensure(std::max<size_t>(fk.size(), 1) * 4))
+        return JCDE_ERR_CUDA;
+    CUDA_TRY(cudaMemsetAsync(t.alive, 0, t.key_cap, s));
+    CUDA_TRY(cudaMemsetAsync(t.ctl, 0, sizeof(RCtl), s));
+    if (verts.size()) CUDA_TRY(cudaMemcpyAsync(d_v.p, verts.data(), verts.size() * sizeof(float2), cudaMemcpyHostToDevice, s));
+    if (recs.size()) CUDA_TRY(cudaMemcpyAsync(d_r.p, recs.data(), recs.size() * sizeof(uint4), cudaMemcpyHostToDevice, s));
+    if (pois.size()) CUDA_TRY(cudaMemcpyAsync(d_p.p, pois.data(), pois.size() * sizeof(float2), cudaMemcpyHostToDevice, s));
+    if (fk.size()) CUDA_TRY(cudaMemcpyAsync(d_k.p, fk.data(), fk.size() * 4, cudaMemcpyHostToDevice, s));
+    r->load_bytes = verts.size() * sizeof(float2) + recs.size() * sizeof(uint4) + pois.size() * sizeof(float2) + fk.size() * 4;
+    res_launch_init(t, d_v.as<float2>(), d_r.as<uint4>(), d_p.as<float2>(), (uint32_t)recs.size(), e->tree.n_slots(),
+                    d_k.as<uint32_t>(), (uint32_t)fk.size(), s);
+    CUDA_TRY(cudaGetLastError());
+    RCtl ctl{};
+    CUDA_TRY(cudaMemcpyAsync(&ctl, t.ctl, sizeof(RCtl), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    r->launches++;
+    r->last = nullptr;
+    return ctl.error ? JCDE_ERR_CAPACITY : JCDE_OK;
 }
 
 extern "C" {
@@ -1344,7 +1403,6 @@ jcde_status jcde_resident_create(jcde_engine* e, const jcde_resident_config* cfg
         for (int d = 0; d <= e->cfg.quadtree_depth && full < (1u << 22); d++, lv *= 4) full += lv;
         c.max_nodes = (uint32_t)std::min<uint64_t>(full, 1u << 22);
     }
-    const auto& hs = e->tree.hazards();
     if (c.max_keys < e->tree.n_slots() || c.max_nodes < 1) return JCDE_ERR_CAPACITY;
     jcde_status st = sync_device(e);
     if (st) return st;
@@ -1390,50 +1448,26 @@ jcde_status jcde_resident_create(jcde_engine* e, const jcde_resident_config* cfg
     t.task_cap = c.max_tasks;
     t.cde = e->tree.bbox();
     t.depth = e->cfg.quadtree_depth;
-    // the engine's live hazards, each under its own key
-    std::vector<float2> verts;
-    std::vector<uint4> recs;
-    std::vector<float2> pois;
-    for (uint32_t k = 0; k < hs.size(); k++) {
-        if (!hs[k].alive) continue;
-        const Polygon& p = hs[k].shape;
-        recs.push_back(make_uint4(k, (uint32_t)hs[k].kind, (uint32_t)verts.size(), (uint32_t)p.v.size()));
-        pois.push_back(make_float2(p.poi.c.x, p.poi.c.y));
-        for (const Pt& v : p.v) verts.push_back(make_float2(v.x, v.y));
-    }
-    const std::vector<uint32_t>& fk = e->tree.free_keys();
-    DevBuf d_v, d_r, d_p, d_k;
-    cudaStream_t s = r->own;
-    ok = d_v.ensure(std::max<size_t>(verts.size(), 1) * sizeof(float2)) &&
-         d_r.ensure(std::max<size_t>(recs.size(), 1) * sizeof(uint4)) &&
-         d_p.ensure(std::max<size_t>(pois.size(), 1) * sizeof(float2)) && d_k.ensure(std::max<size_t>(fk.size(), 1) * 4);
-    if (!ok || cudaMemsetAsync(t.alive, 0, c.max_keys, s) != cudaSuccess ||
-        cudaMemsetAsync(t.ctl, 0, sizeof(RCtl), s) != cudaSuccess ||
-        (verts.size() && cudaMemcpyAsync(d_v.p, verts.data(), verts.size() * sizeof(float2), cudaMemcpyHostToDevice, s)) ||
-        (recs.size() && cudaMemcpyAsync(d_r.p, recs.data(), recs.size() * sizeof(uint4), cudaMemcpyHostToDevice, s)) ||
-        (pois.size() && cudaMemcpyAsync(d_p.p, pois.data(), pois.size() * sizeof(float2), cudaMemcpyHostToDevice, s)) ||
-        (fk.size() && cudaMemcpyAsync(d_k.p, fk.data(), fk.size() * 4, cudaMemcpyHostToDevice, s))) {
+    if ((st = resident_load(r))) {
         delete r;
-        return JCDE_ERR_CUDA;
-    }
-    res_launch_init(t, d_v.as<float2>(), d_r.as<uint4>(), d_p.as<float2>(), (uint32_t)recs.size(), e->tree.n_slots(),
-                    d_k.as<uint32_t>(), (uint32_t)fk.size(), s);
-    RCtl ctl{};
-    if (cudaGetLastError() != cudaSuccess || cudaMemcpyAsync(&ctl, t.ctl, sizeof(RCtl), cudaMemcpyDeviceToHost, s) ||
-        cudaStreamSynchronize(s) != cudaSuccess) {
-        delete r;
-        return JCDE_ERR_CUDA;
-    }
-    r->launches++;
-    if (ctl.error) {
-        delete r;
-        return JCDE_ERR_CAPACITY;
+        return st;
     }
     *out = r;
     return JCDE_OK;
 }
 
 void jcde_resident_destroy(jcde_resident* r) { delete r; }
+
+jcde_status jcde_resident_reset(jcde_resident* r, uint64_t* h2d_bytes) {
+    if (!r) return JCDE_ERR_ARG;
+    if (r->last) CUDA_TRY(cudaStreamSynchronize(r->last));
+    jcde_status st = sync_device(r->e);
+    if (st) return st;
+    r->exterior = r->e->tree.exterior_key();
+    st = resident_load(r);
+    if (h2d_bytes) *h2d_bytes = r->load_bytes;
+    return st;
+}
 
 jcde_status jcde_resident_register_placed(jcde_resident* r, const jcde_query* d_query, uint32_t* d_key, void* stream) {
     if (!r || !d_query) return JCDE_ERR_ARG;
@@ -1596,7 +1630,6 @@ jcde_status jcde_lbf_steps(jcde_resident* r, uint32_t n_steps, uint32_t steps_pe
     cudaStream_t s = stream ? (cudaStream_t)stream : r->own;
     jcde_engine* e = r->e;
     const bool prof = e->prof;
-    e->prof = false;   // per-kernel events are not recorded inside graphs
     uint32_t done = 0;
     if (steps_per_graph > 0 && n_steps >= steps_per_graph) {
         if (!r->exec || r->exec_steps != steps_per_graph || r->exec_stream != s) {
@@ -1605,34 +1638,28 @@ jcde_status jcde_lbf_steps(jcde_resident* r, uint32_t n_steps, uint32_t steps_pe
                 r->exec = nullptr;
             }
             cudaGraph_t g = nullptr;
-            if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
-                e->prof = prof;
-                return JCDE_ERR_CUDA;
-            }
+            if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return JCDE_ERR_CUDA;
             const uint64_t before = r->launches;
+            e->prof = false;   // per-kernel events are not recorded inside graphs
             for (uint32_t i = 0; i < steps_per_graph; i++) lbf_step(r, s);
+            e->prof = prof;
             r->launches = before;
             cudaError_t ce = cudaStreamEndCapture(s, &g);
             if (ce == cudaSuccess && g) ce = cudaGraphInstantiate(&r->exec, g, 0);
             if (g) cudaGraphDestroy(g);
             if (ce != cudaSuccess) {
                 r->exec = nullptr;
-                e->prof = prof;
                 return JCDE_ERR_CUDA;
             }
             r->exec_steps = steps_per_graph;
             r->exec_stream = s;
         }
         for (; done + steps_per_graph <= n_steps; done += steps_per_graph) {
-            if (cudaGraphLaunch(r->exec, s) != cudaSuccess) {
-                e->prof = prof;
-                return JCDE_ERR_CUDA;
-            }
+            if (cudaGraphLaunch(r->exec, s) != cudaSuccess) return JCDE_ERR_CUDA;
             r->launches += 8ull * steps_per_graph;
         }
     }
     for (; done < n_steps; done++) lbf_step(r, s);
-    e->prof = prof;
     CUDA_TRY(cudaGetLastError());
     r->last = s;
     e->last_stream = s;

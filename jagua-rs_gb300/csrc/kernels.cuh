@@ -399,6 +399,87 @@ __global__ void __launch_bounds__(SURR_THREADS) k_surrogate(View v, MultiSrc ms,
     }
 }
 
+// The surrogate pass with one warp per query, for batches too small to fill the GPU with one
+// thread per query (each query's walk then sets the batch's latency).  The warp follows each
+// probe's walk together; at a leaf its lanes test the node's hazards' ff boxes 32 at a time, then
+// the edges of every hazard whose box the probe hits, 32 at a time.  Same tests, same verdict.
+template <class P>
+__device__ __forceinline__ bool leaf_hits_warp(const View& v, const P& p, const DNode& nd, int lane) {
+    for (uint32_t b = 0; b < nd.hz_cnt; b += 32) {
+        const uint32_t k = b + lane;
+        uint32_t eo = 0, ec = 0;
+        bool cand = false;
+        if (k < nd.hz_cnt) {
+            const DEntry e = ld_entry(v, nd.hz_off + k);
+            cand = e.presence == PRES_PARTIAL && !filtered(v, e.hkey) && p_hits_box(p, e.ff);
+            eo = e.edge_off;
+            ec = e.edge_cnt;
+        }
+        uint32_t m = __ballot_sync(FULL, cand);
+        while (m) {
+            const int src = __ffs(m) - 1;
+            m &= m - 1;
+            const uint32_t off = __shfl_sync(FULL, eo, src), cnt = __shfl_sync(FULL, ec, src);
+            for (uint32_t jb = 0; jb < cnt; jb += 32) {
+                const uint32_t j = jb + lane;
+                if (__any_sync(FULL, j < cnt && p_hits_seg(p, ld_edge(v, off + j)))) return true;
+            }
+        }
+    }
+    return false;
+}
+
+template <class P, typename PendT>
+__device__ __forceinline__ bool walk_warp(const View& v, const P& p, int lane) {
+    WalkT<PendT> w{0, 0, 0, (PendT)0};
+    while (w.node >= 0) {
+        const uint32_t st = __ldg(&v.strength[w.node]);
+        if (st == PRES_ENTIRE) return true;
+        if (st == PRES_PARTIAL) {
+            const DNode nd = ld_node(v, w.node);
+            if (nd.child >= 0) {
+                const uint32_t m = p_quad_mask(p, nd.box);
+                if (m) walk_push(w, m, nd.child);
+            } else if (leaf_hits_warp(v, p, nd, lane)) {
+                return true;
+            }
+        }
+        w.node = walk_next(v, w);
+    }
+    return false;
+}
+
+template <typename PendT>
+__global__ void __launch_bounds__(SURR_THREADS) k_surrogate_warp(View v, const uint32_t* __restrict__ q, uint32_t n,
+                                                                 uint8_t* __restrict__ out, uint8_t miss,
+                                                                 const uint32_t* __restrict__ order) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t wpb = SURR_THREADS / 32;
+    for (uint32_t i = blockIdx.x * wpb + (threadIdx.x >> 5); i < n; i += gridDim.x * wpb) {
+        const uint32_t qi = order ? __ldg(&order[i]) : i;
+        const uint32_t* w5 = q + (size_t)qi * 5;
+        const uint32_t item = __ldg(&w5[0]);
+        if (item >= v.n_items) {
+            if (lane == 0) out[qi] = 2;
+            continue;
+        }
+        const float c = __uint_as_float(__ldg(&w5[1])), s = __uint_as_float(__ldg(&w5[2]));
+        const float tx = __uint_as_float(__ldg(&w5[3])), ty = __uint_as_float(__ldg(&w5[4]));
+        const DItem it = v.items[item];
+        bool hit = false;
+        for (uint32_t p = 0; p < it.n_ff_poles && !hit; p++) {
+            const float4 pl = __ldg(&v.poles[it.pole_off + p]);
+            hit = walk_warp<Disk, PendT>(v, Disk{xform(Pt{pl.x, pl.y}, c, s, tx, ty), pl.z}, lane);
+        }
+        for (uint32_t p = 0; p < it.n_piers && !hit; p++) {
+            const float4 pr = __ldg(&v.piers[it.pier_off + p]);
+            hit = walk_warp<Seg, PendT>(v, Seg{xform(Pt{pr.x, pr.y}, c, s, tx, ty), xform(Pt{pr.z, pr.w}, c, s, tx, ty)},
+                                        lane);
+        }
+        if (lane == 0) out[qi] = hit ? (uint8_t)1 : miss;
+    }
+}
+
 // Polygon pass — CDEngine::detect_poly_collision (cd_engine.rs:160-197), one warp per query.
 // With `only_pending`, queries whose slot is not PENDING were decided by the surrogate pass and
 // are skipped.  Writes JCDE_FREE / JCDE_COLLIDES.
@@ -1134,6 +1215,15 @@ __global__ void k_lbf_select(View v, const uint32_t* __restrict__ q, const uint8
                              unsigned long long* __restrict__ best, uint32_t* __restrict__ n_free) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t wpb = blockDim.x >> 5;
+    __shared__ unsigned long long s_best;
+    __shared__ uint32_t s_free;
+    if (threadIdx.x == 0) {
+        s_best = ~0ull;
+        s_free = 0;
+    }
+    __syncthreads();
+    unsigned long long mine = ~0ull;   // the warp's best (lane-uniform)
+    uint32_t nfree = 0;
     for (uint32_t qi = blockIdx.x * wpb + warp; qi < n; qi += gridDim.x * wpb) {
         if (verdicts[qi] != 0) continue;
         const QueryHead qh = load_query(q, qi, lane);
@@ -1142,10 +1232,17 @@ __global__ void k_lbf_select(View v, const uint32_t* __restrict__ q, const uint8
         const QShape sh{v.iverts + it.v_off, it.v_cnt, qh.c, qh.s, qh.tx, qh.ty, false};
         const Box b = warp_bbox(sh, lane);
         const float cost = b.x1 * 10.0f + b.y1;   // LBFLoss::cost (loss.rs:29-31)
-        if (lane == 0) {
-            atomicMin(best, ((unsigned long long)orderable(cost) << 32) | qi);
-            if (n_free) atomicAdd(n_free, 1u);
-        }
+        mine = min(mine, ((unsigned long long)orderable(cost) << 32) | qi);
+        nfree++;
+    }
+    if (lane == 0) {
+        if (mine != ~0ull) atomicMin(&s_best, mine);
+        if (nfree) atomicAdd(&s_free, nfree);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (s_best != ~0ull) atomicMin(best, s_best);
+        if (n_free && s_free) atomicAdd(n_free, s_free);
     }
 }
 

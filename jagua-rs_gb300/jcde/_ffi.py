@@ -102,6 +102,7 @@ SIGNATURES = {
     "jcde_resident_default_config": (None, [P]),
     "jcde_resident_create": (C.c_int32, [P, P, P]),
     "jcde_resident_destroy": (None, [P]),
+    "jcde_resident_reset": (C.c_int32, [P, C.POINTER(C.c_uint64)]),
     "jcde_resident_register_placed": (C.c_int32, [P, P, P, P]),
     "jcde_resident_deregister": (C.c_int32, [P, P, P]),
     "jcde_resident_detect_batch": (C.c_int32, [P, P, C.c_uint32, P, P]),

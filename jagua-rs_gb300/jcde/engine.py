@@ -332,7 +332,7 @@ class CDEngine:
     def kernel_launches(self) -> int:
         return int(lib().jcde_kernel_launches(self.h))
 
-    PROFILE_KINDS = ("surrogate", "poly", "collect", "order", "filter", "proxy")
+    PROFILE_KINDS = ("surrogate", "poly", "collect", "order", "filter", "proxy", "update", "lbf")
 
     def profile(self, enable: bool = True) -> None:
         """Bracket every kernel launch with CUDA events (jcde_profile_enable)."""
@@ -483,6 +483,12 @@ class ResidentEngine:
             except Exception:
                 pass
             self.h = None
+
+    def reset(self) -> int:
+        """Back to a copy of the engine's current hazards; returns the bytes uploaded."""
+        n = C.c_uint64()
+        check(lib().jcde_resident_reset(self.h, C.byref(n)), "resident_reset")
+        return int(n.value)
 
     def register_placed(self, query, key_out=None, stream=None) -> None:
         """query: CUDA uint8 tensor holding one packed query; key_out: CUDA int32 tensor of 1 or None."""

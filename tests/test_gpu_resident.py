@@ -113,6 +113,9 @@ def test_lbf_graph_replay_matches_eager(oracle_mod, jcde_mod):
     graphed, r2 = lbf.run_device(geng2, spec, steps_per_graph=16)   # 7 graph launches + 8 eager steps
     assert eager.same_as(graphed)
     assert np.array_equal(r1.tree_dump(), r2.tree_dump())
+    assert r2.reset() > 0   # back to the engine's hazards: the same build again
+    again, _ = lbf.run_device(geng2, spec, steps_per_graph=16, resident=r2)
+    assert again.same_as(eager)
 
 
 def test_lbf_full_size_matches_oracle(oracle_mod, jcde_mod):
