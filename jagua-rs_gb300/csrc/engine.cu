@@ -338,7 +338,10 @@ static void init_launch_shape(jcde_engine* e) {
 #ifndef JCDE_SPATIAL_ORDER
 #define JCDE_SPATIAL_ORDER 1
 #endif
-constexpr uint32_t ORDER_MIN_BATCH = 4096;   // below this a batch is visited in its own order
+#ifndef JCDE_ORDER_MIN_BATCH
+#define JCDE_ORDER_MIN_BATCH 4096u
+#endif
+constexpr uint32_t ORDER_MIN_BATCH = JCDE_ORDER_MIN_BATCH;   // below this a batch is visited in its own order
 
 // Visit order of a batch: cell-by-cell over the CDE box (k_bucket_*), or nullptr for index order.
 // `slot` selects one of two histogram/order buffer pairs, so that the two streams of the host
@@ -402,7 +405,9 @@ static void launch_passes_t(jcde_engine* e, const View& v, const uint32_t* q, ui
         const uint32_t want = (n + POLY_WARPS - 1) / POLY_WARPS;
         const uint32_t grid = std::min<uint32_t>(want, (uint32_t)(e->n_sms * e->detect_blocks_per_sm));
         cudaEvent_t pa = prof_begin(e, s);
-        k_poly<PendT, false><<<grid, POLY_WARPS * 32, 0, s>>>(v, MultiSrc{}, q, n, dout, raw, mode == 3, order);
+        const bool tab = n <= JCDE_SURR_WARP_MAX;   // small batches: per-query leaf tables (latency)
+        k_poly<PendT, false><<<grid, POLY_WARPS * 32, tab ? POLY_WARPS * sizeof(LeafTab) : 0, s>>>(
+            v, MultiSrc{}, q, n, dout, raw, mode == 3, order, tab);
         prof_end(e, s, pa, JCDE_PROF_POLY);
         e->launches++;
     }
@@ -1028,7 +1033,7 @@ static void multi_launch_t(jcde_multi* m, const uint32_t* q, uint8_t* out, cudaS
                                                                                           PENDING, order);
     const uint32_t pgrid = std::min<uint32_t>((n + POLY_WARPS - 1) / POLY_WARPS, (uint32_t)(m->n_sms * m->poly_blocks));
     k_poly<PendT, true><<<pgrid, POLY_WARPS * 32, 0, s>>>(View{}, ms, q, n, out, RawShape{nullptr, 0, 0, 0, 0}, true,
-                                                          order);
+                                                          order, false);
     m->launches += 5;
 }
 static void multi_launch(jcde_multi* m, const uint32_t* q, uint8_t* out, cudaStream_t s) {
@@ -1301,14 +1306,15 @@ static jcde_status ensure_order_buffers(jcde_resident* r, uint32_t n) {
 static void resident_detect(jcde_resident* r, const uint32_t* q, uint32_t n, uint8_t* dout, cudaStream_t s) {
     jcde_engine* e = r->e;
     const View v = resident_view(r);
+    // small batches (one LBF step's candidates) gain nothing from the visit order
     const uint32_t* order = nullptr;
-    if (JCDE_SPATIAL_ORDER && n >= ORDER_MIN_BATCH)
+    if (JCDE_SPATIAL_ORDER && n > JCDE_SURR_WARP_MAX)
         order = spatial_order_into(e, q, n, s, r->d_hist.as<uint32_t>(), r->d_order.as<uint32_t>());
     launch_passes(e, v, q, n, dout, s, RawShape{}, 3, order);
     r->launches += (order ? 3 : 0) + 2;
 }
 
-// One step of the LBF-style build: 8 launches (generate, order x3, surrogate, polygon, select, commit).
+// One step of the LBF-style build: 5 launches (generate, surrogate, polygon, select, commit).
 static void lbf_step(jcde_resident* r, cudaStream_t s) {
     jcde_engine* e = r->e;
     LbfDev* st = r->d_lbf.as<LbfDev>();
@@ -1656,7 +1662,7 @@ jcde_status jcde_lbf_steps(jcde_resident* r, uint32_t n_steps, uint32_t steps_pe
         }
         for (; done + steps_per_graph <= n_steps; done += steps_per_graph) {
             if (cudaGraphLaunch(r->exec, s) != cudaSuccess) return JCDE_ERR_CUDA;
-            r->launches += 8ull * steps_per_graph;
+            r->launches += 5ull * steps_per_graph;
         }
     }
     for (; done < n_steps; done++) lbf_step(r, s);

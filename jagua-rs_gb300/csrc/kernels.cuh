@@ -480,6 +480,126 @@ __global__ void __launch_bounds__(SURR_THREADS) k_surrogate_warp(View v, const u
     }
 }
 
+// Per-warp table of the Partial leaves a query's bounding box reaches, each with its Partial,
+// unfiltered hazards whose ff box meets that bounding box.  Every edge of the shape lies inside the
+// shape's bounding box, and box_hits_seg rejects an edge whose box misses the rectangle first
+// (rect.rs:301-345), so a hazard whose ff box misses the bounding box is missed by every edge:
+// testing only the tabled hazards of a leaf gives the full leaf loop's answer.  A leaf that is not
+// in the table (no room, or not reached by the box walk) falls back to the full loop.
+// The table costs a walk and a scan of the reached leaves per query; it is built in the
+// latency-bound regime of small batches (k_poly's `leaf_tab`), where it shortens the slowest
+// queries' leaf loops.
+constexpr int LT_LEAVES = 8, LT_ENTS = 64;
+struct LeafTab {
+    float4 ff[LT_ENTS];
+    uint2 ec[LT_ENTS];   // edge offset, edge count
+    int32_t node[LT_LEAVES];
+    uint32_t start[LT_LEAVES + 1];
+    uint32_t n_leaves;
+};
+
+template <typename PendT>
+__device__ __forceinline__ void build_leaf_tab(const View& v, int vr, const Box& sb, LeafTab* lt, int lane) {
+    uint32_t nl = 0, ne = 0;
+    const uint32_t below = (1u << lane) - 1u;
+    WalkT<PendT> w{vr, 0, 0, (PendT)0};
+    while (w.node >= 0) {
+        if (__ldg(&v.strength[w.node]) == PRES_PARTIAL) {
+            const DNode nd = ld_node(v, w.node);
+            if (nd.child >= 0) {
+                const Pt m = box_mid(nd.box);
+                uint32_t msk = 0;
+                JCDE_UNROLL
+                for (int i = 0; i < 4; i++)
+                    if (box_hits_box(quad_box(nd.box, m, i), sb)) msk |= 1u << i;
+                if (msk) walk_push(w, msk, nd.child);
+            } else if (nl < LT_LEAVES) {
+                const uint32_t e0 = ne;
+                bool fits = true;
+                for (uint32_t b = 0; b < nd.hz_cnt; b += 32) {
+                    const uint32_t k = b + lane;
+                    bool c = false;
+                    DEntry e{};
+                    if (k < nd.hz_cnt) {
+                        e = ld_entry(v, nd.hz_off + k);
+                        c = e.presence == PRES_PARTIAL && !filtered(v, e.hkey) && box_hits_box(e.ff, sb);
+                    }
+                    const uint32_t bal = __ballot_sync(FULL, c);
+                    if (ne + __popc(bal) > (uint32_t)LT_ENTS) {
+                        fits = false;
+                        break;
+                    }
+                    if (c) {
+                        const uint32_t at = ne + __popc(bal & below);
+                        lt->ff[at] = make_float4(e.ff.x0, e.ff.y0, e.ff.x1, e.ff.y1);
+                        lt->ec[at] = make_uint2(e.edge_off, e.edge_cnt);
+                    }
+                    ne += __popc(bal);
+                }
+                if (fits) {
+                    if (lane == 0) {
+                        lt->node[nl] = w.node;
+                        lt->start[nl] = e0;
+                    }
+                    nl++;
+                } else {
+                    ne = e0;
+                }
+            }
+        }
+        w.node = walk_next(v, w);
+    }
+    if (lane == 0) {
+        lt->start[nl] = ne;
+        lt->n_leaves = nl;
+    }
+    __syncwarp();
+}
+
+template <class P>
+__device__ __forceinline__ bool leaf_hits_tab(const View& v, const P& p, int node, const DNode& nd, const LeafTab* lt,
+                                              volatile int* stop) {
+    const uint32_t nl = lt->n_leaves;
+    for (uint32_t t = 0; t < nl; t++) {
+        if (lt->node[t] != node) continue;
+        const uint32_t end = lt->start[t + 1];
+        for (uint32_t k = lt->start[t]; k < end; k++) {
+            if (*stop) return false;
+            const float4 f = lt->ff[k];
+            if (!p_hits_box(p, Box{f.x, f.y, f.z, f.w})) continue;   // qt_partial_hazard.rs:67-71
+            const uint2 ec = lt->ec[k];
+            for (uint32_t j = 0; j < ec.y; j++) {
+                if (p_hits_seg(p, ld_edge(v, ec.x + j))) {
+                    *stop = 1;
+                    return true;
+                }
+                if ((j & 7) == 7 && *stop) return false;
+            }
+        }
+        return false;
+    }
+    return leaf_hits(v, p, nd, stop);
+}
+
+// walk_step with the leaf test answered from the warp's leaf table.
+template <class P, typename PendT>
+__device__ __forceinline__ bool walk_step_tab(const View& v, const P& p, WalkT<PendT>& w, volatile int* stop,
+                                              const LeafTab* lt) {
+    const uint32_t st = __ldg(&v.strength[w.node]);
+    if (st == PRES_ENTIRE) return true;
+    if (st == PRES_PARTIAL) {
+        DNode nd = ld_node(v, w.node);
+        if (nd.child >= 0) {
+            const uint32_t m = p_quad_mask(p, nd.box);
+            if (m) walk_push(w, m, nd.child);
+        } else if (lt ? leaf_hits_tab(v, p, w.node, nd, lt, stop) : leaf_hits(v, p, nd, stop)) {
+            return true;
+        }
+    }
+    w.node = walk_next(v, w);
+    return false;
+}
+
 // Polygon pass — CDEngine::detect_poly_collision (cd_engine.rs:160-197), one warp per query.
 // With `only_pending`, queries whose slot is not PENDING were decided by the surrogate pass and
 // are skipped.  Writes JCDE_FREE / JCDE_COLLIDES.
@@ -490,7 +610,7 @@ constexpr uint32_t POLY_MAXV = 256;   // items with more vertices transform edge
 template <typename PendT>
 __device__ __forceinline__ void poly_query(const View& v, const uint32_t* __restrict__ q, uint32_t qi,
                                            uint8_t* __restrict__ out, const RawShape& raw, volatile int* stop,
-                                           float2* tv, uint32_t* jobsw, int lane) {
+                                           float2* tv, uint32_t* jobsw, LeafTab* ltab, int lane) {
     QShape sh;
     Pt spoi;
     if (raw.verts) {
@@ -570,6 +690,11 @@ __device__ __forceinline__ void poly_query(const View& v, const uint32_t* __rest
             }
         }
     }
+    const LeafTab* tab = nullptr;
+    if (ltab && !hit && n_jobs > 0) {
+        build_leaf_tab<PendT>(v, vr, sb, ltab, lane);
+        tab = ltab;
+    }
     // Jobs are handed out dynamically: a lane whose walk is over takes the next unassigned job
     // (ballot rank), so no lane waits for the slowest walk of a fixed round.  Every loop
     // iteration is one node visit per active lane; a hit anywhere ends the query.
@@ -600,7 +725,7 @@ __device__ __forceinline__ void poly_query(const View& v, const uint32_t* __rest
         if (!__any_sync(FULL, active)) break;
         bool h = false;
         if (active) {
-            h = walk_step(v, e, w, stop);
+            h = walk_step_tab(v, e, w, stop, tab);
             if (!h && w.node < 0) w.node = -1;
         }
         hit = __any_sync(FULL, h);
@@ -646,10 +771,11 @@ __device__ __forceinline__ void poly_query(const View& v, const uint32_t* __rest
 template <typename PendT, bool MULTI>
 __global__ void __launch_bounds__(POLY_WARPS * 32, JCDE_POLY_MIN_BLOCKS)
     k_poly(View v, MultiSrc ms, const uint32_t* __restrict__ q, uint32_t n, uint8_t* __restrict__ out,
-           RawShape raw, bool only_pending, const uint32_t* __restrict__ order) {
+           RawShape raw, bool only_pending, const uint32_t* __restrict__ order, bool leaf_tab) {
     __shared__ int stops[POLY_WARPS];
     __shared__ float2 tverts[POLY_WARPS][POLY_MAXV];   // transformed item vertices
     __shared__ uint32_t jobs[POLY_WARPS][POLY_MAXV];   // edge index | children mask below the virtual root << 16
+    extern __shared__ LeafTab ltabs[];                 // POLY_WARPS tables when leaf_tab (dynamic)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     volatile int* stop = &stops[warp];
     const uint32_t stride = gridDim.x * POLY_WARPS;
@@ -657,9 +783,11 @@ __global__ void __launch_bounds__(POLY_WARPS * 32, JCDE_POLY_MIN_BLOCKS)
         const uint32_t qi = order ? __ldg(&order[i]) : i;
         if (only_pending && out[qi] != PENDING) continue;
         if constexpr (MULTI)
-            poly_query<PendT>(ms.views[ms.layout_of(qi)], q, qi, out, raw, stop, tverts[warp], jobs[warp], lane);
+            poly_query<PendT>(ms.views[ms.layout_of(qi)], q, qi, out, raw, stop, tverts[warp], jobs[warp],
+                              leaf_tab ? &ltabs[warp] : nullptr, lane);
         else
-            poly_query<PendT>(v, q, qi, out, raw, stop, tverts[warp], jobs[warp], lane);
+            poly_query<PendT>(v, q, qi, out, raw, stop, tverts[warp], jobs[warp], leaf_tab ? &ltabs[warp] : nullptr,
+                              lane);
     }
 }
 
