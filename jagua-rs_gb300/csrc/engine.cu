@@ -79,6 +79,7 @@ struct jcde_engine {
     // staging for host entry points and single queries
     DevBuf d_q, d_out, d_raw, d_coll;
     DevBuf d_hist, d_order;   // spatial ordering of a query batch
+    DevBuf d_next;            // work counters of the polygon pass (one per pipeline slot)
     // hazard poles binned in a uniform grid (overlap proxy)
     uint64_t pole_version = ~0ull;
     DevBuf d_hpoles, d_hpstart;
@@ -386,7 +387,7 @@ static const uint32_t* spatial_order_into(jcde_engine* e, const uint32_t* q, uin
 #endif
 template <typename PendT>
 static void launch_passes_t(jcde_engine* e, const View& v, const uint32_t* q, uint32_t n, uint8_t* dout,
-                            cudaStream_t s, RawShape raw, int mode, const uint32_t* order) {
+                            cudaStream_t s, RawShape raw, int mode, const uint32_t* order, uint32_t* next) {
     if (mode & 1) {
         const uint8_t miss = mode == 1 ? (uint8_t)0 : PENDING;
         cudaEvent_t pa = prof_begin(e, s);
@@ -405,17 +406,21 @@ static void launch_passes_t(jcde_engine* e, const View& v, const uint32_t* q, ui
         const uint32_t want = (n + POLY_WARPS - 1) / POLY_WARPS;
         const uint32_t grid = std::min<uint32_t>(want, (uint32_t)(e->n_sms * e->detect_blocks_per_sm));
         cudaEvent_t pa = prof_begin(e, s);
-        const bool tab = n <= JCDE_SURR_WARP_MAX;   // small batches: per-query leaf tables (latency)
+        // small batches are latency-bound: per-query leaf tables, and queries handed to warps one at
+        // a time from a counter (`next`) so that no warp queues behind a slow query
+        const bool tab = n <= JCDE_SURR_WARP_MAX;
+        if (!tab || !next || cudaMemsetAsync(next, 0, 4, s) != cudaSuccess) next = nullptr;
         k_poly<PendT, false><<<grid, POLY_WARPS * 32, tab ? POLY_WARPS * sizeof(LeafTab) : 0, s>>>(
-            v, MultiSrc{}, q, n, dout, raw, mode == 3, order, tab);
+            v, MultiSrc{}, q, n, dout, raw, mode == 3, order, tab, next);
         prof_end(e, s, pa, JCDE_PROF_POLY);
         e->launches++;
     }
 }
 static void launch_passes(jcde_engine* e, const View& v, const uint32_t* q, uint32_t n, uint8_t* dout,
-                          cudaStream_t s, RawShape raw, int mode, const uint32_t* order = nullptr) {
-    if (e->cfg.quadtree_depth <= 8) launch_passes_t<uint32_t>(e, v, q, n, dout, s, raw, mode, order);
-    else launch_passes_t<uint64_t>(e, v, q, n, dout, s, raw, mode, order);
+                          cudaStream_t s, RawShape raw, int mode, const uint32_t* order = nullptr,
+                          uint32_t* next = nullptr) {
+    if (e->cfg.quadtree_depth <= 8) launch_passes_t<uint32_t>(e, v, q, n, dout, s, raw, mode, order, next);
+    else launch_passes_t<uint64_t>(e, v, q, n, dout, s, raw, mode, order, next);
 }
 
 // mode 1: surrogate only; 2: polygon only; 3: surrogate pass, then the polygon pass on the
@@ -430,7 +435,8 @@ static jcde_status launch_detect(jcde_engine* e, int mode, const jcde_query* dq,
     if (n == 0) return JCDE_OK;
     const uint32_t* q = reinterpret_cast<const uint32_t*>(dq);
     const uint32_t* order = raw.verts ? nullptr : spatial_order(e, q, n, s, slot, slot_cap);
-    launch_passes(e, v, q, n, dout, s, raw, mode, order);
+    uint32_t* next = e->d_next.ensure(2 * 4) ? e->d_next.as<uint32_t>() + slot : nullptr;
+    launch_passes(e, v, q, n, dout, s, raw, mode, order, next);
     CUDA_TRY(cudaGetLastError());
     e->last_stream = s;
     e->have_last_stream = true;
@@ -1033,7 +1039,7 @@ static void multi_launch_t(jcde_multi* m, const uint32_t* q, uint8_t* out, cudaS
                                                                                           PENDING, order);
     const uint32_t pgrid = std::min<uint32_t>((n + POLY_WARPS - 1) / POLY_WARPS, (uint32_t)(m->n_sms * m->poly_blocks));
     k_poly<PendT, true><<<pgrid, POLY_WARPS * 32, 0, s>>>(View{}, ms, q, n, out, RawShape{nullptr, 0, 0, 0, 0}, true,
-                                                          order, false);
+                                                          order, false, nullptr);
     m->launches += 5;
 }
 static void multi_launch(jcde_multi* m, const uint32_t* q, uint8_t* out, cudaStream_t s) {
@@ -1247,6 +1253,7 @@ struct jcde_resident {
     LbfParams lp{};
     DevBuf d_lbf, d_cand, d_verd, d_place, d_remv, d_free, d_live, d_vlog;
     DevBuf d_hist, d_order;   // spatial ordering of the resident's own query batches
+    DevBuf d_next;            // work counter of its polygon pass
     cudaGraphExec_t exec = nullptr;
     uint32_t exec_steps = 0;
     cudaStream_t exec_stream = nullptr;
@@ -1310,7 +1317,7 @@ static void resident_detect(jcde_resident* r, const uint32_t* q, uint32_t n, uin
     const uint32_t* order = nullptr;
     if (JCDE_SPATIAL_ORDER && n > JCDE_SURR_WARP_MAX)
         order = spatial_order_into(e, q, n, s, r->d_hist.as<uint32_t>(), r->d_order.as<uint32_t>());
-    launch_passes(e, v, q, n, dout, s, RawShape{}, 3, order);
+    launch_passes(e, v, q, n, dout, s, RawShape{}, 3, order, r->d_next.as<uint32_t>());
     r->launches += (order ? 3 : 0) + 2;
 }
 
@@ -1427,7 +1434,8 @@ jcde_status jcde_resident_create(jcde_engine* e, const jcde_resident_config* cfg
               r->d_haz.ensure((size_t)c.max_keys * sizeof(DHaz)) &&
               r->d_hverts.ensure((size_t)c.max_hazard_vertices * sizeof(float2)) && r->d_alive.ensure(c.max_keys) &&
               r->d_qfree.ensure((size_t)nq * 4) && r->d_kfree.ensure((size_t)c.max_keys * 4) &&
-              r->d_tasks.ensure((size_t)c.max_tasks * sizeof(RTask)) && r->d_ctl.ensure(sizeof(RCtl));
+              r->d_tasks.ensure((size_t)c.max_tasks * sizeof(RTask)) && r->d_ctl.ensure(sizeof(RCtl)) &&
+              r->d_next.ensure(4);
     if (!ok || cudaStreamCreateWithFlags(&r->own, cudaStreamNonBlocking) != cudaSuccess) {
         delete r;
         return JCDE_ERR_CUDA;

@@ -771,7 +771,8 @@ __device__ __forceinline__ void poly_query(const View& v, const uint32_t* __rest
 template <typename PendT, bool MULTI>
 __global__ void __launch_bounds__(POLY_WARPS * 32, JCDE_POLY_MIN_BLOCKS)
     k_poly(View v, MultiSrc ms, const uint32_t* __restrict__ q, uint32_t n, uint8_t* __restrict__ out,
-           RawShape raw, bool only_pending, const uint32_t* __restrict__ order, bool leaf_tab) {
+           RawShape raw, bool only_pending, const uint32_t* __restrict__ order, bool leaf_tab,
+           uint32_t* __restrict__ next) {
     __shared__ int stops[POLY_WARPS];
     __shared__ float2 tverts[POLY_WARPS][POLY_MAXV];   // transformed item vertices
     __shared__ uint32_t jobs[POLY_WARPS][POLY_MAXV];   // edge index | children mask below the virtual root << 16
@@ -779,7 +780,14 @@ __global__ void __launch_bounds__(POLY_WARPS * 32, JCDE_POLY_MIN_BLOCKS)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     volatile int* stop = &stops[warp];
     const uint32_t stride = gridDim.x * POLY_WARPS;
-    for (uint32_t i = blockIdx.x * POLY_WARPS + warp; i < n; i += stride) {
+    // queries in grid-stride order, or one at a time from the counter `next`
+    for (uint32_t i = next ? 0u : blockIdx.x * POLY_WARPS + warp;; i += stride) {
+        if (next) {
+            uint32_t t = 0;
+            if (lane == 0) t = atomicAdd(next, 1u);
+            i = __shfl_sync(FULL, t, 0);
+        }
+        if (i >= n) break;
         const uint32_t qi = order ? __ldg(&order[i]) : i;
         if (only_pending && out[qi] != PENDING) continue;
         if constexpr (MULTI)
