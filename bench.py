@@ -57,7 +57,9 @@ def log(*a):
 
 
 def dist_env():
-    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+    from jcde.shards import dist_env as env
+
+    return env()
 
 
 def host_cores() -> int:
@@ -269,7 +271,9 @@ def run_gpu(args):
     lay, _ = make_layout(jcde.GpuBackend)
     eng = gpu_engine_for(lay)
     # weak scaling: every rank answers its own batch of N_QUERIES (distinct query stream per rank)
-    q = W.queries_for(lay, N_QUERIES, SEED, sid=3 + rank)
+    from jcde.shards import max_over_ranks, rank_queries
+
+    q = rank_queries(lay, N_QUERIES, SEED, rank)
     dq = torch.from_numpy(q.view(np.uint8).copy()).cuda()
     out = torch.empty(N_QUERIES, dtype=torch.uint8, device="cuda")
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
@@ -308,11 +312,7 @@ def run_gpu(args):
     torch.cuda.synchronize()
     kprof = eng.profile_read(reset=True)
     eng.profile(False)
-    dev_s = sum(step_ms) / 1e3
-    if world > 1:
-        t = torch.tensor([dev_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        dev_s = float(t.item())
+    dev_s = max_over_ranks(sum(step_ms) / 1e3)
     value = world * N_QUERIES * args.steps / dev_s
     verdicts = out.cpu().numpy()
 
@@ -358,11 +358,7 @@ def run_gpu(args):
     collect_s = sum(a.elapsed_time(b) for a, b in c_ms) / 1e3
     collect_total = int(c_tot.item())
     clk.__exit__(None, None, None)
-    e2e_s = sum(e2e_times)
-    if world > 1:
-        t = torch.tensor([e2e_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(sum(e2e_times))
     e2e_value = world * N_QUERIES * args.steps / e2e_s
     e2e_same = bool(np.array_equal(hout.numpy(), verdicts))
 
