@@ -167,3 +167,26 @@ def run_device(eng, spec: LbfSpec, steps: int | None = None, steps_per_graph: in
     d = r.lbf_read()
     log = LbfLog(d["placements"], d["removals"], d["free_counts"], list(d["verdicts"]))
     return log, r
+
+
+def main(argv=None) -> int:
+    """Run the device build of the strip for some steps and print its counts (a small case for
+    profiling one step's kernels): PYTHONPATH=jagua-rs_gb300 python -m jcde.lbf --steps 1501"""
+    import argparse
+
+    import jcde
+
+    ap = argparse.ArgumentParser(description=main.__doc__)
+    ap.add_argument("--steps", type=int, default=LbfSpec.steps)
+    ap.add_argument("--steps-per-graph", type=int, default=0, help="0: every step launched eagerly")
+    a = ap.parse_args(argv)
+    spec = LbfSpec()
+    _, geng = setup(jcde.GpuBackend, spec)
+    log, r = run_device(geng, spec, steps=a.steps, steps_per_graph=a.steps_per_graph)
+    print(f"steps {len(log.free_counts)} placed {len(log.placements)} removed {len(log.removals)} "
+          f"status {r.status()}")
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())
