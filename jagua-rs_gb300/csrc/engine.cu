@@ -79,7 +79,7 @@ struct jcde_engine {
     // staging for host entry points and single queries
     DevBuf d_q, d_out, d_raw, d_coll;
     DevBuf d_hist, d_order;   // spatial ordering of a query batch
-    DevBuf d_next;            // work counters of the polygon pass (one per pipeline slot)
+    DevBuf d_next;            // work counters of the two passes (a pair per pipeline slot)
     // hazard poles binned in a uniform grid (overlap proxy)
     uint64_t pole_version = ~0ull;
     DevBuf d_hpoles, d_hpstart;
@@ -385,6 +385,12 @@ static const uint32_t* spatial_order_into(jcde_engine* e, const uint32_t* q, uin
 #ifndef JCDE_SURR_WARP_MAX
 #define JCDE_SURR_WARP_MAX (1u << 17)
 #endif
+#ifndef JCDE_POLY_CHUNK
+#define JCDE_POLY_CHUNK 2   // 0: large batches in grid-stride order
+#endif
+#ifndef JCDE_SURR_DYNAMIC
+#define JCDE_SURR_DYNAMIC 1
+#endif
 template <typename PendT>
 static void launch_passes_t(jcde_engine* e, const View& v, const uint32_t* q, uint32_t n, uint8_t* dout,
                             cudaStream_t s, RawShape raw, int mode, const uint32_t* order, uint32_t* next) {
@@ -395,9 +401,16 @@ static void launch_passes_t(jcde_engine* e, const View& v, const uint32_t* q, ui
             const uint32_t wpb = SURR_THREADS / 32;
             const uint32_t grid = std::min<uint32_t>((n + wpb - 1) / wpb, (uint32_t)e->n_sms * 8);
             k_surrogate_warp<PendT><<<grid, SURR_THREADS, 0, s>>>(v, q, n, dout, miss, order);
+        } else if (JCDE_SURR_DYNAMIC && next && cudaMemsetAsync(next, 0, 4, s) == cudaSuccess) {
+            // persistent blocks; each warp takes the next 32 queries from a counter as it finishes
+            int per_sm = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_surrogate<PendT, false>, SURR_THREADS, 0);
+            const uint32_t grid = std::min<uint32_t>((n + SURR_THREADS - 1) / SURR_THREADS,
+                                                     (uint32_t)e->n_sms * (uint32_t)std::max(per_sm, 1));
+            k_surrogate<PendT, false><<<grid, SURR_THREADS, 0, s>>>(v, MultiSrc{}, q, n, dout, miss, order, next);
         } else {
             const uint32_t grid = (n + SURR_THREADS - 1) / SURR_THREADS;
-            k_surrogate<PendT, false><<<grid, SURR_THREADS, 0, s>>>(v, MultiSrc{}, q, n, dout, miss, order);
+            k_surrogate<PendT, false><<<grid, SURR_THREADS, 0, s>>>(v, MultiSrc{}, q, n, dout, miss, order, nullptr);
         }
         prof_end(e, s, pa, JCDE_PROF_SURROGATE);
         e->launches++;
@@ -406,12 +419,14 @@ static void launch_passes_t(jcde_engine* e, const View& v, const uint32_t* q, ui
         const uint32_t want = (n + POLY_WARPS - 1) / POLY_WARPS;
         const uint32_t grid = std::min<uint32_t>(want, (uint32_t)(e->n_sms * e->detect_blocks_per_sm));
         cudaEvent_t pa = prof_begin(e, s);
-        // small batches are latency-bound: per-query leaf tables, and queries handed to warps one at
-        // a time from a counter (`next`) so that no warp queues behind a slow query
+        // Queries are handed to warps from a counter (`next`), so that no warp queues behind slow
+        // queries: one at a time in small batches, JCDE_POLY_CHUNK at a time in large ones.  Small
+        // batches are latency-bound and also build per-query leaf tables.
         const bool tab = n <= JCDE_SURR_WARP_MAX;
-        if (!tab || !next || cudaMemsetAsync(next, 0, 4, s) != cudaSuccess) next = nullptr;
+        if (next) next += 1;   // the polygon pass's own counter
+        if (!next || (!tab && !JCDE_POLY_CHUNK) || cudaMemsetAsync(next, 0, 4, s) != cudaSuccess) next = nullptr;
         k_poly<PendT, false><<<grid, POLY_WARPS * 32, tab ? POLY_WARPS * sizeof(LeafTab) : 0, s>>>(
-            v, MultiSrc{}, q, n, dout, raw, mode == 3, order, tab, next);
+            v, MultiSrc{}, q, n, dout, raw, mode == 3, order, tab, next, tab ? 1u : (uint32_t)JCDE_POLY_CHUNK);
         prof_end(e, s, pa, JCDE_PROF_POLY);
         e->launches++;
     }
@@ -435,7 +450,7 @@ static jcde_status launch_detect(jcde_engine* e, int mode, const jcde_query* dq,
     if (n == 0) return JCDE_OK;
     const uint32_t* q = reinterpret_cast<const uint32_t*>(dq);
     const uint32_t* order = raw.verts ? nullptr : spatial_order(e, q, n, s, slot, slot_cap);
-    uint32_t* next = e->d_next.ensure(2 * 4) ? e->d_next.as<uint32_t>() + slot : nullptr;
+    uint32_t* next = e->d_next.ensure(2 * 2 * 4) ? e->d_next.as<uint32_t>() + 2 * slot : nullptr;
     launch_passes(e, v, q, n, dout, s, raw, mode, order, next);
     CUDA_TRY(cudaGetLastError());
     e->last_stream = s;
@@ -1036,10 +1051,10 @@ static void multi_launch_t(jcde_multi* m, const uint32_t* q, uint8_t* out, cudaS
     k_scan_counts<<<1, 1024, 0, s>>>(hist, L * N_BUCKETS);
     k_mbucket_scatter<<<grid, 256, 0, s>>>(q, n, ms, hist, order);
     k_surrogate<PendT, true><<<(n + SURR_THREADS - 1) / SURR_THREADS, SURR_THREADS, 0, s>>>(View{}, ms, q, n, out,
-                                                                                          PENDING, order);
+                                                                                          PENDING, order, nullptr);
     const uint32_t pgrid = std::min<uint32_t>((n + POLY_WARPS - 1) / POLY_WARPS, (uint32_t)(m->n_sms * m->poly_blocks));
     k_poly<PendT, true><<<pgrid, POLY_WARPS * 32, 0, s>>>(View{}, ms, q, n, out, RawShape{nullptr, 0, 0, 0, 0}, true,
-                                                          order, false, nullptr);
+                                                          order, false, nullptr, 1u);
     m->launches += 5;
 }
 static void multi_launch(jcde_multi* m, const uint32_t* q, uint8_t* out, cudaStream_t s) {
@@ -1253,7 +1268,7 @@ struct jcde_resident {
     LbfParams lp{};
     DevBuf d_lbf, d_cand, d_verd, d_place, d_remv, d_free, d_live, d_vlog;
     DevBuf d_hist, d_order;   // spatial ordering of the resident's own query batches
-    DevBuf d_next;            // work counter of its polygon pass
+    DevBuf d_next;            // work counters of its two passes
     cudaGraphExec_t exec = nullptr;
     uint32_t exec_steps = 0;
     cudaStream_t exec_stream = nullptr;
@@ -1435,7 +1450,7 @@ jcde_status jcde_resident_create(jcde_engine* e, const jcde_resident_config* cfg
               r->d_hverts.ensure((size_t)c.max_hazard_vertices * sizeof(float2)) && r->d_alive.ensure(c.max_keys) &&
               r->d_qfree.ensure((size_t)nq * 4) && r->d_kfree.ensure((size_t)c.max_keys * 4) &&
               r->d_tasks.ensure((size_t)c.max_tasks * sizeof(RTask)) && r->d_ctl.ensure(sizeof(RCtl)) &&
-              r->d_next.ensure(4);
+              r->d_next.ensure(2 * 4);
     if (!ok || cudaStreamCreateWithFlags(&r->own, cudaStreamNonBlocking) != cudaSuccess) {
         delete r;
         return JCDE_ERR_CUDA;

@@ -390,7 +390,24 @@ __device__ __forceinline__ void surrogate_query(const View& v, const uint32_t* _
 template <typename PendT, bool MULTI>
 __global__ void __launch_bounds__(SURR_THREADS) k_surrogate(View v, MultiSrc ms, const uint32_t* __restrict__ q,
                                                             uint32_t n, uint8_t* __restrict__ out, uint8_t miss,
-                                                            const uint32_t* __restrict__ order) {
+                                                            const uint32_t* __restrict__ order,
+                                                            uint32_t* __restrict__ next) {
+    if (next) {   // each warp takes the next 32 queries from the counter as it finishes
+        const int lane = threadIdx.x & 31;
+        for (;;) {
+            uint32_t t = 0;
+            if (lane == 0) t = atomicAdd(next, 32u);
+            const uint32_t base = __shfl_sync(FULL, t, 0);
+            if (base >= n) break;
+            const uint32_t i = base + lane;
+            if (i < n) {
+                const uint32_t qi = order ? __ldg(&order[i]) : i;
+                if constexpr (MULTI) surrogate_query<PendT>(ms.views[ms.layout_of(qi)], q, qi, out, miss);
+                else surrogate_query<PendT>(v, q, qi, out, miss);
+            }
+        }
+        return;
+    }
     const uint32_t stride = gridDim.x * SURR_THREADS;
     for (uint32_t i = blockIdx.x * SURR_THREADS + threadIdx.x; i < n; i += stride) {
         const uint32_t qi = order ? __ldg(&order[i]) : i;
@@ -772,7 +789,7 @@ template <typename PendT, bool MULTI>
 __global__ void __launch_bounds__(POLY_WARPS * 32, JCDE_POLY_MIN_BLOCKS)
     k_poly(View v, MultiSrc ms, const uint32_t* __restrict__ q, uint32_t n, uint8_t* __restrict__ out,
            RawShape raw, bool only_pending, const uint32_t* __restrict__ order, bool leaf_tab,
-           uint32_t* __restrict__ next) {
+           uint32_t* __restrict__ next, uint32_t chunk) {
     __shared__ int stops[POLY_WARPS];
     __shared__ float2 tverts[POLY_WARPS][POLY_MAXV];   // transformed item vertices
     __shared__ uint32_t jobs[POLY_WARPS][POLY_MAXV];   // edge index | children mask below the virtual root << 16
@@ -780,15 +797,24 @@ __global__ void __launch_bounds__(POLY_WARPS * 32, JCDE_POLY_MIN_BLOCKS)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     volatile int* stop = &stops[warp];
     const uint32_t stride = gridDim.x * POLY_WARPS;
-    // queries in grid-stride order, or one at a time from the counter `next`
-    for (uint32_t i = next ? 0u : blockIdx.x * POLY_WARPS + warp;; i += stride) {
-        if (next) {
-            uint32_t t = 0;
-            if (lane == 0) t = atomicAdd(next, 1u);
-            i = __shfl_sync(FULL, t, 0);
+    // queries in grid-stride order, or `chunk` consecutive ones at a time from the counter `next`
+    uint32_t i = 0, end = 0, gs = blockIdx.x * POLY_WARPS + warp;
+    for (;;) {
+        if (i >= end) {
+            if (next) {
+                uint32_t t = 0;
+                if (lane == 0) t = atomicAdd(next, chunk);
+                i = __shfl_sync(FULL, t, 0);
+                end = min(i + chunk, n);
+            } else {
+                i = gs;
+                end = gs + 1;
+                gs += stride;
+            }
+            if (i >= n) break;
         }
-        if (i >= n) break;
         const uint32_t qi = order ? __ldg(&order[i]) : i;
+        i++;
         if (only_pending && out[qi] != PENDING) continue;
         if constexpr (MULTI)
             poly_query<PendT>(ms.views[ms.layout_of(qi)], q, qi, out, raw, stop, tverts[warp], jobs[warp],
