@@ -984,7 +984,9 @@ struct jcde_multi {
     std::vector<View> up_views;       // what d_views / d_offs hold
     std::vector<uint32_t> up_offs;
     DevBuf d_views, d_offs, d_hist, d_order;
+    DevBuf d_next;                    // work counters of the two passes
     bool wide = false;                // a tree deeper than 8 levels needs 64-bit walk masks
+    int surr_blocks = 1;
     int n_sms = 1, poly_blocks = 1;
     // graph replay
     cudaGraphExec_t exec = nullptr;
@@ -1050,11 +1052,14 @@ static void multi_launch_t(jcde_multi* m, const uint32_t* q, uint8_t* out, cudaS
     k_mbucket_count<<<grid, 256, 0, s>>>(q, n, ms, hist);
     k_scan_counts<<<1, 1024, 0, s>>>(hist, L * N_BUCKETS);
     k_mbucket_scatter<<<grid, 256, 0, s>>>(q, n, ms, hist, order);
-    k_surrogate<PendT, true><<<(n + SURR_THREADS - 1) / SURR_THREADS, SURR_THREADS, 0, s>>>(View{}, ms, q, n, out,
-                                                                                          PENDING, order, nullptr);
+    // both passes take their queries from counters (see launch_passes_t)
+    uint32_t* next = m->d_next.as<uint32_t>();
+    cudaMemsetAsync(next, 0, 2 * 4, s);
+    const uint32_t sgrid = std::min<uint32_t>((n + SURR_THREADS - 1) / SURR_THREADS, (uint32_t)(m->n_sms * m->surr_blocks));
+    k_surrogate<PendT, true><<<sgrid, SURR_THREADS, 0, s>>>(View{}, ms, q, n, out, PENDING, order, next);
     const uint32_t pgrid = std::min<uint32_t>((n + POLY_WARPS - 1) / POLY_WARPS, (uint32_t)(m->n_sms * m->poly_blocks));
     k_poly<PendT, true><<<pgrid, POLY_WARPS * 32, 0, s>>>(View{}, ms, q, n, out, RawShape{nullptr, 0, 0, 0, 0}, true,
-                                                          order, false, nullptr, 1u);
+                                                          order, false, next + 1, (uint32_t)std::max(JCDE_POLY_CHUNK, 1));
     m->launches += 5;
 }
 static void multi_launch(jcde_multi* m, const uint32_t* q, uint8_t* out, cudaStream_t s) {
@@ -1079,8 +1084,18 @@ jcde_status jcde_multi_create(jcde_engine* const* engines, uint32_t n, jcde_mult
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&m->n_sms, cudaDevAttrMultiProcessorCount, dev);
-    if (m->wide) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m->poly_blocks, k_poly<uint64_t, true>, POLY_WARPS * 32, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m->poly_blocks, k_poly<uint32_t, true>, POLY_WARPS * 32, 0);
+    if (m->wide) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m->poly_blocks, k_poly<uint64_t, true>, POLY_WARPS * 32, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m->surr_blocks, k_surrogate<uint64_t, true>, SURR_THREADS, 0);
+    } else {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m->poly_blocks, k_poly<uint32_t, true>, POLY_WARPS * 32, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m->surr_blocks, k_surrogate<uint32_t, true>, SURR_THREADS, 0);
+    }
+    if (m->surr_blocks < 1) m->surr_blocks = 1;
+    if (!m->d_next.ensure(2 * 4)) {
+        delete m;
+        return JCDE_ERR_CUDA;
+    }
     if (m->n_sms < 1) m->n_sms = 1;
     if (m->poly_blocks < 1) m->poly_blocks = 1;
     *out = m;
