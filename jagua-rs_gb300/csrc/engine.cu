@@ -391,6 +391,9 @@ static const uint32_t* spatial_order_into(jcde_engine* e, const uint32_t* q, uin
 #ifndef JCDE_SURR_DYNAMIC
 #define JCDE_SURR_DYNAMIC 1
 #endif
+#ifndef JCDE_COLLECT_DYNAMIC
+#define JCDE_COLLECT_DYNAMIC 1
+#endif
 template <typename PendT>
 static void launch_passes_t(jcde_engine* e, const View& v, const uint32_t* q, uint32_t n, uint8_t* dout,
                             cudaStream_t s, RawShape raw, int mode, const uint32_t* order, uint32_t* next) {
@@ -483,11 +486,16 @@ static jcde_status launch_collect(jcde_engine* e, int mode, const jcde_query* dq
     uint32_t want = (n + COLLECT_WARPS - 1) / COLLECT_WARPS;
     uint32_t grid = std::min<uint32_t>(want, (uint32_t)(e->n_sms * per_sm));
     const uint32_t* q = reinterpret_cast<const uint32_t*>(dq);
+    // the detect passes' visit order and work counter (slot 0)
+    const uint32_t* order = raw.verts ? nullptr : spatial_order(e, q, n, s, 0, 0);
+    uint32_t* next = nullptr;
+    if (JCDE_COLLECT_DYNAMIC && e->d_next.ensure(2 * 2 * 4) && cudaMemsetAsync(e->d_next.p, 0, 4, s) == cudaSuccess)
+        next = e->d_next.as<uint32_t>();
     cudaEvent_t pa = prof_begin(e, s);
     switch (mode) {
-        case 1: k_collect<1><<<grid, COLLECT_WARPS * 32, smem, s>>>(v, q, n, words, d_off, d_cnt, d_ids, cap, d_total, raw); break;
-        case 2: k_collect<2><<<grid, COLLECT_WARPS * 32, smem, s>>>(v, q, n, words, d_off, d_cnt, d_ids, cap, d_total, raw); break;
-        default: k_collect<3><<<grid, COLLECT_WARPS * 32, smem, s>>>(v, q, n, words, d_off, d_cnt, d_ids, cap, d_total, raw); break;
+        case 1: k_collect<1><<<grid, COLLECT_WARPS * 32, smem, s>>>(v, q, n, words, d_off, d_cnt, d_ids, cap, d_total, raw, order, next); break;
+        case 2: k_collect<2><<<grid, COLLECT_WARPS * 32, smem, s>>>(v, q, n, words, d_off, d_cnt, d_ids, cap, d_total, raw, order, next); break;
+        default: k_collect<3><<<grid, COLLECT_WARPS * 32, smem, s>>>(v, q, n, words, d_off, d_cnt, d_ids, cap, d_total, raw, order, next); break;
     }
     CUDA_TRY(cudaGetLastError());
     prof_end(e, s, pa, JCDE_PROF_COLLECT);

@@ -832,12 +832,31 @@ template <int MODE>
 __global__ void __launch_bounds__(COLLECT_WARPS * 32) k_collect(View v, const uint32_t* __restrict__ q, uint32_t n,
                                                                 uint32_t words, uint32_t* __restrict__ offsets,
                                                                 uint32_t* __restrict__ counts, uint32_t* __restrict__ ids,
-                                                                uint32_t cap, uint32_t* __restrict__ total, RawShape raw) {
+                                                                uint32_t cap, uint32_t* __restrict__ total, RawShape raw,
+                                                                const uint32_t* __restrict__ order,
+                                                                uint32_t* __restrict__ next) {
     extern __shared__ uint32_t smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     uint32_t* bits = smem + (size_t)warp * words;
     const uint32_t stride = gridDim.x * COLLECT_WARPS;
-    for (uint32_t qi = blockIdx.x * COLLECT_WARPS + warp; qi < n; qi += stride) {
+    // queries in grid-stride order, or two at a time from the counter `next`
+    uint32_t i = 0, end = 0, gs = blockIdx.x * COLLECT_WARPS + warp;
+    for (;;) {
+        if (i >= end) {
+            if (next) {
+                uint32_t t = 0;
+                if (lane == 0) t = atomicAdd(next, 2u);
+                i = __shfl_sync(FULL, t, 0);
+                end = min(i + 2u, n);
+            } else {
+                i = gs;
+                end = gs + 1;
+                gs += stride;
+            }
+            if (i >= n) break;
+        }
+        const uint32_t qi = order ? __ldg(&order[i]) : i;
+        i++;
         QShape sh;
         DItem it{};
         Pt spoi;
@@ -872,15 +891,14 @@ __global__ void __launch_bounds__(COLLECT_WARPS * 32) k_collect(View v, const ui
             const uint32_t n_pier = (MODE & MODE_SURROGATE) ? it.n_piers : 0u;
             const uint32_t n_edge = (MODE & MODE_POLY) ? sh.nv : 0u;
             const uint32_t np = n_pole + n_pier + n_edge;
-            for (uint32_t p = lane; p < np; p += 32) {
+            for (uint32_t p = lane; p < np; p += 32) {   // lane l walks probes l, l+32, ...
                 if (p < n_pole) {
-                    float4 pl = __ldg(&v.poles[it.pole_off + p]);
-                    Disk d{xform(Pt{pl.x, pl.y}, sh.c, sh.s, sh.tx, sh.ty), pl.z};
-                    collect_walk(v, d, 0, bits);
+                    const float4 pl = __ldg(&v.poles[it.pole_off + p]);
+                    collect_walk(v, Disk{xform(Pt{pl.x, pl.y}, sh.c, sh.s, sh.tx, sh.ty), pl.z}, 0, bits);
                 } else if (p < n_pole + n_pier) {
-                    float4 pr = __ldg(&v.piers[it.pier_off + (p - n_pole)]);
-                    Seg sg{xform(Pt{pr.x, pr.y}, sh.c, sh.s, sh.tx, sh.ty), xform(Pt{pr.z, pr.w}, sh.c, sh.s, sh.tx, sh.ty)};
-                    collect_walk(v, sg, 0, bits);
+                    const float4 pr = __ldg(&v.piers[it.pier_off + (p - n_pole)]);
+                    collect_walk(v, Seg{xform(Pt{pr.x, pr.y}, sh.c, sh.s, sh.tx, sh.ty), xform(Pt{pr.z, pr.w}, sh.c, sh.s, sh.tx, sh.ty)},
+                                 0, bits);
                 } else {
                     collect_walk(v, sh.edge(p - n_pole - n_pier), vr, bits);
                 }
