@@ -90,7 +90,7 @@ struct jcde_engine {
     bool have_last_stream = false;
     cudaStream_t own[2] = {nullptr, nullptr};
     int n_sms = 0;
-    int detect_blocks_per_sm = 0, collect_blocks_per_sm = 0;
+    int detect_blocks_per_sm = 0, collect_blocks_per_sm = 0, tab_blocks_per_sm = 0;
     uint64_t launches = 0;
     // optional per-kernel timing (jcde_profile_enable): CUDA events around each launch
     bool prof = false;
@@ -333,6 +333,15 @@ static void init_launch_shape(jcde_engine* e) {
     else
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&e->detect_blocks_per_sm, k_poly<uint64_t, false>, POLY_WARPS * 32, 0);
     if (e->detect_blocks_per_sm < 1) e->detect_blocks_per_sm = 1;
+    // the small-batch polygon pass's leaf tables (dynamic shared memory) take its total above 48 KB
+    const int tab_smem = (int)(POLY_WARPS * sizeof(LeafTab));
+    cudaFuncSetAttribute(k_poly_tab<uint32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, tab_smem);
+    cudaFuncSetAttribute(k_poly_tab<uint64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, tab_smem);
+    if (e->cfg.quadtree_depth <= 8)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&e->tab_blocks_per_sm, k_poly_tab<uint32_t>, POLY_WARPS * 32, tab_smem);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&e->tab_blocks_per_sm, k_poly_tab<uint64_t>, POLY_WARPS * 32, tab_smem);
+    if (e->tab_blocks_per_sm < 1) e->tab_blocks_per_sm = 1;
     if (e->n_sms < 1) e->n_sms = 1;
 }
 
@@ -420,7 +429,7 @@ static void launch_passes_t(jcde_engine* e, const View& v, const uint32_t* q, ui
     }
     if (mode & 2) {
         const uint32_t want = (n + POLY_WARPS - 1) / POLY_WARPS;
-        const uint32_t grid = std::min<uint32_t>(want, (uint32_t)(e->n_sms * e->detect_blocks_per_sm));
+        uint32_t grid = std::min<uint32_t>(want, (uint32_t)(e->n_sms * e->detect_blocks_per_sm));
         cudaEvent_t pa = prof_begin(e, s);
         // Queries are handed to warps from a counter (`next`), so that no warp queues behind slow
         // queries: one at a time in small batches, JCDE_POLY_CHUNK at a time in large ones.  Small
@@ -428,8 +437,14 @@ static void launch_passes_t(jcde_engine* e, const View& v, const uint32_t* q, ui
         const bool tab = n <= JCDE_SURR_WARP_MAX;
         if (next) next += 1;   // the polygon pass's own counter
         if (!next || (!tab && !JCDE_POLY_CHUNK) || cudaMemsetAsync(next, 0, 4, s) != cudaSuccess) next = nullptr;
-        k_poly<PendT, false><<<grid, POLY_WARPS * 32, tab ? POLY_WARPS * sizeof(LeafTab) : 0, s>>>(
-            v, MultiSrc{}, q, n, dout, raw, mode == 3, order, tab, next, tab ? 1u : (uint32_t)JCDE_POLY_CHUNK);
+        if (tab) {
+            grid = std::min<uint32_t>(want, (uint32_t)(e->n_sms * e->tab_blocks_per_sm));
+            k_poly_tab<PendT><<<grid, POLY_WARPS * 32, POLY_WARPS * sizeof(LeafTab), s>>>(v, q, n, dout, raw, mode == 3,
+                                                                                        order, next);
+        } else {
+            k_poly<PendT, false><<<grid, POLY_WARPS * 32, 0, s>>>(v, MultiSrc{}, q, n, dout, raw, mode == 3, order, next,
+                                                                  (uint32_t)JCDE_POLY_CHUNK);
+        }
         prof_end(e, s, pa, JCDE_PROF_POLY);
         e->launches++;
     }
@@ -1067,7 +1082,7 @@ static void multi_launch_t(jcde_multi* m, const uint32_t* q, uint8_t* out, cudaS
     k_surrogate<PendT, true><<<sgrid, SURR_THREADS, 0, s>>>(View{}, ms, q, n, out, PENDING, order, next);
     const uint32_t pgrid = std::min<uint32_t>((n + POLY_WARPS - 1) / POLY_WARPS, (uint32_t)(m->n_sms * m->poly_blocks));
     k_poly<PendT, true><<<pgrid, POLY_WARPS * 32, 0, s>>>(View{}, ms, q, n, out, RawShape{nullptr, 0, 0, 0, 0}, true,
-                                                          order, false, next + 1, (uint32_t)std::max(JCDE_POLY_CHUNK, 1));
+                                                          order, next + 1, (uint32_t)std::max(JCDE_POLY_CHUNK, 1));
     m->launches += 5;
 }
 static void multi_launch(jcde_multi* m, const uint32_t* q, uint8_t* out, cudaStream_t s) {

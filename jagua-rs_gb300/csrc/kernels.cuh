@@ -506,14 +506,19 @@ __global__ void __launch_bounds__(SURR_THREADS) k_surrogate_warp(View v, const u
 // The table costs a walk and a scan of the reached leaves per query; it is built in the
 // latency-bound regime of small batches (k_poly's `leaf_tab`), where it shortens the slowest
 // queries' leaf loops.
-constexpr int LT_LEAVES = 8, LT_ENTS = 64;
+// The table also keeps, per tabled hazard, the edges whose box meets the shape's box: an edge
+// whose box misses the shape's box misses the box of every edge of the shape, and
+// edge_intersection rejects on those boxes first (edge.rs:188-199), so the other edges cannot be hit.
+constexpr int LT_LEAVES = 8, LT_ENTS = 64, LT_EDGES = 96;
 struct LeafTab {
     float4 ff[LT_ENTS];
-    uint2 ec[LT_ENTS];   // edge offset, edge count
+    uint2 ec[LT_ENTS];   // edge offset, edge count; offset | LT_LOCAL: into `edges` below
     int32_t node[LT_LEAVES];
     uint32_t start[LT_LEAVES + 1];
     uint32_t n_leaves;
+    float4 edges[LT_EDGES];
 };
+constexpr uint32_t LT_LOCAL = 0x80000000u;
 
 template <typename PendT>
 __device__ __forceinline__ void build_leaf_tab(const View& v, int vr, const Box& sb, LeafTab* lt, int lane) {
@@ -571,6 +576,35 @@ __device__ __forceinline__ void build_leaf_tab(const View& v, int vr, const Box&
         lt->n_leaves = nl;
     }
     __syncwarp();
+    uint32_t nx = 0;
+    for (uint32_t k = 0; k < ne; k++) {
+        const uint2 ec = lt->ec[k];
+        const uint32_t x0 = nx;
+        bool fits = true;
+        for (uint32_t b = 0; b < ec.y; b += 32) {
+            const uint32_t j = b + lane;
+            bool keep = false;
+            float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (j < ec.y) {
+                f = __ldg(&v.edges[ec.x + j]);
+                keep = !(fmx(fmn(f.x, f.z), sb.x0) > fmn(fmx(f.x, f.z), sb.x1)) &&
+                       !(fmx(fmn(f.y, f.w), sb.y0) > fmn(fmx(f.y, f.w), sb.y1));
+            }
+            const uint32_t bal = __ballot_sync(FULL, keep);
+            if (nx + __popc(bal) > (uint32_t)LT_EDGES) {
+                fits = false;
+                break;
+            }
+            if (keep) lt->edges[nx + __popc(bal & below)] = f;
+            nx += __popc(bal);
+        }
+        if (fits) {
+            if (lane == 0) lt->ec[k] = make_uint2(x0 | LT_LOCAL, nx - x0);
+        } else {
+            nx = x0;   // this hazard keeps its full edge list
+        }
+    }
+    __syncwarp();
 }
 
 template <class P>
@@ -585,6 +619,17 @@ __device__ __forceinline__ bool leaf_hits_tab(const View& v, const P& p, int nod
             const float4 f = lt->ff[k];
             if (!p_hits_box(p, Box{f.x, f.y, f.z, f.w})) continue;   // qt_partial_hazard.rs:67-71
             const uint2 ec = lt->ec[k];
+            if (ec.x & LT_LOCAL) {
+                const float4* es = lt->edges + (ec.x & ~LT_LOCAL);
+                for (uint32_t j = 0; j < ec.y; j++) {
+                    const float4 f = es[j];
+                    if (p_hits_seg(p, Seg{Pt{f.x, f.y}, Pt{f.z, f.w}})) {
+                        *stop = 1;
+                        return true;
+                    }
+                }
+                continue;
+            }
             for (uint32_t j = 0; j < ec.y; j++) {
                 if (p_hits_seg(p, ld_edge(v, ec.x + j))) {
                     *stop = 1;
@@ -624,7 +669,7 @@ __device__ __forceinline__ bool walk_step_tab(const View& v, const P& p, WalkT<P
 #define JCDE_POLY_MIN_BLOCKS 4   // 64 registers: four 256-thread blocks per SM
 #endif
 constexpr uint32_t POLY_MAXV = 256;   // items with more vertices transform edges on the fly
-template <typename PendT>
+template <typename PendT, bool TAB>
 __device__ __forceinline__ void poly_query(const View& v, const uint32_t* __restrict__ q, uint32_t qi,
                                            uint8_t* __restrict__ out, const RawShape& raw, volatile int* stop,
                                            float2* tv, uint32_t* jobsw, LeafTab* ltab, int lane) {
@@ -708,9 +753,11 @@ __device__ __forceinline__ void poly_query(const View& v, const uint32_t* __rest
         }
     }
     const LeafTab* tab = nullptr;
-    if (ltab && !hit && n_jobs > 0) {
-        build_leaf_tab<PendT>(v, vr, sb, ltab, lane);
-        tab = ltab;
+    if constexpr (TAB) {
+        if (!hit && n_jobs > 0) {
+            build_leaf_tab<PendT>(v, vr, sb, ltab, lane);
+            tab = ltab;
+        }
     }
     // Jobs are handed out dynamically: a lane whose walk is over takes the next unassigned job
     // (ballot rank), so no lane waits for the slowest walk of a fixed round.  Every loop
@@ -742,7 +789,8 @@ __device__ __forceinline__ void poly_query(const View& v, const uint32_t* __rest
         if (!__any_sync(FULL, active)) break;
         bool h = false;
         if (active) {
-            h = walk_step_tab(v, e, w, stop, tab);
+            if constexpr (TAB) h = walk_step_tab(v, e, w, stop, tab);
+            else h = walk_step(v, e, w, stop);
             if (!h && w.node < 0) w.node = -1;
         }
         hit = __any_sync(FULL, h);
@@ -788,12 +836,11 @@ __device__ __forceinline__ void poly_query(const View& v, const uint32_t* __rest
 template <typename PendT, bool MULTI>
 __global__ void __launch_bounds__(POLY_WARPS * 32, JCDE_POLY_MIN_BLOCKS)
     k_poly(View v, MultiSrc ms, const uint32_t* __restrict__ q, uint32_t n, uint8_t* __restrict__ out,
-           RawShape raw, bool only_pending, const uint32_t* __restrict__ order, bool leaf_tab,
-           uint32_t* __restrict__ next, uint32_t chunk) {
+           RawShape raw, bool only_pending, const uint32_t* __restrict__ order, uint32_t* __restrict__ next,
+           uint32_t chunk) {
     __shared__ int stops[POLY_WARPS];
     __shared__ float2 tverts[POLY_WARPS][POLY_MAXV];   // transformed item vertices
     __shared__ uint32_t jobs[POLY_WARPS][POLY_MAXV];   // edge index | children mask below the virtual root << 16
-    extern __shared__ LeafTab ltabs[];                 // POLY_WARPS tables when leaf_tab (dynamic)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     volatile int* stop = &stops[warp];
     const uint32_t stride = gridDim.x * POLY_WARPS;
@@ -817,11 +864,39 @@ __global__ void __launch_bounds__(POLY_WARPS * 32, JCDE_POLY_MIN_BLOCKS)
         i++;
         if (only_pending && out[qi] != PENDING) continue;
         if constexpr (MULTI)
-            poly_query<PendT>(ms.views[ms.layout_of(qi)], q, qi, out, raw, stop, tverts[warp], jobs[warp],
-                              leaf_tab ? &ltabs[warp] : nullptr, lane);
+            poly_query<PendT, false>(ms.views[ms.layout_of(qi)], q, qi, out, raw, stop, tverts[warp], jobs[warp],
+                                     nullptr, lane);
         else
-            poly_query<PendT>(v, q, qi, out, raw, stop, tverts[warp], jobs[warp], leaf_tab ? &ltabs[warp] : nullptr,
-                              lane);
+            poly_query<PendT, false>(v, q, qi, out, raw, stop, tverts[warp], jobs[warp], nullptr, lane);
+    }
+}
+
+// The polygon pass of small batches (latency-bound): leaf tables in dynamic shared memory, queries
+// one at a time from the counter `next`, and a register budget of its own (fewer, longer-lived warps).
+#ifndef JCDE_POLY_TAB_MIN_BLOCKS
+#define JCDE_POLY_TAB_MIN_BLOCKS 2
+#endif
+template <typename PendT>
+__global__ void __launch_bounds__(POLY_WARPS * 32, JCDE_POLY_TAB_MIN_BLOCKS)
+    k_poly_tab(View v, const uint32_t* __restrict__ q, uint32_t n, uint8_t* __restrict__ out, RawShape raw,
+               bool only_pending, const uint32_t* __restrict__ order, uint32_t* __restrict__ next) {
+    __shared__ int stops[POLY_WARPS];
+    __shared__ float2 tverts[POLY_WARPS][POLY_MAXV];
+    __shared__ uint32_t jobs[POLY_WARPS][POLY_MAXV];
+    extern __shared__ LeafTab ltabs[];   // one per warp
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    volatile int* stop = &stops[warp];
+    const uint32_t stride = gridDim.x * POLY_WARPS;
+    for (uint32_t i = next ? 0u : blockIdx.x * POLY_WARPS + warp;; i += stride) {
+        if (next) {
+            uint32_t t = 0;
+            if (lane == 0) t = atomicAdd(next, 1u);
+            i = __shfl_sync(FULL, t, 0);
+        }
+        if (i >= n) break;
+        const uint32_t qi = order ? __ldg(&order[i]) : i;
+        if (only_pending && out[qi] != PENDING) continue;
+        poly_query<PendT, true>(v, q, qi, out, raw, stop, tverts[warp], jobs[warp], &ltabs[warp], lane);
     }
 }
 
