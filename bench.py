@@ -279,6 +279,8 @@ def run_gpu(args):
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     stream = torch.cuda.current_stream()
     filt = lay.filter_keys
+    # launch choices timed on this batch before the run (jcde_autotune; verdicts checked identical)
+    tuning, tune_ms = eng.autotune(dq, filter=filt, stream=stream) if args.autotune else (eng.get_tuning(), None)
 
     for _ in range(args.warmup):
         eng.detect_batch(dq, filter=filt, out=out, stream=stream)
@@ -414,6 +416,7 @@ def run_gpu(args):
                     "ms_per_step": 1e3 * collect_s / args.steps, "keys_per_query": collect_total / N_QUERIES,
                     "parity_sample": {"queries": n_cs, "bit_exact": bool(collect_ok)}},
         "gpu_launches": launches,
+        "tuning": {"chosen": tuning, "autotuned": bool(args.autotune), "median_ms_at_tuning": tune_ms},
         "clocks": clocks,
         "wall_s_timed": wall,
         "parity_sample": {"queries": args.cpu_sample, "bit_exact": sample_ok},
@@ -718,6 +721,7 @@ def main():
     ap.add_argument("--impl", default="jcde", choices=["jcde", "reference"])
     ap.add_argument("--cpu-sample", type=int, default=1 << 17)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--autotune", type=int, default=1, help="1: jcde_autotune on the batch before timing")
     ap.add_argument("--lbf-cpu-steps", type=int, default=2000)
     ap.add_argument("--workload", default="star", choices=["star", "multi", "proxy", "lbf"],
                     help="star: the headline single-layout batch; multi: 64 layouts in one launch sequence; "

@@ -297,6 +297,24 @@ jcde_status jcde_lbf_read(jcde_resident* r, uint32_t* counts4, uint32_t* placeme
                           uint32_t* removals, uint32_t removal_cap, uint32_t* free_counts, uint32_t free_cap,
                           uint8_t* verdicts, uint64_t verdict_cap);
 
+/* --- Launch tuning (no counterpart in the reference) ---------------------------------------------
+ * How the detect passes are launched for a batch of n queries.  None of these choices changes a
+ * verdict.  Defaults suit both a 1M-query batch and an LBF step of 16K candidates. */
+typedef struct jcde_tuning {
+    uint32_t surrogate_warp_max;   /* n <= this: one warp per query in the surrogate pass, else one thread */
+    uint32_t leaf_table_max;       /* n <= this: polygon pass with per-query leaf tables, queries one by one */
+    uint32_t poly_chunk;           /* otherwise: queries per counter grab in the polygon pass (0: grid stride) */
+    uint32_t order_min_batch;      /* n >= this: queries visited in Morton order of their translation */
+} jcde_tuning;
+jcde_status jcde_get_tuning(const jcde_engine* e, jcde_tuning* out);
+jcde_status jcde_set_tuning(jcde_engine* e, const jcde_tuning* t);
+/* Times all 16 combinations (surrogate pass warp/thread x polygon pass leaf tables/grabs of 1, 2, 4 x
+ * Morton order on/off) on the caller's batch, checks that every combination gives the same verdicts
+ * (JCDE_ERR_STATE otherwise), keeps the fastest in the engine (its thresholds set so that batches of
+ * this size take it) and returns it with its median time.  Synchronises. */
+jcde_status jcde_autotune(jcde_engine* e, const jcde_query* d_queries, uint32_t n, const jcde_filter* f, void* stream,
+                          jcde_tuning* out, double* best_ms);
+
 /* --- snapshots: CDEngine::save / restore (cd_engine.rs:98-149) ------------------------------- */
 jcde_status jcde_save(const jcde_engine* e, jcde_snapshot** out);
 jcde_status jcde_restore(jcde_engine* e, const jcde_snapshot* s);

@@ -21,6 +21,23 @@ using namespace jcde;
 
 namespace {
 
+// Launch-shape defaults (jcde_tuning changes them per engine).
+#ifndef JCDE_SURR_WARP_MAX
+#define JCDE_SURR_WARP_MAX (1u << 17)
+#endif
+#ifndef JCDE_POLY_CHUNK
+#define JCDE_POLY_CHUNK 2   // 0: large batches in grid-stride order
+#endif
+#ifndef JCDE_SURR_DYNAMIC
+#define JCDE_SURR_DYNAMIC 1
+#endif
+#ifndef JCDE_COLLECT_DYNAMIC
+#define JCDE_COLLECT_DYNAMIC 1
+#endif
+#ifndef JCDE_ORDER_MIN_BATCH
+#define JCDE_ORDER_MIN_BATCH 4096u
+#endif
+
 struct DevBuf {
     void* p = nullptr;
     size_t cap = 0;
@@ -91,6 +108,8 @@ struct jcde_engine {
     cudaStream_t own[2] = {nullptr, nullptr};
     int n_sms = 0;
     int detect_blocks_per_sm = 0, collect_blocks_per_sm = 0, tab_blocks_per_sm = 0;
+    // launch choices of the detect passes (jcde_set_tuning / jcde_autotune)
+    jcde_tuning tune{JCDE_SURR_WARP_MAX, JCDE_SURR_WARP_MAX, (uint32_t)JCDE_POLY_CHUNK, JCDE_ORDER_MIN_BATCH};
     uint64_t launches = 0;
     // optional per-kernel timing (jcde_profile_enable): CUDA events around each launch
     bool prof = false;
@@ -348,10 +367,7 @@ static void init_launch_shape(jcde_engine* e) {
 #ifndef JCDE_SPATIAL_ORDER
 #define JCDE_SPATIAL_ORDER 1
 #endif
-#ifndef JCDE_ORDER_MIN_BATCH
-#define JCDE_ORDER_MIN_BATCH 4096u
-#endif
-constexpr uint32_t ORDER_MIN_BATCH = JCDE_ORDER_MIN_BATCH;   // below this a batch is visited in its own order
+
 
 // Visit order of a batch: cell-by-cell over the CDE box (k_bucket_*), or nullptr for index order.
 // `slot` selects one of two histogram/order buffer pairs, so that the two streams of the host
@@ -360,7 +376,7 @@ static const uint32_t* spatial_order_into(jcde_engine* e, const uint32_t* q, uin
                                           uint32_t* hist, uint32_t* order);
 static const uint32_t* spatial_order(jcde_engine* e, const uint32_t* q, uint32_t n, cudaStream_t s, int slot,
                                      uint32_t slot_cap) {
-    if (!JCDE_SPATIAL_ORDER || n < ORDER_MIN_BATCH) return nullptr;
+    if (!JCDE_SPATIAL_ORDER || n < e->tune.order_min_batch) return nullptr;
     const size_t per_slot = std::max<size_t>(n, slot_cap);
     if (!e->d_hist.ensure(2 * N_BUCKETS * 4)) return nullptr;
     if (e->d_order.cap < 2 * per_slot * 4) {
@@ -391,25 +407,14 @@ static const uint32_t* spatial_order_into(jcde_engine* e, const uint32_t* q, uin
 // The surrogate pass and/or the polygon pass; the walk's pending masks are 32-bit for trees of
 // depth <= 8 and 64-bit above.  Batches of at most JCDE_SURR_WARP_MAX queries take the
 // warp-per-query surrogate pass.
-#ifndef JCDE_SURR_WARP_MAX
-#define JCDE_SURR_WARP_MAX (1u << 17)
-#endif
-#ifndef JCDE_POLY_CHUNK
-#define JCDE_POLY_CHUNK 2   // 0: large batches in grid-stride order
-#endif
-#ifndef JCDE_SURR_DYNAMIC
-#define JCDE_SURR_DYNAMIC 1
-#endif
-#ifndef JCDE_COLLECT_DYNAMIC
-#define JCDE_COLLECT_DYNAMIC 1
-#endif
+
 template <typename PendT>
 static void launch_passes_t(jcde_engine* e, const View& v, const uint32_t* q, uint32_t n, uint8_t* dout,
                             cudaStream_t s, RawShape raw, int mode, const uint32_t* order, uint32_t* next) {
     if (mode & 1) {
         const uint8_t miss = mode == 1 ? (uint8_t)0 : PENDING;
         cudaEvent_t pa = prof_begin(e, s);
-        if (n <= JCDE_SURR_WARP_MAX) {   // too few queries to fill the GPU one thread each
+        if (n <= e->tune.surrogate_warp_max) {   // too few queries to fill the GPU one thread each
             const uint32_t wpb = SURR_THREADS / 32;
             const uint32_t grid = std::min<uint32_t>((n + wpb - 1) / wpb, (uint32_t)e->n_sms * 8);
             k_surrogate_warp<PendT><<<grid, SURR_THREADS, 0, s>>>(v, q, n, dout, miss, order);
@@ -434,16 +439,16 @@ static void launch_passes_t(jcde_engine* e, const View& v, const uint32_t* q, ui
         // Queries are handed to warps from a counter (`next`), so that no warp queues behind slow
         // queries: one at a time in small batches, JCDE_POLY_CHUNK at a time in large ones.  Small
         // batches are latency-bound and also build per-query leaf tables.
-        const bool tab = n <= JCDE_SURR_WARP_MAX;
+        const bool tab = n <= e->tune.leaf_table_max;
         if (next) next += 1;   // the polygon pass's own counter
-        if (!next || (!tab && !JCDE_POLY_CHUNK) || cudaMemsetAsync(next, 0, 4, s) != cudaSuccess) next = nullptr;
+        if (!next || (!tab && !e->tune.poly_chunk) || cudaMemsetAsync(next, 0, 4, s) != cudaSuccess) next = nullptr;
         if (tab) {
             grid = std::min<uint32_t>(want, (uint32_t)(e->n_sms * e->tab_blocks_per_sm));
             k_poly_tab<PendT><<<grid, POLY_WARPS * 32, POLY_WARPS * sizeof(LeafTab), s>>>(v, q, n, dout, raw, mode == 3,
                                                                                         order, next);
         } else {
             k_poly<PendT, false><<<grid, POLY_WARPS * 32, 0, s>>>(v, MultiSrc{}, q, n, dout, raw, mode == 3, order, next,
-                                                                  (uint32_t)JCDE_POLY_CHUNK);
+                                                                  std::max(e->tune.poly_chunk, 1u));
         }
         prof_end(e, s, pa, JCDE_PROF_POLY);
         e->launches++;
@@ -1368,7 +1373,7 @@ static void resident_detect(jcde_resident* r, const uint32_t* q, uint32_t n, uin
     const View v = resident_view(r);
     // small batches (one LBF step's candidates) gain nothing from the visit order
     const uint32_t* order = nullptr;
-    if (JCDE_SPATIAL_ORDER && n > JCDE_SURR_WARP_MAX)
+    if (JCDE_SPATIAL_ORDER && n >= e->tune.order_min_batch && n > e->tune.surrogate_warp_max)
         order = spatial_order_into(e, q, n, s, r->d_hist.as<uint32_t>(), r->d_order.as<uint32_t>());
     launch_passes(e, v, q, n, dout, s, RawShape{}, 3, order, r->d_next.as<uint32_t>());
     r->launches += (order ? 3 : 0) + 2;
@@ -1759,6 +1764,99 @@ jcde_status jcde_lbf_read(jcde_resident* r, uint32_t* counts4, uint32_t* placeme
     RCtl c{};
     CUDA_TRY(cudaMemcpy(&c, r->t.ctl, sizeof(RCtl), cudaMemcpyDeviceToHost));
     return c.error ? JCDE_ERR_CAPACITY : JCDE_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------------------------
+// Launch tuning (no counterpart in the reference).
+// ---------------------------------------------------------------------------------------------
+extern "C" {
+
+jcde_status jcde_get_tuning(const jcde_engine* e, jcde_tuning* out) {
+    if (!e || !out) return JCDE_ERR_ARG;
+    *out = e->tune;
+    return JCDE_OK;
+}
+
+jcde_status jcde_set_tuning(jcde_engine* e, const jcde_tuning* t) {
+    if (!e || !t) return JCDE_ERR_ARG;
+    e->tune = *t;
+    return JCDE_OK;
+}
+
+// Times every combination of the launch choices on the caller's batch (one warm-up, then the median
+// of three timed runs each, CUDA events on `stream`), checks that all of them give the same
+// verdicts, keeps the fastest in the engine and returns it.
+jcde_status jcde_autotune(jcde_engine* e, const jcde_query* d_queries, uint32_t n, const jcde_filter* f, void* stream,
+                          jcde_tuning* out, double* best_ms) {
+    if (!e || !d_queries || !n) return JCDE_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    const jcde_tuning saved = e->tune;
+    DevBuf d_ref, d_out;
+    if (!d_ref.ensure(n) || !d_out.ensure(n)) return JCDE_ERR_CUDA;
+    std::vector<uint8_t> ref(n), got(n);
+    cudaEvent_t a = nullptr, b = nullptr;
+    CUDA_TRY(cudaEventCreate(&a));
+    if (cudaEventCreate(&b) != cudaSuccess) {
+        cudaEventDestroy(a);
+        return JCDE_ERR_CUDA;
+    }
+    jcde_status st = JCDE_OK;
+    jcde_tuning best = saved;
+    double best_t = 1e300;
+    bool have_ref = false;
+    const uint32_t all = 0xFFFFFFFFu;
+    for (int sm = 0; sm < 2 && !st; sm++)            // surrogate pass: warp per query / thread per query
+        for (int pm = 0; pm < 4 && !st; pm++)        // polygon pass: leaf tables / counter grabs of 1, 2, 4
+            for (int om = 0; om < 2 && !st; om++) {  // visit order: Morton / batch order
+                jcde_tuning t;
+                t.surrogate_warp_max = sm == 0 ? all : 0u;
+                t.leaf_table_max = pm == 0 ? all : 0u;
+                t.poly_chunk = pm == 0 ? 1u : (1u << (pm - 1));
+                t.order_min_batch = om == 0 ? 0u : all;
+                e->tune = t;
+                float ms[3] = {0, 0, 0};
+                for (int r = -1; r < 3 && !st; r++) {
+                    if (r >= 0 && cudaEventRecord(a, s) != cudaSuccess) st = JCDE_ERR_CUDA;
+                    if (!st) st = launch_detect(e, 3, d_queries, n, f, d_out.as<uint8_t>(), s, RawShape{nullptr, 0, 0, 0, 0});
+                    if (!st && r >= 0) {
+                        if (cudaEventRecord(b, s) != cudaSuccess || cudaEventSynchronize(b) != cudaSuccess ||
+                            cudaEventElapsedTime(&ms[r], a, b) != cudaSuccess)
+                            st = JCDE_ERR_CUDA;
+                    }
+                }
+                if (st) break;
+                std::sort(ms, ms + 3);
+                if (cudaMemcpy(have_ref ? got.data() : ref.data(), d_out.p, n, cudaMemcpyDeviceToHost) != cudaSuccess) {
+                    st = JCDE_ERR_CUDA;
+                    break;
+                }
+                if (have_ref && std::memcmp(ref.data(), got.data(), n) != 0) {
+                    st = JCDE_ERR_STATE;   // launch choices must never change a verdict
+                    break;
+                }
+                have_ref = true;
+                if (ms[1] < best_t) {
+                    best_t = ms[1];
+                    best = t;
+                }
+            }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    // thresholds of the winner, extended to every batch at least this large / at most this small
+    if (!st) {
+        if (best.surrogate_warp_max == all) best.surrogate_warp_max = std::max(n, saved.surrogate_warp_max);
+        else best.surrogate_warp_max = std::min(n - 1, saved.surrogate_warp_max);
+        if (best.leaf_table_max == all) best.leaf_table_max = std::max(n, saved.leaf_table_max);
+        else best.leaf_table_max = std::min(n - 1, saved.leaf_table_max);
+        if (best.order_min_batch == all) best.order_min_batch = std::max(n + 1, saved.order_min_batch);
+        else best.order_min_batch = std::min(n, saved.order_min_batch);
+    }
+    e->tune = st ? saved : best;
+    if (out) *out = e->tune;
+    if (best_ms) *best_ms = st ? 0.0 : best_t;
+    return st;
 }
 
 }  // extern "C"

@@ -33,6 +33,11 @@ class jcde_lbf_params(C.Structure):
                 ("reserved", C.c_uint32), ("sample_box", jcde_rect)]
 
 
+class jcde_tuning(C.Structure):
+    _fields_ = [("surrogate_warp_max", C.c_uint32), ("leaf_table_max", C.c_uint32), ("poly_chunk", C.c_uint32),
+                ("order_min_batch", C.c_uint32)]
+
+
 class jcde_config(C.Structure):
     _fields_ = [
         ("quadtree_depth", C.c_uint8),
@@ -113,6 +118,9 @@ SIGNATURES = {
     "jcde_lbf_steps": (C.c_int32, [P, C.c_uint32, C.c_uint32, P]),
     "jcde_lbf_read": (C.c_int32, [P, u32p, u32p, C.c_uint32, u32p, C.c_uint32, u32p, C.c_uint32, P, C.c_uint64]),
     "jcde_lbf_select": (C.c_int32, [P, P, P, C.c_uint32, P, P]),
+    "jcde_get_tuning": (C.c_int32, [P, P]),
+    "jcde_set_tuning": (C.c_int32, [P, P]),
+    "jcde_autotune": (C.c_int32, [P, P, C.c_uint32, P, P, P, C.POINTER(C.c_double)]),
     "jcde_proxy_batch": (C.c_int32, [P, P, P, C.c_uint32, C.POINTER(jcde_filter), P, P, P]),
     "jcde_separate_batch": (C.c_int32, [P, P, P, C.c_uint32, C.c_uint32, C.c_float, C.c_float, C.c_float, C.POINTER(jcde_filter), P, P, P]),
     "jcde_resample_batch": (C.c_int32, [P, P, P, C.c_uint32, C.c_uint32, C.c_float, C.c_float, C.c_uint32, P, P]),

@@ -16,7 +16,8 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _ffi
-from ._ffi import check, jcde_config, jcde_filter, jcde_hazard, jcde_lbf_params, jcde_rect, jcde_resident_config, lib
+from ._ffi import (check, jcde_config, jcde_filter, jcde_hazard, jcde_lbf_params, jcde_rect, jcde_resident_config,
+                   jcde_tuning, lib)
 from .workload import QUERY_DTYPE
 
 PLACED_ITEM, EXTERIOR, HOLE, QUALITY_ZONE = 0, 1, 2, 3
@@ -331,6 +332,29 @@ class CDEngine:
 
     def kernel_launches(self) -> int:
         return int(lib().jcde_kernel_launches(self.h))
+
+    TUNING_FIELDS = ("surrogate_warp_max", "leaf_table_max", "poly_chunk", "order_min_batch")
+
+    def get_tuning(self) -> dict:
+        t = jcde_tuning()
+        check(lib().jcde_get_tuning(self.h, C.byref(t)), "get_tuning")
+        return {k: int(getattr(t, k)) for k in self.TUNING_FIELDS}
+
+    def set_tuning(self, **fields) -> None:
+        cur = self.get_tuning()
+        cur.update(fields)
+        t = jcde_tuning(*[int(cur[k]) for k in self.TUNING_FIELDS])
+        check(lib().jcde_set_tuning(self.h, C.byref(t)), "set_tuning")
+
+    def autotune(self, queries, filter=None, stream=None) -> tuple:
+        """jcde_autotune on a CUDA batch: (chosen tuning, its median ms)."""
+        f = _Filter(filter)
+        n = queries.numel() * queries.element_size() // QUERY_DTYPE.itemsize
+        t = jcde_tuning()
+        ms = C.c_double()
+        check(lib().jcde_autotune(self.h, queries.data_ptr(), n, f.ref, _stream_handle(stream), C.byref(t),
+                                  C.byref(ms)), "autotune")
+        return {k: int(getattr(t, k)) for k in self.TUNING_FIELDS}, float(ms.value)
 
     PROFILE_KINDS = ("surrogate", "poly", "collect", "order", "filter", "proxy", "update", "lbf")
 

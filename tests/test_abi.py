@@ -86,3 +86,13 @@ def test_python_engine_errors(jcde_mod):
         eng.deregister_hazard_by_key(3)
     with pytest.raises(KeyError):
         eng.deregister_hazard_by_entity(0, 12345)
+
+
+def test_tuning_round_trip(jcde_mod):
+    eng = jcde_mod.CDEngine((0.0, 0.0, 100.0, 100.0))
+    t = eng.get_tuning()
+    assert t["surrogate_warp_max"] == 1 << 17 and t["poly_chunk"] == 2
+    eng.set_tuning(poly_chunk=4, order_min_batch=0xFFFFFFFF)
+    t2 = eng.get_tuning()
+    assert t2["poly_chunk"] == 4 and t2["order_min_batch"] == 0xFFFFFFFF
+    assert t2["surrogate_warp_max"] == t["surrogate_warp_max"]

@@ -212,3 +212,16 @@ def test_gpu_generated_layout_equals_oracle_layout(strip_layout, jcde_mod):
     assert len(lay_g.hazards) == len(lay_o.hazards)
     for a, b in zip(lay_o.hazards, lay_g.hazards):
         assert a.key == b.key and a.xy.tobytes() == b.xy.tobytes() and a.poi.tobytes() == b.poi.tobytes()
+
+
+def test_autotune_keeps_verdicts(star, oracle_mod):
+    """Every launch choice the autotuner times gives the oracle's verdicts; the chosen one is kept."""
+    lay, oeng, geng = star
+    q = W.queries_for(lay, 1 << 17, 0xA7, sid=9)
+    saved = geng.get_tuning()
+    try:
+        t, ms = geng.autotune(torch_queries(q), filter=lay.filter_keys)
+        assert ms > 0 and geng.get_tuning() == t
+        assert np.array_equal(gpu_detect(geng, q, filter=lay.filter_keys), oeng.detect_batch(q, ignored=lay.filter_keys))
+    finally:
+        geng.set_tuning(**saved)
