@@ -450,6 +450,8 @@ def run_multi(args):
     stream = torch.cuda.Stream()
     m = jcde.MultiEngine(engines)
     qb = W.QUERY_DTYPE.itemsize
+    # launch choices of the batched sequence timed on this batch (jcde_multi_autotune; verdicts checked)
+    multi_tuning, _ = m.autotune(dq, offs, stream=stream) if args.autotune else ({"poly_chunk": 2, "ordered": True}, 0)
 
     def plain():
         for l, eng in enumerate(engines):
@@ -487,6 +489,7 @@ def run_multi(args):
                    "l2": "flushed between steps (256 MB write)"},
         "plain": {"value": n / (res["plain"] / 1e3), "ms_per_step": res["plain"]},
         "speedup_vs_plain": res["plain"] / res["batched"],
+        "batched_tuning": multi_tuning,
         "same_verdicts": same,
         "impl": "jcde",
     }

@@ -1015,6 +1015,8 @@ struct jcde_multi {
     DevBuf d_next;                    // work counters of the two passes
     bool wide = false;                // a tree deeper than 8 levels needs 64-bit walk masks
     int surr_blocks = 1;
+    uint32_t poly_chunk = JCDE_POLY_CHUNK > 0 ? JCDE_POLY_CHUNK : 1;   // launch choices (jcde_multi_autotune)
+    bool ordered = true;
     int n_sms = 1, poly_blocks = 1;
     // graph replay
     cudaGraphExec_t exec = nullptr;
@@ -1074,12 +1076,16 @@ static void multi_launch_t(jcde_multi* m, const uint32_t* q, uint8_t* out, cudaS
     const uint32_t L = (uint32_t)m->engines.size(), n = m->offs[L];
     const MultiSrc ms{m->d_views.as<View>(), m->d_offs.as<uint32_t>(), L};
     uint32_t* hist = m->d_hist.as<uint32_t>();
-    uint32_t* order = m->d_order.as<uint32_t>();
+    uint32_t* order = nullptr;
     const uint32_t grid = std::min<uint32_t>((n + 255) / 256, (uint32_t)m->n_sms * 8);
-    cudaMemsetAsync(hist, 0, (size_t)L * N_BUCKETS * 4, s);
-    k_mbucket_count<<<grid, 256, 0, s>>>(q, n, ms, hist);
-    k_scan_counts<<<1, 1024, 0, s>>>(hist, L * N_BUCKETS);
-    k_mbucket_scatter<<<grid, 256, 0, s>>>(q, n, ms, hist, order);
+    if (m->ordered) {
+        order = m->d_order.as<uint32_t>();
+        cudaMemsetAsync(hist, 0, (size_t)L * N_BUCKETS * 4, s);
+        k_mbucket_count<<<grid, 256, 0, s>>>(q, n, ms, hist);
+        k_scan_counts<<<1, 1024, 0, s>>>(hist, L * N_BUCKETS);
+        k_mbucket_scatter<<<grid, 256, 0, s>>>(q, n, ms, hist, order);
+        m->launches += 3;
+    }
     // both passes take their queries from counters (see launch_passes_t)
     uint32_t* next = m->d_next.as<uint32_t>();
     cudaMemsetAsync(next, 0, 2 * 4, s);
@@ -1087,8 +1093,8 @@ static void multi_launch_t(jcde_multi* m, const uint32_t* q, uint8_t* out, cudaS
     k_surrogate<PendT, true><<<sgrid, SURR_THREADS, 0, s>>>(View{}, ms, q, n, out, PENDING, order, next);
     const uint32_t pgrid = std::min<uint32_t>((n + POLY_WARPS - 1) / POLY_WARPS, (uint32_t)(m->n_sms * m->poly_blocks));
     k_poly<PendT, true><<<pgrid, POLY_WARPS * 32, 0, s>>>(View{}, ms, q, n, out, RawShape{nullptr, 0, 0, 0, 0}, true,
-                                                          order, next + 1, (uint32_t)std::max(JCDE_POLY_CHUNK, 1));
-    m->launches += 5;
+                                                          order, next + 1, m->poly_chunk);
+    m->launches += 2;
 }
 static void multi_launch(jcde_multi* m, const uint32_t* q, uint8_t* out, cudaStream_t s) {
     if (m->wide) multi_launch_t<uint64_t>(m, q, out, s);
@@ -1185,7 +1191,7 @@ jcde_status jcde_multi_detect_graph(jcde_multi* m, const jcde_query* dq, const u
         m->g_offs = m->offs;
     }
     CUDA_TRY(cudaGraphLaunch(m->exec, s));
-    m->launches += 5;
+    m->launches += m->ordered ? 5 : 2;
     for (jcde_engine* e : m->engines) {
         e->last_stream = s;
         e->have_last_stream = true;
@@ -1860,3 +1866,69 @@ jcde_status jcde_autotune(jcde_engine* e, const jcde_query* d_queries, uint32_t 
 }
 
 }  // extern "C"
+
+extern "C" jcde_status jcde_multi_autotune(jcde_multi* m, const jcde_query* dq, const uint32_t* offsets,
+                                           const jcde_filter* filters, uint8_t* d_out, void* stream, uint32_t* out2,
+                                           double* best_ms) {
+    if (!m || !offsets || !dq || !d_out) return JCDE_ERR_ARG;
+    const uint32_t n = offsets[m->engines.size()];
+    if (!n) return JCDE_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    const uint32_t saved_chunk = m->poly_chunk;
+    const bool saved_ordered = m->ordered;
+    std::vector<uint8_t> ref(n), got(n);
+    cudaEvent_t a = nullptr, b = nullptr;
+    CUDA_TRY(cudaEventCreate(&a));
+    if (cudaEventCreate(&b) != cudaSuccess) {
+        cudaEventDestroy(a);
+        return JCDE_ERR_CUDA;
+    }
+    jcde_status st = JCDE_OK;
+    double best_t = 1e300;
+    uint32_t best_chunk = saved_chunk;
+    bool best_ordered = saved_ordered, have_ref = false;
+    for (int om = 0; om < 2 && !st; om++)
+        for (uint32_t chunk = 1; chunk <= 8 && !st; chunk *= 2) {
+            m->ordered = om == 0;
+            m->poly_chunk = chunk;
+            float ms[3] = {0, 0, 0};
+            for (int r = -1; r < 3 && !st; r++) {
+                if (r >= 0 && cudaEventRecord(a, s) != cudaSuccess) st = JCDE_ERR_CUDA;
+                if (!st) st = jcde_multi_detect(m, dq, offsets, filters, d_out, s);
+                if (!st && r >= 0 &&
+                    (cudaEventRecord(b, s) != cudaSuccess || cudaEventSynchronize(b) != cudaSuccess ||
+                     cudaEventElapsedTime(&ms[r], a, b) != cudaSuccess))
+                    st = JCDE_ERR_CUDA;
+            }
+            if (st) break;
+            std::sort(ms, ms + 3);
+            if (cudaMemcpy(have_ref ? got.data() : ref.data(), d_out, n, cudaMemcpyDeviceToHost) != cudaSuccess) {
+                st = JCDE_ERR_CUDA;
+                break;
+            }
+            if (have_ref && std::memcmp(ref.data(), got.data(), n) != 0) {
+                st = JCDE_ERR_STATE;   // launch choices must never change a verdict
+                break;
+            }
+            have_ref = true;
+            if (ms[1] < best_t) {
+                best_t = ms[1];
+                best_chunk = chunk;
+                best_ordered = om == 0;
+            }
+        }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    m->poly_chunk = st ? saved_chunk : best_chunk;
+    m->ordered = st ? saved_ordered : best_ordered;
+    if (m->exec && (m->poly_chunk != saved_chunk || m->ordered != saved_ordered)) {   // recapture next time
+        cudaGraphExecDestroy(m->exec);
+        m->exec = nullptr;
+    }
+    if (out2) {
+        out2[0] = m->poly_chunk;
+        out2[1] = m->ordered ? 1u : 0u;
+    }
+    if (best_ms) *best_ms = st ? 0.0 : best_t;
+    return st;
+}

@@ -484,6 +484,19 @@ class MultiEngine:
     def kernel_launches(self) -> int:
         return int(lib().jcde_multi_kernel_launches(self.h))
 
+    def autotune(self, queries, offsets, filters=None, stream=None) -> tuple:
+        """jcde_multi_autotune: ({"poly_chunk", "ordered"}, median ms of the choice)."""
+        import torch
+
+        offs = np.ascontiguousarray(offsets, dtype=np.uint32)
+        out = torch.empty(int(offs[-1]), dtype=torch.uint8, device=queries.device)
+        farr, keep = self._filters(filters)
+        o2 = (C.c_uint32 * 2)()
+        ms = C.c_double()
+        check(lib().jcde_multi_autotune(self.h, queries.data_ptr(), offs.ctypes.data_as(C.POINTER(C.c_uint32)), farr,
+                                        out.data_ptr(), _stream_handle(stream), o2, C.byref(ms)), "multi_autotune")
+        return {"poly_chunk": int(o2[0]), "ordered": bool(o2[1])}, float(ms.value)
+
 
 
 class ResidentEngine:

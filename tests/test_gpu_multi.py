@@ -75,3 +75,19 @@ def test_multi_graph_replay_and_recapture(bins):
     s.synchronize()
     assert np.array_equal(out.cpu().numpy(), ref2)
     engines[2].register_hazard(jcde.Hazard(hz.kind, hz.xy, hz.poi, hz.dynamic, hz.tag))
+
+
+def test_multi_autotune_keeps_verdicts(bins):
+    import torch
+
+    lays, engines, q, offs = bins
+    ref = _per_engine(engines, q, offs, None)
+    m = jcde.MultiEngine(engines)
+    dq = torch.from_numpy(q.view(np.uint8).copy()).cuda()
+    choice, ms = m.autotune(dq, offs)
+    assert ms > 0 and choice["poly_chunk"] in (1, 2, 4, 8)
+    assert np.array_equal(m.detect(dq, offs).cpu().numpy(), ref)
+    st = torch.cuda.Stream()   # a captured graph needs a stream other than the legacy default one
+    got = m.detect(dq, offs, graph=True, stream=st)
+    torch.cuda.synchronize()
+    assert np.array_equal(got.cpu().numpy(), ref)
