@@ -34,6 +34,9 @@ namespace {
 #ifndef JCDE_COLLECT_DYNAMIC
 #define JCDE_COLLECT_DYNAMIC 1
 #endif
+#ifndef JCDE_HOST_CHUNKS
+#define JCDE_HOST_CHUNKS 2   // pipelined chunks of a large host batch (jcde_detect_batch_host)
+#endif
 #ifndef JCDE_ORDER_MIN_BATCH
 #define JCDE_ORDER_MIN_BATCH 4096u
 #endif
@@ -106,6 +109,7 @@ struct jcde_engine {
     cudaStream_t last_stream = nullptr;
     bool have_last_stream = false;
     cudaStream_t own[2] = {nullptr, nullptr};
+    cudaEvent_t ev_ready = nullptr;   // the host entry point's filter is ready (orders the second stream)
     int n_sms = 0;
     int detect_blocks_per_sm = 0, collect_blocks_per_sm = 0, tab_blocks_per_sm = 0;
     // launch choices of the detect passes (jcde_set_tuning / jcde_autotune)
@@ -123,6 +127,7 @@ struct jcde_engine {
     ~jcde_engine() {
         for (auto& s : own)
             if (s) cudaStreamDestroy(s);
+        if (ev_ready) cudaEventDestroy(ev_ready);
         for (auto& m : prof_open) {
             cudaEventDestroy(m.a);
             cudaEventDestroy(m.b);
@@ -688,12 +693,15 @@ jcde_status jcde_detect_batch_host(jcde_engine* e, const jcde_query* hq, uint32_
     if (!e->d_q.ensure((size_t)n * sizeof(jcde_query)) || !e->d_out.ensure(n)) return JCDE_ERR_CUDA;
     jcde_status st = sync_device(e);
     if (st) return st;
-    // resolve the filter once, on the first stream, before the pipelined chunks
+    // resolve the filter once, on the first stream, before the pipelined chunks (the second stream
+    // waits for it on the device)
     View probe = base_view(e);
     if ((st = apply_filter(e, f, e->own[0], probe))) return st;
-    CUDA_TRY(cudaStreamSynchronize(e->own[0]));
-    // chunks alternate between two streams so that copies overlap the other chunk's kernel
-    const uint32_t n_chunks = n >= (1u << 18) ? 4u : 1u;
+    if (!e->ev_ready) CUDA_TRY(cudaEventCreateWithFlags(&e->ev_ready, cudaEventDisableTiming));
+    CUDA_TRY(cudaEventRecord(e->ev_ready, e->own[0]));
+    CUDA_TRY(cudaStreamWaitEvent(e->own[1], e->ev_ready, 0));
+    // chunks alternate between two streams so that copies overlap the other chunk's kernels
+    const uint32_t n_chunks = n >= (1u << 18) ? (uint32_t)JCDE_HOST_CHUNKS : 1u;
     const uint32_t chunk = (n + n_chunks - 1) / n_chunks;
     jcde_query* dq = e->d_q.as<jcde_query>();
     uint8_t* dout = e->d_out.as<uint8_t>();
