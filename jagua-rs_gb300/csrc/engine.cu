@@ -1258,9 +1258,11 @@ jcde_status jcde_separate_batch(jcde_engine* e, float* d_params, const uint32_t*
     if (st || n == 0) return st;
     const uint32_t per_block = PROXY_WARPS * (32 / JCDE_SEP_LANES);
     const uint32_t grid = std::min<uint32_t>((n + per_block - 1) / per_block, (uint32_t)e->n_sms * 8);
+    uint32_t* next = nullptr;
+    if (e->d_next.ensure(2 * 2 * 4) && cudaMemsetAsync(e->d_next.p, 0, 4, s) == cudaSuccess) next = e->d_next.as<uint32_t>();
     cudaEvent_t pa = prof_begin(e, s);
     k_separate<<<grid, PROXY_WARPS * 32, 0, s>>>(v, d_params, d_items, n, steps, step_t, step_th, clearance,
-                                                reinterpret_cast<uint32_t*>(d_queries), d_value);
+                                                reinterpret_cast<uint32_t*>(d_queries), d_value, next);
     prof_end(e, s, pa, JCDE_PROF_PROXY);
     CUDA_TRY(cudaGetLastError());
     e->launches++;

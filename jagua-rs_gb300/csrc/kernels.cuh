@@ -1355,15 +1355,23 @@ __device__ __forceinline__ ProxyOut proxy_local(const View& v, const DItem& it, 
 __global__ void __launch_bounds__(PROXY_WARPS * 32) k_separate(View v, float* __restrict__ params,
                                                                const uint32_t* __restrict__ items, uint32_t n,
                                                                uint32_t steps, float step_t, float step_th, float clear,
-                                                               uint32_t* __restrict__ qout, float* __restrict__ value) {
+                                                               uint32_t* __restrict__ qout, float* __restrict__ value,
+                                                               uint32_t* __restrict__ next) {
     constexpr int L = JCDE_SEP_LANES, PER_WARP = 32 / L;
     __shared__ float4 local[PROXY_WARPS * PER_WARP][SEP_LOCAL];
-    // PER_WARP candidates per warp, L lanes each
+    // PER_WARP candidates per warp, L lanes each; candidates are taken from the counter `next` (the
+    // descent stops early for candidates that separate, so the work per candidate varies widely)
     const int grp = (threadIdx.x & 31) / L, hl = threadIdx.x % L;
     const uint32_t mask = (L == 32 ? FULL : ((1u << L) - 1u)) << (L * grp);
     float4* list = local[(threadIdx.x >> 5) * PER_WARP + grp];
     const uint32_t groups = gridDim.x * PROXY_WARPS * PER_WARP;
-    for (uint32_t i = (blockIdx.x * PROXY_WARPS + (threadIdx.x >> 5)) * PER_WARP + grp; i < n; i += groups) {
+    for (uint32_t i = next ? 0u : (blockIdx.x * PROXY_WARPS + (threadIdx.x >> 5)) * PER_WARP + grp;; i += groups) {
+        if (next) {
+            uint32_t t = 0;
+            if (hl == 0) t = atomicAdd(next, 1u);
+            i = __shfl_sync(mask, t, L * grp);
+        }
+        if (i >= n) break;
         const uint32_t item = __ldg(&items[i]);
         float th = params[3 * i], tx = params[3 * i + 1], ty = params[3 * i + 2];
         float p = -1.0f;
