@@ -126,3 +126,28 @@ def test_lbf_full_size_matches_oracle(oracle_mod, jcde_mod):
     assert got.same_as(ref)
     assert r.status()["error"] == 0
     assert np.array_equal(r.tree_dump(), oeng.tree_dump())
+
+
+def test_resident_capacity_error_is_sticky_and_reset_clears_it(strip_layout, jcde_mod):
+    """A pool that runs out sets a sticky capacity error; later updates are skipped; reset recovers."""
+    import torch
+
+    lay, oeng = strip_layout
+    geng = W.replay(jcde.GpuBackend, lay)
+    with pytest.raises(jcde.JcdeError):   # the engine's own edges do not fit in 64
+        jcde.ResidentEngine(geng.eng, max_edges=64)
+    r = jcde.ResidentEngine(geng.eng, max_edges=6000)
+    base = r.status()
+    assert base["error"] == 0
+    q = W.make_queries(W.Stream(0x61, 1), 256, len(lay.items), lay.cde_bbox)
+    key = torch.zeros(1, dtype=torch.int32, device="cuda")
+    for i in range(len(q)):
+        r.register_placed(tq(q[i : i + 1]), key)
+    st = r.status()
+    assert st["status"] == -3 and st["error"] == 3   # JCDE_ERR_CAPACITY, edge pool
+    assert st["edges"] <= 6000
+    n_live = st["n_live"]
+    r.register_placed(tq(q[:1]), key)   # skipped
+    assert int(key.item()) == -1 and r.status()["n_live"] == n_live
+    r.reset()
+    assert r.status() == base and np.array_equal(r.tree_dump(), oeng.tree_dump())
