@@ -414,8 +414,10 @@ static const uint32_t* spatial_order_into(jcde_engine* e, const uint32_t* q, uin
 // warp-per-query surrogate pass.
 
 template <typename PendT>
-static void launch_passes_t(jcde_engine* e, const View& v, const uint32_t* q, uint32_t n, uint8_t* dout,
-                            cudaStream_t s, RawShape raw, int mode, const uint32_t* order, uint32_t* next) {
+static bool launch_passes_t(jcde_engine* e, const View& v, const uint32_t* q, uint32_t n, uint8_t* dout,
+                            cudaStream_t s, RawShape raw, int mode, const uint32_t* order, uint32_t* next,
+                            unsigned long long* best, uint32_t* n_free) {
+    bool chose = false;
     if (mode & 1) {
         const uint8_t miss = mode == 1 ? (uint8_t)0 : PENDING;
         cudaEvent_t pa = prof_begin(e, s);
@@ -450,7 +452,8 @@ static void launch_passes_t(jcde_engine* e, const View& v, const uint32_t* q, ui
         if (tab) {
             grid = std::min<uint32_t>(want, (uint32_t)(e->n_sms * e->tab_blocks_per_sm));
             k_poly_tab<PendT><<<grid, POLY_WARPS * 32, POLY_WARPS * sizeof(LeafTab), s>>>(v, q, n, dout, raw, mode == 3,
-                                                                                        order, next);
+                                                                                        order, next, best, n_free);
+            chose = best != nullptr;
         } else {
             k_poly<PendT, false><<<grid, POLY_WARPS * 32, 0, s>>>(v, MultiSrc{}, q, n, dout, raw, mode == 3, order, next,
                                                                   std::max(e->tune.poly_chunk, 1u));
@@ -458,12 +461,16 @@ static void launch_passes_t(jcde_engine* e, const View& v, const uint32_t* q, ui
         prof_end(e, s, pa, JCDE_PROF_POLY);
         e->launches++;
     }
+    return chose;
 }
-static void launch_passes(jcde_engine* e, const View& v, const uint32_t* q, uint32_t n, uint8_t* dout,
+// Returns true when the polygon pass also made the LBF choice into `best` / `n_free` (which it does
+// for batches that take the small-batch kernel; callers launch k_lbf_select otherwise).
+static bool launch_passes(jcde_engine* e, const View& v, const uint32_t* q, uint32_t n, uint8_t* dout,
                           cudaStream_t s, RawShape raw, int mode, const uint32_t* order = nullptr,
-                          uint32_t* next = nullptr) {
-    if (e->cfg.quadtree_depth <= 8) launch_passes_t<uint32_t>(e, v, q, n, dout, s, raw, mode, order, next);
-    else launch_passes_t<uint64_t>(e, v, q, n, dout, s, raw, mode, order, next);
+                          uint32_t* next = nullptr, unsigned long long* best = nullptr, uint32_t* n_free = nullptr) {
+    if (e->cfg.quadtree_depth <= 8)
+        return launch_passes_t<uint32_t>(e, v, q, n, dout, s, raw, mode, order, next, best, n_free);
+    return launch_passes_t<uint64_t>(e, v, q, n, dout, s, raw, mode, order, next, best, n_free);
 }
 
 // mode 1: surrogate only; 2: polygon only; 3: surrogate pass, then the polygon pass on the
@@ -1384,18 +1391,20 @@ static jcde_status ensure_order_buffers(jcde_resident* r, uint32_t n) {
     return JCDE_OK;
 }
 
-static void resident_detect(jcde_resident* r, const uint32_t* q, uint32_t n, uint8_t* dout, cudaStream_t s) {
+static bool resident_detect(jcde_resident* r, const uint32_t* q, uint32_t n, uint8_t* dout, cudaStream_t s,
+                            unsigned long long* best = nullptr, uint32_t* n_free = nullptr) {
     jcde_engine* e = r->e;
     const View v = resident_view(r);
     // small batches (one LBF step's candidates) gain nothing from the visit order
     const uint32_t* order = nullptr;
     if (JCDE_SPATIAL_ORDER && n >= e->tune.order_min_batch && n > e->tune.surrogate_warp_max)
         order = spatial_order_into(e, q, n, s, r->d_hist.as<uint32_t>(), r->d_order.as<uint32_t>());
-    launch_passes(e, v, q, n, dout, s, RawShape{}, 3, order, r->d_next.as<uint32_t>());
+    const bool chose = launch_passes(e, v, q, n, dout, s, RawShape{}, 3, order, r->d_next.as<uint32_t>(), best, n_free);
     r->launches += (order ? 3 : 0) + 2;
+    return chose;
 }
 
-// One step of the LBF-style build: 5 launches (generate, surrogate, polygon, select, commit).
+// One step of the LBF-style build: 4 launches (generate, surrogate, polygon + choice, commit).
 static void lbf_step(jcde_resident* r, cudaStream_t s) {
     jcde_engine* e = r->e;
     LbfDev* st = r->d_lbf.as<LbfDev>();
@@ -1404,19 +1413,22 @@ static void lbf_step(jcde_resident* r, cudaStream_t s) {
     cudaEvent_t pa = prof_begin(e, s);
     res_launch_lbf_gen(r->lp, st, cand, e->n_sms, s);
     prof_end(e, s, pa, JCDE_PROF_LBF);
-    resident_detect(r, cand, r->lp.n_cand, verd, s);
-    const View v = resident_view(r);
-    const uint32_t grid = std::min<uint32_t>((r->lp.n_cand + 7) / 8, (uint32_t)e->n_sms * 8);
-    pa = prof_begin(e, s);
-    k_lbf_select<<<grid, 256, 0, s>>>(v, cand, verd, r->lp.n_cand, &st->best, &st->n_free);
-    prof_end(e, s, pa, JCDE_PROF_LBF);
+    // the polygon pass makes the choice itself when it runs its small-batch kernel
+    if (!resident_detect(r, cand, r->lp.n_cand, verd, s, &st->best, &st->n_free)) {
+        const View v = resident_view(r);
+        const uint32_t grid = std::min<uint32_t>((r->lp.n_cand + 7) / 8, (uint32_t)e->n_sms * 8);
+        pa = prof_begin(e, s);
+        k_lbf_select<<<grid, 256, 0, s>>>(v, cand, verd, r->lp.n_cand, &st->best, &st->n_free);
+        prof_end(e, s, pa, JCDE_PROF_LBF);
+        r->launches++;
+    }
     LbfLogs logs{r->d_place.as<uint32_t>(), r->d_remv.as<uint32_t>(), r->d_free.as<uint32_t>(),
                  r->d_live.as<uint32_t>(), r->lp.vlog_steps ? r->d_vlog.as<uint8_t>() : nullptr};
     pa = prof_begin(e, s);
     res_launch_lbf_commit(r->t, e->d_items.as<DItem>(), e->d_iverts.as<float2>(), (uint32_t)e->items.size(), r->lp,
                           st, cand, verd, logs, s);
     prof_end(e, s, pa, JCDE_PROF_UPDATE);
-    r->launches += 3;
+    r->launches += 2;
 }
 
 // Loads the engine's live hazards, each under its own key, into empty pools (jcde_resident_create
@@ -1744,7 +1756,7 @@ jcde_status jcde_lbf_steps(jcde_resident* r, uint32_t n_steps, uint32_t steps_pe
         }
         for (; done + steps_per_graph <= n_steps; done += steps_per_graph) {
             if (cudaGraphLaunch(r->exec, s) != cudaSuccess) return JCDE_ERR_CUDA;
-            r->launches += 5ull * steps_per_graph;
+            r->launches += 4ull * steps_per_graph;
         }
     }
     for (; done < n_steps; done++) lbf_step(r, s);

@@ -218,6 +218,12 @@ __device__ void collect_walk(const View& v, const P& p, int start, uint32_t* bit
     }
 }
 
+// Float bits mapped to unsigned integers of the same order (for 64-bit atomicMin of (cost, index)).
+__device__ __forceinline__ uint32_t orderable(float f) {
+    const uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
 // Per-query shape: item vertices under the query's transformation, or a raw polygon.
 struct QShape {
     const float2* verts;
@@ -672,7 +678,8 @@ constexpr uint32_t POLY_MAXV = 256;   // items with more vertices transform edge
 template <typename PendT, bool TAB>
 __device__ __forceinline__ void poly_query(const View& v, const uint32_t* __restrict__ q, uint32_t qi,
                                            uint8_t* __restrict__ out, const RawShape& raw, volatile int* stop,
-                                           float2* tv, uint32_t* jobsw, LeafTab* ltab, int lane) {
+                                           float2* tv, uint32_t* jobsw, LeafTab* ltab, int lane,
+                                           unsigned long long* best = nullptr, uint32_t* n_free = nullptr) {
     QShape sh;
     Pt spoi;
     if (raw.verts) {
@@ -830,7 +837,14 @@ __device__ __forceinline__ void poly_query(const View& v, const uint32_t* __rest
             }
         }
     }
-    if (lane == 0) out[qi] = hit ? 1 : 0;
+    if (lane == 0) {
+        out[qi] = hit ? 1 : 0;
+        // the LBF choice of a free candidate (k_lbf_select's rule) while its box is at hand
+        if (best && !hit && !raw.verts) {
+            atomicMin(best, ((unsigned long long)orderable(sb.x1 * 10.0f + sb.y1) << 32) | qi);
+            atomicAdd(n_free, 1u);
+        }
+    }
 }
 
 template <typename PendT, bool MULTI>
@@ -873,13 +887,15 @@ __global__ void __launch_bounds__(POLY_WARPS * 32, JCDE_POLY_MIN_BLOCKS)
 
 // The polygon pass of small batches (latency-bound): leaf tables in dynamic shared memory, queries
 // one at a time from the counter `next`, and a register budget of its own (fewer, longer-lived warps).
+// With `best`, every query found free also enters the LBF choice (as k_lbf_select would).
 #ifndef JCDE_POLY_TAB_MIN_BLOCKS
 #define JCDE_POLY_TAB_MIN_BLOCKS 2
 #endif
 template <typename PendT>
 __global__ void __launch_bounds__(POLY_WARPS * 32, JCDE_POLY_TAB_MIN_BLOCKS)
     k_poly_tab(View v, const uint32_t* __restrict__ q, uint32_t n, uint8_t* __restrict__ out, RawShape raw,
-               bool only_pending, const uint32_t* __restrict__ order, uint32_t* __restrict__ next) {
+               bool only_pending, const uint32_t* __restrict__ order, uint32_t* __restrict__ next,
+               unsigned long long* __restrict__ best, uint32_t* __restrict__ n_free) {
     __shared__ int stops[POLY_WARPS];
     __shared__ float2 tverts[POLY_WARPS][POLY_MAXV];
     __shared__ uint32_t jobs[POLY_WARPS][POLY_MAXV];
@@ -896,7 +912,7 @@ __global__ void __launch_bounds__(POLY_WARPS * 32, JCDE_POLY_TAB_MIN_BLOCKS)
         if (i >= n) break;
         const uint32_t qi = order ? __ldg(&order[i]) : i;
         if (only_pending && out[qi] != PENDING) continue;
-        poly_query<PendT, true>(v, q, qi, out, raw, stop, tverts[warp], jobs[warp], &ltabs[warp], lane);
+        poly_query<PendT, true>(v, q, qi, out, raw, stop, tverts[warp], jobs[warp], &ltabs[warp], lane, best, n_free);
     }
 }
 
@@ -1470,10 +1486,6 @@ __global__ void k_resample(const float* __restrict__ params, const uint32_t* __r
 // transformed shape's bounding box, the lowest index among equal costs (the strict `<` of
 // search.rs:52 keeps the first best).  Costs are mapped to order-preserving integers and
 // packed with the index into one 64-bit atomicMin.
-__device__ __forceinline__ uint32_t orderable(float f) {
-    const uint32_t u = __float_as_uint(f);
-    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
-}
 __global__ void k_lbf_select(View v, const uint32_t* __restrict__ q, const uint8_t* __restrict__ verdicts, uint32_t n,
                              unsigned long long* __restrict__ best, uint32_t* __restrict__ n_free) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
