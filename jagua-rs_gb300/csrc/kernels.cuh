@@ -153,8 +153,9 @@ __device__ __forceinline__ bool leaf_hits(const View& v, const P& p, const DNode
     for (uint32_t k = 0; k < nd.hz_cnt; k++) {
         if (stop && *stop) return false;
         DEntry e = ld_entry(v, nd.hz_off + k);
-        if (e.presence != PRES_PARTIAL || filtered(v, e.hkey)) continue;
-        if (!p_hits_box(p, e.ff)) continue;   // qt_partial_hazard.rs:67-71
+        // (the filter lookup, a dependent load, comes last: the tests commute)
+        if (e.presence != PRES_PARTIAL || !p_hits_box(p, e.ff)) continue;   // qt_partial_hazard.rs:67-71
+        if (filtered(v, e.hkey)) continue;
         for (uint32_t j = 0; j < e.edge_cnt; j++) {
             if (p_hits_seg(p, ld_edge(v, e.edge_off + j))) {
                 if (stop) *stop = 1;
@@ -434,7 +435,7 @@ __device__ __forceinline__ bool leaf_hits_warp(const View& v, const P& p, const 
         bool cand = false;
         if (k < nd.hz_cnt) {
             const DEntry e = ld_entry(v, nd.hz_off + k);
-            cand = e.presence == PRES_PARTIAL && !filtered(v, e.hkey) && p_hits_box(p, e.ff);
+            cand = e.presence == PRES_PARTIAL && p_hits_box(p, e.ff) && !filtered(v, e.hkey);
             eo = e.edge_off;
             ec = e.edge_cnt;
         }
@@ -550,7 +551,7 @@ __device__ __forceinline__ void build_leaf_tab(const View& v, int vr, const Box&
                     DEntry e{};
                     if (k < nd.hz_cnt) {
                         e = ld_entry(v, nd.hz_off + k);
-                        c = e.presence == PRES_PARTIAL && !filtered(v, e.hkey) && box_hits_box(e.ff, sb);
+                        c = e.presence == PRES_PARTIAL && box_hits_box(e.ff, sb) && !filtered(v, e.hkey);
                     }
                     const uint32_t bal = __ballot_sync(FULL, c);
                     if (ne + __popc(bal) > (uint32_t)LT_ENTS) {

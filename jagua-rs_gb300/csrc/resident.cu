@@ -10,6 +10,10 @@
 
 #include <algorithm>
 
+#ifndef JCDE_UNROLL
+#define JCDE_UNROLL _Pragma("unroll")
+#endif
+
 namespace jcde {
 
 constexpr uint32_t FULL = 0xffffffffu;
@@ -166,6 +170,72 @@ __device__ void r_constrict(const RTree& t, RState& s, uint32_t& top, int32_t n,
         } else {
             bool resolved[4];
             const uint32_t lt = (1u << lane) - 1u;
+            constexpr uint32_t HELD = 4;   // edges per lane kept in registers by the one-pass clip
+            if (h.edge_cnt <= 32 * HELD) {
+                // one pass: every lane loads its edges once and tests them against the four
+                // quadrants; exact-size lists are then written from registers
+                float4 f[HELD];
+                uint32_t qm[HELD];
+                JCDE_UNROLL
+                for (uint32_t r = 0; r < HELD; r++) {
+                    const uint32_t k = r * 32 + lane;
+                    f[r] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    qm[r] = 0;
+                    if (k < h.edge_cnt) {
+                        f[r] = t.edges[h.edge_off + k];
+                        const Seg sg{Pt{f[r].x, f[r].y}, Pt{f[r].z, f[r].w}};
+                        for (int i = 0; i < 4; i++)
+                            if (box_hits_seg(q[i], sg)) qm[r] |= 1u << i;
+                    }
+                }
+                uint32_t need = 0, cnt[4];
+                for (int i = 0; i < 4; i++) {
+                    cnt[i] = 0;
+                    JCDE_UNROLL
+                    for (uint32_t r = 0; r < HELD; r++) cnt[i] += __popc(__ballot_sync(FULL, (qm[r] >> i) & 1u));
+                    if (cnt[i] && cnt[i] != h.edge_cnt) need += cnt[i];
+                }
+                if (s.edge_top + need > t.edge_cap) {
+                    r_fail(s, RES_ERR_EDGES);
+                    return;
+                }
+                for (int i = 0; i < 4; i++) {
+                    resolved[i] = cnt[i] > 0;
+                    out[i] = DEntry{Box{0.f, 0.f, 0.f, 0.f}, h.hkey, 0u, 0u, PRES_NONE};
+                    if (cnt[i] == 0) continue;
+                    if (cnt[i] == h.edge_cnt) {   // every edge: the parent's list and ff box
+                        out[i] = h;
+                        continue;
+                    }
+                    const uint32_t dst = s.edge_top;
+                    s.edge_top += cnt[i];
+                    float x0 = INFINITY, y0 = INFINITY, x1 = -INFINITY, y1 = -INFINITY;
+                    uint32_t pos = 0;
+                    JCDE_UNROLL
+                    for (uint32_t r = 0; r < HELD; r++) {
+                        const bool hit = (qm[r] >> i) & 1u;
+                        const uint32_t bal = __ballot_sync(FULL, hit);
+                        if (hit) {
+                            t.edges[dst + pos + __popc(bal & lt)] = f[r];
+                            x0 = fmn(fmn(x0, f[r].x), f[r].z);
+                            y0 = fmn(fmn(y0, f[r].y), f[r].w);
+                            x1 = fmx(fmx(x1, f[r].x), f[r].z);
+                            y1 = fmx(fmx(y1, f[r].y), f[r].w);
+                        }
+                        pos += __popc(bal);
+                    }
+#pragma unroll
+                    for (int o = 16; o; o >>= 1) {
+                        x0 = fmn(x0, __shfl_xor_sync(FULL, x0, o));
+                        y0 = fmn(y0, __shfl_xor_sync(FULL, y0, o));
+                        x1 = fmx(x1, __shfl_xor_sync(FULL, x1, o));
+                        y1 = fmx(y1, __shfl_xor_sync(FULL, y1, o));
+                    }
+                    // QTHazPartial::from_parent (qt_partial_hazard.rs:25-59)
+                    const Box ff = (x0 < x1 && y0 < y1) ? Box{x0, y0, x1, y1} : h.ff;
+                    out[i] = DEntry{ff, h.hkey, dst, cnt[i], PRES_PARTIAL};
+                }
+            } else
             for (int i = 0; i < 4; i++) {
                 // the edges hitting quadrant i, compacted in order at the top of the edge pool
                 if (s.edge_top + h.edge_cnt > t.edge_cap) {
