@@ -203,6 +203,14 @@ jcde_status jcde_collect_surrogate(jcde_engine* e, uint32_t item, const float tr
 jcde_status jcde_set_hazard_poles(jcde_engine* e, uint32_t key, const float* poles_xyr, uint32_t n);
 jcde_status jcde_proxy_batch(jcde_engine* e, const float* d_params, const uint32_t* d_items, uint32_t n,
                              const jcde_filter* filter, float* d_value, float* d_grad, void* stream);
+/* The same as a forward / backward pair (the two halves of a torch.autograd.Function): forward
+ * writes P; backward writes dL/d(theta, tx, ty) = d_grad_value[i] * dP_i/d(theta, tx, ty) (upstream
+ * gradient per candidate; null = all ones). */
+jcde_status jcde_proxy_forward(jcde_engine* e, const float* d_params, const uint32_t* d_items, uint32_t n,
+                               const jcde_filter* filter, float* d_value, void* stream);
+jcde_status jcde_proxy_backward(jcde_engine* e, const float* d_params, const uint32_t* d_items, uint32_t n,
+                                const jcde_filter* filter, const float* d_grad_value, float* d_grad_params,
+                                void* stream);
 /* `steps` descent steps per candidate on P: a step tries t - eta*step_t*dP/dt and
  * theta - eta*step_th/max|p_i|^2*dP/dtheta, keeps it if P drops (eta x1.5, at most 4) and halves eta
  * otherwise (eta starts at 1), stopping once P = 0.  `clearance` grows every hazard pole's radius

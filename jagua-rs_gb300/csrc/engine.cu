@@ -1247,7 +1247,39 @@ jcde_status jcde_proxy_batch(jcde_engine* e, const float* d_params, const uint32
     jcde_status st = proxy_prepare(e, f, s, v);
     if (st || n == 0) return st;
     const uint32_t grid = std::min<uint32_t>((n + PROXY_WARPS - 1) / PROXY_WARPS, (uint32_t)e->n_sms * 8);
-    k_proxy<<<grid, PROXY_WARPS * 32, 0, s>>>(v, d_params, d_items, n, d_value, d_grad);
+    k_proxy<<<grid, PROXY_WARPS * 32, 0, s>>>(v, d_params, d_items, n, d_value, d_grad, nullptr);
+    CUDA_TRY(cudaGetLastError());
+    e->launches++;
+    e->last_stream = s;
+    e->have_last_stream = true;
+    return JCDE_OK;
+}
+
+jcde_status jcde_proxy_forward(jcde_engine* e, const float* d_params, const uint32_t* d_items, uint32_t n,
+                               const jcde_filter* f, float* d_value, void* stream) {
+    if (!e || (n && (!d_params || !d_items || !d_value))) return JCDE_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    View v;
+    jcde_status st = proxy_prepare(e, f, s, v);
+    if (st || n == 0) return st;
+    const uint32_t grid = std::min<uint32_t>((n + PROXY_WARPS - 1) / PROXY_WARPS, (uint32_t)e->n_sms * 8);
+    k_proxy<<<grid, PROXY_WARPS * 32, 0, s>>>(v, d_params, d_items, n, d_value, nullptr, nullptr);
+    CUDA_TRY(cudaGetLastError());
+    e->launches++;
+    e->last_stream = s;
+    e->have_last_stream = true;
+    return JCDE_OK;
+}
+
+jcde_status jcde_proxy_backward(jcde_engine* e, const float* d_params, const uint32_t* d_items, uint32_t n,
+                                const jcde_filter* f, const float* d_grad_value, float* d_grad_params, void* stream) {
+    if (!e || (n && (!d_params || !d_items || !d_grad_params))) return JCDE_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    View v;
+    jcde_status st = proxy_prepare(e, f, s, v);
+    if (st || n == 0) return st;
+    const uint32_t grid = std::min<uint32_t>((n + PROXY_WARPS - 1) / PROXY_WARPS, (uint32_t)e->n_sms * 8);
+    k_proxy<<<grid, PROXY_WARPS * 32, 0, s>>>(v, d_params, d_items, n, nullptr, d_grad_params, d_grad_value);
     CUDA_TRY(cudaGetLastError());
     e->launches++;
     e->last_stream = s;

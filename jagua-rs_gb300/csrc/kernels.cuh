@@ -1252,15 +1252,21 @@ __device__ __forceinline__ ProxyOut proxy_eval(const View& v, const DItem& it, f
 
 constexpr int PROXY_WARPS = 8;
 
-// Forward + adjoint for a batch: params are (theta, tx, ty) per candidate.
+// Forward and/or adjoint for a batch: params are (theta, tx, ty) per candidate.  `value` (may be
+// null) receives P; `grad` (may be null) receives dP/d(theta, tx, ty), times gscale[i] when
+// `gscale` is given (the backward of a loss L with dL/dP = gscale).
 __global__ void __launch_bounds__(PROXY_WARPS * 32) k_proxy(View v, const float* __restrict__ params,
                                                             const uint32_t* __restrict__ items, uint32_t n,
-                                                            float* __restrict__ value, float* __restrict__ grad) {
+                                                            float* __restrict__ value, float* __restrict__ grad,
+                                                            const float* __restrict__ gscale) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (uint32_t i = blockIdx.x * PROXY_WARPS + warp; i < n; i += gridDim.x * PROXY_WARPS) {
         const uint32_t item = __ldg(&items[i]);
         if (item >= v.n_items) {
-            if (lane == 0) value[i] = -1.0f;
+            if (lane == 0) {
+                if (value) value[i] = -1.0f;
+                if (grad) grad[3 * i] = grad[3 * i + 1] = grad[3 * i + 2] = 0.0f;
+            }
             continue;
         }
         const DItem it = v.items[item];
@@ -1268,10 +1274,13 @@ __global__ void __launch_bounds__(PROXY_WARPS * 32) k_proxy(View v, const float*
         sincosf(__ldg(&params[3 * i]), &s, &c);
         const ProxyOut o = proxy_eval(v, it, c, s, __ldg(&params[3 * i + 1]), __ldg(&params[3 * i + 2]), lane, 32, FULL, 0.0f);
         if (lane == 0) {
-            value[i] = o.p;
-            grad[3 * i] = o.gth;
-            grad[3 * i + 1] = o.gx;
-            grad[3 * i + 2] = o.gy;
+            if (value) value[i] = o.p;
+            if (grad) {
+                const float g = gscale ? __ldg(&gscale[i]) : 1.0f;
+                grad[3 * i] = gscale ? o.gth * g : o.gth;
+                grad[3 * i + 1] = gscale ? o.gx * g : o.gx;
+                grad[3 * i + 2] = gscale ? o.gy * g : o.gy;
+            }
         }
     }
 }

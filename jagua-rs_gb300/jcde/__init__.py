@@ -5,8 +5,8 @@ GPU memory and detect / collect queries run as hand-written sm_103a kernels behi
 ``include/jcde.h``.  This package is the Python host side over that ABI.
 """
 from ._ffi import JcdeError, build, lib
-from .engine import (CDEConfig, CDEngine, GpuBackend, GpuEngine, Hazard, MultiEngine, ResidentEngine, spolygon_new,
-                     surrogate_poles)
+from .engine import (CDEConfig, CDEngine, GpuBackend, GpuEngine, Hazard, MultiEngine, ResidentEngine, pole_overlap,
+                     spolygon_new, surrogate_poles)
 from .workload import QUERY_DTYPE
 
 __all__ = [
@@ -16,6 +16,7 @@ __all__ = [
     "GpuEngine",
     "Hazard",
     "MultiEngine",
+    "pole_overlap",
     "ResidentEngine",
     "JcdeError",
     "QUERY_DTYPE",

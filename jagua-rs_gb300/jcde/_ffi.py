@@ -122,6 +122,8 @@ SIGNATURES = {
     "jcde_set_tuning": (C.c_int32, [P, P]),
     "jcde_autotune": (C.c_int32, [P, P, C.c_uint32, P, P, P, C.POINTER(C.c_double)]),
     "jcde_multi_autotune": (C.c_int32, [P, P, u32p, P, P, P, u32p, C.POINTER(C.c_double)]),
+    "jcde_proxy_forward": (C.c_int32, [P, P, P, C.c_uint32, P, P, P]),
+    "jcde_proxy_backward": (C.c_int32, [P, P, P, C.c_uint32, P, P, P, P]),
     "jcde_proxy_batch": (C.c_int32, [P, P, P, C.c_uint32, C.POINTER(jcde_filter), P, P, P]),
     "jcde_separate_batch": (C.c_int32, [P, P, P, C.c_uint32, C.c_uint32, C.c_float, C.c_float, C.c_float, C.POINTER(jcde_filter), P, P, P]),
     "jcde_resample_batch": (C.c_int32, [P, P, P, C.c_uint32, C.c_uint32, C.c_float, C.c_float, C.c_uint32, P, P]),

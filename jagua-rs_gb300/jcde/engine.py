@@ -284,6 +284,28 @@ class CDEngine:
                                      grad.data_ptr(), _stream_handle(stream)), "proxy_batch")
         return val, grad
 
+    def proxy_forward(self, params, items, filter=None, stream=None):
+        import torch
+
+        f = _Filter(filter)
+        n = items.numel()
+        val = torch.empty(n, dtype=torch.float32, device=params.device)
+        check(lib().jcde_proxy_forward(self.h, params.data_ptr(), items.data_ptr(), n, f.ref, val.data_ptr(),
+                                       _stream_handle(stream)), "proxy_forward")
+        return val
+
+    def proxy_backward(self, params, items, grad_value=None, filter=None, stream=None):
+        import torch
+
+        f = _Filter(filter)
+        n = items.numel()
+        grad = torch.empty((n, 3), dtype=torch.float32, device=params.device)
+        gv = None if grad_value is None else grad_value.contiguous()
+        check(lib().jcde_proxy_backward(self.h, params.data_ptr(), items.data_ptr(), n, f.ref,
+                                        None if gv is None else gv.data_ptr(), grad.data_ptr(),
+                                        _stream_handle(stream)), "proxy_backward")
+        return grad
+
     def separate_batch(self, params, items, steps=20, step_t=0.25, step_th=0.25, clearance=0.0, filter=None,
                        stream=None):
         """Gradient-descent separation in place on params [n, 3]; returns (packed queries, final P)."""
@@ -610,3 +632,24 @@ def lbf_select(eng: "GpuEngine", q, verdicts) -> int:
                                 _stream_handle(None)), "lbf_select")
     b = int(best.item()) & 0xFFFFFFFFFFFFFFFF
     return -1 if b == 0xFFFFFFFFFFFFFFFF else int(b & 0xFFFFFFFF)
+
+
+
+def pole_overlap(engine: CDEngine, params, items, filter=None):
+    """The pole-overlap proxy P per candidate as a differentiable torch function of params [n, 3]
+    (theta, tx, ty; float32, CUDA): forward is jcde_proxy_forward, backward jcde_proxy_backward."""
+    import torch
+
+    class _PoleOverlap(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, p):
+            p = p.detach().contiguous()
+            ctx.save_for_backward(p)
+            return engine.proxy_forward(p, items, filter=filter)
+
+        @staticmethod
+        def backward(ctx, grad_value):
+            (p,) = ctx.saved_tensors
+            return engine.proxy_backward(p, items, grad_value=grad_value.contiguous().float(), filter=filter)
+
+    return _PoleOverlap.apply(params)

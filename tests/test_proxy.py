@@ -88,3 +88,32 @@ def test_gpu_separation_then_exact_verdict(oracle_mod, jcde_mod, strip_layout, s
     moved = p0 > 0
     assert (p1[moved] <= p0[moved] + 1e-3).mean() > 0.95   # descent lowers the proxy
     assert v1[moved].mean() < v0[moved].mean()             # and frees some placements
+
+
+@pytest.mark.gpu
+def test_gpu_proxy_forward_backward_pair_and_autograd(oracle_mod, jcde_mod, strip_layout, strip_poles):
+    """The forward/backward pair equals the fused call bit for bit, and drives torch autograd."""
+    import torch
+
+    import jcde
+    from test_gpu_parity import gpu_engine
+
+    lay, _ = strip_layout
+    eng = gpu_engine(lay)
+    for hz in lay.hazards:
+        sel = strip_poles[:, 3].view(np.uint32) == hz.key
+        if sel.any():
+            eng.set_hazard_poles(hz.key, strip_poles[sel, :3])
+    st = W.Stream(0xF4, 4)
+    params, items = W.random_params(st, 4096, len(lay.items), lay.cde_bbox)
+    dp = torch.from_numpy(params).cuda()
+    di = torch.from_numpy(items.astype(np.int32)).cuda()
+    val, grad = eng.proxy_batch(dp, di)
+    assert torch.equal(eng.proxy_forward(dp, di), val)
+    assert torch.equal(eng.proxy_backward(dp, di), grad)
+    w = torch.from_numpy(W.Stream(0xF4, 5).f32(4096)).cuda()
+    x = dp.clone().requires_grad_(True)
+    p = jcde.pole_overlap(eng, x, di)
+    assert torch.equal(p.detach(), val)
+    (w * p).sum().backward()
+    assert torch.equal(x.grad, w[:, None] * grad)   # the same float32 products
