@@ -151,3 +151,23 @@ def test_resident_capacity_error_is_sticky_and_reset_clears_it(strip_layout, jcd
     assert int(key.item()) == -1 and r.status()["n_live"] == n_live
     r.reset()
     assert r.status() == base and np.array_equal(r.tree_dump(), oeng.tree_dump())
+
+
+def test_lbf_select_entry_point_matches_host_choice(oracle_mod, jcde_mod):
+    """jcde_lbf_select picks the host rule's candidate (least cost among free ones, first on ties)."""
+    from jcde.engine import lbf_select
+
+    spec = lbf.LbfSpec(n_types=12, n_cand=4096)
+    lay, geng = lbf.setup(jcde.GpuBackend, spec)
+    rng = np.random.default_rng(11)
+    for step in range(4):
+        q = lbf.step_queries(spec, step)
+        q["item"] = rng.integers(0, spec.n_types, len(q))
+        v = (rng.random(len(q)) < 0.5).astype(np.uint8)
+        assert lbf_select(geng, q, v) == lbf.select_host(lay.items, q, v)
+    q = lbf.step_queries(spec, 0)
+    q[7] = q[3]
+    v = np.ones(len(q), np.uint8)
+    v[[3, 7]] = 0
+    assert lbf_select(geng, q, v) == 3
+    assert lbf_select(geng, q, np.ones(len(q), np.uint8)) == -1
