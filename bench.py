@@ -429,7 +429,7 @@ def run_gpu(args):
 
 
 def run_multi(args):
-    """configs[2]: 64 independent bin layouts, log-uniform 4,096-262,144 queries each, answered by
+    """The multi-layout workload: 64 independent bin layouts, log-uniform 4,096-262,144 queries each, answered by
     one launch sequence (CUDA graph) versus 64 per-layout jcde_detect_batch calls."""
     import torch
 
@@ -498,7 +498,7 @@ def run_multi(args):
 
 
 def run_proxy(args):
-    """configs[4]: the star layout with surrogate poles on every interior hazard; 1,048,576 colliding
+    """The gradient-separation workload: the star layout with surrogate poles on every interior hazard; 1,048,576 colliding
     candidates; 20 gradient steps on the pole-overlap proxy then the exact verdict, versus 20 random
     perturbations per candidate judged by the exact verdict.  Metric: verified collision-free
     placements per second."""
@@ -600,7 +600,7 @@ def run_proxy(args):
 
 
 def run_lbf(args):
-    """configs[3]: LBF-style strip build on the device-resident engine.  2000 steps, each: 16384
+    """The LBF-style strip build on the device-resident engine.  2000 steps, each: 16384
     candidates generated, judged (surrogate + polygon passes), the least-cost free one registered on
     the device, and a random placed item deregistered every 50 steps.  A timed step is one whole build
     from the strip's initial state.  Metric: candidate placements judged per second over the build."""
