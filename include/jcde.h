@@ -292,14 +292,24 @@ typedef struct jcde_lbf_params {
     uint32_t n_types;              /* item types 0..n_types-1 of the engine */
     uint32_t remove_every;         /* 0: no removals */
     uint32_t max_steps;            /* log capacity; steps beyond it do nothing */
-    uint32_t verdict_log_steps;    /* keep the verdicts of the first steps (0: none) */
+    uint32_t verdict_log_steps;    /* keep the verdicts of the first steps (0: none; needs ls_rounds = 0) */
     uint32_t reserved;
     jcde_rect sample_box;
+    /* local search after the uniform round (lbf/src/opt/search.rs:80-101, restated with uniform
+     * offsets): round r = 1..ls_rounds draws ls_candidates placements of the step's item around the
+     * step's best so far from stream (seed, 1000000 + 64 s + r): turns + U[-1,1) sigma_turns_r,
+     * tx, ty + U[-sigma_t_r, sigma_t_r) (draws i, n+i, 2n+i), sigma_r = sigma * decay^(r-1); the
+     * round's least-cost free candidate replaces the best when it costs strictly less. */
+    uint32_t ls_rounds;            /* 0..8 */
+    uint32_t ls_candidates;        /* per round, at most n_candidates */
+    float ls_sigma_t;
+    float ls_decay;
+    double ls_sigma_turns;
 } jcde_lbf_params;
 jcde_status jcde_lbf_begin(jcde_resident* r, const jcde_lbf_params* p);
 jcde_status jcde_lbf_steps(jcde_resident* r, uint32_t n_steps, uint32_t steps_per_graph, void* stream);
 /* Synchronises.  counts4 = steps done, placements, removals, placed items still live.  placements:
- * 8 words each (step, key, candidate, item, cos, sin, tx, ty as float bits); removals: 2 words each
+ * 8 words each (step, key, round << 24 | candidate, item, cos, sin, tx, ty as float bits); removals: 2 words each
  * (step, key); free_counts: free candidates per step; verdicts: step-major verdict log. */
 jcde_status jcde_lbf_read(jcde_resident* r, uint32_t* counts4, uint32_t* placements, uint32_t place_cap,
                           uint32_t* removals, uint32_t removal_cap, uint32_t* free_counts, uint32_t free_cap,

@@ -1364,7 +1364,7 @@ struct jcde_resident {
     // LBF-style build
     bool lbf_ready = false;
     LbfParams lp{};
-    DevBuf d_lbf, d_cand, d_verd, d_place, d_remv, d_free, d_live, d_vlog;
+    DevBuf d_lbf, d_cand, d_candu, d_verd, d_place, d_remv, d_free, d_live, d_vlog;
     DevBuf d_hist, d_order;   // spatial ordering of the resident's own query batches
     DevBuf d_next;            // work counters of its two passes
     cudaGraphExec_t exec = nullptr;
@@ -1436,31 +1436,45 @@ static bool resident_detect(jcde_resident* r, const uint32_t* q, uint32_t n, uin
     return chose;
 }
 
-// One step of the LBF-style build: 4 launches (generate, surrogate, polygon + choice, commit).
+// One step of the LBF-style build: a uniform round and ls_rounds local-search rounds, each
+// generate -> surrogate pass -> polygon pass + choice (-> merge into the step's best), then the
+// commit (4 launches without local search, 4 more per local-search round).
 static void lbf_step(jcde_resident* r, cudaStream_t s) {
     jcde_engine* e = r->e;
     LbfDev* st = r->d_lbf.as<LbfDev>();
     uint32_t* cand = r->d_cand.as<uint32_t>();
+    double* cu = r->d_candu.as<double>();
     uint8_t* verd = r->d_verd.as<uint8_t>();
-    cudaEvent_t pa = prof_begin(e, s);
-    res_launch_lbf_gen(r->lp, st, cand, e->n_sms, s);
-    prof_end(e, s, pa, JCDE_PROF_LBF);
-    // the polygon pass makes the choice itself when it runs its small-batch kernel
-    if (!resident_detect(r, cand, r->lp.n_cand, verd, s, &st->best, &st->n_free)) {
-        const View v = resident_view(r);
-        const uint32_t grid = std::min<uint32_t>((r->lp.n_cand + 7) / 8, (uint32_t)e->n_sms * 8);
-        pa = prof_begin(e, s);
-        k_lbf_select<<<grid, 256, 0, s>>>(v, cand, verd, r->lp.n_cand, &st->best, &st->n_free);
+    const uint32_t rounds = r->lp.ls_rounds;
+    for (uint32_t round = 0; round <= rounds; round++) {
+        const uint32_t n = round ? r->lp.ls_cand : r->lp.n_cand;
+        cudaEvent_t pa = prof_begin(e, s);
+        res_launch_lbf_gen(r->lp, st, cand, cu, round, e->n_sms, s);
         prof_end(e, s, pa, JCDE_PROF_LBF);
         r->launches++;
+        // the polygon pass makes the choice itself when it runs its small-batch kernel
+        if (!resident_detect(r, cand, n, verd, s, &st->best, &st->n_free)) {
+            const View v = resident_view(r);
+            const uint32_t grid = std::min<uint32_t>((n + 7) / 8, (uint32_t)e->n_sms * 8);
+            pa = prof_begin(e, s);
+            k_lbf_select<<<grid, 256, 0, s>>>(v, cand, verd, n, &st->best, &st->n_free);
+            prof_end(e, s, pa, JCDE_PROF_LBF);
+            r->launches++;
+        }
+        if (round < rounds) {
+            pa = prof_begin(e, s);
+            res_launch_lbf_merge(st, cand, cu, round, s);
+            prof_end(e, s, pa, JCDE_PROF_LBF);
+            r->launches++;
+        }
     }
     LbfLogs logs{r->d_place.as<uint32_t>(), r->d_remv.as<uint32_t>(), r->d_free.as<uint32_t>(),
                  r->d_live.as<uint32_t>(), r->lp.vlog_steps ? r->d_vlog.as<uint8_t>() : nullptr};
-    pa = prof_begin(e, s);
+    cudaEvent_t pa = prof_begin(e, s);
     res_launch_lbf_commit(r->t, e->d_items.as<DItem>(), e->d_iverts.as<float2>(), (uint32_t)e->items.size(), r->lp,
-                          st, cand, verd, logs, s);
+                          st, cand, cu, rounds, verd, logs, s);
     prof_end(e, s, pa, JCDE_PROF_UPDATE);
-    r->launches += 2;
+    r->launches++;
 }
 
 // Loads the engine's live hazards, each under its own key, into empty pools (jcde_resident_create
@@ -1741,8 +1755,28 @@ jcde_status jcde_lbf_begin(jcde_resident* r, const jcde_lbf_params* p) {
     lp.y1 = b.y_max;
     lp.x1_below = std::nextafter(b.x_max, b.x_min);
     lp.y1_below = std::nextafter(b.y_max, b.y_min);
+    if (p->ls_rounds > LBF_MAX_LS || (p->ls_rounds && (!p->ls_candidates || p->ls_candidates > p->n_candidates)))
+        return JCDE_ERR_ARG;
+    lp.ls_rounds = p->ls_rounds;
+    lp.ls_cand = p->ls_rounds ? p->ls_candidates : 0;
+    lp.ls_sid_base = 1000000ull;
+    {   // round r's half-widths: sigma * decay^(r-1), float32 (translation) and float64 (turns)
+        float sg = p->ls_sigma_t;
+        double sth = p->ls_sigma_turns;
+        for (uint32_t k = 1; k <= p->ls_rounds; k++) {
+            if (k > 1) {
+                sg = sg * p->ls_decay;
+                sth = sth * (double)p->ls_decay;
+            }
+            lp.ls_sig[k] = sg;
+            lp.ls_sig_below[k] = std::nextafter(sg, -sg);
+            lp.ls_sth[k] = sth;
+        }
+    }
+    if (lp.ls_rounds && lp.vlog_steps) return JCDE_ERR_ARG;   // the verdict log keeps one round per step
     const size_t n = p->n_candidates, ms = p->max_steps;
-    const bool ok = r->d_lbf.ensure(sizeof(LbfDev)) && r->d_cand.ensure(n * 20) && r->d_verd.ensure(n) &&
+    const bool ok = r->d_lbf.ensure(sizeof(LbfDev)) && r->d_cand.ensure(n * 20) && r->d_candu.ensure(n * 8) &&
+                    r->d_verd.ensure(n) &&
                     r->d_place.ensure(ms * 32) && r->d_remv.ensure(ms * 8) && r->d_free.ensure(ms * 4) &&
                     r->d_live.ensure(ms * 4) && (!lp.vlog_steps || r->d_vlog.ensure((size_t)lp.vlog_steps * n));
     if (!ok) return JCDE_ERR_CUDA;
@@ -1788,7 +1822,7 @@ jcde_status jcde_lbf_steps(jcde_resident* r, uint32_t n_steps, uint32_t steps_pe
         }
         for (; done + steps_per_graph <= n_steps; done += steps_per_graph) {
             if (cudaGraphLaunch(r->exec, s) != cudaSuccess) return JCDE_ERR_CUDA;
-            r->launches += 4ull * steps_per_graph;
+            r->launches += (4ull + 4ull * r->lp.ls_rounds) * steps_per_graph;
         }
     }
     for (; done < n_steps; done++) lbf_step(r, s);

@@ -616,29 +616,84 @@ __device__ __forceinline__ float draw_uniform(unsigned long long key, unsigned l
     return fminf(__fadd_rn(lo, __fmul_rn(draw_f32(key, i), __fsub_rn(hi, lo))), hi_below);
 }
 
-// Candidates of the current step: item type t ~ U{0..T-1} from the type stream (one draw per
-// step), rotation ~ U[0, 2pi) and translation ~ U(box) from the step's own stream — the draws of
-// make_queries in the workload generator (draw n+i: rotation, 2n+i: x, 3n+i: y).
-__global__ void k_lbf_gen(LbfParams p, LbfDev* __restrict__ st, uint32_t* __restrict__ q) {
+// Candidates of round `round` of the current step.  Round 0: item type t ~ U{0..T-1} from the type
+// stream (one draw per step), rotation ~ U[0, 2pi) and translation ~ U(box) from the step's own
+// stream — the draws of make_queries in the workload generator (draw n+i: rotation, 2n+i: x,
+// 3n+i: y).  Round r >= 1 (local search): candidates around the step's best so far, from stream
+// (seed, ls_sid_base + 64 step + r): draw i: rotation offset in turns, ls_cand+i: x, 2 ls_cand+i: y;
+// with no best yet the round's candidates are marked invalid.  `qu` keeps each candidate's turns.
+__global__ void k_lbf_gen(LbfParams p, LbfDev* __restrict__ st, uint32_t* __restrict__ q, double* __restrict__ qu,
+                          uint32_t round) {
     const uint32_t step = *(volatile uint32_t*)&st->step;
     if (step >= p.max_steps) return;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         st->best = ~0ull;
-        st->n_free = 0;
+        if (round == 0) {
+            st->n_free = 0;
+            st->rec_cost = ~0u;
+        }
     }
-    const unsigned long long key = stream_key(p.seed, (unsigned long long)p.sid_base + step);
     const uint32_t t = (uint32_t)(draw(p.key_types, step) % p.n_types);
-    const unsigned long long n = p.n_cand;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < p.n_cand; i += gridDim.x * blockDim.x) {
-        float c, s;
-        sincos_turns((double)(draw(key, n + i) >> 11) * 0x1p-53, c, s);
+    if (round == 0) {
+        const unsigned long long key = stream_key(p.seed, (unsigned long long)p.sid_base + step);
+        const unsigned long long n = p.n_cand;
+        for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < p.n_cand; i += gridDim.x * blockDim.x) {
+            float c, s;
+            const double u = (double)(draw(key, n + i) >> 11) * 0x1p-53;
+            sincos_turns(u, c, s);
+            uint32_t* r = q + (size_t)i * 5;
+            r[0] = t;
+            r[1] = __float_as_uint(c);
+            r[2] = __float_as_uint(s);
+            r[3] = __float_as_uint(draw_uniform(key, 2 * n + i, p.x0, p.x1, p.x1_below));
+            r[4] = __float_as_uint(draw_uniform(key, 3 * n + i, p.y0, p.y1, p.y1_below));
+            qu[i] = u;
+        }
+        return;
+    }
+    const volatile LbfDev* vs = st;
+    const bool have = vs->rec_cost != ~0u;
+    const double ub = vs->rec_u;
+    const float txb = __uint_as_float(vs->rec_q[3]), tyb = __uint_as_float(vs->rec_q[4]);
+    const unsigned long long key = stream_key(p.seed, p.ls_sid_base + 64ull * step + round);
+    const unsigned long long m = p.ls_cand;
+    const float sg = p.ls_sig[round], sgb = p.ls_sig_below[round];
+    const double sth = p.ls_sth[round];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < p.ls_cand; i += gridDim.x * blockDim.x) {
         uint32_t* r = q + (size_t)i * 5;
+        if (!have) {
+            r[0] = 0xFFFFFFFFu;   // no best to search around: an invalid item, never free
+            continue;
+        }
+        const double du = (double)(draw(key, i) >> 11) * 0x1p-53;
+        const double x = __dadd_rn(ub, __dmul_rn(__dsub_rn(__dmul_rn(2.0, du), 1.0), sth));
+        const double u = __dsub_rn(x, floor(x));
+        float c, s;
+        sincos_turns(u, c, s);
         r[0] = t;
         r[1] = __float_as_uint(c);
         r[2] = __float_as_uint(s);
-        r[3] = __float_as_uint(draw_uniform(key, 2 * n + i, p.x0, p.x1, p.x1_below));
-        r[4] = __float_as_uint(draw_uniform(key, 3 * n + i, p.y0, p.y1, p.y1_below));
+        r[3] = __float_as_uint(__fadd_rn(txb, draw_uniform(key, m + i, -sg, sg, sgb)));
+        r[4] = __float_as_uint(__fadd_rn(tyb, draw_uniform(key, 2 * m + i, -sg, sg, sgb)));
+        qu[i] = u;
     }
+}
+
+// The step's best so far takes the round's choice when it costs strictly less (the first best
+// is kept on ties, as search.rs:52 keeps it).
+__device__ __forceinline__ void lbf_merge(LbfDev* st, const uint32_t* q, const double* qu, uint32_t round) {
+    const unsigned long long b = st->best;
+    if (b == ~0ull) return;
+    const uint32_t cost = (uint32_t)(b >> 32), idx = (uint32_t)b;
+    if (cost >= st->rec_cost) return;
+    st->rec_cost = cost;
+    st->rec_u = qu[idx];
+    for (int k = 0; k < 5; k++) st->rec_q[k] = q[(size_t)idx * 5 + k];
+    st->rec_cand = (round << 24) | idx;
+}
+__global__ void k_lbf_merge(LbfDev* __restrict__ st, const uint32_t* __restrict__ q, const double* __restrict__ qu,
+                            uint32_t round) {
+    if (threadIdx.x == 0) lbf_merge(st, q, qu, round);
 }
 
 // End of a step: log it, register the chosen candidate, and every `remove_every` steps remove the
@@ -646,6 +701,7 @@ __global__ void k_lbf_gen(LbfParams p, LbfDev* __restrict__ st, uint32_t* __rest
 __global__ void __launch_bounds__(32) k_lbf_commit(RTree t, const DItem* __restrict__ items,
                                                    const float2* __restrict__ iverts, uint32_t n_items, LbfParams p,
                                                    LbfDev* __restrict__ st, const uint32_t* __restrict__ q,
+                                                   const double* __restrict__ qu, uint32_t round,
                                                    const uint8_t* __restrict__ verdicts, LbfLogs logs) {
     const int lane = threadIdx.x;
     volatile LbfDev* vs = st;
@@ -653,14 +709,16 @@ __global__ void __launch_bounds__(32) k_lbf_commit(RTree t, const DItem* __restr
     if (step >= p.max_steps) return;
     RState s = r_load(t.ctl);
     if (s.error) return;
+    if (lane == 0) lbf_merge(st, q, qu, round);   // the last round's choice
+    __syncwarp();
     uint32_t n_live = vs->n_live, n_removed = vs->n_removed, n_placed = vs->n_placed;
-    const unsigned long long best = vs->best;
     if (lane == 0) logs.free_counts[step] = vs->n_free;
-    if (logs.vlog && step < p.vlog_steps)
+    if (logs.vlog && step < p.vlog_steps)   // (the verdicts of the last round)
         for (uint32_t i = lane; i < p.n_cand; i += 32) logs.vlog[(size_t)step * p.n_cand + i] = verdicts[i];
-    if (best != ~0ull) {
-        const uint32_t ci = (uint32_t)best;
-        const RQuery rq = r_query(q, ci);
+    if (vs->rec_cost != ~0u) {
+        const uint32_t ci = vs->rec_cand;
+        const RQuery rq{vs->rec_q[0], __uint_as_float(vs->rec_q[1]), __uint_as_float(vs->rec_q[2]),
+                        __uint_as_float(vs->rec_q[3]), __uint_as_float(vs->rec_q[4])};
         const uint32_t key = rq.item < n_items ? r_insert_item(t, s, items, iverts, rq, lane) : ~0u;
         if (key != ~0u && !s.error) {
             if (lane == 0) {
@@ -719,14 +777,19 @@ void res_launch_insert_placed(const RTree& t, const DItem* items, const float2* 
     k_res_insert_placed<<<1, 32, 0, s>>>(t, items, iverts, n_items, q, out_key);
 }
 void res_launch_remove(const RTree& t, const uint32_t* key, cudaStream_t s) { k_res_remove<<<1, 32, 0, s>>>(t, key); }
-void res_launch_lbf_gen(const LbfParams& p, LbfDev* st, uint32_t* q, int n_sms, cudaStream_t s) {
-    const uint32_t grid = std::min<uint32_t>((p.n_cand + 255) / 256, (uint32_t)std::max(1, n_sms) * 4);
-    k_lbf_gen<<<grid, 256, 0, s>>>(p, st, q);
+void res_launch_lbf_gen(const LbfParams& p, LbfDev* st, uint32_t* q, double* qu, uint32_t round, int n_sms,
+                        cudaStream_t s) {
+    const uint32_t n = round ? p.ls_cand : p.n_cand;
+    const uint32_t grid = std::min<uint32_t>((n + 255) / 256, (uint32_t)std::max(1, n_sms) * 4);
+    k_lbf_gen<<<grid, 256, 0, s>>>(p, st, q, qu, round);
+}
+void res_launch_lbf_merge(LbfDev* st, const uint32_t* q, const double* qu, uint32_t round, cudaStream_t s) {
+    k_lbf_merge<<<1, 32, 0, s>>>(st, q, qu, round);
 }
 void res_launch_lbf_commit(const RTree& t, const DItem* items, const float2* iverts, uint32_t n_items,
-                           const LbfParams& p, LbfDev* st, const uint32_t* q, const uint8_t* verdicts,
-                           const LbfLogs& logs, cudaStream_t s) {
-    k_lbf_commit<<<1, 32, 0, s>>>(t, items, iverts, n_items, p, st, q, verdicts, logs);
+                           const LbfParams& p, LbfDev* st, const uint32_t* q, const double* qu, uint32_t round,
+                           const uint8_t* verdicts, const LbfLogs& logs, cudaStream_t s) {
+    k_lbf_commit<<<1, 32, 0, s>>>(t, items, iverts, n_items, p, st, q, qu, round, verdicts, logs);
 }
 
 }  // namespace jcde

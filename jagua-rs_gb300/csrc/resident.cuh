@@ -88,10 +88,16 @@ struct LbfDev {
     uint32_t n_live;      // placed items not removed
     uint32_t n_removed;   // removals so far (index of the next removal draw)
     uint32_t n_placed;
-    unsigned long long best;   // (order-preserving cost bits << 32) | candidate, ~0 = none free
-    uint32_t n_free;           // free candidates of the current step
-    uint32_t pad[9];
+    unsigned long long best;   // choice of the current round: (order-preserving cost bits << 32) | candidate
+    uint32_t n_free;           // free candidates of the current step (all rounds)
+    uint32_t rec_cost;         // the step's best so far: order-preserving cost bits, ~0 = none
+    double rec_u;              //   its rotation in turns
+    uint32_t rec_q[5];         //   its query record
+    uint32_t rec_cand;         //   round << 24 | candidate index
+    uint32_t pad[2];
 };
+
+constexpr int LBF_MAX_LS = 8;   // local-search rounds per step
 
 struct LbfParams {
     unsigned long long seed;   // candidate stream of step s: (seed, sid_base + s)
@@ -99,6 +105,12 @@ struct LbfParams {
     uint32_t sid_base, n_cand, n_types, remove_every, max_steps, vlog_steps;
     float x0, y0, x1, y1;      // sampling box of the translations
     float x1_below, y1_below;  // the largest float32 below x1 / y1 (draws stay inside the box)
+    // local search: round r of step s draws ls_cand candidates around the step's best from stream
+    // (seed, ls_sid_base + 64 s + r): turns += U[-1,1) ls_sth[r], translation += U[-ls_sig[r], ls_sig[r])
+    uint32_t ls_rounds, ls_cand;
+    unsigned long long ls_sid_base;
+    float ls_sig[LBF_MAX_LS + 1], ls_sig_below[LBF_MAX_LS + 1];
+    double ls_sth[LBF_MAX_LS + 1];
 };
 
 struct LbfLogs {
@@ -115,9 +127,11 @@ void res_launch_init(const RTree& t, const float2* verts, const uint4* recs, con
 void res_launch_insert_placed(const RTree& t, const DItem* items, const float2* iverts, uint32_t n_items,
                               const uint32_t* q, uint32_t* out_key, cudaStream_t s);
 void res_launch_remove(const RTree& t, const uint32_t* key, cudaStream_t s);
-void res_launch_lbf_gen(const LbfParams& p, LbfDev* st, uint32_t* q, int n_sms, cudaStream_t s);
+void res_launch_lbf_gen(const LbfParams& p, LbfDev* st, uint32_t* q, double* qu, uint32_t round, int n_sms,
+                        cudaStream_t s);
+void res_launch_lbf_merge(LbfDev* st, const uint32_t* q, const double* qu, uint32_t round, cudaStream_t s);
 void res_launch_lbf_commit(const RTree& t, const DItem* items, const float2* iverts, uint32_t n_items,
-                           const LbfParams& p, LbfDev* st, const uint32_t* q, const uint8_t* verdicts,
-                           const LbfLogs& logs, cudaStream_t s);
+                           const LbfParams& p, LbfDev* st, const uint32_t* q, const double* qu, uint32_t round,
+                           const uint8_t* verdicts, const LbfLogs& logs, cudaStream_t s);
 
 }  // namespace jcde

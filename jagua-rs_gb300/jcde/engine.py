@@ -588,8 +588,14 @@ class ResidentEngine:
     def kernel_launches(self) -> int:
         return int(lib().jcde_resident_kernel_launches(self.h))
 
-    def lbf_begin(self, seed, n_candidates, n_types, remove_every, max_steps, sample_box, verdict_log_steps=0):
+    def lbf_begin(self, seed, n_candidates, n_types, remove_every, max_steps, sample_box, verdict_log_steps=0,
+                  ls_rounds=0, ls_candidates=0, ls_sigma_t=0.0, ls_sigma_turns=0.0, ls_decay=0.5):
         p = jcde_lbf_params()
+        p.ls_rounds = int(ls_rounds)
+        p.ls_candidates = int(ls_candidates)
+        p.ls_sigma_t = float(np.float32(ls_sigma_t))
+        p.ls_decay = float(np.float32(ls_decay))
+        p.ls_sigma_turns = float(ls_sigma_turns)
         p.seed = int(seed)
         p.n_candidates = int(n_candidates)
         p.n_types = int(n_types)

@@ -26,6 +26,7 @@ from . import workload as W
 
 SEED = 0xC3
 TYPE_SID, REMOVE_SID, CAND_SID_BASE = 2, 4, 10_000   # stream ids of the driver's draws
+LS_SID_BASE = 1_000_000   # local-search round r of step s: stream LS_SID_BASE + 64 s + r
 
 
 @dataclass
@@ -43,6 +44,22 @@ class LbfSpec:
     remove_every: int = 50
     depth: int = W.DEFAULT_DEPTH
     cd_threshold: int = W.DEFAULT_CD_THRESHOLD
+    # local search after the uniform round (0 rounds: off); half-widths shrink by ls_decay per round
+    ls_rounds: int = 0
+    ls_cand: int = 0
+    ls_sigma_t: float = 0.0
+    ls_sigma_turns: float = 0.0
+    ls_decay: float = 0.5
+
+    def ls_sigmas(self):
+        """Per round r = 1..ls_rounds: (translation half-width float32, turns half-width float64)."""
+        out, sg, sth = [], np.float32(self.ls_sigma_t), float(self.ls_sigma_turns)
+        for r in range(1, self.ls_rounds + 1):
+            if r > 1:
+                sg = np.float32(sg * np.float32(self.ls_decay))
+                sth = sth * float(np.float32(self.ls_decay))
+            out.append((sg, sth))
+        return out
 
     @property
     def box(self) -> np.ndarray:
@@ -71,9 +88,14 @@ def select_host(items, q: np.ndarray, verdicts: np.ndarray) -> int:
 
     The transformation is TRANSFORM_FORMULA in float32 (workload.transform_points), vectorised over
     the candidates; min/max and the argmin's first-occurrence rule are exact."""
+    return select_host_cost(items, q, verdicts)[0]
+
+
+def select_host_cost(items, q: np.ndarray, verdicts: np.ndarray):
+    """(index, float32 cost) of the LBF choice, or (-1, None)."""
     free = np.flatnonzero(verdicts == 0)
     if len(free) == 0:
-        return -1
+        return -1, None
     costs = np.empty(len(free), dtype=np.float32)
     item_ids = q["item"][free]
     for t in np.unique(item_ids):
@@ -85,7 +107,8 @@ def select_host(items, q: np.ndarray, verdicts: np.ndarray) -> int:
         ox = (c * xy[None, :, 0] + (-s) * xy[None, :, 1]) + rows["tx"][:, None] * one
         oy = (s * xy[None, :, 0] + c * xy[None, :, 1]) + rows["ty"][:, None] * one
         costs[sel] = ox.max(axis=1) * np.float32(10.0) + oy.max(axis=1)
-    return int(free[int(np.argmin(costs))])
+    k = int(np.argmin(costs))
+    return int(free[k]), costs[k]
 
 
 def _select_host_scalar(items, q: np.ndarray, verdicts: np.ndarray) -> int:
@@ -120,29 +143,68 @@ def step_queries(spec: LbfSpec, step: int) -> np.ndarray:
     return q
 
 
+def _uniform_round(spec: LbfSpec, step: int, t: int):
+    """Round 0 of a step: make_queries' candidates and their rotations in turns."""
+    q = W.make_queries(W.Stream(spec.seed, CAND_SID_BASE + step), spec.n_cand, 1, spec.box)
+    q["item"] = t
+    st = W.Stream(spec.seed, CAND_SID_BASE + step)
+    st.pos = spec.n_cand   # make_queries draws the items first, then the rotations
+    return q, st.f64(spec.n_cand)
+
+
+def _local_round(spec: LbfSpec, step: int, r: int, t: int, best_u: float, best_q, sg, sth):
+    """Round r >= 1: candidates around the step's best (turns offset, then x, then y draws)."""
+    m = spec.ls_cand
+    st = W.Stream(spec.seed, LS_SID_BASE + 64 * step + r)
+    du = st.f64(m)
+    dx = st.uniform_f32(-sg, sg, m)
+    dy = st.uniform_f32(-sg, sg, m)
+    x = best_u + (2.0 * du - 1.0) * sth
+    u = x - np.floor(x)
+    c, s = W.sincos_turns(u)
+    q = np.zeros(m, dtype=W.QUERY_DTYPE)
+    q["item"] = t
+    q["cos"] = c.astype(np.float32)
+    q["sin"] = s.astype(np.float32)
+    q["tx"] = np.float32(best_q["tx"]) + dx
+    q["ty"] = np.float32(best_q["ty"]) + dy
+    return q, u
+
+
 def run_host(lay, eng, spec: LbfSpec, steps: int | None = None, keep_verdicts: int = 0, on_step=None) -> LbfLog:
-    """The build with one engine call per step (oracle or GPU engine)."""
+    """The build with one engine call per round (oracle or GPU engine)."""
     steps = spec.steps if steps is None else steps
     s_rm = W.Stream(spec.seed, REMOVE_SID)
     types = W.Stream(spec.seed, TYPE_SID).u64(steps) % np.uint64(spec.n_types)
+    sigmas = spec.ls_sigmas()
     placements, removals, free_counts, vkeep = [], [], [], []
     live = []   # keys of placed items, in placement order
     for step in range(steps):
-        q = W.make_queries(W.Stream(spec.seed, CAND_SID_BASE + step), spec.n_cand, 1, spec.box)
         t = int(types[step])
-        q["item"] = t
+        q, u = _uniform_round(spec, step, t)
         verdicts = eng.detect_batch(q)
         if step < keep_verdicts:
             vkeep.append(np.asarray(verdicts).copy())
-        free_counts.append(int((verdicts == 0).sum()))
-        best = select_host(lay.items, q, verdicts)
-        if best >= 0:
-            hz = W.placed_hazard(lay.items[t], t, q["cos"][best], q["sin"][best], q["tx"][best], q["ty"][best])
+        n_free = int((verdicts == 0).sum())
+        best, cost = select_host_cost(lay.items, q, verdicts)
+        rec = (cost, float(u[best]), q[best].copy(), best) if best >= 0 else None
+        for r, (sg, sth) in enumerate(sigmas, start=1):
+            if rec is None:
+                break   # nothing to search around (the device marks the round's candidates invalid)
+            ql, ul = _local_round(spec, step, r, t, rec[1], rec[2], sg, sth)
+            vl = eng.detect_batch(ql)
+            n_free += int((vl == 0).sum())
+            b, cb = select_host_cost(lay.items, ql, vl)
+            if b >= 0 and cb < rec[0]:   # strictly better replaces (search.rs:52 keeps the first)
+                rec = (cb, float(ul[b]), ql[b].copy(), (r << 24) | b)
+        free_counts.append(n_free)
+        if rec is not None:
+            r_q = rec[2]
+            hz = W.placed_hazard(lay.items[t], t, r_q["cos"], r_q["sin"], r_q["tx"], r_q["ty"])
             key = eng.register_hazard(hz.kind, hz.dynamic, hz.xy, hz.poi, 1_000_000 + step)
             live.append(key)
-            r = q[best]
-            placements.append([step, key, best, t] +
-                              [int(np.float32(r[f]).view(np.uint32)) for f in ("cos", "sin", "tx", "ty")])
+            placements.append([step, key, rec[3], t] +
+                              [int(np.float32(r_q[f]).view(np.uint32)) for f in ("cos", "sin", "tx", "ty")])
         if spec.remove_every and (step + 1) % spec.remove_every == 0 and live:
             j = int(s_rm.randint(0, len(live) - 1, 1)[0])
             key = live.pop(j)
@@ -162,7 +224,8 @@ def run_device(eng, spec: LbfSpec, steps: int | None = None, steps_per_graph: in
     steps = spec.steps if steps is None else steps
     cde = eng.eng if hasattr(eng, "eng") else eng
     r = resident if resident is not None else ResidentEngine(cde)
-    r.lbf_begin(spec.seed, spec.n_cand, spec.n_types, spec.remove_every, steps, spec.box, keep_verdicts)
+    r.lbf_begin(spec.seed, spec.n_cand, spec.n_types, spec.remove_every, steps, spec.box, keep_verdicts,
+                spec.ls_rounds, spec.ls_cand, spec.ls_sigma_t, spec.ls_sigma_turns, spec.ls_decay)
     r.lbf_steps(steps, steps_per_graph)
     d = r.lbf_read()
     log = LbfLog(d["placements"], d["removals"], d["free_counts"], list(d["verdicts"]))

@@ -171,3 +171,15 @@ def test_lbf_select_entry_point_matches_host_choice(oracle_mod, jcde_mod):
     v[[3, 7]] = 0
     assert lbf_select(geng, q, v) == 3
     assert lbf_select(geng, q, np.ones(len(q), np.uint8)) == -1
+
+
+def test_lbf_with_local_search_matches_oracle(oracle_mod, jcde_mod):
+    """Uniform round plus three local-search rounds per step, on the device and through the oracle."""
+    spec = lbf.LbfSpec(steps=160, n_cand=4096, remove_every=40, ls_rounds=3, ls_cand=1024, ls_sigma_t=150.0,
+                       ls_sigma_turns=0.05)
+    ref, oeng, got, r = _lbf_pair(oracle_mod, spec, steps_per_graph=16)
+    rounds = ref.placements[:, 2] >> 24
+    assert (rounds > 0).sum() > 20   # local search improved many steps
+    assert got.same_as(ref)
+    assert r.status()["error"] == 0
+    assert np.array_equal(r.tree_dump(), oeng.tree_dump())

@@ -59,3 +59,19 @@ def test_step_streams():
                                               np.nextafter(np.float32(spec.width), np.float32(0))))
     t = W.Stream(spec.seed, lbf.TYPE_SID).u64(8)[7] % np.uint64(spec.n_types)
     assert (q["item"] == t).all()
+
+
+def test_host_build_with_local_search(oracle_mod):
+    """Local search never places worse than the uniform round's choice of the same step."""
+    base = dict(n_types=12, n_cand=512, steps=30, remove_every=0)
+    spec0 = lbf.LbfSpec(**base)
+    spec1 = lbf.LbfSpec(**base, ls_rounds=2, ls_cand=256, ls_sigma_t=100.0, ls_sigma_turns=0.05)
+    lay0, eng0 = lbf.setup(oracle_mod.OracleBackend, spec0)
+    lay1, eng1 = lbf.setup(oracle_mod.OracleBackend, spec1)
+    q, _ = lbf._uniform_round(spec1, 0, int(lbf.step_queries(spec1, 0)["item"][0]))
+    b, cost0 = lbf.select_host_cost(lay1.items, q, eng1.detect_batch(q))
+    log1 = lbf.run_host(lay1, eng1, spec1, steps=1)
+    p = log1.placements[0]
+    xy = W.transform_points(lay1.items[int(p[3])].xy, *[np.uint32(v).view(np.float32) for v in p[4:8]])
+    assert lbf.lbf_cost(xy) <= cost0
+    assert len(lbf.run_host(lay0, eng0, spec0, steps=5).placements) == 5
