@@ -666,6 +666,27 @@ def run_lbf(args):
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
         d2h = (log_e2e.placements.nbytes + log_e2e.removals.nbytes + log_e2e.free_counts.nbytes + 16)
     e2e_value = n_cand_total / (np.median(e2e_ms) / 1e3)
+    # the same build with three local-search rounds of 2048 candidates per step (search.rs:80-101 restated)
+    spec_ls = lbf.LbfSpec(ls_rounds=3, ls_cand=2048, ls_sigma_t=200.0, ls_sigma_turns=0.05)
+    ls_ms = []
+    for k in range(2):
+        r.reset()
+        r.lbf_begin(spec_ls.seed, spec_ls.n_cand, spec_ls.n_types, spec_ls.remove_every, spec_ls.steps, spec_ls.box, 0,
+                    spec_ls.ls_rounds, spec_ls.ls_cand, spec_ls.ls_sigma_t, spec_ls.ls_sigma_turns, spec_ls.ls_decay)
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        r.lbf_steps(spec_ls.steps, SPG, stream=sh)
+        b.record(stream)
+        torch.cuda.synchronize()
+        if k:
+            ls_ms.append(a.elapsed_time(b))
+    d_ls = r.lbf_read()
+    ls_cands = spec_ls.steps * (spec_ls.n_cand + spec_ls.ls_rounds * spec_ls.ls_cand)
+    local_search = {"ms_per_build": ls_ms[0], "candidates_per_s": ls_cands / (ls_ms[0] / 1e3),
+                    "rounds": spec_ls.ls_rounds, "candidates_per_round": spec_ls.ls_cand,
+                    "placements_improved_by_local_search": int(((d_ls["placements"][:, 2] >> 24) > 0).sum())}
     # the same build driven step by step from the host through the regular engine (host registration,
     # a re-flattened tree upload per step): a bounded sample of its first steps
     host_steps = 200
@@ -692,6 +713,7 @@ def run_lbf(args):
         "gpu_launches": int(launches),
         "e2e": {"value": e2e_value, "unit": "candidates/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_build": float(np.median(e2e_ms))},
+        "with_local_search": local_search,
         "host_driven_gpu": {"value": host_steps * spec.n_cand / host_s, "unit": "candidates/s",
                             "sample": f"first {host_steps} steps", "same_placements": host_ok},
         "clocks": clk.summary(),
