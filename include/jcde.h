@@ -305,6 +305,16 @@ typedef struct jcde_lbf_params {
     float ls_sigma_t;
     float ls_decay;
     double ls_sigma_turns;
+    /* instance mode (both optional, host arrays copied at jcde_lbf_begin): the item of step s is
+     * item_sequence[s] instead of a type-stream draw; item t rotates to one of its allowed
+     * orientations orientation_cs[2 * (offsets[t] + k)..] (cos, sin), k = (draw n+i) mod count, or
+     * continuously when offsets[t + 1] == offsets[t]; local-search rounds keep a discrete
+     * orientation.  (lbf/src/opt/lbf_spp.rs:37-123 places the instance's items in this order.) */
+    const uint32_t* item_sequence;
+    uint32_t n_sequence;           /* at least max_steps */
+    uint32_t n_orientation_items;  /* the engine's item count when orientation_offsets is given */
+    const uint32_t* orientation_offsets;   /* n_items + 1 */
+    const float* orientation_cs;
 } jcde_lbf_params;
 jcde_status jcde_lbf_begin(jcde_resident* r, const jcde_lbf_params* p);
 jcde_status jcde_lbf_steps(jcde_resident* r, uint32_t n_steps, uint32_t steps_per_graph, void* stream);

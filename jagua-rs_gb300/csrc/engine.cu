@@ -1365,6 +1365,7 @@ struct jcde_resident {
     bool lbf_ready = false;
     LbfParams lp{};
     DevBuf d_lbf, d_cand, d_candu, d_verd, d_place, d_remv, d_free, d_live, d_vlog;
+    DevBuf d_seq, d_orient, d_orient_of;   // instance mode: item sequence, allowed orientations
     DevBuf d_hist, d_order;   // spatial ordering of the resident's own query batches
     DevBuf d_next;            // work counters of its two passes
     cudaGraphExec_t exec = nullptr;
@@ -1733,8 +1734,8 @@ jcde_status jcde_resident_tree_dump(jcde_resident* r, uint32_t* out, uint64_t ca
 uint64_t jcde_resident_kernel_launches(const jcde_resident* r) { return r ? r->launches : 0; }
 
 jcde_status jcde_lbf_begin(jcde_resident* r, const jcde_lbf_params* p) {
-    if (!r || !p || !p->n_candidates || !p->n_types || !p->max_steps) return JCDE_ERR_ARG;
-    if (p->n_types > r->e->items.size()) return JCDE_ERR_ARG;
+    if (!r || !p || !p->n_candidates || !p->max_steps) return JCDE_ERR_ARG;
+    if ((!p->item_sequence && !p->n_types) || p->n_types > r->e->items.size()) return JCDE_ERR_ARG;
     const jcde_rect b = p->sample_box;
     if (!(b.x_min < b.x_max && b.y_min < b.y_max)) return JCDE_ERR_ARG;
     if (r->last) CUDA_TRY(cudaStreamSynchronize(r->last));
@@ -1774,6 +1775,32 @@ jcde_status jcde_lbf_begin(jcde_resident* r, const jcde_lbf_params* p) {
         }
     }
     if (lp.ls_rounds && lp.vlog_steps) return JCDE_ERR_ARG;   // the verdict log keeps one round per step
+    // instance mode: the item sequence and the allowed orientations
+    const uint32_t n_items = (uint32_t)r->e->items.size();
+    if (p->item_sequence) {
+        if (p->n_sequence < p->max_steps) return JCDE_ERR_ARG;
+        for (uint32_t k = 0; k < p->n_sequence; k++)
+            if (p->item_sequence[k] >= n_items) return JCDE_ERR_ARG;
+        if (!r->d_seq.ensure((size_t)p->n_sequence * 4)) return JCDE_ERR_CUDA;
+        CUDA_TRY(cudaMemcpy(r->d_seq.p, p->item_sequence, (size_t)p->n_sequence * 4, cudaMemcpyHostToDevice));
+        lp.seq = r->d_seq.as<uint32_t>();
+    }
+    if (p->orientation_offsets) {
+        if (p->n_orientation_items != n_items || !p->orientation_cs) return JCDE_ERR_ARG;
+        std::vector<uint2> of(n_items);
+        for (uint32_t k = 0; k < n_items; k++) {
+            const uint32_t a = p->orientation_offsets[k], b = p->orientation_offsets[k + 1];
+            if (b < a) return JCDE_ERR_ARG;
+            of[k] = make_uint2(a, b - a);
+        }
+        const uint32_t n_or = p->orientation_offsets[n_items];
+        if (!r->d_orient_of.ensure(of.size() * sizeof(uint2)) || !r->d_orient.ensure(std::max<size_t>(n_or, 1) * 8))
+            return JCDE_ERR_CUDA;
+        CUDA_TRY(cudaMemcpy(r->d_orient_of.p, of.data(), of.size() * sizeof(uint2), cudaMemcpyHostToDevice));
+        if (n_or) CUDA_TRY(cudaMemcpy(r->d_orient.p, p->orientation_cs, (size_t)n_or * 8, cudaMemcpyHostToDevice));
+        lp.orient = r->d_orient.as<float2>();
+        lp.orient_of = r->d_orient_of.as<uint2>();
+    }
     const size_t n = p->n_candidates, ms = p->max_steps;
     const bool ok = r->d_lbf.ensure(sizeof(LbfDev)) && r->d_cand.ensure(n * 20) && r->d_candu.ensure(n * 8) &&
                     r->d_verd.ensure(n) &&

@@ -633,14 +633,28 @@ __global__ void k_lbf_gen(LbfParams p, LbfDev* __restrict__ st, uint32_t* __rest
             st->rec_cost = ~0u;
         }
     }
-    const uint32_t t = (uint32_t)(draw(p.key_types, step) % p.n_types);
+    const uint32_t t = p.seq ? p.seq[step] : (uint32_t)(draw(p.key_types, step) % p.n_types);
+    uint32_t ooff = 0, ocnt = 0;   // allowed orientations of the item (none listed: continuous)
+    if (p.orient_of) {
+        const uint2 oo = p.orient_of[t];
+        ooff = oo.x;
+        ocnt = oo.y;
+    }
     if (round == 0) {
         const unsigned long long key = stream_key(p.seed, (unsigned long long)p.sid_base + step);
         const unsigned long long n = p.n_cand;
         for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < p.n_cand; i += gridDim.x * blockDim.x) {
             float c, s;
-            const double u = (double)(draw(key, n + i) >> 11) * 0x1p-53;
-            sincos_turns(u, c, s);
+            double u = 0.0;
+            const unsigned long long d = draw(key, n + i);
+            if (ocnt) {   // one of the allowed orientations (draw modulo their count)
+                const float2 cs = p.orient[ooff + (uint32_t)(d % ocnt)];
+                c = cs.x;
+                s = cs.y;
+            } else {
+                u = (double)(d >> 11) * 0x1p-53;
+                sincos_turns(u, c, s);
+            }
             uint32_t* r = q + (size_t)i * 5;
             r[0] = t;
             r[1] = __float_as_uint(c);
@@ -665,11 +679,17 @@ __global__ void k_lbf_gen(LbfParams p, LbfDev* __restrict__ st, uint32_t* __rest
             r[0] = 0xFFFFFFFFu;   // no best to search around: an invalid item, never free
             continue;
         }
-        const double du = (double)(draw(key, i) >> 11) * 0x1p-53;
-        const double x = __dadd_rn(ub, __dmul_rn(__dsub_rn(__dmul_rn(2.0, du), 1.0), sth));
-        const double u = __dsub_rn(x, floor(x));
         float c, s;
-        sincos_turns(u, c, s);
+        double u = ub;
+        if (ocnt) {   // discrete orientations: the best's rotation is kept
+            c = __uint_as_float(vs->rec_q[1]);
+            s = __uint_as_float(vs->rec_q[2]);
+        } else {
+            const double du = (double)(draw(key, i) >> 11) * 0x1p-53;
+            const double x = __dadd_rn(ub, __dmul_rn(__dsub_rn(__dmul_rn(2.0, du), 1.0), sth));
+            u = __dsub_rn(x, floor(x));
+            sincos_turns(u, c, s);
+        }
         r[0] = t;
         r[1] = __float_as_uint(c);
         r[2] = __float_as_uint(s);

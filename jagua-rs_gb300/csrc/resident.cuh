@@ -111,6 +111,11 @@ struct LbfParams {
     unsigned long long ls_sid_base;
     float ls_sig[LBF_MAX_LS + 1], ls_sig_below[LBF_MAX_LS + 1];
     double ls_sth[LBF_MAX_LS + 1];
+    // instance mode: the item of step s is seq[s] (else drawn from the type stream); item t rotates
+    // to one of orient[orient_of[t].x ..][0 .. orient_of[t].y) (count 0: continuous rotation)
+    const uint32_t* seq;
+    const float2* orient;
+    const uint2* orient_of;
 };
 
 struct LbfLogs {

@@ -32,7 +32,9 @@ class jcde_lbf_params(C.Structure):
                 ("remove_every", C.c_uint32), ("max_steps", C.c_uint32), ("verdict_log_steps", C.c_uint32),
                 ("reserved", C.c_uint32), ("sample_box", jcde_rect), ("ls_rounds", C.c_uint32),
                 ("ls_candidates", C.c_uint32), ("ls_sigma_t", C.c_float), ("ls_decay", C.c_float),
-                ("ls_sigma_turns", C.c_double)]
+                ("ls_sigma_turns", C.c_double), ("item_sequence", C.POINTER(C.c_uint32)), ("n_sequence", C.c_uint32),
+                ("n_orientation_items", C.c_uint32), ("orientation_offsets", C.POINTER(C.c_uint32)),
+                ("orientation_cs", C.POINTER(C.c_float))]
 
 
 class jcde_tuning(C.Structure):

@@ -589,8 +589,27 @@ class ResidentEngine:
         return int(lib().jcde_resident_kernel_launches(self.h))
 
     def lbf_begin(self, seed, n_candidates, n_types, remove_every, max_steps, sample_box, verdict_log_steps=0,
-                  ls_rounds=0, ls_candidates=0, ls_sigma_t=0.0, ls_sigma_turns=0.0, ls_decay=0.5):
+                  ls_rounds=0, ls_candidates=0, ls_sigma_t=0.0, ls_sigma_turns=0.0, ls_decay=0.5, item_sequence=None,
+                  orientations=None):
+        """orientations: per engine item a float32 [k, 2] (cos, sin) table, or None for continuous rotation."""
         p = jcde_lbf_params()
+        keep = []
+        if item_sequence is not None:
+            seq = np.ascontiguousarray(item_sequence, dtype=np.uint32)
+            keep.append(seq)
+            p.item_sequence = seq.ctypes.data_as(C.POINTER(C.c_uint32))
+            p.n_sequence = len(seq)
+        if orientations is not None:
+            offs = np.zeros(len(orientations) + 1, dtype=np.uint32)
+            for i, o in enumerate(orientations):
+                offs[i + 1] = offs[i] + (0 if o is None else len(o))
+            cs = np.concatenate([np.asarray(o, np.float32).reshape(-1, 2) for o in orientations if o is not None]
+                                or [np.zeros((0, 2), np.float32)]).astype(np.float32)
+            cs = np.ascontiguousarray(cs if len(cs) else np.zeros((1, 2), np.float32))
+            keep += [offs, cs]
+            p.n_orientation_items = len(orientations)
+            p.orientation_offsets = offs.ctypes.data_as(C.POINTER(C.c_uint32))
+            p.orientation_cs = cs.ctypes.data_as(C.POINTER(C.c_float))
         p.ls_rounds = int(ls_rounds)
         p.ls_candidates = int(ls_candidates)
         p.ls_sigma_t = float(np.float32(ls_sigma_t))
@@ -606,6 +625,7 @@ class ResidentEngine:
         p.sample_box = jcde_rect(*[float(x) for x in b])
         self._lbf = p
         check(lib().jcde_lbf_begin(self.h, C.byref(p)), "lbf_begin")
+        del keep   # the arrays are copied by jcde_lbf_begin
 
     def lbf_steps(self, n_steps, steps_per_graph=0, stream=None) -> None:
         check(lib().jcde_lbf_steps(self.h, int(n_steps), int(steps_per_graph), _stream_handle(stream)), "lbf_steps")

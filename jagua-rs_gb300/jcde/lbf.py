@@ -50,6 +50,10 @@ class LbfSpec:
     ls_sigma_t: float = 0.0
     ls_sigma_turns: float = 0.0
     ls_decay: float = 0.5
+    # instance mode: the item of each step (else drawn from the type stream) and, per item, a float32
+    # (cos, sin) table of allowed orientations or None for continuous rotation
+    item_seq: np.ndarray | None = None
+    orient: list | None = None
 
     def ls_sigmas(self):
         """Per round r = 1..ls_rounds: (translation half-width float32, turns half-width float64)."""
@@ -143,13 +147,24 @@ def step_queries(spec: LbfSpec, step: int) -> np.ndarray:
     return q
 
 
+def _orient_of(spec: LbfSpec, t: int):
+    return None if spec.orient is None else spec.orient[t]
+
+
 def _uniform_round(spec: LbfSpec, step: int, t: int):
-    """Round 0 of a step: make_queries' candidates and their rotations in turns."""
+    """Round 0 of a step: make_queries' candidates and their rotations in turns (with allowed
+    orientations: orientation (draw n+i) mod count, turns unused)."""
     q = W.make_queries(W.Stream(spec.seed, CAND_SID_BASE + step), spec.n_cand, 1, spec.box)
     q["item"] = t
     st = W.Stream(spec.seed, CAND_SID_BASE + step)
     st.pos = spec.n_cand   # make_queries draws the items first, then the rotations
-    return q, st.f64(spec.n_cand)
+    o = _orient_of(spec, t)
+    if o is None:
+        return q, st.f64(spec.n_cand)
+    k = (st.u64(spec.n_cand) % np.uint64(len(o))).astype(np.int64)
+    q["cos"] = o[k, 0]
+    q["sin"] = o[k, 1]
+    return q, np.zeros(spec.n_cand)
 
 
 def _local_round(spec: LbfSpec, step: int, r: int, t: int, best_u: float, best_q, sg, sth):
@@ -159,13 +174,18 @@ def _local_round(spec: LbfSpec, step: int, r: int, t: int, best_u: float, best_q
     du = st.f64(m)
     dx = st.uniform_f32(-sg, sg, m)
     dy = st.uniform_f32(-sg, sg, m)
-    x = best_u + (2.0 * du - 1.0) * sth
-    u = x - np.floor(x)
-    c, s = W.sincos_turns(u)
     q = np.zeros(m, dtype=W.QUERY_DTYPE)
     q["item"] = t
-    q["cos"] = c.astype(np.float32)
-    q["sin"] = s.astype(np.float32)
+    if _orient_of(spec, t) is not None:   # discrete orientations: the best's rotation is kept
+        u = np.full(m, best_u)
+        q["cos"] = best_q["cos"]
+        q["sin"] = best_q["sin"]
+    else:
+        x = best_u + (2.0 * du - 1.0) * sth
+        u = x - np.floor(x)
+        c, s = W.sincos_turns(u)
+        q["cos"] = c.astype(np.float32)
+        q["sin"] = s.astype(np.float32)
     q["tx"] = np.float32(best_q["tx"]) + dx
     q["ty"] = np.float32(best_q["ty"]) + dy
     return q, u
@@ -175,12 +195,12 @@ def run_host(lay, eng, spec: LbfSpec, steps: int | None = None, keep_verdicts: i
     """The build with one engine call per round (oracle or GPU engine)."""
     steps = spec.steps if steps is None else steps
     s_rm = W.Stream(spec.seed, REMOVE_SID)
-    types = W.Stream(spec.seed, TYPE_SID).u64(steps) % np.uint64(spec.n_types)
+    types = W.Stream(spec.seed, TYPE_SID).u64(steps) % np.uint64(max(spec.n_types, 1))
     sigmas = spec.ls_sigmas()
     placements, removals, free_counts, vkeep = [], [], [], []
     live = []   # keys of placed items, in placement order
     for step in range(steps):
-        t = int(types[step])
+        t = int(spec.item_seq[step]) if spec.item_seq is not None else int(types[step])
         q, u = _uniform_round(spec, step, t)
         verdicts = eng.detect_batch(q)
         if step < keep_verdicts:
@@ -225,7 +245,8 @@ def run_device(eng, spec: LbfSpec, steps: int | None = None, steps_per_graph: in
     cde = eng.eng if hasattr(eng, "eng") else eng
     r = resident if resident is not None else ResidentEngine(cde)
     r.lbf_begin(spec.seed, spec.n_cand, spec.n_types, spec.remove_every, steps, spec.box, keep_verdicts,
-                spec.ls_rounds, spec.ls_cand, spec.ls_sigma_t, spec.ls_sigma_turns, spec.ls_decay)
+                spec.ls_rounds, spec.ls_cand, spec.ls_sigma_t, spec.ls_sigma_turns, spec.ls_decay,
+                item_sequence=spec.item_seq, orientations=spec.orient)
     r.lbf_steps(steps, steps_per_graph)
     d = r.lbf_read()
     log = LbfLog(d["placements"], d["removals"], d["free_counts"], list(d["verdicts"]))
@@ -253,3 +274,11 @@ def main(argv=None) -> int:
 
 if __name__ == "__main__":
     raise SystemExit(main())
+
+
+def spec_for_instance(setup, **kw) -> LbfSpec:
+    """An LBF build of a strip-packing instance (jcde.instance.setup_spp): every item in the placement
+    order, the strip as the sampling box, no removals."""
+    lay = setup.layout
+    return LbfSpec(n_types=len(lay.items), width=setup.width, height=float(lay.hazards[0].xy[:, 1].max()),
+                   steps=len(setup.sequence), remove_every=0, item_seq=setup.sequence, orient=setup.orient, **kw)

@@ -183,3 +183,19 @@ def test_lbf_with_local_search_matches_oracle(oracle_mod, jcde_mod):
     assert got.same_as(ref)
     assert r.status()["error"] == 0
     assert np.array_equal(r.tree_dump(), oeng.tree_dump())
+
+
+def test_instance_build_matches_oracle(oracle_mod, jcde_mod):
+    """A strip-packing instance (reference JSON format): item sequence, discrete and continuous
+    orientations, local search; the device build places what the oracle-driven build places."""
+    from jcde import instance as I
+    from test_instance import DEMO
+
+    inst = I.load_spp(DEMO)
+    su_o = I.setup_spp(oracle_mod.OracleBackend, inst, 800.0)
+    su_g = I.setup_spp(jcde.GpuBackend, inst, 800.0)
+    spec = lbf.spec_for_instance(su_o, n_cand=2048, ls_rounds=2, ls_cand=512, ls_sigma_t=30.0, ls_sigma_turns=0.05)
+    ref = lbf.run_host(su_o.layout, su_o.engine, spec)
+    got, r = lbf.run_device(su_g.engine, spec, steps_per_graph=4)
+    assert len(ref.placements) == 12 and got.same_as(ref)
+    assert np.array_equal(r.tree_dump(), su_o.engine.tree_dump())
