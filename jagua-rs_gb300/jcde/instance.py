@@ -134,3 +134,24 @@ def setup_spp(backend, inst: SppInstance, strip_width: float, depth: int = W.DEF
         else:
             orient.append(orientation_cs(it.orientations))
     return SppSetup(lay, eng, seq, orient, float(strip_width))
+
+
+def export_solution(setup: SppSetup, inst: SppInstance, placements: np.ndarray, removals=None) -> dict:
+    """The placed items as the reference's external layout (io/ext_repr.rs ExtLayout / ExtPlacedItem):
+    per item its instance id and the transformation of its original shape, rotation in degrees (as
+    From<DTransformation> for ExtTransformation writes it) and translation.  The internal placement
+    (c, s, tx, ty) acts on the centred shape, so the original shape moves by t - R * centroid."""
+    gone = set() if removals is None else {int(k) for _, k in np.asarray(removals).reshape(-1, 2)}
+    placed, area = [], 0.0
+    for p in np.asarray(placements).reshape(-1, 8):
+        if int(p[1]) in gone:
+            continue
+        t = int(p[3])
+        c, s, tx, ty = (float(np.uint32(v).view(np.float32)) for v in p[4:8])
+        cx, cy = setup.layout.items[t].centroid
+        placed.append({"item_id": inst.items[t].id,
+                       "transformation": {"rotation": float(np.degrees(np.arctan2(s, c))),
+                                          "translation": [tx - (c * cx - s * cy), ty - (s * cx + c * cy)]}})
+        area += setup.layout.items[t].area
+    return {"container_id": 0, "placed_items": placed,
+            "density": float(area / (setup.width * inst.strip_height)) if placed else 0.0}

@@ -172,6 +172,7 @@ class Item:
     n_ff_poles: int
     area: float
     diameter: float
+    centroid: tuple = (0.0, 0.0)   # of the imported shape: the centering pre-transform moved it to the origin
 
 
 @dataclass
@@ -205,7 +206,7 @@ def import_item(backend, raw_xy, pole_limits=DEFAULT_POLE_LIMITS, n_ff_poles=DEF
     ixy = transform_points(xy, 1.0, 0.0, -cx, -cy)
     ipoi = np.concatenate([transform_points(poi[None, :2], 1.0, 0.0, -cx, -cy)[0], poi[2:3]]).astype(np.float32)
     poles = backend.surrogate_poles(ixy, area, ipoi, pole_limits)
-    return Item(ixy, ipoi, poles, min(n_ff_poles, len(poles)), float(area), float(diam))
+    return Item(ixy, ipoi, poles, min(n_ff_poles, len(poles)), float(area), float(diam), (float(cx), float(cy)))
 
 
 def import_static(backend, raw_xy, kind) -> HazardSpec:

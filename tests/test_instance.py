@@ -86,3 +86,23 @@ def test_import_simple_polygon_rules(oracle_mod):
     for a, b in ((1.0, 1.0), (0.0, 1e-8), (1.0, float(np.nextafter(np.float32(1), np.float32(2))))):
         assert I.fpa_eq32(a, b) == oracle_mod.fpa_eq(a, b)
     assert not I.fpa_eq32(1.0, 1.001) and not oracle_mod.fpa_eq(1.0, 1.001)
+
+
+def test_export_solution_moves_the_original_shapes(oracle_mod):
+    """Exported transformations applied to the original shapes give the placed hazards' vertices."""
+    inst = I.load_spp(DEMO)
+    su = I.setup_spp(oracle_mod.OracleBackend, inst, 800.0)
+    spec = lbf.spec_for_instance(su, n_cand=1024)
+    log = lbf.run_host(su.layout, su.engine, spec)
+    sol = I.export_solution(su, inst, log.placements)
+    assert len(sol["placed_items"]) == 12 and 0.0 < sol["density"] < 1.0
+    for p, e in zip(log.placements, sol["placed_items"]):
+        t = int(p[3])
+        assert e["item_id"] == inst.items[t].id
+        c, s, tx, ty = (np.uint32(v).view(np.float32) for v in p[4:8])
+        want = W.transform_points(su.layout.items[t].xy, c, s, tx, ty).astype(np.float64)
+        raw = inst.items[t].xy.astype(np.float64)
+        a = np.radians(e["transformation"]["rotation"])
+        got = raw @ np.array([[np.cos(a), np.sin(a)], [-np.sin(a), np.cos(a)]]) + e["transformation"]["translation"]
+        # the importer may reverse a clockwise outline: compare as point sets
+        assert np.abs(np.sort(got, axis=0) - np.sort(want, axis=0)).max() < 1e-2
