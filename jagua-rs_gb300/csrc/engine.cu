@@ -91,7 +91,7 @@ struct jcde_engine {
     FlatTree flat;
     std::vector<DHaz> haz;
     std::vector<float2> hverts;
-    DevBuf d_nodes, d_nedges, d_strength0, d_entries, d_edges, d_haz, d_hverts;
+    DevBuf d_nodes, d_nedges, d_strength0, d_entries, d_edges, d_cbox, d_haz, d_hverts;
     DevBuf d_items, d_iverts, d_poles, d_piers;
     uint32_t n_nodes = 0;
     // filters
@@ -201,6 +201,7 @@ static jcde_status sync_device(jcde_engine* e) {
         if ((st = upload(e->d_strength0, e->flat.strength.data(), e->flat.strength.size()))) return st;
         if ((st = upload(e->d_entries, e->flat.entries.data(), e->flat.entries.size() * sizeof(DEntry)))) return st;
         if ((st = upload(e->d_edges, e->flat.edges.data(), e->flat.edges.size() * 4))) return st;
+        if ((st = upload(e->d_cbox, e->flat.cbox.data(), e->flat.cbox.size() * sizeof(Box)))) return st;
         if ((st = upload(e->d_haz, e->haz.data(), e->haz.size() * sizeof(DHaz)))) return st;
         if ((st = upload(e->d_hverts, e->hverts.data(), e->hverts.size() * sizeof(float2)))) return st;
         e->n_nodes = (uint32_t)e->flat.nodes.size();
@@ -286,6 +287,7 @@ static View base_view(const jcde_engine* e) {
     v.strength = e->d_strength0.as<uint8_t>();
     v.mask = nullptr;
     v.nedges = e->d_nedges.as<uint32_t>();
+    v.cbox = e->d_cbox.as<float4>();
     v.cde = e->tree.bbox();
     v.n_items = (uint32_t)e->items.size();
     v.n_slots = e->tree.n_slots();
@@ -1398,6 +1400,7 @@ static View resident_view(const jcde_resident* r) {
     v.hverts = r->t.hverts;
     v.strength = r->t.strength;
     v.nedges = r->t.nedges;
+    v.cbox = nullptr;   // the resident pools keep no edge-group boxes
     v.mask = nullptr;
     v.n_slots = r->t.key_cap;
     v.exterior = r->exterior;

@@ -82,7 +82,8 @@ struct FlatTree {
     std::vector<uint32_t> nedges;   // n_active_edges per node (collect's cd_threshold rule)
     std::vector<uint8_t> strength;  // strongest presence per node with no filter
     std::vector<DEntry> entries;
-    std::vector<float> edges;       // 4 floats per edge (x1, y1, x2, y2)
+    std::vector<float> edges;       // 4 floats per edge (x1, y1, x2, y2); every list starts at a multiple of 8
+    std::vector<Box> cbox;          // bounding box of each group of 8 edges (edges[8 g .. 8 g + 8) of one list)
 };
 
 class QuadTree {
