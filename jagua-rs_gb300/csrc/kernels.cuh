@@ -42,7 +42,7 @@ struct View {
     const uint8_t* __restrict__ strength;   // strongest unfiltered presence per node
     const uint32_t* __restrict__ mask;      // ignored-key bitmask, nullptr = NoFilter
     const uint32_t* __restrict__ nedges;    // active edges per node (collect)
-    const float4* __restrict__ cbox;        // box of each group of 8 edges (nullptr: not kept)
+    const float4* __restrict__ cbox;        // box of each group of EDGE_GROUP edges (nullptr: not kept)
     Box cde;
     uint32_t n_items, n_slots, cd_threshold;
     int32_t exterior;
@@ -163,15 +163,15 @@ __device__ __forceinline__ bool leaf_hits(const View& v, const P& p, const DNode
         if (filtered(v, e.hkey)) continue;
         if constexpr (std::is_same<P, Seg>::value) {
             if (JCDE_EDGE_GROUPS && v.cbox) {
-                // groups of 8 edges whose box misses the probe's box are skipped: edge_intersection
+                // groups of edges whose box misses the probe's box are skipped: edge_intersection
                 // rejects every edge of such a group on the boxes' overlap (edge.rs:188-199)
                 const float px0 = fmn(p.s.x, p.e.x), px1 = fmx(p.s.x, p.e.x);
                 const float py0 = fmn(p.s.y, p.e.y), py1 = fmx(p.s.y, p.e.y);
-                for (uint32_t g = 0; g * 8 < e.edge_cnt; g++) {
-                    const float4 c = __ldg(&v.cbox[(e.edge_off >> 3) + g]);
+                for (uint32_t g = 0; g * EDGE_GROUP < e.edge_cnt; g++) {
+                    const float4 c = __ldg(&v.cbox[e.edge_off / EDGE_GROUP + g]);
                     if (fmx(px0, c.x) > fmn(px1, c.z) || fmx(py0, c.y) > fmn(py1, c.w)) continue;
-                    const uint32_t end = min(e.edge_cnt, g * 8 + 8);
-                    for (uint32_t j = g * 8; j < end; j++)
+                    const uint32_t end = min(e.edge_cnt, g * EDGE_GROUP + EDGE_GROUP);
+                    for (uint32_t j = g * EDGE_GROUP; j < end; j++)
                         if (p_hits_seg(p, ld_edge(v, e.edge_off + j))) {
                             if (stop) *stop = 1;
                             return true;

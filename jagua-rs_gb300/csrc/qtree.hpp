@@ -15,6 +15,13 @@
 namespace jcde {
 
 enum Presence : uint32_t { PRES_NONE = 0, PRES_PARTIAL = 1, PRES_ENTIRE = 2 };
+
+// Edge lists of the flattened tree start on a multiple of EDGE_GROUP edges, and every group of
+// EDGE_GROUP consecutive edges of a list has a bounding box (FlatTree::cbox).
+#ifndef JCDE_EDGE_GROUP
+#define JCDE_EDGE_GROUP 8
+#endif
+constexpr uint32_t EDGE_GROUP = JCDE_EDGE_GROUP;
 enum Kind : int32_t { KIND_PLACED_ITEM = 0, KIND_EXTERIOR = 1, KIND_HOLE = 2, KIND_QUALITY_ZONE = 3 };
 inline bool kind_is_exterior(int32_t k) { return k == KIND_EXTERIOR; }  // hazard.rs:55-62
 
@@ -82,8 +89,8 @@ struct FlatTree {
     std::vector<uint32_t> nedges;   // n_active_edges per node (collect's cd_threshold rule)
     std::vector<uint8_t> strength;  // strongest presence per node with no filter
     std::vector<DEntry> entries;
-    std::vector<float> edges;       // 4 floats per edge (x1, y1, x2, y2); every list starts at a multiple of 8
-    std::vector<Box> cbox;          // bounding box of each group of 8 edges (edges[8 g .. 8 g + 8) of one list)
+    std::vector<float> edges;       // 4 floats per edge (x1, y1, x2, y2); every list starts at a group boundary
+    std::vector<Box> cbox;          // bounding box of each group of EDGE_GROUP edges of one list
 };
 
 class QuadTree {
