@@ -215,6 +215,29 @@ __device__ __forceinline__ bool bit_get(const uint32_t* bits, uint32_t k) {
     return (((volatile const uint32_t*)bits)[k >> 5] >> (k & 31)) & 1u;
 }
 
+// Any edge of entry e hit by probe p; for an edge probe the edge groups whose box misses the
+// probe's box are skipped (see leaf_hits).
+template <class P>
+__device__ __forceinline__ bool seg_group_hits(const View& v, const P& p, const DEntry& e) {
+    if constexpr (std::is_same<P, Seg>::value) {
+        if (JCDE_EDGE_GROUPS && v.cbox) {
+            const float px0 = fmn(p.s.x, p.e.x), px1 = fmx(p.s.x, p.e.x);
+            const float py0 = fmn(p.s.y, p.e.y), py1 = fmx(p.s.y, p.e.y);
+            for (uint32_t g = 0; g * EDGE_GROUP < e.edge_cnt; g++) {
+                const float4 c = __ldg(&v.cbox[e.edge_off / EDGE_GROUP + g]);
+                if (fmx(px0, c.x) > fmn(px1, c.z) || fmx(py0, c.y) > fmn(py1, c.w)) continue;
+                const uint32_t end = min(e.edge_cnt, g * EDGE_GROUP + EDGE_GROUP);
+                for (uint32_t j = g * EDGE_GROUP; j < end; j++)
+                    if (p_hits_seg(p, ld_edge(v, e.edge_off + j))) return true;
+            }
+            return false;
+        }
+    }
+    for (uint32_t j = 0; j < e.edge_cnt; j++)
+        if (p_hits_seg(p, ld_edge(v, e.edge_off + j))) return true;
+    return false;
+}
+
 // QTNode::collect_collisions (qt_node.rs:151-191) for one probe from node `start`.
 template <class P>
 __device__ void collect_walk(const View& v, const P& p, int start, uint32_t* bits) {
@@ -232,11 +255,7 @@ __device__ void collect_walk(const View& v, const P& p, int start, uint32_t* bit
                 if (e.presence == PRES_ENTIRE) {
                     bit_set(bits, e.hkey);
                 } else if (e.presence == PRES_PARTIAL && p_hits_box(p, e.ff)) {
-                    for (uint32_t j = 0; j < e.edge_cnt; j++)
-                        if (p_hits_seg(p, ld_edge(v, e.edge_off + j))) {
-                            bit_set(bits, e.hkey);
-                            break;
-                        }
+                    if (seg_group_hits(v, p, e)) bit_set(bits, e.hkey);
                 }
             }
         }
