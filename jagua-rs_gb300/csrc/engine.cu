@@ -289,6 +289,7 @@ static View base_view(const jcde_engine* e) {
     v.nedges = e->d_nedges.as<uint32_t>();
     v.cbox = e->d_cbox.as<float4>();
     v.cde = e->tree.bbox();
+    v.coord_max = std::max(std::max(std::fabs(v.cde.x0), std::fabs(v.cde.x1)), std::max(std::fabs(v.cde.y0), std::fabs(v.cde.y1)));
     v.n_items = (uint32_t)e->items.size();
     v.n_slots = e->tree.n_slots();
     v.cd_threshold = e->cfg.cd_threshold;

@@ -44,6 +44,7 @@ struct View {
     const uint32_t* __restrict__ nedges;    // active edges per node (collect)
     const float4* __restrict__ cbox;        // box of each group of EDGE_GROUP edges (nullptr: not kept)
     Box cde;
+    float coord_max;   // the largest coordinate magnitude of the CDE box (every hazard lies inside it)
     uint32_t n_items, n_slots, cd_threshold;
     int32_t exterior;
     // hazard poles binned in a uniform grid over the CDE box (overlap proxy)
@@ -170,6 +171,27 @@ __device__ __forceinline__ bool leaf_hits(const View& v, const P& p, const DNode
                 for (uint32_t g = 0; g * EDGE_GROUP < e.edge_cnt; g++) {
                     const float4 c = __ldg(&v.cbox[e.edge_off / EDGE_GROUP + g]);
                     if (fmx(px0, c.x) > fmn(px1, c.z) || fmx(py0, c.y) > fmn(py1, c.w)) continue;
+                    const uint32_t end = min(e.edge_cnt, g * EDGE_GROUP + EDGE_GROUP);
+                    for (uint32_t j = g * EDGE_GROUP; j < end; j++)
+                        if (p_hits_seg(p, ld_edge(v, e.edge_off + j))) {
+                            if (stop) *stop = 1;
+                            return true;
+                        }
+                    if (stop && *stop) return false;
+                }
+                continue;
+            }
+        }
+        if constexpr (std::is_same<P, Disk>::value) {
+            if (JCDE_EDGE_GROUPS && v.cbox) {
+                // a pole skips the groups farther than its radius plus a margin of 2^-14 of the
+                // CDE box's coordinate magnitude, far above the rounding of the distance test
+                // (circle.rs:506-510 with edge.rs:63-87), so no skipped edge could count as hit
+                const float reach = p.r + v.coord_max * 0x1p-14f;
+                for (uint32_t g = 0; g * EDGE_GROUP < e.edge_cnt; g++) {
+                    const float4 c = __ldg(&v.cbox[e.edge_off / EDGE_GROUP + g]);
+                    if (c.x - p.c.x > reach || p.c.x - c.z > reach || c.y - p.c.y > reach || p.c.y - c.w > reach)
+                        continue;
                     const uint32_t end = min(e.edge_cnt, g * EDGE_GROUP + EDGE_GROUP);
                     for (uint32_t j = g * EDGE_GROUP; j < end; j++)
                         if (p_hits_seg(p, ld_edge(v, e.edge_off + j))) {
