@@ -255,6 +255,19 @@ __device__ __forceinline__ bool seg_group_hits(const View& v, const P& p, const 
             return false;
         }
     }
+    if constexpr (std::is_same<P, Disk>::value) {
+        if (JCDE_EDGE_GROUPS && v.cbox) {   // the margin of leaf_hits
+            const float reach = p.r + v.coord_max * 0x1p-14f;
+            for (uint32_t g = 0; g * EDGE_GROUP < e.edge_cnt; g++) {
+                const float4 c = __ldg(&v.cbox[e.edge_off / EDGE_GROUP + g]);
+                if (c.x - p.c.x > reach || p.c.x - c.z > reach || c.y - p.c.y > reach || p.c.y - c.w > reach) continue;
+                const uint32_t end = min(e.edge_cnt, g * EDGE_GROUP + EDGE_GROUP);
+                for (uint32_t j = g * EDGE_GROUP; j < end; j++)
+                    if (p_hits_seg(p, ld_edge(v, e.edge_off + j))) return true;
+            }
+            return false;
+        }
+    }
     for (uint32_t j = 0; j < e.edge_cnt; j++)
         if (p_hits_seg(p, ld_edge(v, e.edge_off + j))) return true;
     return false;
