@@ -567,6 +567,34 @@ def run_proxy(args):
             succ += int(s_.item())
         res[name] = {"placements_per_s": succ / (ms / 1e3), "verified_free": succ // args.steps,
                      "ms_per_step": ms / args.steps, "candidates": n}
+    # the other settings of both methods (one timed run each): descent lengths and copies per candidate
+    def once(fn):
+        fn()
+        torch.cuda.synchronize()
+        a_ev, b_ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        flush.zero_()
+        a_ev.record()
+        s_ = fn()
+        b_ev.record()
+        torch.cuda.synchronize()
+        return int(s_.item()) / (a_ev.elapsed_time(b_ev) / 1e3)
+
+    sweep = {}
+    for steps in (5, 10, 20):
+        def gd_s(steps=steps):
+            q, _ = eng.separate_batch(P0.clone(), I0, steps=steps, step_t=0.25, step_th=0.25, clearance=CLEARANCE,
+                                      filter=filt)
+            return (eng.detect_batch(q, filter=filt) == 0).sum()
+        sweep[f"gradient_{steps}_steps"] = once(gd_s)
+    for kk in (1, 2, 5, 10, 20):
+        out_kk = torch.empty(n * kk, dtype=torch.uint8, device="cuda")
+        def rnd_k(kk=kk, out_kk=out_kk):
+            q = eng.resample_batch(P0, I0, k=kk, sigma_t=mean_r, sigma_th=0.25, seed=7)
+            eng.detect_batch(q, filter=filt, out=out_kk)
+            return (out_kk.view(n, kk) == 0).any(dim=1).sum()
+        sweep[f"random_{kk}_copies"] = once(rnd_k)
+    best_g = max(v for k, v in sweep.items() if k.startswith("gradient"))
+    best_r = max(v for k, v in sweep.items() if k.startswith("random"))
     # gradient accuracy on a sample against the FP64 oracle (test infrastructure, CPU leg)
     from oracle import oracle as O
 
@@ -591,6 +619,8 @@ def run_proxy(args):
                    "l2": "flushed between steps (256 MB write)"},
         "gradient": res["gradient"], "random": res["random"],
         "speedup_vs_random": res["gradient"]["placements_per_s"] / res["random"]["placements_per_s"],
+        "settings_sweep_placements_per_s": sweep,
+        "best_setting_speedup": best_g / best_r,
         "grad_rel_err_vs_fp64": {"median": float(np.median(rel)), "p99": float(np.percentile(rel, 99)),
                                  "max": float(rel.max()), "samples": int(on.sum())},
         "impl": "jcde",

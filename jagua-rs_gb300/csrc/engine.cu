@@ -102,9 +102,11 @@ struct jcde_engine {
     DevBuf d_next;            // work counters of the two passes (a pair per pipeline slot)
     // hazard poles binned in a uniform grid (overlap proxy)
     uint64_t pole_version = ~0ull;
-    DevBuf d_hpoles, d_hpstart;
+    DevBuf d_hpoles, d_hpstart, d_hpoles_c, d_hpstart_c;
     float hp_x0 = 0, hp_y0 = 0, hp_inv_cs = 0, hp_rmax = 0;
     int32_t hp_g = 1;
+    float hp_inv_cs_c = 0;   // the coarse grid (cells 8x the pole-sized ones)
+    int32_t hp_g_c = 1;
     uint32_t n_hpoles = 0;
     cudaStream_t last_stream = nullptr;
     bool have_last_stream = false;
@@ -228,32 +230,47 @@ static jcde_status sync_device(jcde_engine* e) {
             typical = diam[diam.size() * 3 / 4];
         }
         const float cs = fmaxf(fmaxf(typical, ext / 1024.0f), 1e-6f);
-        const int32_t g = std::max<int32_t>(1, std::min<int32_t>(1024, (int32_t)ceilf(ext / cs)));
-        const float inv = (float)g / fmaxf(ext, 1e-6f);
-        auto cix = [&](float x, float o) { return std::max(0, std::min(g - 1, (int)floorf((x - o) * inv))); };
-        std::vector<uint32_t> start((size_t)g * g + 1, 0u);
-        auto for_cells = [&](const Disk& d, auto&& fn) {
-            const int x0 = cix(d.c.x - d.r, b.x0), x1 = cix(d.c.x + d.r, b.x0);
-            const int y0 = cix(d.c.y - d.r, b.y0), y1 = cix(d.c.y + d.r, b.y0);
-            for (int iy = y0; iy <= y1; iy++)
-                for (int ix = x0; ix <= x1; ix++) fn((uint32_t)iy * (uint32_t)g + (uint32_t)ix);
+        // a grid of cells of size `csz`: cell ranges and the poles binned into every cell they overlap
+        auto build = [&](float csz, std::vector<uint32_t>& start, std::vector<float4>& hp, int32_t& g, float& inv) {
+            g = std::max<int32_t>(1, std::min<int32_t>(1024, (int32_t)ceilf(ext / csz)));
+            inv = (float)g / fmaxf(ext, 1e-6f);
+            const int32_t gg = g;
+            const float iv = inv;
+            auto cix = [&](float x, float o) { return std::max(0, std::min(gg - 1, (int)floorf((x - o) * iv))); };
+            start.assign((size_t)g * g + 1, 0u);
+            auto for_cells = [&](const Disk& d, auto&& fn) {
+                const int x0 = cix(d.c.x - d.r, b.x0), x1 = cix(d.c.x + d.r, b.x0);
+                const int y0 = cix(d.c.y - d.r, b.y0), y1 = cix(d.c.y + d.r, b.y0);
+                for (int iy = y0; iy <= y1; iy++)
+                    for (int ix = x0; ix <= x1; ix++) fn((uint32_t)iy * (uint32_t)gg + (uint32_t)ix);
+            };
+            for (const HazardRec& h : hs)
+                if (h.alive)
+                    for (const Disk& d : h.poles) for_cells(d, [&](uint32_t c) { start[c + 1]++; });
+            for (size_t c = 1; c < start.size(); c++) start[c] += start[c - 1];
+            hp.assign(std::max<uint32_t>(start.back(), 1), make_float4(0.f, 0.f, 0.f, 0.f));
+            std::vector<uint32_t> fill(start.begin(), start.end() - 1);
+            for (uint32_t k = 0; k < hs.size(); k++)
+                if (hs[k].alive)
+                    for (const Disk& d : hs[k].poles) {
+                        float kf;
+                        std::memcpy(&kf, &k, 4);
+                        for_cells(d, [&](uint32_t c) { hp[fill[c]++] = make_float4(d.c.x, d.c.y, d.r, kf); });
+                    }
         };
-        for (const HazardRec& h : hs)
-            if (h.alive)
-                for (const Disk& d : h.poles) for_cells(d, [&](uint32_t c) { start[c + 1]++; });
-        for (size_t c = 1; c < start.size(); c++) start[c] += start[c - 1];
-        std::vector<float4> hp(std::max<uint32_t>(start.back(), 1));
-        std::vector<uint32_t> fill(start.begin(), start.end() - 1);
-        for (uint32_t k = 0; k < hs.size(); k++)
-            if (hs[k].alive)
-                for (const Disk& d : hs[k].poles) {
-                    float kf;
-                    std::memcpy(&kf, &k, 4);
-                    for_cells(d, [&](uint32_t c) { hp[fill[c]++] = make_float4(d.c.x, d.c.y, d.r, kf); });
-                }
+        std::vector<uint32_t> start, start_c;
+        std::vector<float4> hp, hp_c;
+        int32_t g = 1, g_c = 1;
+        float inv = 0.f, inv_c = 0.f;
+        build(cs, start, hp, g, inv);          // pole-sized cells: pair lookups (k_proxy)
+        build(8.0f * cs, start_c, hp_c, g_c, inv_c);   // coarse cells: a candidate's neighbourhood (k_separate)
         jcde_status st;
         if ((st = upload(e->d_hpoles, hp.data(), hp.size() * sizeof(float4)))) return st;
         if ((st = upload(e->d_hpstart, start.data(), start.size() * 4))) return st;
+        if ((st = upload(e->d_hpoles_c, hp_c.data(), hp_c.size() * sizeof(float4)))) return st;
+        if ((st = upload(e->d_hpstart_c, start_c.data(), start_c.size() * 4))) return st;
+        e->hp_inv_cs_c = inv_c;
+        e->hp_g_c = g_c;
         e->hp_x0 = b.x0;
         e->hp_y0 = b.y0;
         e->hp_inv_cs = inv;
@@ -301,6 +318,10 @@ static View base_view(const jcde_engine* e) {
     v.hp_inv_cs = e->hp_inv_cs;
     v.hp_rmax = e->hp_rmax;
     v.hp_g = e->hp_g;
+    v.hpoles_c = e->d_hpoles_c.as<float4>();
+    v.hp_start_c = e->d_hpstart_c.as<uint32_t>();
+    v.hp_inv_cs_c = e->hp_inv_cs_c;
+    v.hp_g_c = e->hp_g_c;
     return v;
 }
 

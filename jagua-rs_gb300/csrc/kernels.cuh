@@ -52,6 +52,10 @@ struct View {
     const uint32_t* __restrict__ hp_start;  // cell c holds hpoles[hp_start[c], hp_start[c+1])
     float hp_x0, hp_y0, hp_inv_cs, hp_rmax;
     int32_t hp_g;
+    const float4* __restrict__ hpoles_c;      // the same poles binned in a coarse grid (cells 8x larger)
+    const uint32_t* __restrict__ hp_start_c;
+    float hp_inv_cs_c;
+    int32_t hp_g_c;
 };
 
 // A raw (already transformed) query shape for the single-polygon entry points.
@@ -1378,48 +1382,40 @@ __global__ void __launch_bounds__(PROXY_WARPS * 32) k_proxy(View v, const float*
 constexpr uint32_t SEP_LOCAL = 96;   // hazard poles kept per candidate for its descent
 
 // The hazard poles a candidate at (cx, cy) can meet while it moves less than `margin`: every
-// pole box overlapping the square of half-size `reach` around it, gathered once from the grid (a
-// pole is taken from the cell holding the low corner of its box's overlap with the square).
+// pole box overlapping the square of half-size `reach` around it, gathered once from the coarse
+// grid (a pole is taken from the cell holding the low corner of its box's overlap with the square).
 // Radii are stored grown by `clear`.  Returns the count, or SEP_LOCAL + 1 when they do not fit.
 __device__ __forceinline__ uint32_t gather_poles(const View& v, float cx, float cy, float reach, float clear,
                                                  float4* list, int lane, int nsub, uint32_t mask) {
-    const int g = v.hp_g;
+    const int g = v.hp_g_c;
     const float gx0 = cx - reach, gy0 = cy - reach, gx1 = cx + reach, gy1 = cy + reach;
-    const int ix0 = pole_cell(gx0, v.hp_x0, v.hp_inv_cs, g), ix1 = pole_cell(gx1, v.hp_x0, v.hp_inv_cs, g);
-    const int iy0 = pole_cell(gy0, v.hp_y0, v.hp_inv_cs, g), iy1 = pole_cell(gy1, v.hp_y0, v.hp_inv_cs, g);
-    const int nx = ix1 - ix0 + 1, ncell = nx * (iy1 - iy0 + 1);
+    const int ix0 = pole_cell(gx0, v.hp_x0, v.hp_inv_cs_c, g), ix1 = pole_cell(gx1, v.hp_x0, v.hp_inv_cs_c, g);
+    const int iy0 = pole_cell(gy0, v.hp_y0, v.hp_inv_cs_c, g), iy1 = pole_cell(gy1, v.hp_y0, v.hp_inv_cs_c, g);
+    const uint32_t below = mask & ((1u << (threadIdx.x & 31)) - 1u);
     uint32_t cnt = 0;
-    for (int base = 0; base < ncell; base += nsub) {
-        const int ci = base + lane;
-        uint32_t a = 0, b = 0;
-        int ix = 0, iy = 0;
-        if (ci < ncell) {
-            ix = ix0 + ci % nx;
-            iy = iy0 + ci / nx;
+    for (int iy = iy0; iy <= iy1; iy++)
+        for (int ix = ix0; ix <= ix1; ix++) {   // the coarse cells of the square, lanes over each cell's poles
             const uint32_t cell = (uint32_t)iy * (uint32_t)g + (uint32_t)ix;
-            a = __ldg(&v.hp_start[cell]);
-            b = __ldg(&v.hp_start[cell + 1]);
-        }
-        for (uint32_t j = a;; j++) {   // lanes walk their own cells; appends are ballot-compacted
-            const bool live = j < b;
-            bool take = false;
-            float4 h = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (live) {
-                h = __ldg(&v.hpoles[j]);
-                const float mx = fmaxf(gx0, h.x - h.z), my = fmaxf(gy0, h.y - h.z);
-                take = mx <= fminf(gx1, h.x + h.z) && my <= fminf(gy1, h.y + h.z) &&
-                       pole_cell(mx, v.hp_x0, v.hp_inv_cs, g) == ix && pole_cell(my, v.hp_y0, v.hp_inv_cs, g) == iy &&
-                       !filtered(v, __float_as_uint(h.w));
+            const uint32_t a = __ldg(&v.hp_start_c[cell]), b = __ldg(&v.hp_start_c[cell + 1]);
+            for (uint32_t j0 = a; j0 < b; j0 += nsub) {
+                const uint32_t j = j0 + lane;
+                bool take = false;
+                float4 h = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (j < b) {
+                    h = __ldg(&v.hpoles_c[j]);
+                    const float mx = fmaxf(gx0, h.x - h.z), my = fmaxf(gy0, h.y - h.z);
+                    take = mx <= fminf(gx1, h.x + h.z) && my <= fminf(gy1, h.y + h.z) &&
+                           pole_cell(mx, v.hp_x0, v.hp_inv_cs_c, g) == ix && pole_cell(my, v.hp_y0, v.hp_inv_cs_c, g) == iy &&
+                           !filtered(v, __float_as_uint(h.w));
+                }
+                const uint32_t bal = __ballot_sync(mask, take);
+                if (take) {
+                    const uint32_t pos = cnt + __popc(bal & below);
+                    if (pos < SEP_LOCAL) list[pos] = make_float4(h.x, h.y, h.z + clear, 0.0f);
+                }
+                cnt += __popc(bal & mask);
             }
-            const uint32_t bal = __ballot_sync(mask, take);
-            if (take) {
-                const uint32_t pos = cnt + __popc(bal & mask & ((1u << (threadIdx.x & 31)) - 1u));
-                if (pos < SEP_LOCAL) list[pos] = make_float4(h.x, h.y, h.z + clear, 0.0f);
-            }
-            cnt += __popc(bal & mask);
-            if (!__any_sync(mask, live)) break;
         }
-    }
     __syncwarp(mask);
     return cnt <= SEP_LOCAL ? cnt : SEP_LOCAL + 1;
 }
