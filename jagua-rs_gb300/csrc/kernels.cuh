@@ -1385,8 +1385,8 @@ constexpr uint32_t SEP_LOCAL = 96;   // hazard poles kept per candidate for its 
 // pole box overlapping the square of half-size `reach` around it, gathered once from the coarse
 // grid (a pole is taken from the cell holding the low corner of its box's overlap with the square).
 // Radii are stored grown by `clear`.  Returns the count, or SEP_LOCAL + 1 when they do not fit.
-__device__ __forceinline__ uint32_t gather_poles(const View& v, float cx, float cy, float reach, float clear,
-                                                 float4* list, int lane, int nsub, uint32_t mask) {
+__device__ __forceinline__ uint32_t gather_poles(const View& v, float cx, float cy, float reach, float rdisk,
+                                                 float clear, float4* list, int lane, int nsub, uint32_t mask) {
     const int g = v.hp_g_c;
     const float gx0 = cx - reach, gy0 = cy - reach, gx1 = cx + reach, gy1 = cy + reach;
     const int ix0 = pole_cell(gx0, v.hp_x0, v.hp_inv_cs_c, g), ix1 = pole_cell(gx1, v.hp_x0, v.hp_inv_cs_c, g);
@@ -1404,9 +1404,10 @@ __device__ __forceinline__ uint32_t gather_poles(const View& v, float cx, float 
                 if (j < b) {
                     h = __ldg(&v.hpoles_c[j]);
                     const float mx = fmaxf(gx0, h.x - h.z), my = fmaxf(gy0, h.y - h.z);
+                    const float dx = h.x - cx, dy = h.y - cy, rr = rdisk + h.z;
                     take = mx <= fminf(gx1, h.x + h.z) && my <= fminf(gy1, h.y + h.z) &&
                            pole_cell(mx, v.hp_x0, v.hp_inv_cs_c, g) == ix && pole_cell(my, v.hp_y0, v.hp_inv_cs_c, g) == iy &&
-                           !filtered(v, __float_as_uint(h.w));
+                           dx * dx + dy * dy <= rr * rr && !filtered(v, __float_as_uint(h.w));
                 }
                 const uint32_t bal = __ballot_sync(mask, take);
                 if (take) {
@@ -1481,13 +1482,16 @@ __global__ void __launch_bounds__(PROXY_WARPS * 32) k_separate(View v, float* __
             const float kth = step_th / fmaxf(it.pole_r2max, 1.0f);
             const float margin = JCDE_SEP_MARGIN * it.pole_bound;   // motion allowed before gathering again
             const float reach = it.pole_bound + clear + margin;
+            // a hazard pole can meet an item pole only within pole_bound + clear of the item's
+            // origin, and the origin moves at most margin * sqrt(2) before the list is gathered again
+            const float rdisk = it.pole_bound + clear + 1.4143f * margin;
             float ox = tx, oy = ty;
-            uint32_t m = gather_poles(v, ox, oy, reach, clear, list, hl, L, mask);
+            uint32_t m = gather_poles(v, ox, oy, reach, rdisk, clear, list, hl, L, mask);
             auto eval = [&](float c, float s, float x, float y) -> ProxyOut {
                 if (fabsf(x - ox) > margin || fabsf(y - oy) > margin) {
                     ox = x;
                     oy = y;
-                    m = gather_poles(v, ox, oy, reach, clear, list, hl, L, mask);
+                    m = gather_poles(v, ox, oy, reach, rdisk, clear, list, hl, L, mask);
                 }
                 return m <= SEP_LOCAL ? proxy_local(v, it, c, s, x, y, list, m, hl, L, mask)
                                       : proxy_eval(v, it, c, s, x, y, hl, L, mask, clear);
