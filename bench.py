@@ -629,6 +629,116 @@ def run_proxy(args):
     return 0
 
 
+def run_prep(args):
+    """Item preparation: the poi and surrogate poles (lbf's default limits) of 1024 star item shapes
+    of 8-200 vertices, radius 20-60.  One step = the two pole-search launches over the whole batch
+    (shapes, areas and poi resident on the device).  e2e = jcde.prep.import_items from host arrays
+    (host orientation / area / centring, copies, both launches, poles read back).  CPU baseline: the
+    oracle's Importer::import_item restatement on a sample of the shapes, one shape per host thread."""
+    import torch
+
+    import jcde
+    from jcde import prep
+    from jcde import workload as W
+
+    jcde.lib()
+    n_shapes = 1024
+    st = W.Stream(0xC2, 7)
+    raws = []
+    for _ in range(n_shapes):
+        nv = int(st.randint(8, 200, 1)[0])
+        raws.append(W.star_polygon(st, nv, 20.0, 60.0))
+    items = prep.import_items(raws)   # also the untimed first run
+    shp = [prep.spolygon_shape(r)[0] for r in raws]
+    b_raw = prep.ShapeBatch(shp)
+    b_int = prep.ShapeBatch([it.xy for it in items])
+    area = torch.tensor([it.area for it in items], dtype=torch.float32, device="cuda")
+    poi = torch.from_numpy(np.stack([it.poi for it in items])).cuda()
+    cap = 128
+    out = torch.empty((n_shapes, cap, 3), dtype=torch.float32, device="cuda")
+    cnt = torch.empty(n_shapes, dtype=torch.int32, device="cuda")
+    sts = torch.empty(n_shapes, dtype=torch.int32, device="cuda")
+    poi_o = torch.empty((n_shapes, 3), dtype=torch.float32, device="cuda")
+    poi_s = torch.empty(n_shapes, dtype=torch.int32, device="cuda")
+    stream = torch.cuda.Stream()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def step(ev=None):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            if ev:
+                ev[0].record(stream)
+            b_raw.poi(poi_o, poi_s, stream=stream)
+            if ev:
+                ev[1].record(stream)
+            b_int.poles(area, poi, cap=cap, out=out, counts=cnt, status=sts, stream=stream)
+            if ev:
+                ev[2].record(stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    clk = ClockSampler(0)
+    clk.__enter__()
+    t_poi, t_poles = [], []
+    for _ in range(args.steps):
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        step(ev)
+        torch.cuda.synchronize()
+        t_poi.append(ev[0].elapsed_time(ev[1]))
+        t_poles.append(ev[1].elapsed_time(ev[2]))
+    # end to end through the public API from host arrays
+    e2e_ms = []
+    for _ in range(max(1, min(args.steps, 5))):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        got = prep.import_items(raws)
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    clk.__exit__()
+    same = all(np.array_equal(g.poles, it.poles) for g, it in zip(got, items))
+    ok = bool((sts.cpu().numpy() == 0).all() and (poi_s.cpu().numpy() == 0).all())
+    ms = float(np.sum(t_poi) + np.sum(t_poles))
+    value = n_shapes * args.steps / (ms / 1e3)
+    n_poles = [len(it.poles) for it in items]
+    h2d = sum(r.nbytes for r in raws) + 4 * (n_shapes + 1) * 2 + 16 * n_shapes
+    d2h = 12 * n_shapes + n_shapes * cap * 12 + 8 * n_shapes
+    line = {
+        "metric": "item shapes prepared per second (poi + surrogate poles)",
+        "value": value, "unit": "shapes/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"{n_shapes} star item shapes (8-200 vertices, radius 20-60), poi then surrogate "
+                               "poles with lbf's default limits (100, 0), (20, 0.75), (10, 0.9); one step = "
+                               "jcde_poi_batch + jcde_surrogate_poles_batch over the batch",
+                   "l2": "flushed before each step (256 MB write)"},
+        "ms_poi": float(np.median(t_poi)), "ms_poles": float(np.median(t_poles)),
+        "poles_per_shape": {"mean": float(np.mean(n_poles)), "min": int(min(n_poles)), "max": int(max(n_poles))},
+        "all_status_ok": ok, "gpu_launches": 2 * args.steps,
+        "e2e": {"value": n_shapes / (np.median(e2e_ms) / 1e3), "unit": "shapes/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "ms_per_batch": float(np.median(e2e_ms)),
+                "same_poles_as_device_step": bool(same)},
+        "clocks": clk.summary(),
+        "impl": "jcde",
+    }
+    if not args.no_cpu:
+        from concurrent.futures import ThreadPoolExecutor
+
+        from oracle import oracle as O
+
+        O.build()
+        n_s = min(n_shapes, 4 * host_cores())
+        t0 = time.perf_counter()
+        with ThreadPoolExecutor(host_cores()) as ex:   # ctypes calls release the GIL
+            ref = list(ex.map(lambda r: W.import_item(O.OracleBackend, r), raws[:n_s]))
+        cpu_s = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": n_s / cpu_s, "unit": "shapes/s", "cores": host_cores(), "kind": "port",
+                                "sample": f"first {n_s} of {n_shapes} shapes, oracle import_item, one shape per thread",
+                                "same_poles": bool(all(np.array_equal(a.poles, b.poles)
+                                                       for a, b in zip(ref, items[:n_s])))}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_lbf(args):
     """The LBF-style strip build on the device-resident engine.  2000 steps, each: 16384
     candidates generated, judged (surrogate + polygon passes), the least-cost free one registered on
@@ -778,10 +888,11 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--autotune", type=int, default=1, help="1: jcde_autotune on the batch before timing")
     ap.add_argument("--lbf-cpu-steps", type=int, default=2000)
-    ap.add_argument("--workload", default="star", choices=["star", "multi", "proxy", "lbf"],
+    ap.add_argument("--workload", default="star", choices=["star", "multi", "proxy", "lbf", "prep"],
                     help="star: the headline single-layout batch; multi: 64 layouts in one launch sequence; "
                          "proxy: gradient separation of colliding candidates vs random resampling; "
-                         "lbf: LBF-style build on the device-resident engine")
+                         "lbf: LBF-style build on the device-resident engine; "
+                         "prep: poi + surrogate poles of 1024 item shapes on the device")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -791,6 +902,8 @@ def main():
         return run_proxy(args)
     if args.workload == "lbf":
         return run_lbf(args)
+    if args.workload == "prep":
+        return run_prep(args)
     return run_gpu(args)
 
 

@@ -356,12 +356,45 @@ void jcde_snapshot_free(jcde_snapshot* s);
 
 /* --- shape preparation (host): SPolygon::new (simple_polygon.rs:41-71) and surrogate poles
  *     (fail_fast/pole.rs:12-47) — what Item::new / Container::new compute once per shape ------ */
-/* xy_out: n_vertices (x, y) in internal counter-clockwise order; bbox_out[4]; area_diam[2]; poi[3] */
+/* xy_out: n_vertices (x, y) in internal counter-clockwise order; bbox_out[4]; area_diam[2]; poi[3]
+ * (poi NULL: the poi is not computed, e.g. when jcde_poi_batch computes it on the device) */
 jcde_status jcde_spolygon_new(const float* xy, uint32_t n_vertices, float* xy_out, float* bbox_out,
                               float* area_diam, float* poi);
+/* jcde_spolygon_new without the poi for n shapes at once (host buffers): xy holds the shapes' (x, y)
+ * vertices back to back, voff[n + 1] the offsets; xy_out the same layout in internal order, bbox_out
+ * 4 per shape, area_diam 2 per shape, status[i] 0 or JCDE_ERR_ARG for an invalid polygon.  Shapes
+ * are spread over n_threads host threads (0: one per hardware thread). */
+jcde_status jcde_spolygon_batch(const float* xy, const uint32_t* voff, uint32_t n, float* xy_out, float* bbox_out,
+                                float* area_diam, int32_t* status, uint32_t n_threads);
 /* poles of an internal shape with the given area and poi; *n_out receives the count (even when > cap) */
 jcde_status jcde_surrogate_poles(const float* xy, uint32_t n_vertices, float area, const float poi[3],
                                  const jcde_config* cfg, float* poles_xyr, uint32_t cap, uint32_t* n_out);
+
+/* --- shape preparation on the device, many shapes per call (no counterpart in the reference: the
+ *     reference runs compute_pole, fail_fast/pole.rs:52-77, once per shape on the host).  The same
+ *     poles as jcde_spolygon_new / jcde_surrogate_poles, bit for bit.  Device buffers, stream
+ *     ordered: d_xy holds every shape's (x, y) vertices back to back (the internal counter-clockwise
+ *     order), d_voff[n_shapes + 1] the vertex offsets, max_vertices bounds every shape's count.
+ *     d_status[i] is written per shape: 0 ok, 1 invalid shape (fewer than 3 or more than
+ *     max_vertices vertices), 2 no pole found, 3 a thousand poles reached (pole.rs:42-45), 4 a level of
+ *     the cell tree wider than the device lists hold, 5 more poles than `cap`.  d_order (may be NULL: batch
+ *     order) is a permutation of the shapes giving the order CTAs take them in; larger shapes first
+ *     (e.g. by descending vertex count) shortens the tail of a batch.  d_workspace may be NULL
+ *     (allocated per call, stream ordered) or hold jcde_poles_workspace_bytes bytes, 256-byte aligned. */
+uint64_t jcde_poles_workspace_bytes(uint32_t n_shapes, uint32_t max_vertices, int with_poles);
+/* the pole of inaccessibility of each shape (SPolygon::calculate_poi, simple_polygon.rs:152-171):
+ * d_poi n_shapes x (x, y, r) */
+jcde_status jcde_poi_batch(const float* d_xy, const uint32_t* d_voff, uint32_t n_shapes, uint32_t max_vertices,
+                           float* d_poi, int32_t* d_status, const uint32_t* d_order, void* d_workspace,
+                           uint64_t workspace_bytes, void* stream);
+/* generate_surrogate_poles (pole.rs:12-47) of each shape with its area (d_area) and poi (d_poi, 3 per
+ * shape) under cfg's pole limits: d_poles n_shapes x cap x (x, y, r), pole 0 = the poi; d_n_out the
+ * count per shape */
+jcde_status jcde_surrogate_poles_batch(const float* d_xy, const uint32_t* d_voff, uint32_t n_shapes,
+                                       uint32_t max_vertices, const float* d_area, const float* d_poi,
+                                       const jcde_config* cfg, float* d_poles, uint32_t cap, uint32_t* d_n_out,
+                                       int32_t* d_status, const uint32_t* d_order, void* d_workspace,
+                                       uint64_t workspace_bytes, void* stream);
 
 /* --- introspection (tests, tooling) ----------------------------------------------------------- */
 /* canonical dump of the quadtree (pre-order, hazards by key, edges sorted); *n_words always set */

@@ -9,6 +9,8 @@
 #include <list>
 #include <mutex>
 #include <string>
+#include <thread>
+#include <atomic>
 #include <vector>
 
 #include "../../include/jcde.h"
@@ -867,11 +869,11 @@ jcde_status jcde_restore(jcde_engine* e, const jcde_snapshot* s) {
 void jcde_snapshot_free(jcde_snapshot* s) { delete s; }
 
 jcde_status jcde_spolygon_new(const float* xy, uint32_t nv, float* xy_out, float* bbox_out, float* area_diam, float* poi) {
-    if (!xy || !xy_out || !bbox_out || !area_diam || !poi || nv < 3) return JCDE_ERR_ARG;
+    if (!xy || !xy_out || !bbox_out || !area_diam || nv < 3) return JCDE_ERR_ARG;
     std::vector<Pt> pts(nv);
     for (uint32_t i = 0; i < nv; i++) pts[i] = Pt{xy[2 * i], xy[2 * i + 1]};
     PreparedPolygon p;
-    if (spolygon_new(std::move(pts), &p)) return JCDE_ERR_ARG;
+    if (spolygon_new(std::move(pts), &p, poi != nullptr)) return JCDE_ERR_ARG;
     for (uint32_t i = 0; i < nv; i++) {
         xy_out[2 * i] = p.v[i].x;
         xy_out[2 * i + 1] = p.v[i].y;
@@ -879,7 +881,30 @@ jcde_status jcde_spolygon_new(const float* xy, uint32_t nv, float* xy_out, float
     bbox_out[0] = p.bbox.x0; bbox_out[1] = p.bbox.y0; bbox_out[2] = p.bbox.x1; bbox_out[3] = p.bbox.y1;
     area_diam[0] = p.area;
     area_diam[1] = p.diameter;
-    poi[0] = p.poi.c.x; poi[1] = p.poi.c.y; poi[2] = p.poi.r;
+    if (poi) {
+        poi[0] = p.poi.c.x; poi[1] = p.poi.c.y; poi[2] = p.poi.r;
+    }
+    return JCDE_OK;
+}
+
+jcde_status jcde_spolygon_batch(const float* xy, const uint32_t* voff, uint32_t n, float* xy_out, float* bbox_out,
+                                float* area_diam, int32_t* status, uint32_t n_threads) {
+    if (n && (!xy || !voff || !xy_out || !bbox_out || !area_diam || !status)) return JCDE_ERR_ARG;
+    if (n_threads == 0) n_threads = std::max(1u, std::thread::hardware_concurrency());
+    n_threads = std::min<uint32_t>(n_threads, std::max<uint32_t>(1u, n / 8));
+    std::atomic<uint32_t> next{0};
+    auto work = [&]() {
+        for (uint32_t i; (i = next.fetch_add(1)) < n;) {
+            const uint32_t v0 = voff[i], nv = voff[i + 1] - voff[i];
+            status[i] = nv < 3 ? JCDE_ERR_ARG
+                               : jcde_spolygon_new(xy + 2 * (size_t)v0, nv, xy_out + 2 * (size_t)v0, bbox_out + 4 * (size_t)i,
+                                                   area_diam + 2 * (size_t)i, nullptr);
+        }
+    };
+    std::vector<std::thread> pool;
+    for (uint32_t t = 1; t < n_threads; t++) pool.emplace_back(work);
+    work();
+    for (auto& t : pool) t.join();
     return JCDE_OK;
 }
 

@@ -109,7 +109,7 @@ static bool compute_pole(const Polygon& poly, const std::vector<Disk>& poles, Di
     return have;
 }
 
-int spolygon_new(std::vector<Pt> pts, PreparedPolygon* out) {
+int spolygon_new(std::vector<Pt> pts, PreparedPolygon* out, bool with_poi) {
     if (pts.size() < 3) return -1;
     for (size_t i = 0; i < pts.size(); i++)
         for (size_t j = i + 1; j < pts.size(); j++)
@@ -125,8 +125,8 @@ int spolygon_new(std::vector<Pt> pts, PreparedPolygon* out) {
     Polygon p;
     p.v = pts;
     p.bbox = bounding_box(pts.data(), pts.size());
-    Disk poi;
-    if (!compute_pole(p, {}, &poi)) return -1;   // calculate_poi (simple_polygon.rs:152-171)
+    Disk poi{Pt{0.0f, 0.0f}, 0.0f};
+    if (with_poi && !compute_pole(p, {}, &poi)) return -1;   // calculate_poi (simple_polygon.rs:152-171)
     out->v = std::move(pts);
     out->bbox = p.bbox;
     out->poi = poi;

@@ -21,8 +21,9 @@ struct PoleLimit {
 };
 
 float polygon_area(const Pt* v, size_t n);
-// SPolygon::new (simple_polygon.rs:41-71): 0 on success, -1 for an invalid polygon
-int spolygon_new(std::vector<Pt> pts, PreparedPolygon* out);
+// SPolygon::new (simple_polygon.rs:41-71): 0 on success, -1 for an invalid polygon; without
+// `with_poi` the poi is left zero (computed elsewhere, e.g. by the device batch)
+int spolygon_new(std::vector<Pt> pts, PreparedPolygon* out, bool with_poi = true);
 // generate_surrogate_poles (pole.rs:12-47) of an internal shape with the given area and poi
 int surrogate_poles(const std::vector<Pt>& v, float area, Disk poi, const PoleLimit* lim, int n_lim,
                     std::vector<Disk>* poles);

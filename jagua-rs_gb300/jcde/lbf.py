@@ -125,15 +125,21 @@ def _select_host_scalar(items, q: np.ndarray, verdicts: np.ndarray) -> int:
     return best
 
 
+def raw_shapes(spec: LbfSpec) -> list:
+    """The item types' star shapes as drawn (before import): stream (seed, 1)."""
+    st = W.Stream(spec.seed, 1)
+    out = []
+    for _ in range(spec.n_types):
+        nv = int(st.randint(spec.v_range[0], spec.v_range[1], 1)[0])
+        out.append(W.star_polygon(st, nv, *spec.r_range))
+    return out
+
+
 def setup(backend, spec: LbfSpec, item_pool=None):
     """Items, the strip container (an Exterior hazard) and a fresh engine: (layout, engine)."""
-    st = W.Stream(spec.seed, 1)
     items = item_pool
     if items is None:
-        items = []
-        for _ in range(spec.n_types):
-            nv = int(st.randint(spec.v_range[0], spec.v_range[1], 1)[0])
-            items.append(W.import_item(backend, W.star_polygon(st, nv, *spec.r_range)))
+        items = [W.import_item(backend, xy) for xy in raw_shapes(spec)]
     outer = W.import_static(backend, W.rect_polygon(0.0, 0.0, spec.width, spec.height), W.EXTERIOR)
     lay = W.Layout("lbf-strip", spec.depth, spec.cd_threshold, W.inflate_to_square(W.bbox_of(outer.xy)), items=items)
     lay.hazards.append(outer)

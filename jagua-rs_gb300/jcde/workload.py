@@ -145,6 +145,36 @@ def centroid_f32(xy: np.ndarray, area) -> tuple:
     return np.float32(cx / six_a), np.float32(cy / six_a)
 
 
+def centroids_f32(shapes, areas) -> np.ndarray:
+    """centroid_f32 of many shapes at once: the same sequential float32 accumulation per shape,
+    vectorised across shapes (vertex i of every shape per numpy step).  Returns (n, 2) float32."""
+    n = len(shapes)
+    nv = np.array([len(s) for s in shapes], dtype=np.int64)
+    m = int(nv.max()) if n else 0
+    X = np.zeros((n, m + 1), np.float32)
+    Y = np.zeros((n, m + 1), np.float32)
+    for k, s in enumerate(shapes):
+        s = np.asarray(s, dtype=np.float32)
+        X[k, : len(s)] = s[:, 0]
+        Y[k, : len(s)] = s[:, 1]
+        X[k, len(s)] = s[0, 0]   # the closing edge (i = n-1, j = 0)
+        Y[k, len(s)] = s[0, 1]
+    cx = np.zeros(n, np.float32)
+    cy = np.zeros(n, np.float32)
+    for i in range(m):
+        live = i < nv
+        xi, yi, xj, yj = X[:, i], Y[:, i], X[:, i + 1], Y[:, i + 1]
+        # a shape's last vertex pairs with its first
+        last = i == nv - 1
+        xj = np.where(last, X[:, 0], xj)
+        yj = np.where(last, Y[:, 0], yj)
+        cr = xi * yj - xj * yi
+        cx = np.where(live, (cx + (xi + xj) * cr).astype(np.float32), cx)
+        cy = np.where(live, (cy + (yi + yj) * cr).astype(np.float32), cy)
+    six_a = np.float32(6.0) * np.asarray(areas, dtype=np.float32)
+    return np.stack([cx / six_a, cy / six_a], axis=1).astype(np.float32)
+
+
 def star_polygon(st: Stream, nv: int, r_lo: float, r_hi: float, center=(0.0, 0.0)) -> np.ndarray:
     """Star-shaped simple polygon: sorted uniform angles, radii R*U[0.6, 1.0], R ~ U[r_lo, r_hi]."""
     R = r_lo + st.f64(1)[0] * (r_hi - r_lo)
