@@ -634,7 +634,8 @@ def run_prep(args):
     of 8-200 vertices, radius 20-60.  One step = the two pole-search launches over the whole batch
     (shapes, areas and poi resident on the device).  e2e = jcde.prep.import_items from host arrays
     (host orientation / area / centring, copies, both launches, poles read back).  CPU baseline: the
-    oracle's Importer::import_item restatement on a sample of the shapes, one shape per host thread."""
+    oracle's Importer::import_item restatement on a sample of the shapes, one shape per host thread.
+    A second leg imports with lbf's default simplification (tolerance 0.001, shape_modification.rs)."""
     import torch
 
     import jcde
@@ -642,7 +643,7 @@ def run_prep(args):
     from jcde import workload as W
 
     jcde.lib()
-    n_shapes = 1024
+    n_shapes = args.prep_shapes
     st = W.Stream(0xC2, 7)
     raws = []
     for _ in range(n_shapes):
@@ -694,6 +695,26 @@ def run_prep(args):
         t0 = time.perf_counter()
         got = prep.import_items(raws)
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    # lbf's default import simplifies each item (tolerance 0.001) before its poi and poles: the
+    # simplification pass alone on the device, and the whole import with it end to end
+    area_o = torch.tensor([it.area for it in items], dtype=torch.float32, device="cuda")
+    t_simp = []
+    for k in range(args.warmup + args.steps):
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            ev[0].record(stream)
+            prep.simplify_device(b_int, area_o, False, 0.001, stream=stream)
+            ev[1].record(stream)
+        torch.cuda.synchronize()
+        if k >= args.warmup:
+            t_simp.append(ev[0].elapsed_time(ev[1]))
+    e2e_simp = []
+    for _ in range(max(1, min(args.steps, 5))):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        got_s = prep.import_items(raws, simplify_tolerance=0.001)
+        e2e_simp.append((time.perf_counter() - t0) * 1e3)
     clk.__exit__()
     same = all(np.array_equal(g.poles, it.poles) for g, it in zip(got, items))
     ok = bool((sts.cpu().numpy() == 0).all() and (poi_s.cpu().numpy() == 0).all())
@@ -717,6 +738,11 @@ def run_prep(args):
         "e2e": {"value": n_shapes / (np.median(e2e_ms) / 1e3), "unit": "shapes/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_batch": float(np.median(e2e_ms)),
                 "same_poles_as_device_step": bool(same)},
+        "with_simplification": {"tolerance": 0.001, "ms_simplify_pass": float(np.median(t_simp)),
+                                "vertices_before": int(sum(len(it.xy) for it in items)),
+                                "vertices_after": int(sum(len(it.xy) for it in got_s)),
+                                "e2e": {"value": n_shapes / (np.median(e2e_simp) / 1e3), "unit": "shapes/s",
+                                        "ms_per_batch": float(np.median(e2e_simp))}},
         "clocks": clk.summary(),
         "impl": "jcde",
     }
@@ -735,6 +761,14 @@ def run_prep(args):
                                 "sample": f"first {n_s} of {n_shapes} shapes, oracle import_item, one shape per thread",
                                 "same_poles": bool(all(np.array_equal(a.poles, b.poles)
                                                        for a, b in zip(ref, items[:n_s])))}
+        t0 = time.perf_counter()
+        with ThreadPoolExecutor(host_cores()) as ex:
+            ref_s = list(ex.map(lambda r: W.import_item(O.OracleBackend, r, simplify_tolerance=0.001), raws[:n_s]))
+        cpu_s2 = time.perf_counter() - t0
+        line["with_simplification"]["cpu_baseline"] = {
+            "value": n_s / cpu_s2, "unit": "shapes/s", "cores": host_cores(), "kind": "port",
+            "same_items": bool(all(np.array_equal(a.poles, b.poles) and np.array_equal(a.xy, b.xy)
+                                   for a, b in zip(ref_s, got_s[:n_s])))}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -888,6 +922,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--autotune", type=int, default=1, help="1: jcde_autotune on the batch before timing")
     ap.add_argument("--lbf-cpu-steps", type=int, default=2000)
+    ap.add_argument("--prep-shapes", type=int, default=1024, help="prep workload: shapes per batch")
     ap.add_argument("--workload", default="star", choices=["star", "multi", "proxy", "lbf", "prep"],
                     help="star: the headline single-layout batch; multi: 64 layouts in one launch sequence; "
                          "proxy: gradient separation of colliding candidates vs random resampling; "

@@ -382,6 +382,15 @@ jcde_status jcde_surrogate_poles(const float* xy, uint32_t n_vertices, float are
  *     (e.g. by descending vertex count) shortens the tail of a batch.  d_workspace may be NULL
  *     (allocated per call, stream ordered) or hold jcde_poles_workspace_bytes bytes, 256-byte aligned. */
 uint64_t jcde_poles_workspace_bytes(uint32_t n_shapes, uint32_t max_vertices, int with_poles);
+/* simplify_shape (geometry/shape_modification.rs:48-144) of each shape up to its final
+ * SPolygon::new: d_area the shape's area, deflate 0 = ShapeModifyMode::Inflate (items), 1 = Deflate
+ * (container outers), tolerance = max_area_change_ratio.  d_xy_out has the layout of d_xy (each
+ * shape's simplified vertices from its own offset on), d_n_out the simplified counts, d_status 0 or
+ * 1 (invalid shape).  Items of lbf's default config are simplified with tolerance 0.001
+ * (lbf/src/config.rs:42) before their poi and poles are computed (original_shape.rs:23-50). */
+jcde_status jcde_simplify_batch(const float* d_xy, const uint32_t* d_voff, uint32_t n_shapes, uint32_t max_vertices,
+                                const float* d_area, int deflate, float tolerance, float* d_xy_out, uint32_t* d_n_out,
+                                int32_t* d_status, void* stream);
 /* the pole of inaccessibility of each shape (SPolygon::calculate_poi, simple_polygon.rs:152-171):
  * d_poi n_shapes x (x, y, r) */
 jcde_status jcde_poi_batch(const float* d_xy, const uint32_t* d_voff, uint32_t n_shapes, uint32_t max_vertices,

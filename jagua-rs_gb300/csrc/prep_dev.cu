@@ -29,8 +29,9 @@
 namespace jcde {
 namespace {
 
-constexpr int PP_THREADS = 512;
-constexpr int PP_WARPS = PP_THREADS / 32;
+// threads of one shape's CTA: 512 (two CTAs per SM) for batches that fill the GPU, 1024 (one per
+// SM, twice the lanes on each level) for batches of at most one shape per SM
+constexpr int PP_THREADS_WIDE = 1024;
 constexpr uint32_t PP_LEVEL_CAP = 16384;   // cells of one level of one compute_pole
 constexpr uint32_t PP_MAX_POLES = 1000;    // generate_surrogate_poles' bound (pole.rs:42-45)
 constexpr int PP_DEPTH = 10;               // MAX_POI_TREE_DEPTH (pole.rs:79)
@@ -58,7 +59,9 @@ struct PoleArgs {
     uint32_t* next;      // shape counter
 };
 
+template <int PP_THREADS>
 struct PoleShared {
+    static constexpr int PP_WARPS = PP_THREADS / 32;
     float d[PP_THREADS];
     float r[PP_THREADS];
     float wmax[PP_WARPS];
@@ -75,7 +78,10 @@ __device__ __forceinline__ Box box_of(const float4& f) { return Box{f.x, f.y, f.
 
 // compute_pole (pole.rs:52-77) over the shape and poles in shared memory; the result lands in
 // sh.best_c / sh.best_r with sh.have, or sh.err is set.  Called by every thread of the CTA.
-__device__ void compute_pole(PoleShared& sh, const float2* v, const float4* poles, float4* lvl_a, float4* lvl_b) {
+template <int PP_THREADS>
+__device__ void compute_pole(PoleShared<PP_THREADS>& sh, const float2* v, const float4* poles, float4* lvl_a,
+                             float4* lvl_b) {
+    constexpr int PP_WARPS = PP_THREADS / 32;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint32_t below = (1u << lane) - 1u;
     if (tid == 0) {
@@ -198,9 +204,10 @@ __device__ void compute_pole(PoleShared& sh, const float2* v, const float4* pole
     __syncthreads();
 }
 
-__global__ void __launch_bounds__(PP_THREADS, 2) k_poles(PoleArgs a) {
+template <int PP_THREADS>
+__global__ void __launch_bounds__(PP_THREADS, 1024 / PP_THREADS) k_poles(PoleArgs a) {
     extern __shared__ float4 dyn[];
-    __shared__ PoleShared sh;
+    __shared__ PoleShared<PP_THREADS> sh;
     float4* poles = dyn;   // PP_MAX_POLES (poles mode) or the one result slot (poi mode)
     float2* v = reinterpret_cast<float2*>(dyn + (a.area ? PP_MAX_POLES : 1));
     float4* lvl_a = a.scratch + (size_t)blockIdx.x * 2 * PP_LEVEL_CAP;
@@ -296,21 +303,258 @@ __global__ void __launch_bounds__(PP_THREADS, 2) k_poles(PoleArgs a) {
     }
 }
 
+// ------------------------------------------------------------------------------------------
+// simplify_shape (geometry/shape_modification.rs:48-144), one warp per shape.
+//
+// Each round lists the removal candidates in corner order (Concave / Collinear corners, Convex
+// after Convex pairs; shape_modification.rs:62-99), orders them by area change with ties kept in
+// corner order (a stable sort, NaN last as OrderedFloat puts it), and executes the first valid one
+// if the whole shape's area stays within the tolerance.  The warp takes the candidates in that
+// order without sorting: the next one is the least (area change, corner position) above the last
+// rejected one, found by a warp minimum over 64-bit keys; validity tests the shape's edges over
+// lanes.  The new area is summed by one lane in the reference's order (simple_polygon.rs:137-150).
+// ------------------------------------------------------------------------------------------
+constexpr int SP_WARPS = 4;   // shapes per CTA at a time
+
+struct SimpArgs {
+    const float2* verts;
+    const uint32_t* voff;
+    uint32_t n_shapes, vmax;
+    const float* area;   // the shape's area (SPolygon::area)
+    int deflate;         // ShapeModifyMode::Deflate (else Inflate)
+    float tolerance;     // max_area_change_ratio
+    float2* out;         // same layout as verts
+    uint32_t* n_out;
+    int32_t* status;
+};
+
+enum : int { SC_CONCAVE = 0, SC_COLLINEAR = 1, SC_CONVEX = 2 };
+enum : int { SK_NONE = 0, SK_CONCAVE = 1, SK_COLLINEAR = 2, SK_CONVEX_CONVEX = 3 };
+
+struct SCorner { uint32_t a, b, c; };
+
+// corner at position k of the corner list (shape_modification.rs:62-77): (k-1, k, k+1), or for
+// Deflate the reversed list with every corner flipped
+__device__ __forceinline__ SCorner corner_at(uint32_t k, uint32_t n, int deflate) {
+    if (!deflate) return SCorner{k == 0 ? n - 1 : k - 1, k, k + 1 == n ? 0 : k + 1};
+    const uint32_t i = n - 1 - k;
+    return SCorner{i + 1 == n ? 0 : i + 1, i, i == 0 ? n - 1 : i - 1};
+}
+
+// CornerType::from (shape_modification.rs:317-327)
+__device__ __forceinline__ int corner_kind(float2 p1, float2 p2, float2 p3) {
+    const float ax = p2.x - p1.x, ay = p2.y - p1.y;
+    const float bx = p3.x - p1.x, by = p3.y - p1.y;
+    const float cross = ax * by - ay * bx;
+    return cross < 0.0f ? SC_CONCAVE : (cross == 0.0f ? SC_COLLINEAR : SC_CONVEX);
+}
+
+// calculate_intersection_in_front (shape_modification.rs:248-283) of edge (p1, p2) and edge (p3, p4)
+__device__ __forceinline__ bool in_front(float2 p1, float2 p2, float2 p3, float2 p4, float2* out) {
+    const float x1 = p1.x, y1 = p1.y, x2 = p2.x, y2 = p2.y, x3 = p3.x, y3 = p3.y, x4 = p4.x, y4 = p4.y;
+    const float t_nom = (x2 - x4) * (y4 - y3) - (y2 - y4) * (x4 - x3);
+    const float t_den = (x2 - x1) * (y4 - y3) - (y2 - y1) * (x4 - x3);
+    const float u_nom = (x2 - x4) * (y2 - y1) - (y2 - y4) * (x2 - x1);
+    const float u_den = (x2 - x1) * (y4 - y3) - (y2 - y1) * (x4 - x3);
+    const float t = t_den != 0.0f ? t_nom / t_den : 0.0f;
+    const float u = u_den != 0.0f ? u_nom / u_den : 0.0f;
+    if (t < 0.0f && u < 0.0f) {
+        *out = make_float2(x2 + t * (x1 - x2), y2 + t * (y1 - y2));
+        return true;
+    }
+    return false;
+}
+
+// |triangle area| of calculate_area_delta (shape_modification.rs:146-174)
+__device__ __forceinline__ float tri_area(float2 p0, float2 p1, float2 p2) {
+    const float x0 = p0.x, y0 = p0.y, x1 = p1.x, y1 = p1.y, x2 = p2.x, y2 = p2.y;
+    return fabsf((x0 * y1 + x1 * y2 + x2 * y0 - x0 * y2 - x1 * y0 - x2 * y1) / 2.0f);
+}
+
+__device__ __forceinline__ bool same_pt(float2 a, float2 b) { return a.x == b.x && a.y == b.y; }
+__device__ __forceinline__ Seg seg_of(float2 a, float2 b) { return Seg{Pt{a.x, a.y}, Pt{b.x, b.y}}; }
+
+// the candidate at position k: its kind, sort key bits (NaN last) and, for a convex pair, the
+// replacing vertex (replacing_vertex_convex_convex_candidate, shape_modification.rs:234-246)
+struct SCand {
+    int kind;
+    uint32_t key;
+    bool has_v;
+    float2 v;
+    SCorner c1, c2;
+};
+
+__device__ __forceinline__ SCand cand_at(const float2* P, uint32_t k, uint32_t n, int deflate) {
+    SCand r{};
+    r.c2 = corner_at(k, n, deflate);
+    const int t = corner_kind(P[r.c2.a], P[r.c2.b], P[r.c2.c]);
+    float key = 0.0f;
+    if (t == SC_CONCAVE) {
+        r.kind = SK_CONCAVE;
+        r.c1 = r.c2;
+        key = tri_area(P[r.c2.a], P[r.c2.b], P[r.c2.c]);
+    } else if (t == SC_COLLINEAR) {
+        r.kind = SK_COLLINEAR;
+        r.c1 = r.c2;
+    } else {
+        r.c1 = corner_at(k == 0 ? n - 1 : k - 1, n, deflate);
+        if (corner_kind(P[r.c1.a], P[r.c1.b], P[r.c1.c]) != SC_CONVEX) return r;   // SK_NONE
+        r.kind = SK_CONVEX_CONVEX;
+        r.has_v = in_front(P[r.c1.a], P[r.c1.b], P[r.c2.c], P[r.c2.b], &r.v);
+        key = r.has_v ? tri_area(P[r.c1.b], r.v, P[r.c2.b]) : INFINITY;
+    }
+    r.key = key != key ? 0x7FFFFFFFu : __float_as_uint(key);
+    return r;
+}
+
+__global__ void __launch_bounds__(SP_WARPS * 32) k_simplify(SimpArgs a) {
+    extern __shared__ float2 sp_dyn[];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    float2* P = sp_dyn + (size_t)w * a.vmax;
+    for (uint32_t s = blockIdx.x * SP_WARPS + w; s < a.n_shapes; s += gridDim.x * SP_WARPS) {
+        const uint32_t v0 = a.voff[s], n0 = a.voff[s + 1] - v0;
+        if (n0 < 3 || n0 > a.vmax) {
+            if (lane == 0) {
+                a.status[s] = PS_BAD_SHAPE;
+                a.n_out[s] = 0;
+            }
+            continue;
+        }
+        for (uint32_t j = lane; j < n0; j += 32) P[j] = a.verts[v0 + j];
+        __syncwarp();
+        const float area0 = a.area[s];
+        uint32_t n = n0;
+        for (uint32_t it = 0; it < n0 && n >= 4; it++) {
+            // candidates in (key, position) order until a valid one (shape_modification.rs:101-108)
+            unsigned long long lo = 0ull;
+            SCand best{};
+            bool found = false;
+            for (;;) {
+                unsigned long long m = ~0ull;
+                for (uint32_t k = lane; k < n; k += 32) {
+                    const SCand c = cand_at(P, k, n, a.deflate);
+                    const unsigned long long key = ((unsigned long long)c.key << 32) | k;
+                    if (c.kind != SK_NONE && key >= lo && key < m) m = key;
+                }
+#pragma unroll
+                for (int o = 16; o; o >>= 1) {
+                    const unsigned long long x = __shfl_xor_sync(FULL, m, o);
+                    m = x < m ? x : m;
+                }
+                if (m == ~0ull) break;   // no (further) candidate
+                const SCand c = cand_at(P, (uint32_t)(m & 0xFFFFFFFFu), n, a.deflate);
+                // candidate_is_valid (shape_modification.rs:176-207)
+                bool bad = false;
+                if (c.kind == SK_CONVEX_CONVEX && !c.has_v) {
+                    bad = true;
+                } else if (c.kind != SK_COLLINEAR) {
+                    float2 af[4];
+                    int n_af;
+                    Seg e1, e2;
+                    if (c.kind == SK_CONCAVE) {
+                        af[0] = P[c.c1.a];
+                        af[1] = P[c.c1.b];
+                        af[2] = P[c.c1.c];
+                        af[3] = af[2];
+                        n_af = 3;
+                        e1 = seg_of(P[c.c1.a], P[c.c1.c]);
+                        e2 = e1;
+                    } else {
+                        af[0] = P[c.c1.b];
+                        af[1] = P[c.c1.a];
+                        af[2] = P[c.c2.b];
+                        af[3] = P[c.c2.c];
+                        n_af = 4;
+                        e1 = seg_of(P[c.c1.a], c.v);
+                        e2 = seg_of(c.v, P[c.c2.c]);
+                    }
+                    for (uint32_t i = lane; i < n && !bad; i += 32) {
+                        const float2 ls = P[i], le = P[i + 1 == n ? 0 : i + 1];
+                        bool touch = false;
+                        for (int q = 0; q < n_af; q++) touch |= same_pt(af[q], ls) || same_pt(af[q], le);
+                        if (touch) continue;
+                        const Seg l = seg_of(ls, le);
+                        bad = seg_hits_seg(l, e1) || (c.kind == SK_CONVEX_CONVEX && seg_hits_seg(l, e2));
+                    }
+                    bad = __any_sync(FULL, bad);
+                }
+                if (!bad) {
+                    best = c;
+                    found = true;
+                    break;
+                }
+                lo = m + 1;
+            }
+            if (!found) break;
+            // execute_candidate (shape_modification.rs:217-232): drop corner c1.b; a convex pair
+            // also puts the replacing vertex in place of c2.b.  Area of the result first, in the
+            // reference's order (one lane), the shape updated only if it stays within tolerance.
+            const uint32_t gone = best.c1.b;
+            const bool repl = best.kind == SK_CONVEX_CONVEX;
+            const uint32_t at = best.c2.b;
+            int keep = 0;
+            if (lane == 0) {
+                const uint32_t m = n - 1;
+                float sigma = 0.0f;
+                auto vtx = [&](uint32_t i) {   // vertex i of the new list
+                    const uint32_t src = i < gone ? i : i + 1;
+                    return (repl && src == at) ? best.v : P[src];
+                };
+                float2 cur = vtx(0), first = cur;
+                for (uint32_t i = 0; i < m; i++) {
+                    const float2 nx = i + 1 == m ? first : vtx(i + 1);
+                    sigma += (cur.y + nx.y) * (cur.x - nx.x);
+                    cur = nx;
+                }
+                const float new_area = 0.5f * sigma;
+                keep = fabsf(new_area - area0) / area0 <= a.tolerance;
+            }
+            keep = __shfl_sync(FULL, keep, 0);
+            if (!keep) break;
+            if (repl && lane == 0) P[at] = best.v;
+            __syncwarp();
+            for (uint32_t base = gone; base + 1 < n; base += 32) {   // close the gap at `gone`
+                const uint32_t j = base + lane;
+                const float2 nx = j + 1 < n ? P[j + 1] : make_float2(0.f, 0.f);
+                __syncwarp();
+                if (j + 1 < n) P[j] = nx;
+                __syncwarp();
+            }
+            n--;
+        }
+        for (uint32_t j = lane; j < n; j += 32) a.out[v0 + j] = P[j];
+        if (lane == 0) {
+            a.n_out[s] = n;
+            a.status[s] = PS_OK;
+        }
+        __syncwarp();
+    }
+}
+
 size_t pole_smem(uint32_t vmax, bool poles_mode) {
     return (poles_mode ? PP_MAX_POLES : 1) * sizeof(float4) + (size_t)vmax * sizeof(float2);
 }
 
-// CTAs of one launch: every SM's worth of resident CTAs, at most one per shape
-jcde_status pole_grid(uint32_t n_shapes, uint32_t vmax, bool poles_mode, uint32_t* grid) {
+// CTAs of one launch: every SM's worth of resident CTAs, at most one per shape; *wide selects the
+// 1024-thread CTA (batches of at most one shape per SM)
+template <int T>
+jcde_status pole_occupancy(size_t smem, int* per_sm) {
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(k_poles<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return JCDE_ERR_ARG;   // more vertices than shared memory holds
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_poles<T>, T, smem) != cudaSuccess || *per_sm < 1)
+        return JCDE_ERR_ARG;
+    return JCDE_OK;
+}
+
+jcde_status pole_grid(uint32_t n_shapes, uint32_t vmax, bool poles_mode, uint32_t* grid, bool* wide) {
     const size_t smem = pole_smem(vmax, poles_mode);
     int dev = 0, n_sms = 0, per_sm = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
         return JCDE_ERR_CUDA;
-    if (smem > 48 * 1024 &&
-        cudaFuncSetAttribute(k_poles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-        return JCDE_ERR_ARG;   // more vertices than shared memory holds
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_poles, PP_THREADS, smem) != cudaSuccess || per_sm < 1)
-        return JCDE_ERR_ARG;
+    *wide = n_shapes <= (uint32_t)n_sms;
+    jcde_status st = *wide ? pole_occupancy<PP_THREADS_WIDE>(smem, &per_sm) : pole_occupancy<512>(smem, &per_sm);
+    if (st) return st;
     *grid = std::max<uint32_t>(1u, std::min<uint32_t>(n_shapes, (uint32_t)(n_sms * per_sm)));
     return JCDE_OK;
 }
@@ -324,7 +568,8 @@ size_t pole_workspace(uint32_t n_shapes, uint32_t grid) {
 jcde_status launch_poles(PoleArgs a, void* ws, uint64_t ws_bytes, cudaStream_t s) {
     if (a.n_shapes == 0) return JCDE_OK;
     uint32_t grid = 0;
-    jcde_status st = pole_grid(a.n_shapes, a.vmax, a.area != nullptr, &grid);
+    bool wide = false;
+    jcde_status st = pole_grid(a.n_shapes, a.vmax, a.area != nullptr, &grid, &wide);
     if (st) return st;
     const size_t need = pole_workspace(a.n_shapes, grid);
     void* own = nullptr;
@@ -340,7 +585,9 @@ jcde_status launch_poles(PoleArgs a, void* ws, uint64_t ws_bytes, cudaStream_t s
     a.scratch = reinterpret_cast<float4*>(w + 256 + (((size_t)a.n_shapes * sizeof(uint32_t) + 255) & ~(size_t)255));
     if (cudaMemsetAsync(a.next, 0, sizeof(uint32_t), s) != cudaSuccess) st = JCDE_ERR_CUDA;
     if (!st) {
-        k_poles<<<grid, PP_THREADS, pole_smem(a.vmax, a.area != nullptr), s>>>(a);
+        const size_t smem = pole_smem(a.vmax, a.area != nullptr);
+        if (wide) k_poles<PP_THREADS_WIDE><<<grid, PP_THREADS_WIDE, smem, s>>>(a);
+        else k_poles<512><<<grid, 512, smem, s>>>(a);
         if (cudaGetLastError() != cudaSuccess) st = JCDE_ERR_CUDA;
     }
     if (own && cudaFreeAsync(own, s) != cudaSuccess) st = JCDE_ERR_CUDA;
@@ -352,9 +599,31 @@ jcde_status launch_poles(PoleArgs a, void* ws, uint64_t ws_bytes, cudaStream_t s
 
 using namespace jcde;
 
+extern "C" jcde_status jcde_simplify_batch(const float* d_xy, const uint32_t* d_voff, uint32_t n_shapes,
+                                           uint32_t max_vertices, const float* d_area, int deflate, float tolerance,
+                                           float* d_xy_out, uint32_t* d_n_out, int32_t* d_status, void* stream) {
+    if (n_shapes == 0) return JCDE_OK;
+    if (!d_xy || !d_voff || !d_area || !d_xy_out || !d_n_out || !d_status || max_vertices < 3) return JCDE_ERR_ARG;
+    SimpArgs a{reinterpret_cast<const float2*>(d_xy), d_voff, n_shapes, max_vertices, d_area, deflate != 0, tolerance,
+               reinterpret_cast<float2*>(d_xy_out), d_n_out, d_status};
+    const size_t smem = (size_t)SP_WARPS * max_vertices * sizeof(float2);
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(k_simplify, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return JCDE_ERR_ARG;   // more vertices than shared memory holds
+    int dev = 0, n_sms = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return JCDE_ERR_CUDA;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_simplify, SP_WARPS * 32, smem) != cudaSuccess || per_sm < 1)
+        return JCDE_ERR_ARG;
+    const uint32_t grid = std::min<uint32_t>((n_shapes + SP_WARPS - 1) / SP_WARPS, (uint32_t)(n_sms * per_sm));
+    k_simplify<<<grid, SP_WARPS * 32, smem, (cudaStream_t)stream>>>(a);
+    return cudaGetLastError() == cudaSuccess ? JCDE_OK : JCDE_ERR_CUDA;
+}
+
 extern "C" uint64_t jcde_poles_workspace_bytes(uint32_t n_shapes, uint32_t max_vertices, int with_poles) {
     uint32_t grid = 0;
-    if (n_shapes == 0 || pole_grid(n_shapes, max_vertices, with_poles != 0, &grid)) return 0;
+    bool wide = false;
+    if (n_shapes == 0 || pole_grid(n_shapes, max_vertices, with_poles != 0, &grid, &wide)) return 0;
     return pole_workspace(n_shapes, grid);
 }
 

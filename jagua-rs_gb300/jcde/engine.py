@@ -458,6 +458,13 @@ class GpuBackend:
     surrogate_poles = staticmethod(surrogate_poles)
 
     @staticmethod
+    def simplify_shape(xy, area, deflate, tolerance):
+        """simplify_shape before its final SPolygon::new, on the device (jcde_simplify_batch)."""
+        from . import prep
+
+        return prep.simplify_batch([xy], [area], deflate, tolerance)[0]
+
+    @staticmethod
     def new_engine(depth: int, cd_threshold: int, bbox):
         return GpuEngine(depth, cd_threshold, bbox)
 

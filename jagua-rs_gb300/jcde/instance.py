@@ -115,9 +115,10 @@ class SppSetup:
 
 
 def setup_spp(backend, inst: SppInstance, strip_width: float, depth: int = W.DEFAULT_DEPTH,
-              cd_threshold: int = W.DEFAULT_CD_THRESHOLD) -> SppSetup:
-    """Items imported, a strip of `strip_width` x strip_height as the container, a fresh engine."""
-    items = [W.import_item(backend, it.xy) for it in inst.items]
+              cd_threshold: int = W.DEFAULT_CD_THRESHOLD, simplify_tolerance=None) -> SppSetup:
+    """Items imported, a strip of `strip_width` x strip_height as the container, a fresh engine.
+    `simplify_tolerance` simplifies the items as lbf's importer does (its default config: 0.001)."""
+    items = [W.import_item(backend, it.xy, simplify_tolerance=simplify_tolerance) for it in inst.items]
     outer = W.import_static(backend, W.rect_polygon(0.0, 0.0, strip_width, inst.strip_height), W.EXTERIOR)
     lay = W.Layout(inst.name or "spp", depth, cd_threshold, W.inflate_to_square(W.bbox_of(outer.xy)), items=items)
     lay.hazards.append(outer)

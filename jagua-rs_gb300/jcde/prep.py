@@ -103,6 +103,35 @@ class ShapeBatch:
         return out, counts, status
 
 
+def simplify_device(batch: "ShapeBatch", area, deflate: bool, tolerance: float, stream=None):
+    """Launch jcde_simplify_batch on a packed batch: area (n,) float32 device tensor in; the
+    simplified vertices (same layout as the batch), counts and statuses as device tensors out."""
+    torch = _torch()
+    out = torch.empty_like(batch.xy)
+    cnt = torch.empty(batch.n, dtype=torch.int32, device=batch.device)
+    st = torch.empty(batch.n, dtype=torch.int32, device=batch.device)
+    check(lib().jcde_simplify_batch(C.c_void_p(batch.xy.data_ptr()), C.c_void_p(batch.voff.data_ptr()), batch.n,
+                                    batch.vmax, C.c_void_p(area.data_ptr()), int(bool(deflate)), float(tolerance),
+                                    C.c_void_p(out.data_ptr()), C.c_void_p(cnt.data_ptr()), C.c_void_p(st.data_ptr()),
+                                    _stream_ptr(stream)), "simplify_batch")
+    return out, cnt, st
+
+
+def simplify_batch(shapes, areas, deflate: bool, tolerance: float) -> list:
+    """simplify_shape (shape_modification.rs:48-144, before its final SPolygon::new) of each internal
+    shape on the device: a list of (k, 2) float32 vertex arrays."""
+    torch = _torch()
+    if not len(shapes):
+        return []
+    flat, off = pack(shapes)
+    b = ShapeBatch(packed=(flat, off))
+    area = torch.from_numpy(np.ascontiguousarray(areas, np.float32)).to(b.device)
+    out, cnt, st = simplify_device(b, area, deflate, tolerance)
+    _raise_on(st.cpu().numpy(), "simplify_batch")
+    o, c = out.view(-1, 2).cpu().numpy(), cnt.cpu().numpy()
+    return [o[off[i]: off[i] + int(c[i])].copy() for i in range(b.n)]
+
+
 def _raise_on(status: np.ndarray, what: str, allow=()):
     bad = [(i, int(s)) for i, s in enumerate(status) if s != 0 and s not in allow]
     if bad:
@@ -168,28 +197,43 @@ def spolygon_batch(raw_shapes, n_threads: int = 0):
     return xo, off, bbox, ad
 
 
-def import_items(raw_shapes, pole_limits=W.DEFAULT_POLE_LIMITS, n_ff_poles=W.DEFAULT_N_FF_POLES) -> list:
-    """Importer::import_item (io/import.rs:47-98, no simplification) for every shape of the list, the
-    poi and surrogate poles searched on the device: the same Items as workload.import_item."""
+def import_items(raw_shapes, pole_limits=W.DEFAULT_POLE_LIMITS, n_ff_poles=W.DEFAULT_N_FF_POLES,
+                 simplify_tolerance=None) -> list:
+    """Importer::import_item (io/import.rs:47-98) for every shape of the list, the poi and surrogate
+    poles searched on the device: the same Items as workload.import_item.  With a
+    `simplify_tolerance` the centred shapes are simplified on the device (ShapeModifyMode::Inflate,
+    original_shape.rs:23-50) and the poi is that of the simplified shape."""
     torch = _torch()
     n = len(raw_shapes)
     if n == 0:
         return []
     flat, off, _, ad = spolygon_batch(raw_shapes)
-    b = ShapeBatch(packed=(flat, off))
-    poi_d, st = b.poi()
     shapes = [flat[off[i]: off[i + 1]] for i in range(n)]
+    if simplify_tolerance is None:
+        b = ShapeBatch(packed=(flat, off))
+        poi_d, st = b.poi()
     cent = W.centroids_f32(shapes, ad[:, 0])   # meanwhile on the host
-    st_h = st.cpu().numpy()
-    _raise_on(st_h, "poi_batch")
-    poi = poi_d.cpu().numpy()
     # centering_transformation (io/import.rs:214-217) as in workload.import_item, every shape at once
     reps = np.diff(off).astype(np.int64)
     cxy = W.transform_points(flat, 1.0, 0.0, np.repeat(-cent[:, 0], reps), np.repeat(-cent[:, 1], reps))
-    ipoi = np.concatenate([W.transform_points(poi[:, :2], 1.0, 0.0, -cent[:, 0], -cent[:, 1]), poi[:, 2:3]],
-                          axis=1).astype(np.float32)
-    bc = ShapeBatch(packed=(cxy, off))
-    area_d = torch.from_numpy(np.ascontiguousarray(ad[:, 0])).to(bc.device)
+    area_int = ad[:, 0]
+    diam_int = ad[:, 1]
+    if simplify_tolerance is None:
+        _raise_on(st.cpu().numpy(), "poi_batch")
+        poi = poi_d.cpu().numpy()
+        ipoi = np.concatenate([W.transform_points(poi[:, :2], 1.0, 0.0, -cent[:, 0], -cent[:, 1]), poi[:, 2:3]],
+                              axis=1).astype(np.float32)
+        bc = ShapeBatch(packed=(cxy, off))
+    else:
+        # simplify_shape, then its SPolygon::new: orientation, area, diameter on the host, poi on the device
+        simp = simplify_batch([cxy[off[i]: off[i + 1]] for i in range(n)], area_int, False, simplify_tolerance)
+        cxy, off, _, ad2 = spolygon_batch(simp)
+        area_int, diam_int = ad2[:, 0], ad2[:, 1]
+        bc = ShapeBatch(packed=(cxy, off))
+        poi_d, st = bc.poi()
+        _raise_on(st.cpu().numpy(), "poi_batch")
+        ipoi = poi_d.cpu().numpy()
+    area_d = torch.from_numpy(np.ascontiguousarray(area_int, np.float32)).to(bc.device)
     cap = 128
     out, cnt, sp = bc.poles(area_d, torch.from_numpy(ipoi).to(bc.device), pole_limits, cap)
     sp_h = sp.cpu().numpy()
@@ -203,5 +247,5 @@ def import_items(raw_shapes, pole_limits=W.DEFAULT_POLE_LIMITS, n_ff_poles=W.DEF
     for i in range(n):
         p = o[i, : int(c[i])].copy()
         items.append(W.Item(cxy[off[i]: off[i + 1]].copy(), ipoi[i].copy(), p, min(n_ff_poles, len(p)),
-                            float(ad[i, 0]), float(ad[i, 1]), (float(cent[i, 0]), float(cent[i, 1]))))
+                            float(ad[i, 0]), float(diam_int[i]), (float(cent[i, 0]), float(cent[i, 1]))))
     return items

@@ -228,22 +228,38 @@ class Layout:
     n_failed_placements: int = 0
 
 
-def import_item(backend, raw_xy, pole_limits=DEFAULT_POLE_LIMITS, n_ff_poles=DEFAULT_N_FF_POLES) -> Item:
-    """Importer::import_item without simplification (io/import.rs:47-98, entities/item.rs:27-48)."""
+def import_item(backend, raw_xy, pole_limits=DEFAULT_POLE_LIMITS, n_ff_poles=DEFAULT_N_FF_POLES,
+                simplify_tolerance=None) -> Item:
+    """Importer::import_item (io/import.rs:47-98, entities/item.rs:27-48) with
+    OriginalShape::convert_to_internal (original_shape.rs:23-50): the centred shape, simplified
+    (ShapeModifyMode::Inflate) when a tolerance is given — lbf's default config uses 0.001
+    (lbf/src/config.rs:42).  Item.area is the original shape's (Item::area), the diameter that of
+    the internal shape (the one item_placement_order sorts by)."""
     xy, bbox, area, diam, poi = backend.spolygon_new(raw_xy)
     cx, cy = centroid_f32(xy, area)
     # centering_transformation (io/import.rs:214-217): DTransformation(0, (-cx, -cy)); sin_cos(0) = (0, 1)
     ixy = transform_points(xy, 1.0, 0.0, -cx, -cy)
     ipoi = np.concatenate([transform_points(poi[None, :2], 1.0, 0.0, -cx, -cy)[0], poi[2:3]]).astype(np.float32)
-    poles = backend.surrogate_poles(ixy, area, ipoi, pole_limits)
-    return Item(ixy, ipoi, poles, min(n_ff_poles, len(poles)), float(area), float(diam), (float(cx), float(cy)))
+    iarea, idiam = area, diam
+    if simplify_tolerance is not None:
+        # simplify_shape ends in SPolygon::new: new area, diameter and poi for the internal shape
+        simp = backend.simplify_shape(ixy, area, False, simplify_tolerance)
+        ixy, _, iarea, idiam, ipoi = backend.spolygon_new(simp)
+    poles = backend.surrogate_poles(ixy, iarea, ipoi, pole_limits)
+    return Item(ixy, ipoi, poles, min(n_ff_poles, len(poles)), float(area), float(idiam), (float(cx), float(cy)))
 
 
-def import_static(backend, raw_xy, kind) -> HazardSpec:
-    """Container outer / hole / zone: SPolygon::new then the empty pre-transform (io/import.rs:119-124)."""
+def import_static(backend, raw_xy, kind, simplify_tolerance=None) -> HazardSpec:
+    """Container outer / hole / zone: SPolygon::new then the empty pre-transform (io/import.rs:119-124);
+    with a tolerance simplified as OriginalShape::convert_to_internal does (original_shape.rs:23-50):
+    the outer with ShapeModifyMode::Deflate (io/import.rs:123), holes and zones with Inflate
+    (io/import.rs:181)."""
     xy, bbox, area, diam, poi = backend.spolygon_new(raw_xy)
     ixy = transform_points(xy, 1.0, 0.0, 0.0, 0.0)
     ipoi = np.concatenate([transform_points(poi[None, :2], 1.0, 0.0, 0.0, 0.0)[0], poi[2:3]]).astype(np.float32)
+    if simplify_tolerance is not None:
+        simp = backend.simplify_shape(ixy, area, kind == EXTERIOR, simplify_tolerance)
+        ixy, _, _, _, ipoi = backend.spolygon_new(simp)
     return HazardSpec(kind, False, ixy, ipoi)
 
 

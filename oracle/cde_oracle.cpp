@@ -1023,6 +1023,162 @@ static void dump_node(const QTNode& n, std::vector<uint32_t>& o) {
         for (int i = 0; i < 4; i++) dump_node(n.children[i], o);
 }
 
+// ------------------------------------------------------------------------------------------
+// shape simplification  (geometry/shape_modification.rs:48-328)
+// ------------------------------------------------------------------------------------------
+enum CornerType { CORNER_CONCAVE, CORNER_COLLINEAR, CORNER_CONVEX };
+struct Corner { size_t a, b, c; };   // shape_modification.rs:296-308 (left-hand side of a-b-c)
+enum CandKind { CAND_CONCAVE, CAND_CONVEX_CONVEX, CAND_COLLINEAR };
+struct Candidate { CandKind kind; Corner c1, c2; };
+
+// shape_modification.rs:317-327
+static CornerType corner_type(Point p1, Point p2, Point p3) {
+    float ax = p2.x - p1.x, ay = p2.y - p1.y;
+    float bx = p3.x - p1.x, by = p3.y - p1.y;
+    float cross = ax * by - ay * bx;
+    if (cross < 0.0f) return CORNER_CONCAVE;
+    if (cross == 0.0f) return CORNER_COLLINEAR;
+    return CORNER_CONVEX;   // NaN panics in the reference (`expect`); not reached for valid shapes
+}
+
+// shape_modification.rs:248-283 (calculate_intersection_in_front)
+static bool intersection_in_front(const Edge& l1, const Edge& l2, Point* out) {
+    float x1 = l1.s.x, y1 = l1.s.y, x2 = l1.e.x, y2 = l1.e.y;
+    float x3 = l2.s.x, y3 = l2.s.y, x4 = l2.e.x, y4 = l2.e.y;
+    float t_nom = (x2 - x4) * (y4 - y3) - (y2 - y4) * (x4 - x3);
+    float t_denom = (x2 - x1) * (y4 - y3) - (y2 - y1) * (x4 - x3);
+    float u_nom = (x2 - x4) * (y2 - y1) - (y2 - y4) * (x2 - x1);
+    float u_denom = (x2 - x1) * (y4 - y3) - (y2 - y1) * (x4 - x3);
+    float t = t_denom != 0.0f ? t_nom / t_denom : 0.0f;
+    float u = u_denom != 0.0f ? u_nom / u_denom : 0.0f;
+    if (t < 0.0f && u < 0.0f) {
+        *out = Point{x2 + t * (x1 - x2), y2 + t * (y1 - y2)};
+        return true;
+    }
+    return false;
+}
+
+// shape_modification.rs:234-246
+static bool replacing_vertex(const std::vector<Point>& s, const Corner& c1, const Corner& c2, Point* out) {
+    return intersection_in_front(Edge{s[c1.a], s[c1.b]}, Edge{s[c2.c], s[c2.b]}, out);
+}
+
+static float triangle_area_abs(Point p0, Point p1, Point p2) {
+    float x0 = p0.x, y0 = p0.y, x1 = p1.x, y1 = p1.y, x2 = p2.x, y2 = p2.y;
+    float area = (x0 * y1 + x1 * y2 + x2 * y0 - x0 * y2 - x1 * y0 - x2 * y1) / 2.0f;
+    return std::fabs(area);
+}
+
+// shape_modification.rs:146-174 — INFINITY stands for the Err of an invalid convex-convex candidate
+static float area_delta(const std::vector<Point>& s, const Candidate& c) {
+    switch (c.kind) {
+        case CAND_COLLINEAR: return 0.0f;
+        case CAND_CONCAVE: return triangle_area_abs(s[c.c1.a], s[c.c1.b], s[c.c1.c]);
+        default: {
+            Point v;
+            if (!replacing_vertex(s, c.c1, c.c2, &v)) return INFINITY;
+            return triangle_area_abs(s[c.c1.b], v, s[c.c2.b]);
+        }
+    }
+}
+
+static bool same_point(Point a, Point b) { return a.x == b.x && a.y == b.y; }
+
+// shape_modification.rs:176-207
+static bool candidate_valid(const std::vector<Point>& s, const Candidate& c) {
+    const size_t n = s.size();
+    if (c.kind == CAND_COLLINEAR) return true;
+    std::vector<Edge> news;
+    std::vector<Point> affected;
+    if (c.kind == CAND_CONCAVE) {
+        news.push_back(Edge{s[c.c1.a], s[c.c1.c]});
+        affected = {s[c.c1.a], s[c.c1.b], s[c.c1.c]};
+    } else {
+        Point v;
+        if (!replacing_vertex(s, c.c1, c.c2, &v)) return false;
+        news.push_back(Edge{s[c.c1.a], v});
+        news.push_back(Edge{v, s[c.c2.c]});
+        affected = {s[c.c1.b], s[c.c1.a], s[c.c2.b], s[c.c2.c]};
+    }
+    for (size_t i = 0; i < n; i++) {
+        Edge l{s[i], s[(i + 1) % n]};
+        bool touches = false;
+        for (const Point& p : affected) touches = touches || same_point(p, l.s) || same_point(p, l.e);
+        if (touches) continue;
+        for (const Edge& ne : news)
+            if (edge_intersection(l, ne)) return false;
+    }
+    return true;
+}
+
+// shape_modification.rs:217-232
+static std::vector<Point> execute_candidate(const std::vector<Point>& s, const Candidate& c) {
+    std::vector<Point> p = s;
+    if (c.kind != CAND_CONVEX_CONVEX) {
+        p.erase(p.begin() + c.c1.b);
+    } else {
+        Point v;
+        replacing_vertex(s, c.c1, c.c2, &v);
+        p.erase(p.begin() + c.c1.b);
+        size_t other = c.c1.b < c.c2.b ? c.c2.b - 1 : c.c2.b;
+        p.erase(p.begin() + other);
+        p.insert(p.begin() + other, v);
+    }
+    return p;
+}
+
+// simplify_shape (shape_modification.rs:48-144) up to its final SPolygon::new: the simplified
+// vertices.  deflate selects ShapeModifyMode::Deflate.
+static std::vector<Point> simplify_shape(const std::vector<Point>& shape, float shape_area, bool deflate,
+                                         float max_area_change_ratio) {
+    std::vector<Point> ref = shape;
+    for (size_t it = 0; it < shape.size(); it++) {
+        const size_t n = ref.size();
+        if (n < 4) break;
+        std::vector<Corner> corners(n);
+        for (size_t i = 0; i < n; i++) corners[i] = Corner{(i + n - 1) % n, i, (i + 1) % n};
+        if (deflate) {
+            std::reverse(corners.begin(), corners.end());
+            for (Corner& c : corners) std::swap(c.a, c.c);
+        }
+        auto type_of = [&](const Corner& c) { return corner_type(ref[c.a], ref[c.b], ref[c.c]); };
+        std::vector<Candidate> cands;
+        Corner prev = corners.back();
+        CornerType prev_t = type_of(prev);
+        for (const Corner& c : corners) {
+            CornerType t = type_of(c);
+            if (t == CORNER_CONCAVE) cands.push_back(Candidate{CAND_CONCAVE, c, c});
+            else if (t == CORNER_COLLINEAR) cands.push_back(Candidate{CAND_COLLINEAR, c, c});
+            else if (prev_t == CORNER_CONVEX) cands.push_back(Candidate{CAND_CONVEX_CONVEX, prev, c});
+            prev = c;
+            prev_t = t;
+        }
+        // sorted_by_cached_key(OrderedFloat(delta)) is a stable sort; OrderedFloat puts NaN last
+        std::vector<std::pair<float, size_t>> keyed(cands.size());
+        for (size_t k = 0; k < cands.size(); k++) keyed[k] = {area_delta(ref, cands[k]), k};
+        auto key_less = [](float a, float b) {
+            if (std::isnan(a)) return false;
+            if (std::isnan(b)) return true;
+            return a < b;
+        };
+        std::stable_sort(keyed.begin(), keyed.end(),
+                         [&](const std::pair<float, size_t>& x, const std::pair<float, size_t>& y) { return key_less(x.first, y.first); });
+        const Candidate* best = nullptr;
+        for (const auto& kk : keyed)
+            if (candidate_valid(ref, cands[kk.second])) {
+                best = &cands[kk.second];
+                break;
+            }
+        if (!best) break;
+        std::vector<Point> next = execute_candidate(ref, *best);
+        float next_area = calculate_area(next);
+        float delta = std::fabs(next_area - shape_area) / shape_area;
+        if (delta <= max_area_change_ratio) ref = next;
+        else break;
+    }
+    return ref;
+}
+
 }  // namespace oracle
 
 // ==========================================================================================
@@ -1263,6 +1419,18 @@ void or_centroid(const float* xy, uint32_t nv, float area, float* out2) {
     cy /= 6.0f * area;
     out2[0] = cx;
     out2[1] = cy;
+}
+
+// simplify_shape (shape_modification.rs:48-144) of an internal shape with the given area, without
+// the final SPolygon::new: *n_out receives the simplified vertex count.  deflate: 0 Inflate, 1 Deflate.
+int32_t or_simplify_shape(const float* xy, uint32_t nv, float area, int32_t deflate, float tolerance, float* xy_out,
+                          uint32_t* n_out) {
+    std::vector<Point> pts(nv);
+    for (uint32_t i = 0; i < nv; i++) pts[i] = Point{xy[2 * i], xy[2 * i + 1]};
+    std::vector<Point> r = simplify_shape(pts, area, deflate != 0, tolerance);
+    *n_out = (uint32_t)r.size();
+    for (size_t i = 0; i < r.size(); i++) { xy_out[2 * i] = r[i].x; xy_out[2 * i + 1] = r[i].y; }
+    return 0;
 }
 
 // Primitive probes for known-answer tests.

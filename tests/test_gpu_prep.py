@@ -99,3 +99,55 @@ def test_item_pool_of_the_lbf_build(oracle_mod, jcde_mod):
     for d, ref in zip(dev, lay.items):
         assert np.array_equal(d.poles.view(np.uint32), ref.poles.view(np.uint32))
         assert np.array_equal(d.xy.view(np.uint32), ref.xy.view(np.uint32))
+
+
+@gpu
+@pytest.mark.parametrize("tol", [0.0, 0.001, 0.01, 0.05, 0.3])
+def test_simplify_batch_matches_oracle(oracle_mod, jcde_mod, tol):
+    """simplify_shape on the device (one warp per shape), both modes, bit-exact with the oracle."""
+    from jcde import prep
+
+    raws = _shapes()
+    shapes, areas = [], []
+    for r in raws:
+        xy, _, area, _, _ = oracle_mod.OracleBackend.spolygon_new(r)
+        shapes.append(xy)
+        areas.append(area)
+    for deflate in (False, True):
+        got = prep.simplify_batch(shapes, areas, deflate, tol)
+        for i, (xy, a) in enumerate(zip(shapes, areas)):
+            ref = oracle_mod.OracleBackend.simplify_shape(xy, a, deflate, tol)
+            assert got[i].shape == ref.shape and np.array_equal(got[i].view(np.uint32), ref.view(np.uint32)), \
+                (i, deflate, len(got[i]), len(ref))
+
+
+@gpu
+def test_import_items_simplified_matches_oracle(oracle_mod, jcde_mod):
+    """Importer::import_item with lbf's default simplification (0.001) and a coarse one: simplified
+    shape, recomputed poi, poles, area and diameter all equal to the oracle's import."""
+    from jcde import prep
+
+    raws = _shapes()[:16] + _shapes()[24:]
+    for tol in (0.001, 0.05):
+        dev = prep.import_items(raws, simplify_tolerance=tol)
+        for i, r in enumerate(raws):
+            ref = W.import_item(oracle_mod.OracleBackend, r, simplify_tolerance=tol)
+            d = dev[i]
+            assert np.array_equal(d.xy.view(np.uint32), ref.xy.view(np.uint32)), (tol, i)
+            assert np.array_equal(d.poi.view(np.uint32), ref.poi.view(np.uint32)), (tol, i)
+            assert np.array_equal(d.poles.view(np.uint32), ref.poles.view(np.uint32)), (tol, i)
+            assert (d.area, d.diameter, d.centroid) == (ref.area, ref.diameter, ref.centroid)
+
+
+@gpu
+def test_batch_wider_than_the_gpu(oracle_mod, jcde_mod):
+    """More shapes than SMs: the 512-thread CTAs, several shapes per CTA from the counter."""
+    from jcde import prep
+
+    st = W.Stream(0xC0, 3)
+    raws = [W.star_polygon(st, int(st.randint(8, 24, 1)[0]), 20.0, 60.0) for _ in range(200)]
+    dev = prep.import_items(raws)
+    for d, r in zip(dev, raws):
+        ref = W.import_item(oracle_mod.OracleBackend, r)
+        assert np.array_equal(d.poi.view(np.uint32), ref.poi.view(np.uint32))
+        assert np.array_equal(d.poles.view(np.uint32), ref.poles.view(np.uint32))

@@ -1,0 +1,87 @@
+"""Shape simplification (shape_modification.rs:48-144) in the oracle: the invariants the reference
+states for it, on star items, concave shapes and the reference's own instances."""
+import glob
+import json
+import os
+
+import numpy as np
+import pytest
+
+from jcde import workload as W
+
+REF_ASSETS = "/root/reference/assets"
+
+
+def _stars(n=24, seed=0xC2):
+    st = W.Stream(seed, 7)
+    return [W.star_polygon(st, int(st.randint(8, 200, 1)[0]), 20.0, 60.0) for _ in range(n)]
+
+
+@pytest.mark.parametrize("tol", [0.001, 0.01, 0.05, 0.2])
+def test_simplify_invariants(oracle_mod, tol):
+    """Fewer or equal vertices, area change within the tolerance, Inflate never shrinks and Deflate
+    never grows the shape, and the result is a valid simple polygon (SPolygon::new accepts it)."""
+    B = oracle_mod.OracleBackend
+    for raw in _stars():
+        xy, _, area, _, _ = B.spolygon_new(raw)
+        for deflate in (False, True):
+            s = B.simplify_shape(xy, area, deflate, tol)
+            assert 3 <= len(s) <= len(xy)
+            s_xy, _, s_area, _, _ = B.spolygon_new(s)
+            assert abs(float(s_area) - float(area)) / float(area) <= tol * (1 + 1e-5)
+            assert (s_area <= area) if deflate else (s_area >= area)
+            assert np.array_equal(s_xy, s)   # stays counter-clockwise
+
+
+def test_simplify_keeps_what_it_cannot_change(oracle_mod):
+    B = oracle_mod.OracleBackend
+    rect = W.rect_polygon(0.0, 0.0, 10.0, 5.0)
+    assert np.array_equal(B.simplify_shape(rect, 50.0, False, 0.5), rect)   # 4 convex corners, no 4th-vertex removal
+    tri = np.array([[0, 0], [4, 0], [0, 3]], np.float32)
+    assert np.array_equal(B.simplify_shape(tri, 6.0, False, 0.5), tri)      # fewer than 4 vertices
+    # a collinear vertex costs no area: removed at any tolerance
+    sq = np.array([[0, 0], [5, 0], [10, 0], [10, 10], [0, 10]], np.float32)
+    out = B.simplify_shape(sq, 100.0, False, 0.0)
+    assert len(out) == 4 and not any((out == [5, 0]).all(1))
+    # tolerance 0 keeps every corner that changes the area
+    star = _stars(1)[0]
+    xy, _, area, _, _ = B.spolygon_new(star)
+    assert len(B.simplify_shape(xy, area, False, 0.0)) == len(xy)
+
+
+def test_import_item_with_simplification(oracle_mod):
+    """lbf's default import (tolerance 0.001): the internal shape is simplified, its poi recomputed,
+    the item keeps the original area."""
+    B = oracle_mod.OracleBackend
+    raw = _stars(1)[0]
+    plain = W.import_item(B, raw)
+    simp = W.import_item(B, raw, simplify_tolerance=0.05)
+    assert len(simp.xy) < len(plain.xy) and simp.area == plain.area
+    assert simp.poles[0].tolist() == simp.poi.tolist()
+
+
+def _ref_instances():
+    return sorted(glob.glob(os.path.join(REF_ASSETS, "*.json")))
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_ASSETS), reason="reference assets not present")
+def test_reference_instances_simplify(oracle_mod):
+    """Every simple-polygon item of the reference's instances (read in place) simplifies at lbf's
+    default tolerance within its invariants."""
+    from jcde import instance as I
+
+    B = oracle_mod.OracleBackend
+    seen = 0
+    for path in _ref_instances():
+        try:
+            inst = I.load_spp(path)
+        except (KeyError, ValueError, json.JSONDecodeError):
+            continue   # bin-packing or other formats
+        for it in inst.items[:8]:
+            xy, _, area, _, _ = B.spolygon_new(it.xy)
+            s = B.simplify_shape(xy, area, False, 0.001)
+            _, _, s_area, _, _ = B.spolygon_new(s)
+            assert len(s) <= len(xy) and s_area >= area
+            assert abs(float(s_area) - float(area)) / float(area) <= 0.001 * (1 + 1e-5)
+            seen += 1
+    assert seen > 0
