@@ -773,6 +773,67 @@ def run_prep(args):
     return 0
 
 
+def run_bpp(args):
+    """Bin packing with lbf_bpp.rs's optimizer: a seeded instance of 60 star item types (8-60
+    vertices, 2-8 copies each, some needing quality 1 or turning by 90 degrees only) and 6 bins
+    with holes and quality zones; 4096 candidates per layout searched.  One step = one whole solve
+    on the GPU engines through the package's API (host-driven: every search's layouts judged in one
+    multi-layout launch sequence, the choice and the registration on the host).  CPU baseline: the
+    same solve on the oracle engines (detect on all host cores), the same placements."""
+    import torch
+
+    import jcde
+    from jcde import bpp
+
+    jcde.lib()
+    inst = bpp.load_bpp(bpp.synthetic_instance(n_types=60, demand_range=(2, 8), n_bins=6))
+    spec = bpp.BppSpec(n_cand=4096)
+    su = bpp.setup_bpp(jcde.GpuBackend, inst)
+    for _ in range(max(1, min(args.warmup, 2))):
+        bpp.run_bpp(jcde.GpuBackend, su, spec)
+    clk = ClockSampler(0)
+    clk.__enter__()
+    ts, log = [], None
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        log = bpp.run_bpp(jcde.GpuBackend, su, spec)
+        ts.append(time.perf_counter() - t0)
+    clk.__exit__()
+    t_med = float(np.median(ts))
+    sol = bpp.export_solution(su, log)
+    n_copies = sum(it.demand for it in inst.items)
+    line = {
+        "metric": "bin-packing items placed per second (LBF solve, host-driven)",
+        "value": len(log.placements) / t_med, "unit": "items/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_med * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"bin packing: {len(inst.items)} star item types, {n_copies} copies, {len(inst.bins)} bins "
+                               f"with holes and quality zones, {spec.n_cand} candidates per layout searched; one "
+                               "step = one whole solve (wall clock, host-driven through the package API)"},
+        "items_placed": int(len(log.placements)), "unplaced": {str(k): v for k, v in log.unplaced.items()},
+        "layouts": len(log.layouts), "cost": sol["cost"], "density": sol["density"],
+        "candidates_judged_per_s": log.judged / t_med,
+        "clocks": clk.summary(),
+        "impl": "jcde",
+    }
+    if not args.no_cpu:
+        from oracle import oracle as O
+
+        O.build()
+        su_o = bpp.setup_bpp(O.OracleBackend, inst)
+        t0 = time.perf_counter()
+        log_o = bpp.run_bpp(O.OracleBackend, su_o, spec)
+        cpu_s = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": len(log_o.placements) / cpu_s, "unit": "items/s", "cores": host_cores(),
+                                "kind": "port", "ms_per_solve": cpu_s * 1e3,
+                                "sample": "the whole solve on the oracle engines (layouts searched one by one)",
+                                "same_solution": bool(log_o.same_as(log))}
+        line["solve_speedup_vs_cpu"] = cpu_s / t_med
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_lbf(args):
     """The LBF-style strip build on the device-resident engine.  2000 steps, each: 16384
     candidates generated, judged (surrogate + polygon passes), the least-cost free one registered on
@@ -923,11 +984,12 @@ def main():
     ap.add_argument("--autotune", type=int, default=1, help="1: jcde_autotune on the batch before timing")
     ap.add_argument("--lbf-cpu-steps", type=int, default=2000)
     ap.add_argument("--prep-shapes", type=int, default=1024, help="prep workload: shapes per batch")
-    ap.add_argument("--workload", default="star", choices=["star", "multi", "proxy", "lbf", "prep"],
+    ap.add_argument("--workload", default="star", choices=["star", "multi", "proxy", "lbf", "prep", "bpp"],
                     help="star: the headline single-layout batch; multi: 64 layouts in one launch sequence; "
                          "proxy: gradient separation of colliding candidates vs random resampling; "
                          "lbf: LBF-style build on the device-resident engine; "
-                         "prep: poi + surrogate poles of 1024 item shapes on the device")
+                         "prep: poi + surrogate poles of 1024 item shapes on the device; "
+                         "bpp: bin packing with lbf's bin-packing optimizer")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -939,6 +1001,8 @@ def main():
         return run_lbf(args)
     if args.workload == "prep":
         return run_prep(args)
+    if args.workload == "bpp":
+        return run_bpp(args)
     return run_gpu(args)
 
 

@@ -233,6 +233,15 @@ jcde_status jcde_resample_batch(jcde_engine* e, const float* d_params, const uin
  * (order-preserving cost bits << 32) | index, or all ones when no candidate is free. */
 jcde_status jcde_lbf_select(jcde_engine* e, const jcde_query* d_queries, const uint8_t* d_verdicts, uint32_t n,
                             uint64_t* d_best, void* stream);
+/* n candidate placements of one item drawn on the device from the counter-based stream (seed, sid)
+ * — the generator of the LBF build's uniform round (no counterpart in the reference, whose samplers
+ * draw from its own RNG, lbf/src/samplers/uniform_rect_sampler.rs): draw n+i gives the rotation (a
+ * turn u in [0, 1), or one of the n_orient allowed (cos, sin) pairs of d_orient by the draw modulo
+ * n_orient), draws 2n+i and 3n+i the translation, uniform over `box`.  d_turns (may be NULL) gets
+ * each candidate's u (0 for allowed orientations).  Device buffers, stream ordered. */
+jcde_status jcde_gen_candidates(uint64_t seed, uint64_t sid, uint32_t n, uint32_t item, jcde_rect box,
+                                const float* d_orient, uint32_t n_orient, jcde_query* d_queries, double* d_turns,
+                                void* stream);
 
 /* --- Device-resident engine: register / deregister on the GPU ---------------------------------
  * A copy of an engine's quadtree in device pools that single-warp kernels update in place,

@@ -1464,6 +1464,22 @@ static inline uint64_t host_stream_key(uint64_t seed, uint64_t sid) {
     return host_mix64(seed * 0x100000001B3ull + sid * 0x9E3779B97F4A7C15ull);
 }
 
+extern "C" jcde_status jcde_gen_candidates(uint64_t seed, uint64_t sid, uint32_t n, uint32_t item, jcde_rect box,
+                                           const float* d_orient, uint32_t n_orient, jcde_query* d_queries,
+                                           double* d_turns, void* stream) {
+    if (n == 0) return JCDE_OK;
+    if (!d_queries || (n_orient && !d_orient) || !(box.x_min < box.x_max) || !(box.y_min < box.y_max))
+        return JCDE_ERR_ARG;
+    int dev = 0, n_sms = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    CUDA_TRY(cudaDeviceGetAttribute(&n_sms, cudaDevAttrMultiProcessorCount, dev));
+    const float b[4] = {box.x_min, box.y_min, box.x_max, box.y_max};
+    res_launch_gen_candidates(host_stream_key(seed, sid), n, item, b, reinterpret_cast<const float2*>(d_orient),
+                              n_orient, reinterpret_cast<uint32_t*>(d_queries), d_turns, n_sms, (cudaStream_t)stream);
+    CUDA_TRY(cudaGetLastError());
+    return JCDE_OK;
+}
+
 // The resident's ordering buffers hold a batch of n queries (growing them waits for queued work).
 static jcde_status ensure_order_buffers(jcde_resident* r, uint32_t n) {
     if (!r->d_hist.ensure(N_BUCKETS * 4)) return JCDE_ERR_CUDA;

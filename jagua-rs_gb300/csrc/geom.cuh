@@ -211,24 +211,14 @@ JCDE_UNROLL
     return hit;
 }
 
-// edge.rs:63-87 + edge.rs:152-159 — squared distance from p to the segment.
-// The quotient dot / len_sq is only needed where its branch is not already known.  For a finite,
-// nonzero len_sq (so c and d are finite): dot < 0 makes the correctly rounded quotient negative
-// (param < 0: the first endpoint) or -0 (the last branch at x1 + (-0) * c = x1 up to the sign of a
-// zero, which the squares below remove) — the first endpoint either way; dot > 2 len_sq (exact
-// doubling) makes the quotient at least 2 (param > 1: the second endpoint).  Every other case, NaN
-// included, divides as the reference does.
+// edge.rs:63-87 + edge.rs:152-159 — squared distance from p to the segment
 JHD float seg_sq_dist(const Seg& e, Pt p) {
     float x1 = e.s.x, y1 = e.s.y, x2 = e.e.x, y2 = e.e.y;
     float a = p.x - x1, b = p.y - y1, c = x2 - x1, d = y2 - y1;
     float dot = a * c + b * d;
     float len_sq = c * c + d * d;
     float param = -1.0f;
-    if (len_sq != 0.0f) {
-        if (len_sq < INFINITY && dot < 0.0f) param = -1.0f;
-        else if (len_sq < INFINITY && dot > 2.0f * len_sq) param = 2.0f;
-        else param = dot / len_sq;
-    }
+    if (len_sq != 0.0f) param = dot / len_sq;
     float xx, yy;
     if (param < 0.0f) { xx = x1; yy = y1; }
     else if (param > 1.0f) { xx = x2; yy = y2; }

@@ -616,6 +616,42 @@ __device__ __forceinline__ float draw_uniform(unsigned long long key, unsigned l
     return fminf(__fadd_rn(lo, __fmul_rn(draw_f32(key, i), __fsub_rn(hi, lo))), hi_below);
 }
 
+struct GenBox {
+    float x0, x1, x1_below, y0, y1, y1_below;
+};
+
+// Candidate i of n of item t from the stream `key` — make_queries' draws in the workload generator:
+// draw n+i: rotation (turns through sincos_turns, or one of the ocnt allowed (cos, sin) pairs by
+// the draw modulo their count), 2n+i: x, 3n+i: y, uniform over the box.  qu[i] keeps the turns.
+__device__ __forceinline__ void gen_uniform(unsigned long long key, unsigned long long n, uint32_t i, uint32_t t,
+                                            const GenBox& b, const float2* orient, uint32_t ocnt, uint32_t* q,
+                                            double* qu) {
+    float c, s;
+    double u = 0.0;
+    const unsigned long long d = draw(key, n + i);
+    if (ocnt) {
+        const float2 cs = orient[(uint32_t)(d % ocnt)];
+        c = cs.x;
+        s = cs.y;
+    } else {
+        u = (double)(d >> 11) * 0x1p-53;
+        sincos_turns(u, c, s);
+    }
+    uint32_t* r = q + (size_t)i * 5;
+    r[0] = t;
+    r[1] = __float_as_uint(c);
+    r[2] = __float_as_uint(s);
+    r[3] = __float_as_uint(draw_uniform(key, 2 * n + i, b.x0, b.x1, b.x1_below));
+    r[4] = __float_as_uint(draw_uniform(key, 3 * n + i, b.y0, b.y1, b.y1_below));
+    if (qu) qu[i] = u;
+}
+
+__global__ void k_gen_candidates(unsigned long long key, uint32_t n, uint32_t t, GenBox b, const float2* orient,
+                                 uint32_t ocnt, uint32_t* q, double* qu) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        gen_uniform(key, n, i, t, b, orient, ocnt, q, qu);
+}
+
 // Candidates of round `round` of the current step.  Round 0: item type t ~ U{0..T-1} from the type
 // stream (one draw per step), rotation ~ U[0, 2pi) and translation ~ U(box) from the step's own
 // stream — the draws of make_queries in the workload generator (draw n+i: rotation, 2n+i: x,
@@ -642,27 +678,9 @@ __global__ void k_lbf_gen(LbfParams p, LbfDev* __restrict__ st, uint32_t* __rest
     }
     if (round == 0) {
         const unsigned long long key = stream_key(p.seed, (unsigned long long)p.sid_base + step);
-        const unsigned long long n = p.n_cand;
-        for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < p.n_cand; i += gridDim.x * blockDim.x) {
-            float c, s;
-            double u = 0.0;
-            const unsigned long long d = draw(key, n + i);
-            if (ocnt) {   // one of the allowed orientations (draw modulo their count)
-                const float2 cs = p.orient[ooff + (uint32_t)(d % ocnt)];
-                c = cs.x;
-                s = cs.y;
-            } else {
-                u = (double)(d >> 11) * 0x1p-53;
-                sincos_turns(u, c, s);
-            }
-            uint32_t* r = q + (size_t)i * 5;
-            r[0] = t;
-            r[1] = __float_as_uint(c);
-            r[2] = __float_as_uint(s);
-            r[3] = __float_as_uint(draw_uniform(key, 2 * n + i, p.x0, p.x1, p.x1_below));
-            r[4] = __float_as_uint(draw_uniform(key, 3 * n + i, p.y0, p.y1, p.y1_below));
-            qu[i] = u;
-        }
+        const GenBox b{p.x0, p.x1, p.x1_below, p.y0, p.y1, p.y1_below};
+        for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < p.n_cand; i += gridDim.x * blockDim.x)
+            gen_uniform(key, p.n_cand, i, t, b, p.orient + ooff, ocnt, q, qu);
         return;
     }
     const volatile LbfDev* vs = st;
@@ -802,6 +820,13 @@ void res_launch_lbf_gen(const LbfParams& p, LbfDev* st, uint32_t* q, double* qu,
     const uint32_t n = round ? p.ls_cand : p.n_cand;
     const uint32_t grid = std::min<uint32_t>((n + 255) / 256, (uint32_t)std::max(1, n_sms) * 4);
     k_lbf_gen<<<grid, 256, 0, s>>>(p, st, q, qu, round);
+}
+void res_launch_gen_candidates(unsigned long long key, uint32_t n, uint32_t item, const float box[4],
+                               const float2* orient, uint32_t n_orient, uint32_t* q, double* qu, int n_sms,
+                               cudaStream_t s) {
+    const GenBox b{box[0], box[2], std::nextafter(box[2], box[0]), box[1], box[3], std::nextafter(box[3], box[1])};
+    const uint32_t grid = std::min<uint32_t>((n + 255) / 256, (uint32_t)std::max(1, n_sms) * 4);
+    k_gen_candidates<<<std::max(grid, 1u), 256, 0, s>>>(key, n, item, b, orient, n_orient, q, qu);
 }
 void res_launch_lbf_merge(LbfDev* st, const uint32_t* q, const double* qu, uint32_t round, cudaStream_t s) {
     k_lbf_merge<<<1, 32, 0, s>>>(st, q, qu, round);

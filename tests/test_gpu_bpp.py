@@ -1,0 +1,50 @@
+"""Bin packing on the GPU engines (jcde.bpp): the same layouts, placements and skipped items as the
+oracle run, with every search's layouts evaluated in one multi-layout launch sequence or one by one."""
+import numpy as np
+import pytest
+
+from jcde import bpp
+
+gpu = pytest.mark.gpu
+
+
+@gpu
+@pytest.mark.parametrize("ls", [0, 2])
+def test_bpp_matches_oracle(oracle_mod, jcde_mod, ls):
+    import jcde
+
+    inst = bpp.load_bpp(bpp.synthetic_instance(n_types=16, n_bins=4))
+    spec = bpp.BppSpec(n_cand=2048, ls_rounds=ls, ls_cand=512 if ls else 0, ls_sigma_t=50.0, ls_sigma_turns=0.05)
+    ref = bpp.run_bpp(oracle_mod.OracleBackend, bpp.setup_bpp(oracle_mod.OracleBackend, inst), spec)
+    su = bpp.setup_bpp(jcde.GpuBackend, inst)
+    got = bpp.run_bpp(jcde.GpuBackend, su, spec, batched=True)
+    assert got.same_as(ref), (len(got.placements), len(ref.placements), got.layouts, ref.layouts)
+    seq = bpp.run_bpp(jcde.GpuBackend, bpp.setup_bpp(jcde.GpuBackend, inst), spec, batched=False)
+    assert seq.same_as(ref)
+    assert np.isclose(bpp.export_solution(su, got)["density"], bpp.export_solution(su, ref)["density"])
+
+
+@gpu
+def test_device_candidates_equal_host_round(jcde_mod):
+    """jcde_gen_candidates draws the host round's candidates bit for bit (continuous rotation and
+    allowed orientations)."""
+    import torch
+
+    from jcde import instance as I
+    from jcde import workload as W
+    from jcde._ffi import check, jcde_rect, lib
+
+    spec = bpp.BppSpec(n_cand=3000)
+    box = np.array([-5.0, 2.0, 612.5, 480.0], np.float32)
+    for orient in (None, I.orientation_cs([0.0, 90.0, 180.0, 270.0])):
+        q, u = bpp._round(spec, 7, 2049, 3, box, orient)
+        dq = torch.empty(len(q) * W.QUERY_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+        du = torch.empty(len(q), dtype=torch.float64, device="cuda")
+        do = None if orient is None else torch.from_numpy(np.ascontiguousarray(orient)).cuda()
+        check(lib().jcde_gen_candidates(spec.seed, bpp.BPP_SID_BASE + 4096 * 7 + 2049, len(q), 3,
+                                        jcde_rect(*[float(v) for v in box]), None if do is None else do.data_ptr(),
+                                        0 if do is None else len(do), dq.data_ptr(), du.data_ptr(), None), "gen")
+        torch.cuda.synchronize()
+        got = dq.cpu().numpy().view(W.QUERY_DTYPE)
+        assert np.array_equal(got.view(np.uint8), q.view(np.uint8))
+        assert np.array_equal(du.cpu().numpy(), u)
