@@ -177,10 +177,10 @@ static jcde_status upload(DevBuf& b, const void* src, size_t bytes) {
     return JCDE_OK;
 }
 
-// Bring the device mirror up to date with the host quadtree and item table.
+// Bring the device mirror up to date with the host quadtree and item table.  (The hazard-pole
+// grids of the proxy kernels are refreshed separately, by sync_poles, only where they are used.)
 static jcde_status sync_device(jcde_engine* e) {
-    if (e->tree_version == e->tree.version() && !e->items_dirty && e->pole_version == e->tree.pole_version())
-        return JCDE_OK;
+    if (e->tree_version == e->tree.version() && !e->items_dirty) return JCDE_OK;
     // queries already queued on the caller's stream may still read the old image
     if (e->have_last_stream) CUDA_TRY(cudaStreamSynchronize(e->last_stream));
     if (e->tree_version != e->tree.version()) {
@@ -211,7 +211,24 @@ static jcde_status sync_device(jcde_engine* e) {
         e->n_nodes = (uint32_t)e->flat.nodes.size();
         e->tree_version = e->tree.version();
     }
-    if (e->pole_version != e->tree.pole_version()) {
+    if (e->items_dirty) {
+        jcde_status st;
+        if ((st = upload(e->d_items, e->items.data(), e->items.size() * sizeof(DItem)))) return st;
+        if ((st = upload(e->d_iverts, e->iverts.data(), e->iverts.size() * sizeof(float2)))) return st;
+        if ((st = upload(e->d_poles, e->poles.data(), e->poles.size() * sizeof(float4)))) return st;
+        if ((st = upload(e->d_piers, e->piers.data(), e->piers.size() * sizeof(float4)))) return st;
+        e->items_dirty = false;
+    }
+    return JCDE_OK;
+}
+
+// The hazard-pole grids of the pole-overlap proxy (k_proxy, k_separate), rebuilt when the hazards
+// or their poles changed since the last build.
+static jcde_status sync_poles(jcde_engine* e) {
+    if (e->pole_version == e->tree.pole_version()) return JCDE_OK;
+    // proxy launches already queued on the caller's stream may still read the old grids
+    if (e->have_last_stream) CUDA_TRY(cudaStreamSynchronize(e->last_stream));
+    {
         // bin every live hazard pole into each grid cell its bounding box overlaps; a pair of poles
         // is then examined in one cell only, the one holding the low corner of their boxes' overlap
         const auto& hs = e->tree.hazards();
@@ -280,14 +297,6 @@ static jcde_status sync_device(jcde_engine* e) {
         e->hp_g = g;
         e->n_hpoles = np;
         e->pole_version = e->tree.pole_version();
-    }
-    if (e->items_dirty) {
-        jcde_status st;
-        if ((st = upload(e->d_items, e->items.data(), e->items.size() * sizeof(DItem)))) return st;
-        if ((st = upload(e->d_iverts, e->iverts.data(), e->iverts.size() * sizeof(float2)))) return st;
-        if ((st = upload(e->d_poles, e->poles.data(), e->poles.size() * sizeof(float4)))) return st;
-        if ((st = upload(e->d_piers, e->piers.data(), e->piers.size() * sizeof(float4)))) return st;
-        e->items_dirty = false;
     }
     return JCDE_OK;
 }
@@ -1032,8 +1041,7 @@ extern "C" jcde_status jcde_detect_batch_noalloc(jcde_engine* e, const jcde_quer
     const uint32_t n_keys = f ? f->n_ignored : 0u;
     if (n_keys && !f->ignored) return JCDE_ERR_ARG;
     // bringing the device mirror up to date may allocate: it must already be current
-    if (e->tree_version != e->tree.version() || e->items_dirty || e->pole_version != e->tree.pole_version())
-        return JCDE_ERR_STATE;
+    if (e->tree_version != e->tree.version() || e->items_dirty) return JCDE_ERR_STATE;
     const uint32_t words = mask_words(e);
     const size_t keys_b = align256((size_t)n_keys * 4), mask_b = align256((size_t)words * 4);
     const size_t str_b = align256(e->n_nodes);
@@ -1283,6 +1291,7 @@ jcde_status jcde_set_hazard_poles(jcde_engine* e, uint32_t key, const float* xyr
 static jcde_status proxy_prepare(jcde_engine* e, const jcde_filter* f, cudaStream_t s, View& v) {
     jcde_status st = sync_device(e);
     if (st) return st;
+    if ((st = sync_poles(e))) return st;
     init_launch_shape(e);
     v = base_view(e);
     return apply_filter(e, f, s, v);
