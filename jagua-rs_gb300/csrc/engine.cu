@@ -1143,6 +1143,13 @@ static jcde_status multi_prepare(jcde_multi* m, const uint32_t* offsets, const j
     return JCDE_OK;
 }
 
+#ifndef JCDE_MULTI_ORDER_MIN
+#define JCDE_MULTI_ORDER_MIN (1u << 17)   // smaller multi-layout batches are visited in batch order
+#endif
+// Whether the current multi-layout batch is visited in Morton order: the tuned choice, for batches
+// large enough that the ordering launches pay for themselves.
+static bool multi_orders(const jcde_multi* m) { return m->ordered && !m->offs.empty() && m->offs.back() >= JCDE_MULTI_ORDER_MIN; }
+
 template <typename PendT>
 static void multi_launch_t(jcde_multi* m, const uint32_t* q, uint8_t* out, cudaStream_t s) {
     const uint32_t L = (uint32_t)m->engines.size(), n = m->offs[L];
@@ -1150,7 +1157,7 @@ static void multi_launch_t(jcde_multi* m, const uint32_t* q, uint8_t* out, cudaS
     uint32_t* hist = m->d_hist.as<uint32_t>();
     uint32_t* order = nullptr;
     const uint32_t grid = std::min<uint32_t>((n + 255) / 256, (uint32_t)m->n_sms * 8);
-    if (m->ordered) {
+    if (multi_orders(m)) {
         order = m->d_order.as<uint32_t>();
         cudaMemsetAsync(hist, 0, (size_t)L * N_BUCKETS * 4, s);
         k_mbucket_count<<<grid, 256, 0, s>>>(q, n, ms, hist);
@@ -1263,7 +1270,7 @@ jcde_status jcde_multi_detect_graph(jcde_multi* m, const jcde_query* dq, const u
         m->g_offs = m->offs;
     }
     CUDA_TRY(cudaGraphLaunch(m->exec, s));
-    m->launches += m->ordered ? 5 : 2;
+    m->launches += multi_orders(m) ? 5 : 2;
     for (jcde_engine* e : m->engines) {
         e->last_stream = s;
         e->have_last_stream = true;

@@ -238,6 +238,8 @@ class BppLog:
     placements: np.ndarray   # (n, 9) uint32: attempt, layout, bin, item, candidate, cos, sin, tx, ty (f32 bits)
     layouts: list            # bin id per opened layout, in opening order
     unplaced: dict           # item id -> copies left when no layout fitted
+    layout_objs: list = field(default_factory=list)   # the opened Layouts (engines and placed items)
+    judged: int = 0          # candidates judged (all layouts of a batched search, else up to the chosen one)
 
     def same_as(self, other: "BppLog") -> bool:
         return (np.array_equal(self.placements, other.placements) and self.layouts == other.layouts
@@ -329,10 +331,8 @@ def run_bpp(backend, su: BppSetup, spec: BppSpec, batched: bool = True) -> BppLo
                               [int(np.float32(r_q[f]).view(np.uint32)) for f in ("cos", "sin", "tx", "ty")])
             demand[t] -= 1
             attempt += 1
-    log = BppLog(np.array(placements, dtype=np.uint32).reshape(-1, 9), [l.bin for l in layouts], unplaced)
-    log.layout_objs = layouts
-    log.judged = judged
-    return log
+    return BppLog(np.array(placements, dtype=np.uint32).reshape(-1, 9), [l.bin for l in layouts], unplaced, layouts,
+                  judged)
 
 
 class _GpuSearch:
