@@ -371,10 +371,12 @@ jcde_status jcde_spolygon_new(const float* xy, uint32_t n_vertices, float* xy_ou
                               float* area_diam, float* poi);
 /* jcde_spolygon_new without the poi for n shapes at once (host buffers): xy holds the shapes' (x, y)
  * vertices back to back, voff[n + 1] the offsets; xy_out the same layout in internal order, bbox_out
- * 4 per shape, area_diam 2 per shape, status[i] 0 or JCDE_ERR_ARG for an invalid polygon.  Shapes
- * are spread over n_threads host threads (0: one per hardware thread). */
+ * 4 per shape, area_diam 2 per shape, centroid_out (may be NULL) 2 per shape — SPolygon::centroid
+ * (simple_polygon.rs:173-192) of the internal vertices, the importer's centring point
+ * (io/import.rs:214-217) — and status[i] 0 or JCDE_ERR_ARG for an invalid polygon.  Shapes are
+ * spread over n_threads host threads (0: one per hardware thread). */
 jcde_status jcde_spolygon_batch(const float* xy, const uint32_t* voff, uint32_t n, float* xy_out, float* bbox_out,
-                                float* area_diam, int32_t* status, uint32_t n_threads);
+                                float* area_diam, float* centroid_out, int32_t* status, uint32_t n_threads);
 /* poles of an internal shape with the given area and poi; *n_out receives the count (even when > cap) */
 jcde_status jcde_surrogate_poles(const float* xy, uint32_t n_vertices, float area, const float poi[3],
                                  const jcde_config* cfg, float* poles_xyr, uint32_t cap, uint32_t* n_out);

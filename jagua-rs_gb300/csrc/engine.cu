@@ -896,8 +896,23 @@ jcde_status jcde_spolygon_new(const float* xy, uint32_t nv, float* xy_out, float
     return JCDE_OK;
 }
 
+// SPolygon::centroid (simple_polygon.rs:173-192): sequential float32 sums over the edges
+static void polygon_centroid(const float* xy, uint32_t nv, float area, float* out2) {
+    float cx = 0.0f, cy = 0.0f;
+    for (uint32_t i = 0; i < nv; i++) {
+        const uint32_t j = i + 1 == nv ? 0 : i + 1;
+        const float xi = xy[2 * i], yi = xy[2 * i + 1], xj = xy[2 * j], yj = xy[2 * j + 1];
+        const float cr = xi * yj - xj * yi;
+        cx = cx + (xi + xj) * cr;
+        cy = cy + (yi + yj) * cr;
+    }
+    const float six_a = 6.0f * area;
+    out2[0] = cx / six_a;
+    out2[1] = cy / six_a;
+}
+
 jcde_status jcde_spolygon_batch(const float* xy, const uint32_t* voff, uint32_t n, float* xy_out, float* bbox_out,
-                                float* area_diam, int32_t* status, uint32_t n_threads) {
+                                float* area_diam, float* centroid_out, int32_t* status, uint32_t n_threads) {
     if (n && (!xy || !voff || !xy_out || !bbox_out || !area_diam || !status)) return JCDE_ERR_ARG;
     if (n_threads == 0) n_threads = std::max(1u, std::thread::hardware_concurrency());
     n_threads = std::min<uint32_t>(n_threads, std::max<uint32_t>(1u, n / 8));
@@ -908,6 +923,8 @@ jcde_status jcde_spolygon_batch(const float* xy, const uint32_t* voff, uint32_t 
             status[i] = nv < 3 ? JCDE_ERR_ARG
                                : jcde_spolygon_new(xy + 2 * (size_t)v0, nv, xy_out + 2 * (size_t)v0, bbox_out + 4 * (size_t)i,
                                                    area_diam + 2 * (size_t)i, nullptr);
+            if (centroid_out && status[i] == JCDE_OK)
+                polygon_centroid(xy_out + 2 * (size_t)v0, nv, area_diam[2 * (size_t)i], centroid_out + 2 * (size_t)i);
         }
     };
     std::vector<std::thread> pool;

@@ -69,7 +69,8 @@ struct PoleShared {
     Box bbox;
     Pt best_c;
     float best_r, total;
-    uint32_t nv, np, n_cells, n_child, first, shape, have, done;
+    uint32_t first2[2];   // first cell reaching a chunk's maximum, alternating between chunks
+    uint32_t nv, np, shape, have, done;
     int32_t err;
 };
 
@@ -78,6 +79,10 @@ __device__ __forceinline__ Box box_of(const float4& f) { return Box{f.x, f.y, f.
 
 // compute_pole (pole.rs:52-77) over the shape and poles in shared memory; the result lands in
 // sh.best_c / sh.best_r with sh.have, or sh.err is set.  Called by every thread of the CTA.
+// The queue's state (running best, children count) is kept by every thread in registers, updated
+// identically from shared values, so a chunk of cells costs three barriers: after the scores,
+// after the warp maxima, after the split counts.  The first-maximum slot alternates between two
+// words, so the reset of one never races with a late read of the other.
 template <int PP_THREADS>
 __device__ void compute_pole(PoleShared<PP_THREADS>& sh, const float2* v, const float4* poles, float4* lvl_a,
                              float4* lvl_b) {
@@ -86,22 +91,22 @@ __device__ void compute_pole(PoleShared<PP_THREADS>& sh, const float2* v, const 
     const uint32_t below = (1u << lane) - 1u;
     if (tid == 0) {
         lvl_a[0] = box4(box_square(sh.bbox));
-        sh.n_cells = 1;
-        sh.best_r = 0.0f;
-        sh.have = 0;
-        sh.first = PP_THREADS;
+        sh.first2[0] = PP_THREADS;
+        sh.first2[1] = PP_THREADS;
     }
     __syncthreads();
     const uint32_t nv = sh.nv, np = sh.np;
     const Box bb = sh.bbox;
-    for (int lev = PP_DEPTH; lev >= 0; lev--) {
-        const uint32_t n = sh.n_cells;
-        if (n == 0 || sh.err) break;
+    float best_r = 0.0f;            // the queue's best so far (0 before any: pole.rs:57)
+    Pt best_c{0.f, 0.f};
+    bool have = false, overflow = false;
+    uint32_t n = 1, parity = 0;
+    for (int lev = PP_DEPTH; lev >= 0 && n > 0 && !overflow; lev--) {
         uint32_t G = 32;
         while (G > 1 && (uint32_t)PP_THREADS / G < n) G >>= 1;
         const uint32_t per = PP_THREADS / G;
-        if (tid == 0) sh.n_child = 0;
-        for (uint32_t c0 = 0; c0 < n; c0 += per) {
+        uint32_t n_child = 0;
+        for (uint32_t c0 = 0; c0 < n; c0 += per, parity ^= 1u) {
             const uint32_t slot = tid / G, lig = tid % G, ci = c0 + slot;
             const bool valid = ci < n;
             Pt c{0.f, 0.f};
@@ -141,7 +146,8 @@ __device__ void compute_pole(PoleShared<PP_THREADS>& sh, const float2* v, const 
                 sh.d[slot] = inside ? dist : -dist;
                 sh.r[slot] = box_diameter(cb) / 2.0f;
             }
-            __syncthreads();
+            __syncthreads();   // A: the chunk's scores
+            if (tid == 0) sh.first2[parity ^ 1u] = PP_THREADS;   // the other word, for the next chunk
             // the queue's running best at each cell of the chunk: an inclusive prefix maximum
             const uint32_t nc = min(per, n - c0);
             const bool mine = (uint32_t)tid < nc;
@@ -153,8 +159,8 @@ __device__ void compute_pole(PoleShared<PP_THREADS>& sh, const float2* v, const 
                 if (lane >= o) m = fmaxf(m, x);
             }
             if (lane == 31) sh.wmax[warp] = m;
-            const float carry = sh.best_r;
-            __syncthreads();
+            __syncthreads();   // B: the warps' maxima
+            const float carry = best_r;
             float pre = carry, all = carry;
             for (int w = 0; w < PP_WARPS; w++) {
                 if (w < warp) pre = fmaxf(pre, sh.wmax[w]);
@@ -166,41 +172,43 @@ __device__ void compute_pole(PoleShared<PP_THREADS>& sh, const float2* v, const 
             const uint32_t bal = __ballot_sync(FULL, split);
             if (lane == 0) sh.wsum[warp] = __popc(bal);
             // strict `>` keeps the first cell reaching the chunk's maximum
-            if (mine && all > carry && dt == all) atomicMin(&sh.first, (uint32_t)tid);
-            __syncthreads();
-            uint32_t base = sh.n_child, total = 0;
+            if (mine && all > carry && dt == all) atomicMin(&sh.first2[parity], (uint32_t)tid);
+            __syncthreads();   // C: the split counts and the first maximum
+            uint32_t base = n_child, total = 0;
             for (int w = 0; w < PP_WARPS; w++) {
                 if (w < warp) base += sh.wsum[w];
                 total += sh.wsum[w];
             }
             base += __popc(bal & below);
-            const bool room = sh.n_child + total <= PP_LEVEL_CAP / 4;
-            if (split && room) {
+            if (n_child + total > PP_LEVEL_CAP / 4) {
+                overflow = true;
+                break;
+            }
+            if (split) {
                 const Box pb = box_of(lvl_a[c0 + tid]);
 #pragma unroll
                 for (int q = 0; q < 4; q++) lvl_b[4 * base + q] = box4(box_quadrant(pb, q));
             }
-            __syncthreads();
-            if (tid == 0) {
-                if (!room) sh.err = PS_LEVEL_CAP;
-                if (all > carry) {
-                    sh.best_r = all;
-                    sh.best_c = box_mid(box_of(lvl_a[c0 + sh.first]));
-                    sh.have = 1;
-                }
-                sh.first = PP_THREADS;
-                sh.n_child += total;
+            if (all > carry) {
+                best_r = all;
+                best_c = box_mid(box_of(lvl_a[c0 + sh.first2[parity]]));
+                have = true;
             }
-            __syncthreads();
-            if (sh.err) break;
+            n_child += total;
         }
+        __syncthreads();   // the next level reads the children written above
         float4* t = lvl_a;
         lvl_a = lvl_b;
         lvl_b = t;
-        if (tid == 0) sh.n_cells = 4 * sh.n_child;   // four quadrants per split cell
-        __syncthreads();
+        n = 4 * n_child;   // four quadrants per split cell
     }
-    if (tid == 0 && !sh.err && !sh.have) sh.err = PS_NO_POLE;
+    if (tid == 0) {
+        if (overflow) sh.err = PS_LEVEL_CAP;
+        else if (!have) sh.err = PS_NO_POLE;
+        sh.best_c = best_c;
+        sh.best_r = best_r;
+        sh.have = have;
+    }
     __syncthreads();
 }
 
@@ -297,7 +305,6 @@ __global__ void __launch_bounds__(PP_THREADS, 1024 / PP_THREADS) k_poles(PoleArg
         if (tid == 0) {
             a.n_out[s] = sh.err ? 0u : np;
             a.status[s] = sh.err ? sh.err : (np > a.cap ? PS_OUT_CAP : PS_OK);
-            sh.first = PP_THREADS;
         }
         __syncthreads();
     }

@@ -179,22 +179,25 @@ def spolygon_shape(raw_xy):
     return xo, bbox, ad[0], ad[1]
 
 
-def spolygon_batch(raw_shapes, n_threads: int = 0):
+def spolygon_batch(raw_shapes, n_threads: int = 0, centroids: bool = False):
     """spolygon_shape of every shape in one call (host threads): packed internal vertices and
-    offsets, (n, 4) bboxes, (n, 2) area / diameter."""
+    offsets, (n, 4) bboxes, (n, 2) area / diameter, and with `centroids` the (n, 2) centroids
+    (SPolygon::centroid, the same float32 sums as workload.centroid_f32)."""
     flat, off = pack(raw_shapes)
     n = len(off) - 1
     xo = np.empty_like(flat)
     bbox = np.empty((n, 4), np.float32)
     ad = np.empty((n, 2), np.float32)
+    cen = np.empty((n, 2), np.float32) if centroids else None
     st = np.empty(n, np.int32)
     f32p, u32p = C.POINTER(C.c_float), C.POINTER(C.c_uint32)
     check(lib().jcde_spolygon_batch(flat.ctypes.data_as(f32p), off.ctypes.data_as(u32p), n, xo.ctypes.data_as(f32p),
-                                    bbox.ctypes.data_as(f32p), ad.ctypes.data_as(f32p), C.c_void_p(st.ctypes.data),
+                                    bbox.ctypes.data_as(f32p), ad.ctypes.data_as(f32p),
+                                    None if cen is None else C.c_void_p(cen.ctypes.data), C.c_void_p(st.ctypes.data),
                                     n_threads), "spolygon_batch")
     if (st != 0).any():
         raise JcdeError(-1, f"spolygon_batch: shape {int(np.flatnonzero(st)[0])} is not a valid simple polygon")
-    return xo, off, bbox, ad
+    return (xo, off, bbox, ad, cen) if centroids else (xo, off, bbox, ad)
 
 
 def import_items(raw_shapes, pole_limits=W.DEFAULT_POLE_LIMITS, n_ff_poles=W.DEFAULT_N_FF_POLES,
@@ -207,12 +210,10 @@ def import_items(raw_shapes, pole_limits=W.DEFAULT_POLE_LIMITS, n_ff_poles=W.DEF
     n = len(raw_shapes)
     if n == 0:
         return []
-    flat, off, _, ad = spolygon_batch(raw_shapes)
-    shapes = [flat[off[i]: off[i + 1]] for i in range(n)]
+    flat, off, _, ad, cent = spolygon_batch(raw_shapes, centroids=True)
     if simplify_tolerance is None:
         b = ShapeBatch(packed=(flat, off))
         poi_d, st = b.poi()
-    cent = W.centroids_f32(shapes, ad[:, 0])   # meanwhile on the host
     # centering_transformation (io/import.rs:214-217) as in workload.import_item, every shape at once
     reps = np.diff(off).astype(np.int64)
     cxy = W.transform_points(flat, 1.0, 0.0, np.repeat(-cent[:, 0], reps), np.repeat(-cent[:, 1], reps))
