@@ -599,7 +599,16 @@ __global__ void __launch_bounds__(SURR_THREADS) k_surrogate_warp(View v, const u
 // The table also keeps, per tabled hazard, the edges whose box meets the shape's box: an edge
 // whose box misses the shape's box misses the box of every edge of the shape, and
 // edge_intersection rejects on those boxes first (edge.rs:188-199), so the other edges cannot be hit.
-constexpr int LT_LEAVES = 8, LT_ENTS = 64, LT_EDGES = 96;
+#ifndef JCDE_LT_LEAVES
+#define JCDE_LT_LEAVES 8
+#endif
+#ifndef JCDE_LT_ENTS
+#define JCDE_LT_ENTS 64
+#endif
+#ifndef JCDE_LT_EDGES
+#define JCDE_LT_EDGES 96
+#endif
+constexpr int LT_LEAVES = JCDE_LT_LEAVES, LT_ENTS = JCDE_LT_ENTS, LT_EDGES = JCDE_LT_EDGES;
 struct LeafTab {
     float4 ff[LT_ENTS];
     uint2 ec[LT_ENTS];   // edge offset, edge count; offset | LT_LOCAL: into `edges` below

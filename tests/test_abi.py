@@ -96,3 +96,47 @@ def test_tuning_round_trip(jcde_mod):
     t2 = eng.get_tuning()
     assert t2["poly_chunk"] == 4 and t2["order_min_batch"] == 0xFFFFFFFF
     assert t2["surrogate_warp_max"] == t["surrogate_warp_max"]
+
+
+def test_batch_prep_and_generator_arguments(jcde_mod):
+    """The device batch entry points of item preparation, simplification and candidate generation
+    check their arguments before any CUDA call: null buffers and bad sizes are JCDE_ERR_ARG, empty
+    batches succeed without touching the device."""
+    from jcde._ffi import jcde_config, jcde_rect, lib
+
+    L = lib()
+    ARG = -1
+    cfg = jcde_config()
+    L.jcde_default_config(C.byref(cfg))
+    # empty batches
+    assert L.jcde_poi_batch(None, None, 0, 3, None, None, None, None, 0, None) == 0
+    assert L.jcde_surrogate_poles_batch(None, None, 0, 3, None, None, C.byref(cfg), None, 1, None, None, None, None, 0,
+                                        None) == 0
+    assert L.jcde_simplify_batch(None, None, 0, 3, None, 0, 0.001, None, None, None, None) == 0
+    assert L.jcde_gen_candidates(1, 2, 0, 0, jcde_rect(0, 0, 1, 1), None, 0, None, None, None) == 0
+    assert L.jcde_poles_workspace_bytes(0, 8, 1) == 0
+    # null buffers, bad sizes, bad config
+    assert L.jcde_poi_batch(None, None, 4, 8, None, None, None, None, 0, None) == ARG
+    assert L.jcde_surrogate_poles_batch(None, None, 4, 8, None, None, None, None, 1, None, None, None, None, 0,
+                                        None) == ARG
+    bad = jcde_config()
+    L.jcde_default_config(C.byref(bad))
+    bad.n_pole_limits = 4
+    assert L.jcde_surrogate_poles_batch(None, None, 0, 3, None, None, C.byref(bad), None, 1, None, None, None, None, 0,
+                                        None) == ARG
+    assert L.jcde_simplify_batch(None, None, 4, 8, None, 0, 0.001, None, None, None, None) == ARG
+    assert L.jcde_gen_candidates(1, 2, 16, 0, jcde_rect(0, 0, 1, 1), None, 0, None, None, None) == ARG
+    assert L.jcde_gen_candidates(1, 2, 16, 0, jcde_rect(1, 0, 1, 1), None, 0, 1024, None, None) == ARG   # empty box
+    assert L.jcde_gen_candidates(1, 2, 16, 0, jcde_rect(0, 0, 1, 1), None, 3, 1024, None, None) == ARG   # no table
+    # the host batch of SPolygon::new: status per shape, no CUDA
+    xy = np.array([[0, 0], [1, 0], [1, 1], [0, 1], [0, 0], [1, 0], [0, 0]], np.float32)
+    off = np.array([0, 4, 7], np.uint32)
+    out = np.zeros_like(xy)
+    bb = np.zeros((2, 4), np.float32)
+    ad = np.zeros((2, 2), np.float32)
+    st = np.zeros(2, np.int32)
+    f32p, u32p = C.POINTER(C.c_float), C.POINTER(C.c_uint32)
+    assert L.jcde_spolygon_batch(xy.ctypes.data_as(f32p), off.ctypes.data_as(u32p), 2, out.ctypes.data_as(f32p),
+                                 bb.ctypes.data_as(f32p), ad.ctypes.data_as(f32p), None, C.c_void_p(st.ctypes.data),
+                                 1) == 0
+    assert st.tolist() == [0, ARG] and ad[0, 0] == 1.0
