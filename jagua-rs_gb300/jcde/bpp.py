@@ -170,8 +170,10 @@ class BppSetup:
 
 
 def setup_bpp(backend, inst: BppInstance, simplify_tolerance=None, depth: int = W.DEFAULT_DEPTH,
-              cd_threshold: int = W.DEFAULT_CD_THRESHOLD) -> BppSetup:
-    items = [W.import_item(backend, it.xy, simplify_tolerance=simplify_tolerance) for it in inst.items]
+              cd_threshold: int = W.DEFAULT_CD_THRESHOLD, device_prep: bool = False) -> BppSetup:
+    """Items and bins imported (see the module notes); `device_prep` imports the items in one
+    jcde.prep batch with the pole searches on the GPU (the same items)."""
+    items = I.import_items(backend, [it.xy for it in inst.items], simplify_tolerance, device_prep)
     bins = []
     for b in inst.bins:
         outer = W.import_static(backend, b.outer, W.EXTERIOR, simplify_tolerance)

@@ -48,3 +48,16 @@ def test_device_candidates_equal_host_round(jcde_mod):
         got = dq.cpu().numpy().view(W.QUERY_DTYPE)
         assert np.array_equal(got.view(np.uint8), q.view(np.uint8))
         assert np.array_equal(du.cpu().numpy(), u)
+
+
+@gpu
+def test_device_prep_setup_equals_host(oracle_mod, jcde_mod):
+    """setup_bpp with the items prepared on the device gives the host preparation's items."""
+    import jcde
+
+    inst = bpp.load_bpp(bpp.synthetic_instance(n_types=10, n_bins=2))
+    a = bpp.setup_bpp(oracle_mod.OracleBackend, inst, simplify_tolerance=0.001)
+    b = bpp.setup_bpp(jcde.GpuBackend, inst, simplify_tolerance=0.001, device_prep=True)
+    for x, y in zip(a.items, b.items):
+        assert np.array_equal(x.xy, y.xy) and np.array_equal(x.poles, y.poles) and np.array_equal(x.poi, y.poi)
+    assert a.order == b.order
