@@ -233,6 +233,11 @@ jcde_status jcde_resample_batch(jcde_engine* e, const float* d_params, const uin
  * (order-preserving cost bits << 32) | index, or all ones when no candidate is free. */
 jcde_status jcde_lbf_select(jcde_engine* e, const jcde_query* d_queries, const uint8_t* d_verdicts, uint32_t n,
                             uint64_t* d_best, void* stream);
+/* jcde_lbf_select for n_segments batches of n queries each, back to back (d_queries + k n,
+ * d_verdicts + k n): d_best[k] is segment k's choice (index within the segment), in one launch.
+ * The engine supplies the item shapes only. */
+jcde_status jcde_lbf_select_segments(jcde_engine* e, const jcde_query* d_queries, const uint8_t* d_verdicts,
+                                     uint32_t n, uint32_t n_segments, uint64_t* d_best, void* stream);
 /* n candidate placements of one item drawn on the device from the counter-based stream (seed, sid)
  * — the generator of the LBF build's uniform round (no counterpart in the reference, whose samplers
  * draw from its own RNG, lbf/src/samplers/uniform_rect_sampler.rs): draw n+i gives the rotation (a
@@ -242,6 +247,11 @@ jcde_status jcde_lbf_select(jcde_engine* e, const jcde_query* d_queries, const u
 jcde_status jcde_gen_candidates(uint64_t seed, uint64_t sid, uint32_t n, uint32_t item, jcde_rect box,
                                 const float* d_orient, uint32_t n_orient, jcde_query* d_queries, double* d_turns,
                                 void* stream);
+/* The same for n_segments streams at once: segment k draws n candidates from stream (seed, sids[k])
+ * over boxes[k] (host arrays) into d_queries + k n and d_turns + k n — one launch per 64 segments. */
+jcde_status jcde_gen_candidates_segments(uint64_t seed, const uint64_t* sids, const jcde_rect* boxes,
+                                         uint32_t n_segments, uint32_t n, uint32_t item, const float* d_orient,
+                                         uint32_t n_orient, jcde_query* d_queries, double* d_turns, void* stream);
 
 /* --- Device-resident engine: register / deregister on the GPU ---------------------------------
  * A copy of an engine's quadtree in device pools that single-warp kernels update in place,

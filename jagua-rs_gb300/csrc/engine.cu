@@ -1415,17 +1415,22 @@ jcde_status jcde_resample_batch(jcde_engine* e, const float* d_params, const uin
 // ---------------------------------------------------------------------------------------------
 extern "C" jcde_status jcde_lbf_select(jcde_engine* e, const jcde_query* d_queries, const uint8_t* d_verdicts,
                                         uint32_t n, uint64_t* d_best, void* stream) {
-    if (!e || !d_best || (n && (!d_queries || !d_verdicts))) return JCDE_ERR_ARG;
+    return jcde_lbf_select_segments(e, d_queries, d_verdicts, n, 1, d_best, stream);
+}
+
+extern "C" jcde_status jcde_lbf_select_segments(jcde_engine* e, const jcde_query* d_queries, const uint8_t* d_verdicts,
+                                                 uint32_t n, uint32_t n_segments, uint64_t* d_best, void* stream) {
+    if (!e || !d_best || n_segments == 0 || n_segments > 65535 || (n && (!d_queries || !d_verdicts))) return JCDE_ERR_ARG;
     cudaStream_t s = (cudaStream_t)stream;
     jcde_status st = sync_device(e);
     if (st) return st;
     init_launch_shape(e);
-    CUDA_TRY(cudaMemsetAsync(d_best, 0xFF, 8, s));
+    CUDA_TRY(cudaMemsetAsync(d_best, 0xFF, 8 * (size_t)n_segments, s));
     if (n == 0) return JCDE_OK;
     const View v = base_view(e);
-    const uint32_t grid = std::min<uint32_t>((n + 7) / 8, (uint32_t)e->n_sms * 8);
-    k_lbf_select<<<grid, 256, 0, s>>>(v, reinterpret_cast<const uint32_t*>(d_queries), d_verdicts, n,
-                                      reinterpret_cast<unsigned long long*>(d_best), nullptr);
+    const uint32_t gx = std::max<uint32_t>(1u, std::min<uint32_t>((n + 7) / 8, (uint32_t)e->n_sms * 8 / n_segments));
+    k_lbf_select<<<dim3(gx, n_segments), 256, 0, s>>>(v, reinterpret_cast<const uint32_t*>(d_queries), d_verdicts, n,
+                                                      reinterpret_cast<unsigned long long*>(d_best), nullptr);
     CUDA_TRY(cudaGetLastError());
     e->launches++;
     e->last_stream = s;
@@ -1500,16 +1505,36 @@ static inline uint64_t host_stream_key(uint64_t seed, uint64_t sid) {
 extern "C" jcde_status jcde_gen_candidates(uint64_t seed, uint64_t sid, uint32_t n, uint32_t item, jcde_rect box,
                                            const float* d_orient, uint32_t n_orient, jcde_query* d_queries,
                                            double* d_turns, void* stream) {
-    if (n == 0) return JCDE_OK;
-    if (!d_queries || (n_orient && !d_orient) || !(box.x_min < box.x_max) || !(box.y_min < box.y_max))
-        return JCDE_ERR_ARG;
+    return jcde_gen_candidates_segments(seed, &sid, &box, 1, n, item, d_orient, n_orient, d_queries, d_turns, stream);
+}
+
+extern "C" jcde_status jcde_gen_candidates_segments(uint64_t seed, const uint64_t* sids, const jcde_rect* boxes,
+                                                    uint32_t n_segments, uint32_t n, uint32_t item, const float* d_orient,
+                                                    uint32_t n_orient, jcde_query* d_queries, double* d_turns,
+                                                    void* stream) {
+    if (n == 0 || n_segments == 0) return JCDE_OK;
+    if (!sids || !boxes || !d_queries || (n_orient && !d_orient)) return JCDE_ERR_ARG;
+    for (uint32_t k = 0; k < n_segments; k++)
+        if (!(boxes[k].x_min < boxes[k].x_max) || !(boxes[k].y_min < boxes[k].y_max)) return JCDE_ERR_ARG;
     int dev = 0, n_sms = 0;
     CUDA_TRY(cudaGetDevice(&dev));
     CUDA_TRY(cudaDeviceGetAttribute(&n_sms, cudaDevAttrMultiProcessorCount, dev));
-    const float b[4] = {box.x_min, box.y_min, box.x_max, box.y_max};
-    res_launch_gen_candidates(host_stream_key(seed, sid), n, item, b, reinterpret_cast<const float2*>(d_orient),
-                              n_orient, reinterpret_cast<uint32_t*>(d_queries), d_turns, n_sms, (cudaStream_t)stream);
-    CUDA_TRY(cudaGetLastError());
+    for (uint32_t k0 = 0; k0 < n_segments; k0 += RES_GEN_SEGMENTS) {   // segments by kernel-parameter batches
+        const uint32_t m = std::min<uint32_t>(RES_GEN_SEGMENTS, n_segments - k0);
+        unsigned long long keys[RES_GEN_SEGMENTS];
+        float bx[RES_GEN_SEGMENTS][4];
+        for (uint32_t k = 0; k < m; k++) {
+            keys[k] = host_stream_key(seed, sids[k0 + k]);
+            bx[k][0] = boxes[k0 + k].x_min;
+            bx[k][1] = boxes[k0 + k].y_min;
+            bx[k][2] = boxes[k0 + k].x_max;
+            bx[k][3] = boxes[k0 + k].y_max;
+        }
+        res_launch_gen_candidates(keys, bx, m, n, item, reinterpret_cast<const float2*>(d_orient), n_orient,
+                                  reinterpret_cast<uint32_t*>(d_queries + (size_t)k0 * n),
+                                  d_turns ? d_turns + (size_t)k0 * n : nullptr, n_sms, (cudaStream_t)stream);
+        CUDA_TRY(cudaGetLastError());
+    }
     return JCDE_OK;
 }
 

@@ -1584,8 +1584,14 @@ __global__ void k_resample(const float* __restrict__ params, const uint32_t* __r
 // transformed shape's bounding box, the lowest index among equal costs (the strict `<` of
 // search.rs:52 keeps the first best).  Costs are mapped to order-preserving integers and
 // packed with the index into one 64-bit atomicMin.
+// With a grid of several rows (blockIdx.y), row y chooses among its own segment of n queries
+// (queries, verdicts and the result word offset by y): one launch for several batches.
 __global__ void k_lbf_select(View v, const uint32_t* __restrict__ q, const uint8_t* __restrict__ verdicts, uint32_t n,
                              unsigned long long* __restrict__ best, uint32_t* __restrict__ n_free) {
+    q += (size_t)blockIdx.y * n * 5;
+    verdicts += (size_t)blockIdx.y * n;
+    best += blockIdx.y;
+    if (n_free) n_free += blockIdx.y;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t wpb = blockDim.x >> 5;
     __shared__ unsigned long long s_best;

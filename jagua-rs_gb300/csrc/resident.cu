@@ -646,10 +646,18 @@ __device__ __forceinline__ void gen_uniform(unsigned long long key, unsigned lon
     if (qu) qu[i] = u;
 }
 
-__global__ void k_gen_candidates(unsigned long long key, uint32_t n, uint32_t t, GenBox b, const float2* orient,
-                                 uint32_t ocnt, uint32_t* q, double* qu) {
+struct GenSegs {   // per segment (blockIdx.y): stream key and box, passed by value
+    unsigned long long key[RES_GEN_SEGMENTS];
+    GenBox box[RES_GEN_SEGMENTS];
+};
+
+__global__ void k_gen_candidates(GenSegs g, uint32_t n, uint32_t t, const float2* orient, uint32_t ocnt, uint32_t* q,
+                                 double* qu) {
+    const uint32_t k = blockIdx.y;
+    uint32_t* qk = q + (size_t)k * n * 5;
+    double* uk = qu ? qu + (size_t)k * n : nullptr;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        gen_uniform(key, n, i, t, b, orient, ocnt, q, qu);
+        gen_uniform(g.key[k], n, i, t, g.box[k], orient, ocnt, qk, uk);
 }
 
 // Candidates of round `round` of the current step.  Round 0: item type t ~ U{0..T-1} from the type
@@ -821,12 +829,18 @@ void res_launch_lbf_gen(const LbfParams& p, LbfDev* st, uint32_t* q, double* qu,
     const uint32_t grid = std::min<uint32_t>((n + 255) / 256, (uint32_t)std::max(1, n_sms) * 4);
     k_lbf_gen<<<grid, 256, 0, s>>>(p, st, q, qu, round);
 }
-void res_launch_gen_candidates(unsigned long long key, uint32_t n, uint32_t item, const float box[4],
-                               const float2* orient, uint32_t n_orient, uint32_t* q, double* qu, int n_sms,
-                               cudaStream_t s) {
-    const GenBox b{box[0], box[2], std::nextafter(box[2], box[0]), box[1], box[3], std::nextafter(box[3], box[1])};
-    const uint32_t grid = std::min<uint32_t>((n + 255) / 256, (uint32_t)std::max(1, n_sms) * 4);
-    k_gen_candidates<<<std::max(grid, 1u), 256, 0, s>>>(key, n, item, b, orient, n_orient, q, qu);
+void res_launch_gen_candidates(const unsigned long long* keys, const float (*bx)[4], uint32_t m, uint32_t n,
+                               uint32_t item, const float2* orient, uint32_t n_orient, uint32_t* q, double* qu,
+                               int n_sms, cudaStream_t s) {
+    GenSegs g;
+    for (uint32_t k = 0; k < m; k++) {
+        g.key[k] = keys[k];
+        g.box[k] = GenBox{bx[k][0], bx[k][2], std::nextafter(bx[k][2], bx[k][0]),
+                          bx[k][1], bx[k][3], std::nextafter(bx[k][3], bx[k][1])};
+    }
+    const uint32_t per_seg = std::max<uint32_t>(1u, (uint32_t)std::max(1, n_sms) * 4 / m);
+    const uint32_t gx = std::max<uint32_t>(1u, std::min<uint32_t>((n + 255) / 256, per_seg));
+    k_gen_candidates<<<dim3(gx, m), 256, 0, s>>>(g, n, item, orient, n_orient, q, qu);
 }
 void res_launch_lbf_merge(LbfDev* st, const uint32_t* q, const double* qu, uint32_t round, cudaStream_t s) {
     k_lbf_merge<<<1, 32, 0, s>>>(st, q, qu, round);

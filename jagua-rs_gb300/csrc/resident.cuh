@@ -132,10 +132,12 @@ void res_launch_init(const RTree& t, const float2* verts, const uint4* recs, con
 void res_launch_insert_placed(const RTree& t, const DItem* items, const float2* iverts, uint32_t n_items,
                               const uint32_t* q, uint32_t* out_key, cudaStream_t s);
 void res_launch_remove(const RTree& t, const uint32_t* key, cudaStream_t s);
-// n candidates of one item from the stream with key `key` (the LBF build's uniform round)
-void res_launch_gen_candidates(unsigned long long key, uint32_t n, uint32_t item, const float box[4],
-                               const float2* orient, uint32_t n_orient, uint32_t* q, double* qu, int n_sms,
-                               cudaStream_t s);
+// n candidates of one item per segment k < m, from the stream with key keys[k] over box bx[k] (the
+// LBF build's uniform round), written at q + k n (5 words each) and qu + k n
+constexpr uint32_t RES_GEN_SEGMENTS = 64;
+void res_launch_gen_candidates(const unsigned long long* keys, const float (*bx)[4], uint32_t m, uint32_t n,
+                               uint32_t item, const float2* orient, uint32_t n_orient, uint32_t* q, double* qu,
+                               int n_sms, cudaStream_t s);
 void res_launch_lbf_gen(const LbfParams& p, LbfDev* st, uint32_t* q, double* qu, uint32_t round, int n_sms,
                         cudaStream_t s);
 void res_launch_lbf_merge(LbfDev* st, const uint32_t* q, const double* qu, uint32_t round, cudaStream_t s);

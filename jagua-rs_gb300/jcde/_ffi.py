@@ -105,6 +105,9 @@ SIGNATURES = {
     "jcde_spolygon_batch": (C.c_int32, [f32p, u32p, C.c_uint32, f32p, f32p, f32p, P, P, C.c_uint32]),
     "jcde_simplify_batch": (C.c_int32, [P, P, C.c_uint32, C.c_uint32, P, C.c_int, C.c_float, P, P, P, P]),
     "jcde_gen_candidates": (C.c_int32, [C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint32, jcde_rect, P, C.c_uint32, P, P, P]),
+    "jcde_gen_candidates_segments": (C.c_int32, [C.c_uint64, P, P, C.c_uint32, C.c_uint32, C.c_uint32, P, C.c_uint32, P,
+                                                 P, P]),
+    "jcde_lbf_select_segments": (C.c_int32, [P, P, P, C.c_uint32, C.c_uint32, P, P]),
     "jcde_poles_workspace_bytes": (C.c_uint64, [C.c_uint32, C.c_uint32, C.c_int]),
     "jcde_poi_batch": (C.c_int32, [P, P, C.c_uint32, C.c_uint32, P, P, P, P, C.c_uint64, P]),
     "jcde_surrogate_poles_batch": (C.c_int32, [P, P, C.c_uint32, C.c_uint32, P, P, C.POINTER(jcde_config), P, C.c_uint32,

@@ -375,20 +375,18 @@ class _GpuSearch:
         L, n, qs = len(slots), self.n, W.QUERY_DTYPE.itemsize
         sh = _stream_handle(None)
         o = self.orient[t]
-        for j, (slot, _, _, b) in enumerate(slots):
-            bx = su.bins[b].box
-            rect = jcde_rect(float(bx[0]), float(bx[1]), float(bx[2]), float(bx[3]))
-            check(lib().jcde_gen_candidates(spec.seed, BPP_SID_BASE + 4096 * attempt + slot, n, t, rect,
-                                            None if o is None else o.data_ptr(), 0 if o is None else len(o),
-                                            self.dq.data_ptr() + j * n * qs, self.du.data_ptr() + j * n * 8, sh),
-                  "gen_candidates")
+        sids = (C.c_uint64 * L)(*[BPP_SID_BASE + 4096 * attempt + slot for slot, _, _, _ in slots])
+        rects = (jcde_rect * L)(*[jcde_rect(*[float(x) for x in su.bins[b].box]) for _, _, _, b in slots])
+        check(lib().jcde_gen_candidates_segments(spec.seed, sids, rects, L, n, t, None if o is None else o.data_ptr(),
+                                                 0 if o is None else len(o), self.dq.data_ptr(), self.du.data_ptr(),
+                                                 sh), "gen_candidates_segments")
         cdes = [e.eng for _, e, _, _ in slots]
         offs = np.arange(L + 1, dtype=np.uint32) * np.uint32(n)
         self._group(cdes).detect(self.dq[: L * n * qs], offs, filters=[list(f) if f else [] for f in filts],
                                  out=self.dv[: L * n])
-        for j, cde in enumerate(cdes):
-            check(lib().jcde_lbf_select(cde.h, self.dq.data_ptr() + j * n * qs, self.dv.data_ptr() + j * n, n,
-                                        self.best.data_ptr() + 8 * j, sh), "lbf_select")
+        # every engine holds the same items: one of them serves the choice of all segments
+        check(lib().jcde_lbf_select_segments(cdes[0].h, self.dq.data_ptr(), self.dv.data_ptr(), n, L,
+                                             self.best.data_ptr(), sh), "lbf_select_segments")
         best = self.best[:L].cpu().numpy().view(np.uint64)
         for j in range(L):
             if best[j] != np.uint64(0xFFFFFFFFFFFFFFFF):
