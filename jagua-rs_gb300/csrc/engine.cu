@@ -457,8 +457,8 @@ static bool launch_passes_t(jcde_engine* e, const View& v, const uint32_t* q, ui
         const uint8_t miss = mode == 1 ? (uint8_t)0 : PENDING;
         cudaEvent_t pa = prof_begin(e, s);
         if (n <= e->tune.surrogate_warp_max) {   // too few queries to fill the GPU one thread each
-            const uint32_t wpb = SURR_THREADS / 32;
-            const uint32_t grid = std::min<uint32_t>((n + wpb - 1) / wpb, (uint32_t)e->n_sms * 8);
+            const uint32_t gpb = SURR_THREADS / JCDE_SURR_GROUP;   // query groups per block
+            const uint32_t grid = std::min<uint32_t>((n + gpb - 1) / gpb, (uint32_t)e->n_sms * 8);
             k_surrogate_warp<PendT><<<grid, SURR_THREADS, 0, s>>>(v, q, n, dout, miss, order);
         } else if (JCDE_SURR_DYNAMIC && next && cudaMemsetAsync(next, 0, 4, s) == cudaSuccess) {
             // persistent blocks; each warp takes the next 32 queries from a counter as it finishes

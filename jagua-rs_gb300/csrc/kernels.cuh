@@ -427,6 +427,15 @@ constexpr int MODE_SURROGATE = 1;
 constexpr int MODE_POLY = 2;
 constexpr int POLY_WARPS = 8;
 constexpr int SURR_THREADS = 256;
+// Blocks per SM the surrogate passes are compiled for (the register budget): 0 leaves it to ptxas.
+#ifndef JCDE_SURR_MIN_BLOCKS
+#define JCDE_SURR_MIN_BLOCKS 0
+#endif
+#if JCDE_SURR_MIN_BLOCKS > 0
+#define JCDE_SURR_BOUNDS __launch_bounds__(SURR_THREADS, JCDE_SURR_MIN_BLOCKS)
+#else
+#define JCDE_SURR_BOUNDS __launch_bounds__(SURR_THREADS)
+#endif
 constexpr uint8_t PENDING = 0xFFu;   // verdict slot of a query the surrogate pass left undecided
 
 // Surrogate pass — CDEngine::detect_surrogate_collision (cd_engine.rs:204-223), one thread per
@@ -478,7 +487,7 @@ __device__ __forceinline__ void surrogate_query(const View& v, const uint32_t* _
 }
 
 template <typename PendT, bool MULTI>
-__global__ void __launch_bounds__(SURR_THREADS) k_surrogate(View v, MultiSrc ms, const uint32_t* __restrict__ q,
+__global__ void JCDE_SURR_BOUNDS k_surrogate(View v, MultiSrc ms, const uint32_t* __restrict__ q,
                                                             uint32_t n, uint8_t* __restrict__ out, uint8_t miss,
                                                             const uint32_t* __restrict__ order,
                                                             uint32_t* __restrict__ next) {
@@ -506,14 +515,28 @@ __global__ void __launch_bounds__(SURR_THREADS) k_surrogate(View v, MultiSrc ms,
     }
 }
 
-// The surrogate pass with one warp per query, for batches too small to fill the GPU with one
-// thread per query (each query's walk then sets the batch's latency).  The warp follows each
-// probe's walk together; at a leaf its lanes test the node's hazards' ff boxes 32 at a time, then
-// the edges of every hazard whose box the probe hits, 32 at a time.  Same tests, same verdict.
-template <class P>
-__device__ __forceinline__ bool leaf_hits_warp(const View& v, const P& p, const DNode& nd, int lane) {
-    for (uint32_t b = 0; b < nd.hz_cnt; b += 32) {
-        const uint32_t k = b + lane;
+// The surrogate pass with a group of G lanes per query (a warp at G = 32), for batches too small to
+// fill the GPU with one thread per query (each query's walk then sets the batch's latency).  The
+// group follows each probe's walk together; at a leaf its lanes test the node's hazards' ff boxes
+// G at a time, then the edges of every hazard whose box the probe hits, G at a time.  Same tests,
+// same verdict.  Groups of one warp run their own queries independently (group-masked votes).
+#ifndef JCDE_SURR_GROUP
+#define JCDE_SURR_GROUP 32   // lanes per query in the small-batch surrogate pass
+#endif
+template <int G>
+struct LaneGroup {
+    static_assert(G == 1 || G == 2 || G == 4 || G == 8 || G == 16 || G == 32, "group sizes divide a warp");
+    uint32_t lig, base;
+    unsigned mask;
+    __device__ __forceinline__ explicit LaneGroup(int lane)
+        : lig((uint32_t)lane % G), base((uint32_t)lane - (uint32_t)lane % G),
+          mask(G == 32 ? FULL : (((1u << (G & 31)) - 1u) << ((uint32_t)lane - (uint32_t)lane % G))) {}
+};
+
+template <class P, int G>
+__device__ __forceinline__ bool leaf_hits_group(const View& v, const P& p, const DNode& nd, const LaneGroup<G>& g) {
+    for (uint32_t b = 0; b < nd.hz_cnt; b += G) {
+        const uint32_t k = b + g.lig;
         uint32_t eo = 0, ec = 0;
         bool cand = false;
         if (k < nd.hz_cnt) {
@@ -522,22 +545,23 @@ __device__ __forceinline__ bool leaf_hits_warp(const View& v, const P& p, const 
             eo = e.edge_off;
             ec = e.edge_cnt;
         }
-        uint32_t m = __ballot_sync(FULL, cand);
+        uint32_t m = __ballot_sync(g.mask, cand) >> g.base;   // the group's lanes, from bit 0
         while (m) {
             const int src = __ffs(m) - 1;
             m &= m - 1;
-            const uint32_t off = __shfl_sync(FULL, eo, src), cnt = __shfl_sync(FULL, ec, src);
-            for (uint32_t jb = 0; jb < cnt; jb += 32) {
-                const uint32_t j = jb + lane;
-                if (__any_sync(FULL, j < cnt && p_hits_seg(p, ld_edge(v, off + j)))) return true;
+            const uint32_t off = __shfl_sync(g.mask, eo, (int)g.base + src);
+            const uint32_t cnt = __shfl_sync(g.mask, ec, (int)g.base + src);
+            for (uint32_t jb = 0; jb < cnt; jb += G) {
+                const uint32_t j = jb + g.lig;
+                if (__any_sync(g.mask, j < cnt && p_hits_seg(p, ld_edge(v, off + j)))) return true;
             }
         }
     }
     return false;
 }
 
-template <class P, typename PendT>
-__device__ __forceinline__ bool walk_warp(const View& v, const P& p, int lane) {
+template <class P, typename PendT, int G>
+__device__ __forceinline__ bool walk_group(const View& v, const P& p, const LaneGroup<G>& g) {
     WalkT<PendT> w{0, 0, 0, (PendT)0};
     while (w.node >= 0) {
         const uint32_t st = __ldg(&v.strength[w.node]);
@@ -547,7 +571,7 @@ __device__ __forceinline__ bool walk_warp(const View& v, const P& p, int lane) {
             if (nd.child >= 0) {
                 const uint32_t m = p_quad_mask(p, nd.box);
                 if (m) walk_push(w, m, nd.child);
-            } else if (leaf_hits_warp(v, p, nd, lane)) {
+            } else if (leaf_hits_group<P, G>(v, p, nd, g)) {
                 return true;
             }
         }
@@ -556,18 +580,18 @@ __device__ __forceinline__ bool walk_warp(const View& v, const P& p, int lane) {
     return false;
 }
 
-template <typename PendT>
-__global__ void __launch_bounds__(SURR_THREADS) k_surrogate_warp(View v, const uint32_t* __restrict__ q, uint32_t n,
+template <typename PendT, int G = JCDE_SURR_GROUP>
+__global__ void JCDE_SURR_BOUNDS k_surrogate_warp(View v, const uint32_t* __restrict__ q, uint32_t n,
                                                                  uint8_t* __restrict__ out, uint8_t miss,
                                                                  const uint32_t* __restrict__ order) {
-    const int lane = threadIdx.x & 31;
-    const uint32_t wpb = SURR_THREADS / 32;
-    for (uint32_t i = blockIdx.x * wpb + (threadIdx.x >> 5); i < n; i += gridDim.x * wpb) {
+    const LaneGroup<G> g(threadIdx.x & 31);
+    constexpr uint32_t gpb = SURR_THREADS / G;   // groups per block
+    for (uint32_t i = blockIdx.x * gpb + threadIdx.x / G; i < n; i += gridDim.x * gpb) {
         const uint32_t qi = order ? __ldg(&order[i]) : i;
         const uint32_t* w5 = q + (size_t)qi * 5;
         const uint32_t item = __ldg(&w5[0]);
         if (item >= v.n_items) {
-            if (lane == 0) out[qi] = 2;
+            if (g.lig == 0) out[qi] = 2;
             continue;
         }
         const float c = __uint_as_float(__ldg(&w5[1])), s = __uint_as_float(__ldg(&w5[2]));
@@ -576,14 +600,14 @@ __global__ void __launch_bounds__(SURR_THREADS) k_surrogate_warp(View v, const u
         bool hit = false;
         for (uint32_t p = 0; p < it.n_ff_poles && !hit; p++) {
             const float4 pl = __ldg(&v.poles[it.pole_off + p]);
-            hit = walk_warp<Disk, PendT>(v, Disk{xform(Pt{pl.x, pl.y}, c, s, tx, ty), pl.z}, lane);
+            hit = walk_group<Disk, PendT, G>(v, Disk{xform(Pt{pl.x, pl.y}, c, s, tx, ty), pl.z}, g);
         }
         for (uint32_t p = 0; p < it.n_piers && !hit; p++) {
             const float4 pr = __ldg(&v.piers[it.pier_off + p]);
-            hit = walk_warp<Seg, PendT>(v, Seg{xform(Pt{pr.x, pr.y}, c, s, tx, ty), xform(Pt{pr.z, pr.w}, c, s, tx, ty)},
-                                        lane);
+            hit = walk_group<Seg, PendT, G>(v, Seg{xform(Pt{pr.x, pr.y}, c, s, tx, ty), xform(Pt{pr.z, pr.w}, c, s, tx, ty)},
+                                            g);
         }
-        if (lane == 0) out[qi] = hit ? (uint8_t)1 : miss;
+        if (g.lig == 0) out[qi] = hit ? (uint8_t)1 : miss;
     }
 }
 
@@ -1013,7 +1037,15 @@ constexpr int COLLECT_WARPS = 4;
 
 // Collect: sorted colliding hazard keys per query, compacted with one atomicAdd per query.
 template <int MODE>
-__global__ void __launch_bounds__(COLLECT_WARPS * 32) k_collect(View v, const uint32_t* __restrict__ q, uint32_t n,
+#ifndef JCDE_COLLECT_MIN_BLOCKS
+#define JCDE_COLLECT_MIN_BLOCKS 0   // blocks per SM the collect pass is compiled for (0: ptxas decides)
+#endif
+#if JCDE_COLLECT_MIN_BLOCKS > 0
+#define JCDE_COLLECT_BOUNDS __launch_bounds__(COLLECT_WARPS * 32, JCDE_COLLECT_MIN_BLOCKS)
+#else
+#define JCDE_COLLECT_BOUNDS __launch_bounds__(COLLECT_WARPS * 32)
+#endif
+__global__ void JCDE_COLLECT_BOUNDS k_collect(View v, const uint32_t* __restrict__ q, uint32_t n,
                                                                 uint32_t words, uint32_t* __restrict__ offsets,
                                                                 uint32_t* __restrict__ counts, uint32_t* __restrict__ ids,
                                                                 uint32_t cap, uint32_t* __restrict__ total, RawShape raw,
