@@ -836,9 +836,11 @@ def run_bpp(args):
 
 def run_lbf(args):
     """The LBF-style strip build on the device-resident engine.  2000 steps, each: 16384
-    candidates generated, judged (surrogate + polygon passes), the least-cost free one registered on
-    the device, and a random placed item deregistered every 50 steps.  A timed step is one whole build
-    from the strip's initial state.  Metric: candidate placements judged per second over the build."""
+    candidates generated and searched as lbf's search does (surrogate pass for all; the polygon pass
+    for those that could still beat the best free one, search.rs:52-56), the least-cost free one
+    registered on the device, and a random placed item deregistered every 50 steps.  A timed step is
+    one whole build from the strip's initial state.  Metric: candidate placements searched per
+    second over the build."""
     import torch
 
     import jcde
@@ -931,7 +933,7 @@ def run_lbf(args):
     host_s = time.perf_counter() - t0
     host_ok = bool(np.array_equal(hlog.placements, d["placements"][: len(hlog.placements)]))
     line = {
-        "metric": "LBF candidate placements judged per second (device-resident build)",
+        "metric": "LBF candidate placements searched per second (device-resident build)",
         "value": value, "unit": "candidates/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic",

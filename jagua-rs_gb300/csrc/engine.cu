@@ -448,10 +448,13 @@ static const uint32_t* spatial_order_into(jcde_engine* e, const uint32_t* q, uin
 // depth <= 8 and 64-bit above.  Batches of at most JCDE_SURR_WARP_MAX queries take the
 // warp-per-query surrogate pass.
 
+// With `n_pending`, the surrogate pass counts the queries it leaves to the polygon pass; with `best`
+// the small-batch polygon pass makes the LBF choice, and with `skip` it leaves unjudged the queries
+// that can no longer win it.
 template <typename PendT>
 static bool launch_passes_t(jcde_engine* e, const View& v, const uint32_t* q, uint32_t n, uint8_t* dout,
                             cudaStream_t s, RawShape raw, int mode, const uint32_t* order, uint32_t* next,
-                            unsigned long long* best, uint32_t* n_free) {
+                            unsigned long long* best, uint32_t* n_pending, bool skip) {
     bool chose = false;
     if (mode & 1) {
         const uint8_t miss = mode == 1 ? (uint8_t)0 : PENDING;
@@ -459,17 +462,19 @@ static bool launch_passes_t(jcde_engine* e, const View& v, const uint32_t* q, ui
         if (n <= e->tune.surrogate_warp_max) {   // too few queries to fill the GPU one thread each
             const uint32_t gpb = SURR_THREADS / JCDE_SURR_GROUP;   // query groups per block
             const uint32_t grid = std::min<uint32_t>((n + gpb - 1) / gpb, (uint32_t)e->n_sms * 8);
-            k_surrogate_warp<PendT><<<grid, SURR_THREADS, 0, s>>>(v, q, n, dout, miss, order);
+            k_surrogate_warp<PendT><<<grid, SURR_THREADS, 0, s>>>(v, q, n, dout, miss, order, n_pending);
         } else if (JCDE_SURR_DYNAMIC && next && cudaMemsetAsync(next, 0, 4, s) == cudaSuccess) {
             // persistent blocks; each warp takes the next 32 queries from a counter as it finishes
             int per_sm = 0;
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_surrogate<PendT, false>, SURR_THREADS, 0);
             const uint32_t grid = std::min<uint32_t>((n + SURR_THREADS - 1) / SURR_THREADS,
                                                      (uint32_t)e->n_sms * (uint32_t)std::max(per_sm, 1));
-            k_surrogate<PendT, false><<<grid, SURR_THREADS, 0, s>>>(v, MultiSrc{}, q, n, dout, miss, order, next);
+            k_surrogate<PendT, false><<<grid, SURR_THREADS, 0, s>>>(v, MultiSrc{}, q, n, dout, miss, order, next,
+                                                                    n_pending);
         } else {
             const uint32_t grid = (n + SURR_THREADS - 1) / SURR_THREADS;
-            k_surrogate<PendT, false><<<grid, SURR_THREADS, 0, s>>>(v, MultiSrc{}, q, n, dout, miss, order, nullptr);
+            k_surrogate<PendT, false><<<grid, SURR_THREADS, 0, s>>>(v, MultiSrc{}, q, n, dout, miss, order, nullptr,
+                                                                    n_pending);
         }
         prof_end(e, s, pa, JCDE_PROF_SURROGATE);
         e->launches++;
@@ -487,7 +492,7 @@ static bool launch_passes_t(jcde_engine* e, const View& v, const uint32_t* q, ui
         if (tab) {
             grid = std::min<uint32_t>(want, (uint32_t)(e->n_sms * e->tab_blocks_per_sm));
             k_poly_tab<PendT><<<grid, POLY_WARPS * 32, POLY_WARPS * sizeof(LeafTab), s>>>(v, q, n, dout, raw, mode == 3,
-                                                                                        order, next, best, n_free);
+                                                                                        order, next, best, skip);
             chose = best != nullptr;
         } else {
             k_poly<PendT, false><<<grid, POLY_WARPS * 32, 0, s>>>(v, MultiSrc{}, q, n, dout, raw, mode == 3, order, next,
@@ -498,14 +503,15 @@ static bool launch_passes_t(jcde_engine* e, const View& v, const uint32_t* q, ui
     }
     return chose;
 }
-// Returns true when the polygon pass also made the LBF choice into `best` / `n_free` (which it does
-// for batches that take the small-batch kernel; callers launch k_lbf_select otherwise).
+// Returns true when the polygon pass also made the LBF choice into `best` (which it does for
+// batches that take the small-batch kernel; callers launch k_lbf_select otherwise).
 static bool launch_passes(jcde_engine* e, const View& v, const uint32_t* q, uint32_t n, uint8_t* dout,
                           cudaStream_t s, RawShape raw, int mode, const uint32_t* order = nullptr,
-                          uint32_t* next = nullptr, unsigned long long* best = nullptr, uint32_t* n_free = nullptr) {
+                          uint32_t* next = nullptr, unsigned long long* best = nullptr, uint32_t* n_pending = nullptr,
+                          bool skip = false) {
     if (e->cfg.quadtree_depth <= 8)
-        return launch_passes_t<uint32_t>(e, v, q, n, dout, s, raw, mode, order, next, best, n_free);
-    return launch_passes_t<uint64_t>(e, v, q, n, dout, s, raw, mode, order, next, best, n_free);
+        return launch_passes_t<uint32_t>(e, v, q, n, dout, s, raw, mode, order, next, best, n_pending, skip);
+    return launch_passes_t<uint64_t>(e, v, q, n, dout, s, raw, mode, order, next, best, n_pending, skip);
 }
 
 // mode 1: surrogate only; 2: polygon only; 3: surrogate pass, then the polygon pass on the
@@ -1549,14 +1555,15 @@ static jcde_status ensure_order_buffers(jcde_resident* r, uint32_t n) {
 }
 
 static bool resident_detect(jcde_resident* r, const uint32_t* q, uint32_t n, uint8_t* dout, cudaStream_t s,
-                            unsigned long long* best = nullptr, uint32_t* n_free = nullptr) {
+                            unsigned long long* best = nullptr, uint32_t* n_pending = nullptr, bool skip = false) {
     jcde_engine* e = r->e;
     const View v = resident_view(r);
     // small batches (one LBF step's candidates) gain nothing from the visit order
     const uint32_t* order = nullptr;
     if (JCDE_SPATIAL_ORDER && n >= e->tune.order_min_batch && n > e->tune.surrogate_warp_max)
         order = spatial_order_into(e, q, n, s, r->d_hist.as<uint32_t>(), r->d_order.as<uint32_t>());
-    const bool chose = launch_passes(e, v, q, n, dout, s, RawShape{}, 3, order, r->d_next.as<uint32_t>(), best, n_free);
+    const bool chose =
+        launch_passes(e, v, q, n, dout, s, RawShape{}, 3, order, r->d_next.as<uint32_t>(), best, n_pending, skip);
     r->launches += (order ? 3 : 0) + 2;
     return chose;
 }
@@ -1577,12 +1584,15 @@ static void lbf_step(jcde_resident* r, cudaStream_t s) {
         res_launch_lbf_gen(r->lp, st, cand, cu, round, e->n_sms, s);
         prof_end(e, s, pa, JCDE_PROF_LBF);
         r->launches++;
-        // the polygon pass makes the choice itself when it runs its small-batch kernel
-        if (!resident_detect(r, cand, n, verd, s, &st->best, &st->n_free)) {
+        // the polygon pass makes the choice itself when it runs its small-batch kernel, skipping the
+        // candidates that can no longer win unless every verdict is logged; n_free counts the
+        // candidates the surrogate pass leaves to the polygon pass
+        const bool skip = r->lp.vlog_steps == 0;
+        if (!resident_detect(r, cand, n, verd, s, &st->best, &st->n_free, skip)) {
             const View v = resident_view(r);
             const uint32_t grid = std::min<uint32_t>((n + 7) / 8, (uint32_t)e->n_sms * 8);
             pa = prof_begin(e, s);
-            k_lbf_select<<<grid, 256, 0, s>>>(v, cand, verd, n, &st->best, &st->n_free);
+            k_lbf_select<<<grid, 256, 0, s>>>(v, cand, verd, n, &st->best, nullptr);
             prof_end(e, s, pa, JCDE_PROF_LBF);
             r->launches++;
         }

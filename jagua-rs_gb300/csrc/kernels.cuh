@@ -458,9 +458,11 @@ struct MultiSrc {
     }
 };
 
+// With `n_pending`, every query the pass leaves undecided (miss = PENDING) is counted there.
 template <typename PendT>
 __device__ __forceinline__ void surrogate_query(const View& v, const uint32_t* __restrict__ q, uint32_t qi,
-                                                uint8_t* __restrict__ out, uint8_t miss) {
+                                                uint8_t* __restrict__ out, uint8_t miss,
+                                                uint32_t* __restrict__ n_pending = nullptr) {
     const uint32_t* w5 = q + (size_t)qi * 5;
     const uint32_t item = __ldg(&w5[0]);
     const float c = __uint_as_float(__ldg(&w5[1])), s = __uint_as_float(__ldg(&w5[2]));
@@ -484,13 +486,15 @@ __device__ __forceinline__ void surrogate_query(const View& v, const uint32_t* _
         while (w.node >= 0 && !hit) hit = walk_step(v, sg, w, nullptr);
     }
     out[qi] = hit ? (uint8_t)1 : miss;
+    if (n_pending && !hit && miss == PENDING) atomicAdd(n_pending, 1u);
 }
 
 template <typename PendT, bool MULTI>
 __global__ void JCDE_SURR_BOUNDS k_surrogate(View v, MultiSrc ms, const uint32_t* __restrict__ q,
                                                             uint32_t n, uint8_t* __restrict__ out, uint8_t miss,
                                                             const uint32_t* __restrict__ order,
-                                                            uint32_t* __restrict__ next) {
+                                                            uint32_t* __restrict__ next,
+                                                            uint32_t* __restrict__ n_pending = nullptr) {
     if (next) {   // each warp takes the next 32 queries from the counter as it finishes
         const int lane = threadIdx.x & 31;
         for (;;) {
@@ -502,7 +506,7 @@ __global__ void JCDE_SURR_BOUNDS k_surrogate(View v, MultiSrc ms, const uint32_t
             if (i < n) {
                 const uint32_t qi = order ? __ldg(&order[i]) : i;
                 if constexpr (MULTI) surrogate_query<PendT>(ms.views[ms.layout_of(qi)], q, qi, out, miss);
-                else surrogate_query<PendT>(v, q, qi, out, miss);
+                else surrogate_query<PendT>(v, q, qi, out, miss, n_pending);
             }
         }
         return;
@@ -511,7 +515,7 @@ __global__ void JCDE_SURR_BOUNDS k_surrogate(View v, MultiSrc ms, const uint32_t
     for (uint32_t i = blockIdx.x * SURR_THREADS + threadIdx.x; i < n; i += stride) {
         const uint32_t qi = order ? __ldg(&order[i]) : i;
         if constexpr (MULTI) surrogate_query<PendT>(ms.views[ms.layout_of(qi)], q, qi, out, miss);
-        else surrogate_query<PendT>(v, q, qi, out, miss);
+        else surrogate_query<PendT>(v, q, qi, out, miss, n_pending);
     }
 }
 
@@ -583,7 +587,8 @@ __device__ __forceinline__ bool walk_group(const View& v, const P& p, const Lane
 template <typename PendT, int G = JCDE_SURR_GROUP>
 __global__ void JCDE_SURR_BOUNDS k_surrogate_warp(View v, const uint32_t* __restrict__ q, uint32_t n,
                                                                  uint8_t* __restrict__ out, uint8_t miss,
-                                                                 const uint32_t* __restrict__ order) {
+                                                                 const uint32_t* __restrict__ order,
+                                                                 uint32_t* __restrict__ n_pending = nullptr) {
     const LaneGroup<G> g(threadIdx.x & 31);
     constexpr uint32_t gpb = SURR_THREADS / G;   // groups per block
     for (uint32_t i = blockIdx.x * gpb + threadIdx.x / G; i < n; i += gridDim.x * gpb) {
@@ -607,7 +612,10 @@ __global__ void JCDE_SURR_BOUNDS k_surrogate_warp(View v, const uint32_t* __rest
             hit = walk_group<Seg, PendT, G>(v, Seg{xform(Pt{pr.x, pr.y}, c, s, tx, ty), xform(Pt{pr.z, pr.w}, c, s, tx, ty)},
                                             g);
         }
-        if (g.lig == 0) out[qi] = hit ? (uint8_t)1 : miss;
+        if (g.lig == 0) {
+            out[qi] = hit ? (uint8_t)1 : miss;
+            if (n_pending && !hit && miss == PENDING) atomicAdd(n_pending, 1u);
+        }
     }
 }
 
@@ -796,7 +804,7 @@ template <typename PendT, bool TAB>
 __device__ __forceinline__ void poly_query(const View& v, const uint32_t* __restrict__ q, uint32_t qi,
                                            uint8_t* __restrict__ out, const RawShape& raw, volatile int* stop,
                                            float2* tv, uint32_t* jobsw, LeafTab* ltab, int lane,
-                                           unsigned long long* best = nullptr, uint32_t* n_free = nullptr) {
+                                           unsigned long long* best = nullptr, bool skip = false) {
     QShape sh;
     Pt spoi;
     if (raw.verts) {
@@ -836,6 +844,16 @@ __device__ __forceinline__ void poly_query(const View& v, const uint32_t* __rest
         sb = Box{x0, y0, x1, y1};   // SPolygon::generate_bounding_box (simple_polygon.rs:122-133)
     }
     __syncwarp();
+    // lbf's search tests a sample's polygon only if it could still beat the best free sample
+    // (search.rs:52-56): with `skip`, a query whose (cost, index) exceeds the batch's best so far
+    // is left unjudged (3); the best only falls, so no skipped query could have been the choice.
+    if (skip && best && !raw.verts) {
+        const unsigned long long key = ((unsigned long long)orderable(sb.x1 * 10.0f + sb.y1) << 32) | qi;
+        if (key > *(volatile unsigned long long*)best) {
+            if (lane == 0) out[qi] = 3;
+            return;
+        }
+    }
     auto edge_of = [&](uint32_t k) -> Seg {
         if (!cached) return sh.edge(k);
         const float2 a = tv[k], b = tv[k + 1 == sh.nv ? 0 : k + 1];
@@ -957,10 +975,8 @@ __device__ __forceinline__ void poly_query(const View& v, const uint32_t* __rest
     if (lane == 0) {
         out[qi] = hit ? 1 : 0;
         // the LBF choice of a free candidate (k_lbf_select's rule) while its box is at hand
-        if (best && !hit && !raw.verts) {
+        if (best && !hit && !raw.verts)
             atomicMin(best, ((unsigned long long)orderable(sb.x1 * 10.0f + sb.y1) << 32) | qi);
-            atomicAdd(n_free, 1u);
-        }
     }
 }
 
@@ -1004,7 +1020,8 @@ __global__ void __launch_bounds__(POLY_WARPS * 32, JCDE_POLY_MIN_BLOCKS)
 
 // The polygon pass of small batches (latency-bound): leaf tables in dynamic shared memory, queries
 // one at a time from the counter `next`, and a register budget of its own (fewer, longer-lived warps).
-// With `best`, every query found free also enters the LBF choice (as k_lbf_select would).
+// With `best`, every query found free also enters the LBF choice (as k_lbf_select would), and with
+// `skip` the queries that can no longer win it are left unjudged (see poly_query).
 #ifndef JCDE_POLY_TAB_MIN_BLOCKS
 #define JCDE_POLY_TAB_MIN_BLOCKS 2
 #endif
@@ -1012,7 +1029,7 @@ template <typename PendT>
 __global__ void __launch_bounds__(POLY_WARPS * 32, JCDE_POLY_TAB_MIN_BLOCKS)
     k_poly_tab(View v, const uint32_t* __restrict__ q, uint32_t n, uint8_t* __restrict__ out, RawShape raw,
                bool only_pending, const uint32_t* __restrict__ order, uint32_t* __restrict__ next,
-               unsigned long long* __restrict__ best, uint32_t* __restrict__ n_free) {
+               unsigned long long* __restrict__ best, bool skip) {
     __shared__ int stops[POLY_WARPS];
     __shared__ float2 tverts[POLY_WARPS][POLY_MAXV];
     __shared__ uint32_t jobs[POLY_WARPS][POLY_MAXV];
@@ -1029,14 +1046,11 @@ __global__ void __launch_bounds__(POLY_WARPS * 32, JCDE_POLY_TAB_MIN_BLOCKS)
         if (i >= n) break;
         const uint32_t qi = order ? __ldg(&order[i]) : i;
         if (only_pending && out[qi] != PENDING) continue;
-        poly_query<PendT, true>(v, q, qi, out, raw, stop, tverts[warp], jobs[warp], &ltabs[warp], lane, best, n_free);
+        poly_query<PendT, true>(v, q, qi, out, raw, stop, tverts[warp], jobs[warp], &ltabs[warp], lane, best, skip);
     }
 }
 
 constexpr int COLLECT_WARPS = 4;
-
-// Collect: sorted colliding hazard keys per query, compacted with one atomicAdd per query.
-template <int MODE>
 #ifndef JCDE_COLLECT_MIN_BLOCKS
 #define JCDE_COLLECT_MIN_BLOCKS 0   // blocks per SM the collect pass is compiled for (0: ptxas decides)
 #endif
@@ -1045,6 +1059,9 @@ template <int MODE>
 #else
 #define JCDE_COLLECT_BOUNDS __launch_bounds__(COLLECT_WARPS * 32)
 #endif
+
+// Collect: sorted colliding hazard keys per query, compacted with one atomicAdd per query.
+template <int MODE>
 __global__ void JCDE_COLLECT_BOUNDS k_collect(View v, const uint32_t* __restrict__ q, uint32_t n,
                                                                 uint32_t words, uint32_t* __restrict__ offsets,
                                                                 uint32_t* __restrict__ counts, uint32_t* __restrict__ ids,

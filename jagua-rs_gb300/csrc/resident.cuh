@@ -89,7 +89,7 @@ struct LbfDev {
     uint32_t n_removed;   // removals so far (index of the next removal draw)
     uint32_t n_placed;
     unsigned long long best;   // choice of the current round: (order-preserving cost bits << 32) | candidate
-    uint32_t n_free;           // free candidates of the current step (all rounds)
+    uint32_t n_free;           // candidates the surrogate pass left to the polygon pass (all rounds)
     uint32_t rec_cost;         // the step's best so far: order-preserving cost bits, ~0 = none
     double rec_u;              //   its rotation in turns
     uint32_t rec_q[5];         //   its query record

@@ -446,6 +446,15 @@ class GpuEngine:
     def detect_batch(self, queries, ignored=None):
         return self.eng.detect_batch(np.ascontiguousarray(queries, dtype=QUERY_DTYPE), filter=ignored)
 
+    def detect_with_surrogate(self, queries, ignored=None):
+        """(verdicts, number of queries the surrogate pass left undecided)."""
+        import torch
+
+        q = np.ascontiguousarray(queries, dtype=QUERY_DTYPE)
+        dq = torch.from_numpy(q.view(np.uint8).copy()).cuda()
+        sv = self.eng.detect_batch(dq, filter=ignored, mode="surrogate").cpu().numpy()
+        return self.detect_batch(q, ignored), int((sv == 0).sum())
+
     def tree_dump(self):
         return self.eng.tree_dump()
 

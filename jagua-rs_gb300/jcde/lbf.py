@@ -14,7 +14,10 @@ Two drivers share the definition: `run_host` (one engine call per step from Pyth
 or the GPU engine with host-side registration) and `run_device` (jcde_lbf_*: generation, verdicts,
 choice, registration and removal all on the GPU, no host round trip per step).  Both return the
 same log: placements (step, key, candidate, item, cos, sin, tx, ty as float32 bits), removals
-(step, key) and free-candidate counts per step.
+(step, key) and, per step, the number of candidates the surrogate pass left to the polygon pass.
+As in lbf's search (search.rs:52-56, "worth testing"), a candidate only needs its polygon test if
+it could still beat the best free candidate: the device skips the others (unless it logs every
+verdict), which changes no choice.
 """
 from __future__ import annotations
 
@@ -208,18 +211,17 @@ def run_host(lay, eng, spec: LbfSpec, steps: int | None = None, keep_verdicts: i
     for step in range(steps):
         t = int(spec.item_seq[step]) if spec.item_seq is not None else int(types[step])
         q, u = _uniform_round(spec, step, t)
-        verdicts = eng.detect_batch(q)
+        verdicts, n_free = eng.detect_with_surrogate(q)
         if step < keep_verdicts:
             vkeep.append(np.asarray(verdicts).copy())
-        n_free = int((verdicts == 0).sum())
         best, cost = select_host_cost(lay.items, q, verdicts)
         rec = (cost, float(u[best]), q[best].copy(), best) if best >= 0 else None
         for r, (sg, sth) in enumerate(sigmas, start=1):
             if rec is None:
                 break   # nothing to search around (the device marks the round's candidates invalid)
             ql, ul = _local_round(spec, step, r, t, rec[1], rec[2], sg, sth)
-            vl = eng.detect_batch(ql)
-            n_free += int((vl == 0).sum())
+            vl, nf = eng.detect_with_surrogate(ql)
+            n_free += nf
             b, cb = select_host_cost(lay.items, ql, vl)
             if b >= 0 and cb < rec[0]:   # strictly better replaces (search.rs:52 keeps the first)
                 rec = (cb, float(ul[b]), ql[b].copy(), (r << 24) | b)

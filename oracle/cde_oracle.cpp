@@ -1271,7 +1271,15 @@ void or_detect_batch(void* ep, const or_query* q, uint64_t n, const uint32_t* fi
             Transform t{q[i].cos, q[i].sin, q[i].tx, q[i].ty};
             if (q[i].item >= e->items.size()) { out[i] = 2; continue; }
             if (mode == 1) out[i] = e->detect_surrogate_collision(e->items[q[i].item], t, f) ? 1 : 0;
-            else if (mode == 2) {
+            else if (mode == 4) {   // the verdict with the pass that decided it: 1 surrogate, 3 polygon, 0 free
+                const Item& it = e->items[q[i].item];
+                if (e->detect_surrogate_collision(it, t, f)) {
+                    out[i] = 1;
+                } else {
+                    e->transform_item(it, t, buf);
+                    out[i] = e->detect_poly_collision(buf, f) ? 3 : 0;
+                }
+            } else if (mode == 2) {
                 e->transform_item(e->items[q[i].item], t, buf);
                 out[i] = e->detect_poly_collision(buf, f) ? 1 : 0;
             } else out[i] = e->detect_query(q[i].item, t, f, buf) ? 1 : 0;

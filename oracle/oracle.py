@@ -126,7 +126,8 @@ class OracleEngine:
         return int(r)
 
     def detect_batch(self, queries: np.ndarray, ignored=None, n_threads: int = 0, counts=None, mode: int = 3) -> np.ndarray:
-        """mode 3: surrogate || polygon (ci_bench.rs:111-119); 1: surrogate only; 2: polygon only."""
+        """mode 3: surrogate || polygon (ci_bench.rs:111-119); 1: surrogate only; 2: polygon only;
+        4: as 3, with 1 for collisions the surrogate found and 3 for those the polygon pass found."""
         q = np.ascontiguousarray(queries, dtype=QUERY_DTYPE)
         out = np.zeros(len(q), dtype=np.uint8)
         ids, nf = _filter_arr(ignored)
@@ -135,6 +136,11 @@ class OracleEngine:
         lib().or_detect_batch(self.h, q.ctypes.data, len(q), _ptr(ids, C.c_uint32), nf, _ptr(out, C.c_uint8), nt,
                               _ptr(cnt, C.c_uint64) if cnt is not None else None, mode)
         return out
+
+    def detect_with_surrogate(self, queries: np.ndarray, ignored=None):
+        """(verdicts, number of queries the surrogate pass left undecided) in one pass."""
+        v = self.detect_batch(queries, ignored, mode=4)
+        return np.where(v == 3, 1, v).astype(np.uint8), int(((v == 0) | (v == 3)).sum())
 
     def collect_batch(self, queries: np.ndarray, ignored=None, n_threads: int = 0):
         """Returns (counts, ids): CSR of the sorted colliding hazard keys per query."""
