@@ -75,3 +75,15 @@ def test_host_build_with_local_search(oracle_mod):
     xy = W.transform_points(lay1.items[int(p[3])].xy, *[np.uint32(v).view(np.float32) for v in p[4:8]])
     assert lbf.lbf_cost(xy) <= cost0
     assert len(lbf.run_host(lay0, eng0, spec0, steps=5).placements) == 5
+
+
+def test_detect_with_surrogate_counts(oracle_mod):
+    """The oracle's one-pass verdicts-with-surrogate-count equal the separate full and surrogate passes."""
+    spec = lbf.LbfSpec(n_types=12, n_cand=2048)
+    lay, eng = lbf.setup(oracle_mod.OracleBackend, spec)
+    q = lbf.step_queries(spec, 3)
+    q["item"][::97] = 999   # invalid items: verdict 2, never counted
+    v, n_und = eng.detect_with_surrogate(q)
+    assert np.array_equal(v, eng.detect_batch(q))
+    sv = eng.detect_batch(q, mode=1)
+    assert n_und == int((sv == 0).sum())
