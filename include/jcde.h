@@ -339,7 +339,10 @@ jcde_status jcde_lbf_begin(jcde_resident* r, const jcde_lbf_params* p);
 jcde_status jcde_lbf_steps(jcde_resident* r, uint32_t n_steps, uint32_t steps_per_graph, void* stream);
 /* Synchronises.  counts4 = steps done, placements, removals, placed items still live.  placements:
  * 8 words each (step, key, round << 24 | candidate, item, cos, sin, tx, ty as float bits); removals: 2 words each
- * (step, key); free_counts: free candidates per step; verdicts: step-major verdict log. */
+ * (step, key); free_counts: per step, the candidates the surrogate pass left to the polygon pass
+ * (all rounds); verdicts: step-major verdict log.  Without a verdict log the polygon pass only
+ * judges candidates that could still beat the step's best free one (search.rs:52-56), which
+ * changes no placement. */
 jcde_status jcde_lbf_read(jcde_resident* r, uint32_t* counts4, uint32_t* placements, uint32_t place_cap,
                           uint32_t* removals, uint32_t removal_cap, uint32_t* free_counts, uint32_t free_cap,
                           uint8_t* verdicts, uint64_t verdict_cap);
