@@ -390,6 +390,12 @@ jcde_status jcde_spolygon_new(const float* xy, uint32_t n_vertices, float* xy_ou
  * spread over n_threads host threads (0: one per hardware thread). */
 jcde_status jcde_spolygon_batch(const float* xy, const uint32_t* voff, uint32_t n, float* xy_out, float* bbox_out,
                                 float* area_diam, float* centroid_out, int32_t* status, uint32_t n_threads);
+/* close_narrow_concavities (geometry/shape_modification.rs:374-478) of a shape after SPolygon::new
+ * (host): deflate 0 = ShapeModifyMode::Inflate, 1 = Deflate; ratio = the cutoff as a fraction of the
+ * diameter (lbf's default config: 0.01, applied between a simplification and one at a tenth of its
+ * tolerance, original_shape.rs:33-42).  xy_out holds up to n_vertices (x, y); *n_out the count. */
+jcde_status jcde_close_concavities(const float* xy, uint32_t n_vertices, int deflate, float ratio, float* xy_out,
+                                   uint32_t* n_out);
 /* poles of an internal shape with the given area and poi; *n_out receives the count (even when > cap) */
 jcde_status jcde_surrogate_poles(const float* xy, uint32_t n_vertices, float area, const float poi[3],
                                  const jcde_config* cfg, float* poles_xyr, uint32_t cap, uint32_t* n_out);

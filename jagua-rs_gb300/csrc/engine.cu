@@ -940,6 +940,20 @@ jcde_status jcde_spolygon_batch(const float* xy, const uint32_t* voff, uint32_t 
     return JCDE_OK;
 }
 
+jcde_status jcde_close_concavities(const float* xy, uint32_t nv, int deflate, float ratio, float* xy_out,
+                                   uint32_t* n_out) {
+    if (!xy || !xy_out || !n_out || nv < 3) return JCDE_ERR_ARG;
+    std::vector<Pt> pts(nv), out;
+    for (uint32_t i = 0; i < nv; i++) pts[i] = Pt{xy[2 * i], xy[2 * i + 1]};
+    if (close_concavities(std::move(pts), deflate != 0, ratio, &out)) return JCDE_ERR_ARG;
+    *n_out = (uint32_t)out.size();
+    for (size_t i = 0; i < out.size(); i++) {
+        xy_out[2 * i] = out[i].x;
+        xy_out[2 * i + 1] = out[i].y;
+    }
+    return JCDE_OK;
+}
+
 jcde_status jcde_surrogate_poles(const float* xy, uint32_t nv, float area, const float poi[3], const jcde_config* cfg,
                                  float* poles_xyr, uint32_t cap, uint32_t* n_out) {
     if (!xy || nv < 3 || !poi || !valid_config(cfg) || !n_out || (cap && !poles_xyr)) return JCDE_ERR_ARG;

@@ -133,6 +133,67 @@ int spolygon_new(std::vector<Pt> pts, PreparedPolygon* out, bool with_poi) {
     return 0;
 }
 
+// close_narrow_concavities (shape_modification.rs:374-478), on the host: each round bridges the
+// pair of non-adjacent vertices that eliminates the most vertices among those whose connecting
+// edge, shrunk by Edge::scale(0.9999) (edge.rs:39-46), is at most ratio x diameter long, lies
+// outside the shape (inflate) or inside it (deflate) at both ends, crosses none of its edges and cuts
+// off a chain of negative area; ties keep the first pair in (i, j) order.  The shape is rebuilt by
+// SPolygon::new after every bridge (its diameter bounds the next round).
+int close_concavities(std::vector<Pt> pts, bool deflate, float ratio, std::vector<Pt>* out) {
+    PreparedPolygon shape;
+    if (spolygon_new(std::move(pts), &shape, false)) return -1;
+    const size_t rounds = shape.v.size();
+    for (size_t it = 0; it < rounds; it++) {
+        const size_t n = shape.v.size();
+        Polygon poly;
+        poly.v = shape.v;
+        poly.bbox = shape.bbox;
+        const float f = 0.9999f;
+        size_t best_i = 0, best_j = 0, best_elim = 0;
+        bool found = false;
+        for (size_t i = 0; i < n; i++) {
+            for (size_t j = 0; j < n; j++) {
+                if (i == j || (i + 1) % n == j || (j + 1) % n == i) continue;
+                const Pt a = shape.v[i], b = shape.v[j];
+                const float dx = b.x - a.x, dy = b.y - a.y;
+                const Seg c{Pt{a.x - dx * (f - 1.0f) / 2.0f, a.y - dy * (f - 1.0f) / 2.0f},
+                            Pt{b.x + dx * (f - 1.0f) / 2.0f, b.y + dy * (f - 1.0f) / 2.0f}};
+                const float lx = c.s.x - c.e.x, ly = c.s.y - c.e.y;
+                if (sqrtf(lx * lx + ly * ly) > ratio * shape.diameter) continue;
+                const bool in_s = polygon_contains(poly, c.s), in_e = polygon_contains(poly, c.e);
+                if (deflate ? !(in_s && in_e) : (in_s || in_e)) continue;
+                bool crossing = false;
+                for (size_t k = 0; k < n && !crossing; k++)
+                    crossing = seg_hits_seg(Seg{shape.v[k], shape.v[k + 1 == n ? 0 : k + 1]}, c);
+                if (crossing) continue;
+                // the chain from i up to (not including) j
+                std::vector<Pt> chain;
+                for (size_t k = i; k != j; k = k + 1 == n ? 0 : k + 1) chain.push_back(shape.v[k]);
+                if (polygon_area(chain.data(), chain.size()) >= 0.0f) continue;
+                const size_t elim = j > i ? j - i - 1 : n - i + j - 1;
+                if (!found || elim > best_elim) {
+                    found = true;
+                    best_i = i;
+                    best_j = j;
+                    best_elim = elim;
+                }
+            }
+        }
+        if (!found) break;
+        // drop the vertices strictly between best_i and best_j (wrapping), keeping the list's order
+        std::vector<Pt> next;
+        for (size_t k = 0; k < n; k++) {
+            const bool gone = best_j > best_i ? (k > best_i && k < best_j) : (k > best_i || k < best_j);
+            if (!gone) next.push_back(shape.v[k]);
+        }
+        PreparedPolygon rebuilt;
+        if (spolygon_new(std::move(next), &rebuilt, false)) return -2;   // the reference panics here
+        shape = std::move(rebuilt);
+    }
+    *out = shape.v;
+    return 0;
+}
+
 int surrogate_poles(const std::vector<Pt>& v, float area, Disk poi, const PoleLimit* lim, int n_lim,
                     std::vector<Disk>* poles) {
     Polygon p;

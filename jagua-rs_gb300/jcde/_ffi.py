@@ -102,6 +102,7 @@ SIGNATURES = {
     "jcde_snapshot_free": (None, [P]),
     "jcde_spolygon_new": (C.c_int32, [f32p, C.c_uint32, f32p, f32p, f32p, f32p]),
     "jcde_surrogate_poles": (C.c_int32, [f32p, C.c_uint32, C.c_float, f32p, C.POINTER(jcde_config), f32p, C.c_uint32, u32p]),
+    "jcde_close_concavities": (C.c_int32, [f32p, C.c_uint32, C.c_int, C.c_float, f32p, u32p]),
     "jcde_spolygon_batch": (C.c_int32, [f32p, u32p, C.c_uint32, f32p, f32p, f32p, P, P, C.c_uint32]),
     "jcde_simplify_batch": (C.c_int32, [P, P, C.c_uint32, C.c_uint32, P, C.c_int, C.c_float, P, P, P, P]),
     "jcde_gen_candidates": (C.c_int32, [C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint32, jcde_rect, P, C.c_uint32, P, P, P]),

@@ -474,6 +474,13 @@ class GpuBackend:
         return prep.simplify_batch([xy], [area], deflate, tolerance)[0]
 
     @staticmethod
+    def close_concavities(xy, deflate, ratio):
+        """close_narrow_concavities after SPolygon::new (jcde_close_concavities, host)."""
+        from . import prep
+
+        return prep.close_concavities(xy, deflate, ratio)
+
+    @staticmethod
     def new_engine(depth: int, cd_threshold: int, bbox):
         return GpuEngine(depth, cd_threshold, bbox)
 

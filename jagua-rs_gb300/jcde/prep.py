@@ -132,6 +132,20 @@ def simplify_batch(shapes, areas, deflate: bool, tolerance: float) -> list:
     return [o[off[i]: off[i] + int(c[i])].copy() for i in range(b.n)]
 
 
+def close_concavities(xy, deflate: bool, ratio: float) -> np.ndarray:
+    """close_narrow_concavities (shape_modification.rs:374-478) of one shape, on the host
+    (jcde_close_concavities): a pairwise search over the shape's vertices, run between two
+    simplification passes."""
+    xy = np.ascontiguousarray(xy, np.float32).reshape(-1, 2)
+    out = np.zeros_like(xy)
+    n = np.zeros(1, np.uint32)
+    f32p = C.POINTER(C.c_float)
+    check(lib().jcde_close_concavities(xy.ctypes.data_as(f32p), len(xy), int(bool(deflate)), float(np.float32(ratio)),
+                                       out.ctypes.data_as(f32p), n.ctypes.data_as(C.POINTER(C.c_uint32))),
+          "close_concavities")
+    return out[: int(n[0])].copy()
+
+
 def _raise_on(status: np.ndarray, what: str, allow=()):
     bad = [(i, int(s)) for i, s in enumerate(status) if s != 0 and s not in allow]
     if bad:
@@ -201,11 +215,13 @@ def spolygon_batch(raw_shapes, n_threads: int = 0, centroids: bool = False):
 
 
 def import_items(raw_shapes, pole_limits=W.DEFAULT_POLE_LIMITS, n_ff_poles=W.DEFAULT_N_FF_POLES,
-                 simplify_tolerance=None) -> list:
+                 simplify_tolerance=None, narrow_concavity_ratio=None) -> list:
     """Importer::import_item (io/import.rs:47-98) for every shape of the list, the poi and surrogate
     poles searched on the device: the same Items as workload.import_item.  With a
     `simplify_tolerance` the centred shapes are simplified on the device (ShapeModifyMode::Inflate,
-    original_shape.rs:23-50) and the poi is that of the simplified shape."""
+    original_shape.rs:23-50), with `narrow_concavity_ratio` their narrow concavities are then closed
+    (host) and the shapes simplified again at a tenth of the tolerance, and the poi is that of the
+    final shape."""
     torch = _torch()
     n = len(raw_shapes)
     if n == 0:
@@ -228,6 +244,12 @@ def import_items(raw_shapes, pole_limits=W.DEFAULT_POLE_LIMITS, n_ff_poles=W.DEF
     else:
         # simplify_shape, then its SPolygon::new: orientation, area, diameter on the host, poi on the device
         simp = simplify_batch([cxy[off[i]: off[i + 1]] for i in range(n)], area_int, False, simplify_tolerance)
+        if narrow_concavity_ratio is not None:
+            # close_narrow_concavities (host), then simplify_shape at a tenth of the tolerance
+            closed = [close_concavities(s_, False, narrow_concavity_ratio) for s_ in simp]
+            cflat, coff, _, cad = spolygon_batch(closed)
+            simp = simplify_batch([cflat[coff[i]: coff[i + 1]] for i in range(n)], cad[:, 0], False,
+                                  float(np.float32(simplify_tolerance) / np.float32(10.0)))
         cxy, off, _, ad2 = spolygon_batch(simp)
         area_int, diam_int = ad2[:, 0], ad2[:, 1]
         bc = ShapeBatch(packed=(cxy, off))

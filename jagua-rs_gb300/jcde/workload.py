@@ -228,13 +228,27 @@ class Layout:
     n_failed_placements: int = 0
 
 
+def modify_shape(backend, xy, area, deflate: bool, simplify_tolerance, narrow_concavity_ratio=None):
+    """The shape modification of OriginalShape::convert_to_internal (original_shape.rs:33-42):
+    simplify_shape at the tolerance, then — with a narrow-concavity cutoff — close_narrow_concavities
+    and simplify_shape at a tenth of the tolerance.  Returns the vertices before the final
+    SPolygon::new."""
+    xy = backend.simplify_shape(xy, area, deflate, simplify_tolerance)
+    if narrow_concavity_ratio is not None:
+        xy = backend.close_concavities(xy, deflate, narrow_concavity_ratio)
+        cxy, _, carea, _, _ = backend.spolygon_new(xy)
+        xy = backend.simplify_shape(cxy, carea, deflate, np.float32(simplify_tolerance) / np.float32(10.0))
+    return xy
+
+
 def import_item(backend, raw_xy, pole_limits=DEFAULT_POLE_LIMITS, n_ff_poles=DEFAULT_N_FF_POLES,
-                simplify_tolerance=None) -> Item:
+                simplify_tolerance=None, narrow_concavity_ratio=None) -> Item:
     """Importer::import_item (io/import.rs:47-98, entities/item.rs:27-48) with
     OriginalShape::convert_to_internal (original_shape.rs:23-50): the centred shape, simplified
     (ShapeModifyMode::Inflate) when a tolerance is given — lbf's default config uses 0.001
-    (lbf/src/config.rs:42).  Item.area is the original shape's (Item::area), the diameter that of
-    the internal shape (the one item_placement_order sorts by)."""
+    (lbf/src/config.rs:42), with narrow concavities closed when a cutoff is given as well (lbf's
+    default: 0.01, config.rs:43).  Item.area is the original shape's (Item::area), the diameter that
+    of the internal shape (the one item_placement_order sorts by)."""
     xy, bbox, area, diam, poi = backend.spolygon_new(raw_xy)
     cx, cy = centroid_f32(xy, area)
     # centering_transformation (io/import.rs:214-217): DTransformation(0, (-cx, -cy)); sin_cos(0) = (0, 1)
@@ -243,13 +257,13 @@ def import_item(backend, raw_xy, pole_limits=DEFAULT_POLE_LIMITS, n_ff_poles=DEF
     iarea, idiam = area, diam
     if simplify_tolerance is not None:
         # simplify_shape ends in SPolygon::new: new area, diameter and poi for the internal shape
-        simp = backend.simplify_shape(ixy, area, False, simplify_tolerance)
+        simp = modify_shape(backend, ixy, area, False, simplify_tolerance, narrow_concavity_ratio)
         ixy, _, iarea, idiam, ipoi = backend.spolygon_new(simp)
     poles = backend.surrogate_poles(ixy, iarea, ipoi, pole_limits)
     return Item(ixy, ipoi, poles, min(n_ff_poles, len(poles)), float(area), float(idiam), (float(cx), float(cy)))
 
 
-def import_static(backend, raw_xy, kind, simplify_tolerance=None) -> HazardSpec:
+def import_static(backend, raw_xy, kind, simplify_tolerance=None, narrow_concavity_ratio=None) -> HazardSpec:
     """Container outer / hole / zone: SPolygon::new then the empty pre-transform (io/import.rs:119-124);
     with a tolerance simplified as OriginalShape::convert_to_internal does (original_shape.rs:23-50):
     the outer with ShapeModifyMode::Deflate (io/import.rs:123), holes and zones with Inflate
@@ -258,7 +272,7 @@ def import_static(backend, raw_xy, kind, simplify_tolerance=None) -> HazardSpec:
     ixy = transform_points(xy, 1.0, 0.0, 0.0, 0.0)
     ipoi = np.concatenate([transform_points(poi[None, :2], 1.0, 0.0, 0.0, 0.0)[0], poi[2:3]]).astype(np.float32)
     if simplify_tolerance is not None:
-        simp = backend.simplify_shape(ixy, area, kind == EXTERIOR, simplify_tolerance)
+        simp = modify_shape(backend, ixy, area, kind == EXTERIOR, simplify_tolerance, narrow_concavity_ratio)
         ixy, _, _, _, ipoi = backend.spolygon_new(simp)
     return HazardSpec(kind, False, ixy, ipoi)
 

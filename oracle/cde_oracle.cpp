@@ -1179,6 +1179,68 @@ static std::vector<Point> simplify_shape(const std::vector<Point>& shape, float 
     return ref;
 }
 
+// close_narrow_concavities (shape_modification.rs:374-478): repeatedly bridge the pair of
+// non-adjacent vertices whose (0.9999-scaled) connecting edge is shorter than ratio x diameter,
+// stays outside (Inflate) or inside (Deflate) the shape, crosses none of its edges and cuts off a
+// negative-area chain; the pair eliminating the most vertices wins (the first on ties).
+static std::vector<Point> close_narrow_concavities(std::vector<Point> pts, bool deflate, float ratio) {
+    SPolygon shape;
+    if (!spolygon_new(pts, &shape)) return pts;
+    const size_t rounds = shape.v.size();
+    for (size_t it = 0; it < rounds; it++) {
+        const size_t n = shape.v.size();
+        auto elim = [n](size_t i, size_t j) { return j > i ? j - i - 1 : n - i + j - 1; };
+        bool have = false;
+        size_t bi = 0, bj = 0;
+        for (size_t i = 0; i < n; i++) {
+            for (size_t j = 0; j < n; j++) {
+                if (i == j || (i + 1) % n == j || (j + 1) % n == i) continue;
+                const Point a = shape.v[i], b = shape.v[j];
+                // Edge::scale(0.9999) (edge.rs:39-46)
+                const float f = 0.9999f;
+                const float dx = b.x - a.x, dy = b.y - a.y;
+                const Point s{a.x - dx * (f - 1.0f) / 2.0f, a.y - dy * (f - 1.0f) / 2.0f};
+                const Point e{b.x + dx * (f - 1.0f) / 2.0f, b.y + dy * (f - 1.0f) / 2.0f};
+                const float ex = s.x - e.x, ey = s.y - e.y;
+                const float len = std::sqrt(ex * ex + ey * ey);   // Point::distance_to (point.rs:45-47)
+                if (len > ratio * shape.diameter) continue;
+                const bool s_in = poly_collides_point(shape, s), e_in = poly_collides_point(shape, e);
+                if (!deflate && (s_in || e_in)) continue;
+                if (deflate && !(s_in && e_in)) continue;
+                const Edge c{s, e};
+                bool crosses = false;
+                for (size_t k = 0; k < n && !crosses; k++) crosses = edge_intersection(shape.edge(k), c);
+                if (crosses) continue;
+                std::vector<Point> sub;
+                if (j > i) sub.assign(shape.v.begin() + i, shape.v.begin() + j);
+                else {
+                    sub.assign(shape.v.begin() + i, shape.v.end());
+                    sub.insert(sub.end(), shape.v.begin(), shape.v.begin() + j);
+                }
+                if (calculate_area(sub) >= 0.0f) continue;
+                if (!have || elim(i, j) > elim(bi, bj)) {
+                    have = true;
+                    bi = i;
+                    bj = j;
+                }
+            }
+        }
+        if (!have) break;
+        std::vector<Point> r = shape.v;
+        const long start = (long)bi + 1, end = (long)bj - 1;
+        if (start <= end) {
+            r.erase(r.begin() + start, r.begin() + end + 1);
+        } else {
+            if ((size_t)start < n) r.erase(r.begin() + start, r.end());
+            if (end >= 0) r.erase(r.begin(), r.begin() + end + 1);
+        }
+        SPolygon next;
+        if (!spolygon_new(r, &next)) break;   // the reference panics here (expect)
+        shape = next;
+    }
+    return shape.v;
+}
+
 }  // namespace oracle
 
 // ==========================================================================================
@@ -1436,6 +1498,18 @@ int32_t or_simplify_shape(const float* xy, uint32_t nv, float area, int32_t defl
     std::vector<Point> pts(nv);
     for (uint32_t i = 0; i < nv; i++) pts[i] = Point{xy[2 * i], xy[2 * i + 1]};
     std::vector<Point> r = simplify_shape(pts, area, deflate != 0, tolerance);
+    *n_out = (uint32_t)r.size();
+    for (size_t i = 0; i < r.size(); i++) { xy_out[2 * i] = r[i].x; xy_out[2 * i + 1] = r[i].y; }
+    return 0;
+}
+
+// close_narrow_concavities (shape_modification.rs:374-478) of a shape (SPolygon::new is applied
+// first, as the reference's input is an SPolygon); *n_out receives the resulting vertex count.
+int32_t or_close_concavities(const float* xy, uint32_t nv, int32_t deflate, float ratio, float* xy_out,
+                             uint32_t* n_out) {
+    std::vector<Point> pts(nv);
+    for (uint32_t i = 0; i < nv; i++) pts[i] = Point{xy[2 * i], xy[2 * i + 1]};
+    std::vector<Point> r = close_narrow_concavities(pts, deflate != 0, ratio);
     *n_out = (uint32_t)r.size();
     for (size_t i = 0; i < r.size(); i++) { xy_out[2 * i] = r[i].x; xy_out[2 * i + 1] = r[i].y; }
     return 0;

@@ -59,6 +59,7 @@ def lib():
             "or_surrogate_poles": (C.c_int32, [f32p, C.c_uint32, C.c_float, f32p, u32p, f32p, C.c_int32, f32p, C.c_uint32, u32p]),
             "or_centroid": (None, [f32p, C.c_uint32, C.c_float, f32p]),
             "or_simplify_shape": (C.c_int32, [f32p, C.c_uint32, C.c_float, C.c_int32, C.c_float, f32p, u32p]),
+            "or_close_concavities": (C.c_int32, [f32p, C.c_uint32, C.c_int32, C.c_float, f32p, u32p]),
             "or_fpa_eq": (C.c_int32, [C.c_float, C.c_float]),
             "or_edge_intersection": (C.c_int32, [f32p, f32p]),
             "or_rect_collides_edge": (C.c_int32, [f32p, f32p]),
@@ -218,6 +219,16 @@ class OracleBackend:
         n = np.zeros(1, np.uint32)
         lib().or_simplify_shape(_ptr(xy, C.c_float), len(xy), np.float32(area), int(bool(deflate)), np.float32(tolerance),
                                 _ptr(out, C.c_float), _ptr(n, C.c_uint32))
+        return out[: int(n[0])].copy()
+
+    @staticmethod
+    def close_concavities(xy, deflate, ratio):
+        """close_narrow_concavities (shape_modification.rs:374-478), after SPolygon::new of xy."""
+        xy = _f32(xy)
+        out = np.zeros_like(xy)
+        n = np.zeros(1, np.uint32)
+        lib().or_close_concavities(_ptr(xy, C.c_float), len(xy), int(bool(deflate)), np.float32(ratio),
+                                   _ptr(out, C.c_float), _ptr(n, C.c_uint32))
         return out[: int(n[0])].copy()
 
     @staticmethod

@@ -151,3 +151,18 @@ def test_batch_wider_than_the_gpu(oracle_mod, jcde_mod):
         ref = W.import_item(oracle_mod.OracleBackend, r)
         assert np.array_equal(d.poi.view(np.uint32), ref.poi.view(np.uint32))
         assert np.array_equal(d.poles.view(np.uint32), ref.poles.view(np.uint32))
+
+
+@gpu
+def test_import_items_lbf_default_matches_oracle(oracle_mod, jcde_mod):
+    """lbf's default import (simplify 0.001, close concavities at 1% and 20% of the diameter,
+    simplify again at a tenth): the device batch import equals the oracle's, bit for bit."""
+    from jcde import prep
+
+    raws = _shapes()[:12]
+    for ratio in (0.01, 0.2):
+        dev = prep.import_items(raws, simplify_tolerance=0.001, narrow_concavity_ratio=ratio)
+        for i, r in enumerate(raws):
+            ref = W.import_item(oracle_mod.OracleBackend, r, simplify_tolerance=0.001, narrow_concavity_ratio=ratio)
+            assert np.array_equal(dev[i].xy.view(np.uint32), ref.xy.view(np.uint32)), (ratio, i)
+            assert np.array_equal(dev[i].poles.view(np.uint32), ref.poles.view(np.uint32)), (ratio, i)

@@ -85,3 +85,35 @@ def test_reference_instances_simplify(oracle_mod):
             assert abs(float(s_area) - float(area)) / float(area) <= 0.001 * (1 + 1e-5)
             seen += 1
     assert seen > 0
+
+
+@pytest.mark.parametrize("ratio", [0.01, 0.05, 0.2])
+def test_close_concavities_product_equals_oracle(oracle_mod, jcde_mod, ratio):
+    """close_narrow_concavities: the product's host implementation (jcde_close_concavities) and
+    the oracle's give the same vertices, in both modes; bridges only ever remove vertices."""
+    from jcde import prep
+
+    B = oracle_mod.OracleBackend
+    shapes = _stars(16, seed=0xCC)
+    shapes.append(np.array([[0, 0], [60, 0], [60, 20], [21, 20], [21, 50], [19, 50], [19, 20], [0, 20]], np.float32))
+    changed = 0
+    for raw in shapes:
+        xy, _, area, _, _ = B.spolygon_new(raw)
+        for deflate in (False, True):
+            a = B.close_concavities(xy, deflate, ratio)
+            b = prep.close_concavities(xy, deflate, ratio)
+            assert a.shape == b.shape and np.array_equal(a.view(np.uint32), b.view(np.uint32))
+            assert len(a) <= len(xy)
+            changed += len(a) < len(xy)
+    if ratio >= 0.05:
+        assert changed > 0
+
+
+def test_lbf_default_import(oracle_mod):
+    """lbf's default import: simplify 0.001, close concavities under 1% of the diameter, simplify
+    0.0001; the result never has more vertices than the plain simplification."""
+    B = oracle_mod.OracleBackend
+    for raw in _stars(6, seed=0xCD):
+        a = W.import_item(B, raw, simplify_tolerance=0.001)
+        b = W.import_item(B, raw, simplify_tolerance=0.001, narrow_concavity_ratio=0.01)
+        assert len(b.xy) <= len(a.xy) and b.area == a.area
