@@ -170,17 +170,19 @@ class BppSetup:
 
 
 def setup_bpp(backend, inst: BppInstance, simplify_tolerance=None, depth: int = W.DEFAULT_DEPTH,
-              cd_threshold: int = W.DEFAULT_CD_THRESHOLD, device_prep: bool = False) -> BppSetup:
+              cd_threshold: int = W.DEFAULT_CD_THRESHOLD, device_prep: bool = False,
+              narrow_concavity_ratio=None) -> BppSetup:
     """Items and bins imported (see the module notes); `device_prep` imports the items in one
     jcde.prep batch with the pole searches on the GPU (the same items)."""
-    items = I.import_items(backend, [it.xy for it in inst.items], simplify_tolerance, device_prep)
+    items = I.import_items(backend, [it.xy for it in inst.items], simplify_tolerance, device_prep,
+                           narrow_concavity_ratio)
     bins = []
     for b in inst.bins:
-        outer = W.import_static(backend, b.outer, W.EXTERIOR, simplify_tolerance)
+        outer = W.import_static(backend, b.outer, W.EXTERIOR, simplify_tolerance, narrow_concavity_ratio)
         hz, qs = [outer], [None]
         q0_area = 0.0
         for q, xy in b.zones:
-            hz.append(W.import_static(backend, xy, W.QUALITY_ZONE, simplify_tolerance))
+            hz.append(W.import_static(backend, xy, W.QUALITY_ZONE, simplify_tolerance, narrow_concavity_ratio))
             qs.append(q)
             if q == 0:
                 q0_area += float(backend.spolygon_new(xy)[2])

@@ -105,13 +105,16 @@ def orientation_cs(degrees) -> np.ndarray:
     return np.stack([c.astype(np.float32), s.astype(np.float32)], axis=1)
 
 
-def import_items(backend, raws, simplify_tolerance=None, device_prep: bool = False) -> list:
+def import_items(backend, raws, simplify_tolerance=None, device_prep: bool = False,
+                 narrow_concavity_ratio=None) -> list:
     """workload.import_item for every shape, or with `device_prep` one jcde.prep batch (GPU)."""
     if device_prep:
         from . import prep
 
-        return prep.import_items(raws, simplify_tolerance=simplify_tolerance)
-    return [W.import_item(backend, xy, simplify_tolerance=simplify_tolerance) for xy in raws]
+        return prep.import_items(raws, simplify_tolerance=simplify_tolerance,
+                                 narrow_concavity_ratio=narrow_concavity_ratio)
+    return [W.import_item(backend, xy, simplify_tolerance=simplify_tolerance,
+                          narrow_concavity_ratio=narrow_concavity_ratio) for xy in raws]
 
 
 @dataclass
@@ -124,12 +127,13 @@ class SppSetup:
 
 
 def setup_spp(backend, inst: SppInstance, strip_width: float, depth: int = W.DEFAULT_DEPTH,
-              cd_threshold: int = W.DEFAULT_CD_THRESHOLD, simplify_tolerance=None, device_prep: bool = False) -> SppSetup:
+              cd_threshold: int = W.DEFAULT_CD_THRESHOLD, simplify_tolerance=None, device_prep: bool = False,
+              narrow_concavity_ratio=None) -> SppSetup:
     """Items imported, a strip of `strip_width` x strip_height as the container, a fresh engine.
     `simplify_tolerance` simplifies the items as lbf's importer does (its default config: 0.001);
     `device_prep` imports all items in one batch with the pole searches on the GPU (jcde.prep,
     the same items)."""
-    items = import_items(backend, [it.xy for it in inst.items], simplify_tolerance, device_prep)
+    items = import_items(backend, [it.xy for it in inst.items], simplify_tolerance, device_prep, narrow_concavity_ratio)
     outer = W.import_static(backend, W.rect_polygon(0.0, 0.0, strip_width, inst.strip_height), W.EXTERIOR)
     lay = W.Layout(inst.name or "spp", depth, cd_threshold, W.inflate_to_square(W.bbox_of(outer.xy)), items=items)
     lay.hazards.append(outer)

@@ -85,3 +85,14 @@ def test_reference_instance_on_the_oracle(oracle_mod):
     log = bpp.run_bpp(oracle_mod.OracleBackend, su, bpp.BppSpec(n_cand=512))
     assert len(log.placements) + sum(log.unplaced.values()) == sum(it.demand for it in inst.items)
     _replay_free(oracle_mod, su, log)
+
+
+@pytest.mark.skipif(not os.path.exists(REF_BALDACCI), reason="reference assets not present")
+def test_reference_instance_lbf_default_import(oracle_mod):
+    """The reference instance imported as lbf's default config does (simplification 0.001 and
+    concavities under 1% closed, items inflated, the container outers deflated) still packs."""
+    inst = bpp.load_bpp(REF_BALDACCI)
+    su = bpp.setup_bpp(oracle_mod.OracleBackend, inst, simplify_tolerance=0.001, narrow_concavity_ratio=0.01)
+    log = bpp.run_bpp(oracle_mod.OracleBackend, su, bpp.BppSpec(n_cand=256))
+    assert len(log.placements) > 0
+    _replay_free(oracle_mod, su, log)
