@@ -1,4 +1,5 @@
-// Shape preparation on the device: the poles of many shapes at once.
+// Shape preparation on the device: the poles (k_poles) and the simplification (k_simplify) of many
+// shapes at once.
 //
 // compute_pole (fail_fast/pole.rs:52-77) is a breadth-first branch and bound over a cell tree of
 // MAX_POI_TREE_DEPTH = 10 levels (pole.rs:79): each cell's centre is scored by its signed distance to
@@ -16,7 +17,7 @@
 // generate_surrogate_poles (pole.rs:12-47) then repeats compute_pole with the coverage limits, one
 // CTA per shape (shapes handed out by a counter), the shape's vertices and poles in shared memory.
 // Every score uses the predicates of geom.cuh, compiled with the same rounding rules as the host
-// restatement, so each pole is bit-identical to the host's and to the reference's.
+// preparation, so each pole is bit-identical to the host's (and the oracle's).
 #include <cuda_runtime.h>
 
 #include <algorithm>
