@@ -117,3 +117,25 @@ def test_lbf_default_import(oracle_mod):
         a = W.import_item(B, raw, simplify_tolerance=0.001)
         b = W.import_item(B, raw, simplify_tolerance=0.001, narrow_concavity_ratio=0.01)
         assert len(b.xy) <= len(a.xy) and b.area == a.area
+
+
+def test_known_answers(oracle_mod):
+    """Hand-derived cases.  A notch 1 unit wide and 10 deep in a 20 x 20 square: at a 20% cutoff
+    (diameter 28.3, so bridges up to 5.66) the notch is bridged (Inflate) and its two inner
+    vertices go; at 1% nothing is short enough.  Deflate never bridges outside the shape."""
+    B = oracle_mod.OracleBackend
+    notch = np.array([[0, 0], [20, 0], [20, 20], [10.5, 20], [10.5, 10], [9.5, 10], [9.5, 20], [0, 20]],
+                     np.float32)
+    xy, _, area, diam, _ = B.spolygon_new(notch)
+    assert abs(float(diam) - 20 * np.sqrt(2)) < 1e-3
+    closed = B.close_concavities(xy, False, 0.2)
+    assert len(closed) == 6
+    assert not any((closed == [10.5, 10]).all(1)) and not any((closed == [9.5, 10]).all(1))
+    assert len(B.close_concavities(xy, False, 0.01)) == 8
+    assert len(B.close_concavities(xy, True, 0.2)) == 8
+    # simplify_shape on the notch: the concave corners are the cheapest candidates; removing one
+    # changes the area by 5 (a triangle of half 1 x 10), 1.25% of 395
+    s1 = B.simplify_shape(xy, area, False, 0.02)
+    _, _, a1, _, _ = B.spolygon_new(s1)
+    assert len(s1) < 8 and float(a1) > float(area)
+    assert len(B.simplify_shape(xy, area, False, 0.001)) == 8
