@@ -77,7 +77,7 @@ class LbfSpec:
 class LbfLog:
     placements: np.ndarray   # (n, 8) uint32
     removals: np.ndarray     # (m, 2) uint32
-    free_counts: np.ndarray  # (steps,) uint32
+    free_counts: np.ndarray  # (steps,) uint32: candidates the surrogate pass left to the polygon pass
     verdicts: list = field(default_factory=list)   # per-step verdict arrays (host driver, if kept)
 
     def same_as(self, other: "LbfLog") -> bool:
