@@ -422,6 +422,74 @@ def queries_for(lay: Layout, n: int, seed: int, sid: int = 3) -> np.ndarray:
     return make_queries(Stream(seed, sid), n, len(lay.items), lay.cde_bbox)
 
 
+_RIGHT_COS = np.array([1, 0, -1, 0], np.float32)
+_RIGHT_SIN = np.array([0, 1, 0, -1], np.float32)
+
+
+def boundary_queries(lay: Layout, n: int, seed: int) -> np.ndarray:
+    """Queries on the quadtree's split lines at right-angle rotations (cos / sin exactly 0 or +-1),
+    a third of them nudged by one ULP: the closed-interval, half-intersection and FPA cases."""
+    st = Stream(seed, 1)
+    b = np.asarray(lay.cde_bbox, dtype=np.float32)
+    lines_x = b[0] + (b[2] - b[0]) * np.arange(33, dtype=np.float32) / np.float32(32)
+    lines_y = b[1] + (b[3] - b[1]) * np.arange(33, dtype=np.float32) / np.float32(32)
+    q = np.zeros(n, dtype=QUERY_DTYPE)
+    q["item"] = st.randint(0, len(lay.items) - 1, n).astype(np.uint32)
+    rot = st.randint(0, 3, n)
+    q["cos"] = _RIGHT_COS[rot]
+    q["sin"] = _RIGHT_SIN[rot]
+    ix, iy = st.randint(0, 32, n), st.randint(0, 32, n)
+    tx, ty = lines_x[ix], lines_y[iy]
+    free_x = st.f32(n) < 0.3   # a coordinate off the lines keeps the other one on a line
+    tx = np.where(free_x, st.uniform_f32(b[0], b[2], n), tx).astype(np.float32)
+    nudge = st.randint(0, 2, n) - 1   # -1, 0, +1 ULP
+    q["tx"] = np.where(nudge < 0, np.nextafter(tx, np.float32(-np.inf)),
+                       np.where(nudge > 0, np.nextafter(tx, np.float32(np.inf)), tx))
+    q["ty"] = ty
+    return q
+
+
+def touch_queries(lay: Layout, n: int, seed: int) -> np.ndarray:
+    """Queries whose item touches a hazard: at a right-angle rotation, one item vertex is put on a
+    hazard vertex, on a hazard edge's midpoint or at a random point of a hazard edge (up to the
+    rounding of the translation), and half of them are moved one ULP in x or y.  These are the
+    exact-touch cases of edge_intersection (edge.rs:180-228), of the closed box tests and of the
+    FPA vertex guard."""
+    st = Stream(seed, 1)
+    hz = lay.hazards
+    hi = st.randint(0, len(hz) - 1, n)
+    it = st.randint(0, len(lay.items) - 1, n)
+    rot = st.randint(0, 3, n)
+    mode = st.randint(0, 2, n)          # 0: on a vertex, 1: on an edge midpoint, 2: on an edge at random t
+    tt = st.f32(n)
+    r1, r2 = st.u64(n), st.u64(n)
+    nudge = st.randint(0, 7, n)         # 1-4: one ULP in +x, -x, +y, -y
+    hv_n = np.array([len(h.xy) for h in hz], np.uint64)
+    iv_n = np.array([len(i.xy) for i in lay.items], np.uint64)
+    hoff = np.concatenate([[0], np.cumsum(hv_n)]).astype(np.int64)
+    ioff = np.concatenate([[0], np.cumsum(iv_n)]).astype(np.int64)
+    hxy = np.concatenate([h.xy for h in hz]).astype(np.float32)
+    ixy = np.concatenate([i.xy for i in lay.items]).astype(np.float32)
+    a = (r1 % hv_n[hi]).astype(np.int64)
+    b = np.where(a + 1 == hv_n[hi].astype(np.int64), 0, a + 1)
+    pa, pb = hxy[hoff[hi] + a], hxy[hoff[hi] + b]
+    t = np.where(mode == 1, np.float32(0.5), tt).astype(np.float32)[:, None]
+    p = np.where((mode == 0)[:, None], pa, (pa + t * (pb - pa)).astype(np.float32)).astype(np.float32)
+    v = ixy[ioff[it] + (r2 % iv_n[it]).astype(np.int64)]
+    c, s = _RIGHT_COS[rot], _RIGHT_SIN[rot]
+    px = (c * v[:, 0]).astype(np.float32) + (-s * v[:, 1]).astype(np.float32)
+    py = (s * v[:, 0]).astype(np.float32) + (c * v[:, 1]).astype(np.float32)
+    tx = (p[:, 0] - px).astype(np.float32)
+    ty = (p[:, 1] - py).astype(np.float32)
+    up, dn = np.float32(np.inf), np.float32(-np.inf)
+    tx = np.where(nudge == 1, np.nextafter(tx, up), np.where(nudge == 2, np.nextafter(tx, dn), tx))
+    ty = np.where(nudge == 3, np.nextafter(ty, up), np.where(nudge == 4, np.nextafter(ty, dn), ty))
+    q = np.zeros(n, dtype=QUERY_DTYPE)
+    q["item"] = it.astype(np.uint32)
+    q["cos"], q["sin"], q["tx"], q["ty"] = c, s, tx, ty
+    return q
+
+
 def multi_layouts(backend, seed=0xC2, n_layouts=64, n_types=40, v_range=(8, 200), r_range=(20.0, 60.0),
                   items_range=(20, 400), container_v=(32, 128), radius_per_sqrt_item=70.0, depth=DEFAULT_DEPTH,
                   cd_threshold=DEFAULT_CD_THRESHOLD, chunk=256, max_attempts=1 << 14, item_pool=None):

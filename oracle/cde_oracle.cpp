@@ -6,8 +6,10 @@
 //
 // PARITY UNPINNED: the reference is Rust, no Rust toolchain exists where this is built, and the
 // reference ships no golden vectors or known-answer tests for the CDE.  The restatement follows
-// the reference line by line (file:line cited at every function) and is itself pinned by
-// hand-derived known-answer tests (tests/test_oracle_kat.py) and a brute-force cross-check.
+// the reference line by line (file:line cited at every function) and is itself checked by
+// hand-derived known-answer tests (tests/test_oracle_kat.py, tests/test_naive_crosscheck.py) and
+// by a tree-free brute-force checker written apart from this file (naive.cpp: every query against
+// every hazard edge, no quadtree), which must report the same verdicts and collected sets.
 // The FPA tolerance comes from the float-cmp 0.10 crate (not vendored in the reference tree);
 // its documented default margin (epsilon = f32::EPSILON, 4 ULPs) is restated in fpa_eq().
 //

@@ -12,41 +12,7 @@ from jcde import workload as W
 pytestmark = pytest.mark.gpu
 
 
-def torch_queries(q):
-    import torch
-
-    return torch.from_numpy(np.ascontiguousarray(q, dtype=W.QUERY_DTYPE).view(np.uint8).copy()).cuda()
-
-
-def gpu_engine(lay):
-    eng = jcde.CDEngine(lay.cde_bbox, (), jcde.CDEConfig(quadtree_depth=lay.depth, cd_threshold=lay.cd_threshold))
-    for it in lay.items:
-        eng.register_item(it.xy, it.poi, it.poles)
-    for hz in lay.hazards:
-        assert eng.register_hazard(jcde.Hazard(hz.kind, hz.xy, hz.poi, hz.dynamic, hz.tag)) == hz.key
-    return eng
-
-
-def gpu_detect(eng, q, filter=None, mode="both"):
-    import torch
-
-    out = eng.detect_batch(torch_queries(q), filter=filter, mode=mode)
-    torch.cuda.synchronize()
-    return out.cpu().numpy()
-
-
-def gpu_collect(eng, q, filter=None):
-    off, cnt, ids, total = eng.collect_batch(torch_queries(q), filter=filter)
-    off, cnt, ids = off.cpu().numpy(), cnt.cpu().numpy(), ids.cpu().numpy()
-    return [ids[o : o + c].tolist() for o, c in zip(off, cnt)]
-
-
-def oracle_sets(counts, ids):
-    out, o = [], 0
-    for c in counts:
-        out.append(ids[o : o + c].tolist())
-        o += c
-    return out
+from helpers import csr_lists as oracle_sets, gpu_collect, gpu_detect, gpu_engine, torch_queries  # noqa: E402
 
 
 @pytest.fixture(scope="module")
@@ -227,32 +193,9 @@ def test_autotune_keeps_verdicts(star, oracle_mod):
         geng.set_tuning(**saved)
 
 
-def _boundary_queries(lay, n_items, seed):
-    """Queries placed on the quadtree's split lines and at right-angle rotations (cos/sin exactly 0
-    or +-1), a fraction nudged by one ULP: the closed-interval, half-intersection and FPA cases."""
-    st = W.Stream(seed, 1)
-    b = np.asarray(lay.cde_bbox, dtype=np.float32)
-    lines_x = b[0] + (b[2] - b[0]) * np.arange(33, dtype=np.float32) / np.float32(32)
-    lines_y = b[1] + (b[3] - b[1]) * np.arange(33, dtype=np.float32) / np.float32(32)
-    n = 1 << 16
-    q = np.zeros(n, dtype=W.QUERY_DTYPE)
-    q["item"] = st.randint(0, n_items - 1, n).astype(np.uint32)
-    rot = st.randint(0, 3, n)
-    q["cos"] = np.array([1, 0, -1, 0], np.float32)[rot]
-    q["sin"] = np.array([0, 1, 0, -1], np.float32)[rot]
-    ix, iy = st.randint(0, 32, n), st.randint(0, 32, n)
-    tx, ty = lines_x[ix], lines_y[iy]
-    free_x = st.f32(n) < 0.3   # a coordinate off the lines keeps the other one on a line
-    tx = np.where(free_x, st.uniform_f32(b[0], b[2], n), tx).astype(np.float32)
-    nudge = st.randint(0, 2, n) - 1   # -1, 0, +1 ULP
-    q["tx"] = np.where(nudge < 0, np.nextafter(tx, np.float32(-np.inf)), np.where(nudge > 0, np.nextafter(tx, np.float32(np.inf)), tx))
-    q["ty"] = ty
-    return q
-
-
 def test_boundary_queries_detect_and_collect(star, oracle_mod):
     lay, oeng, geng = star
-    q = _boundary_queries(lay, len(lay.items), 0xB0)
+    q = W.boundary_queries(lay, 1 << 16, 0xB0)
     got = gpu_detect(geng, q, filter=lay.filter_keys)
     assert np.array_equal(got, oeng.detect_batch(q, ignored=lay.filter_keys))
     assert 0.05 < got.mean() < 0.99
