@@ -1391,36 +1391,200 @@ __device__ __forceinline__ ProxyOut proxy_eval(const View& v, const DItem& it, f
     return o;
 }
 
+// ---------------------------------------------------------------------------------------------
+// Float-float ("double-single") arithmetic for the proxy's forward / adjoint: a value is hi + lo
+// with |lo| <= ulp(hi) / 2, about 48 significant bits.  Built from the error-free transforms
+// TwoSum (Knuth) and FMA-based TwoProduct (Dekker 1971; Ogita, Rump and Oishi 2005).  The file is
+// compiled with -fmad=false, so only the explicit __fmaf_rn below is fused.
+//
+// Why: the penetration depth r_i + r_j - |c_i - c_j| of a shallow contact cancels most of its
+// digits (coordinates ~2000, depths ~0.01-1), so a plain float32 depth carries a relative error
+// of up to ~1e-3; float-float keeps it near 1e-10 and the gradient then agrees with a float64
+// evaluation of the same float32 inputs to far better than 1e-4.
+// ---------------------------------------------------------------------------------------------
+struct FF {
+    float hi, lo;
+};
+__device__ __forceinline__ FF ff_two_sum(float a, float b) {
+    const float s = a + b, bb = s - a;
+    return FF{s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ FF ff_fast_sum(float a, float b) {   // |a| >= |b|
+    const float s = a + b;
+    return FF{s, b - (s - a)};
+}
+__device__ __forceinline__ FF ff_two_prod(float a, float b) {
+    const float p = a * b;
+    return FF{p, __fmaf_rn(a, b, -p)};
+}
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+    FF s = ff_two_sum(a.hi, b.hi);
+    const FF t = ff_two_sum(a.lo, b.lo);
+    s = ff_fast_sum(s.hi, s.lo + t.hi);
+    return ff_fast_sum(s.hi, s.lo + t.lo);
+}
+__device__ __forceinline__ FF ff_neg(FF a) { return FF{-a.hi, -a.lo}; }
+__device__ __forceinline__ FF ff_mul(FF a, FF b) {
+    const FF p = ff_two_prod(a.hi, b.hi);
+    return ff_fast_sum(p.hi, p.lo + (a.hi * b.lo + a.lo * b.hi));
+}
+__device__ __forceinline__ FF ff_mul_f(FF a, float b) {
+    const FF p = ff_two_prod(a.hi, b);
+    return ff_fast_sum(p.hi, p.lo + a.lo * b);
+}
+// square root of a > 0: one Newton correction of the float32 root
+__device__ __forceinline__ FF ff_sqrt(FF a) {
+    const float x = sqrtf(a.hi);
+    const FF r = ff_add(a, ff_neg(ff_two_prod(x, x)));
+    return ff_fast_sum(x, r.hi / (2.0f * x));
+}
+// a / b: quotient digits by long division (three float32 partial quotients)
+__device__ __forceinline__ FF ff_div(FF a, FF b) {
+    const float q1 = a.hi / b.hi;
+    FF r = ff_add(a, ff_neg(ff_mul_f(b, q1)));
+    const float q2 = r.hi / b.hi;
+    r = ff_add(r, ff_neg(ff_mul_f(b, q2)));
+    const float q3 = r.hi / b.hi;
+    return ff_add(ff_fast_sum(q1, q2), FF{q3, 0.0f});
+}
+__device__ __forceinline__ float ff_f(FF a) { return a.hi + a.lo; }
+
+// cos and sin of a float32 angle in float-float: Cody-Waite reduction by pi/2 (split into three
+// float32 parts, the first with 8 significant bits so that k * part is exact for |k| < 2^16, the
+// other two products taken exactly by TwoProduct), then the Taylor series of sin and cos of the
+// reduced argument (|r| <= ~pi/4 + rounding) in Horner form, to the term where it stops changing
+// float-float digits (sin to r^17, cos to r^18).  Coefficients are 1/n! split into hi + lo.
+__constant__ float c_inv_fact[19][2] = {
+    {0x1p+0f, 0.0f}, {0x1p+0f, 0.0f}, {0x1p-1f, 0.0f},
+    {0x1.555556p-3f, -0x1.555556p-28f}, {0x1.555556p-5f, -0x1.555556p-30f},
+    {0x1.111112p-7f, -0x1.ddddde0p-32f}, {0x1.6c16c2p-10f, -0x1.27d27ep-35f},
+    {0x1.a01a02p-13f, -0x1.7f97fap-39f}, {0x1.a01a02p-16f, -0x1.7f97fap-42f},
+    {0x1.71de3ap-19f, 0x1.55b1ccp-45f}, {0x1.27e4fcp-22f, -0x1.10ec14p-47f},
+    {0x1.ae6456p-26f, 0x1.fd5138p-52f}, {0x1.1eed8ep-29f, 0x1.ff1b12p-54f},
+    {0x1.612462p-33f, -0x1.8af25ep-58f}, {0x1.93974ap-37f, 0x1.180f94p-62f},
+    {0x1.ae7f3ep-41f, 0x1.ccee08p-67f}, {0x1.ae7f3ep-45f, 0x1.ccee08p-71f},
+    {0x1.952c78p-49f, -0x1.f9ea56p-74f}, {0x1.682786p-53f, 0x1.dcbeccp-80f}};
+
+__device__ __forceinline__ void ff_sincos(float theta, FF& s_out, FF& c_out) {
+    const float P1 = 0x1.92p+0f, P2 = 0x1.fb5444p-12f, P3 = 0x1.68c234p-39f;   // pi/2 = P1 + P2 + P3 + O(1e-19)
+    const float k = rintf(theta * 0x1.45f306p-1f);                               // theta * 2/pi
+    FF r = ff_two_sum(theta, -(k * P1));
+    r = ff_add(r, ff_neg(ff_two_prod(k, P2)));
+    r = ff_add(r, ff_neg(ff_two_prod(k, P3)));
+    const FF r2 = ff_mul(r, r);
+    // sin r = r (1 - r^2/3! + r^4/5! - ...), cos r = 1 - r^2/2! + r^4/4! - ...
+    FF ps = FF{c_inv_fact[17][0], c_inv_fact[17][1]};
+    for (int n = 15; n >= 1; n -= 2) {
+        ps = ff_add(FF{c_inv_fact[n][0], c_inv_fact[n][1]}, ff_neg(ff_mul(ps, r2)));
+    }
+    FF pc = FF{c_inv_fact[18][0], c_inv_fact[18][1]};
+    for (int n = 16; n >= 0; n -= 2) {
+        pc = ff_add(FF{c_inv_fact[n][0], c_inv_fact[n][1]}, ff_neg(ff_mul(pc, r2)));
+    }
+    const FF sr = ff_mul(ps, r), cr = pc;
+    const int q = ((int)k) & 3;
+    s_out = q == 0 ? sr : q == 1 ? cr : q == 2 ? ff_neg(sr) : ff_neg(cr);
+    c_out = q == 0 ? cr : q == 1 ? ff_neg(sr) : q == 2 ? ff_neg(cr) : sr;
+}
+
+// The proxy and its adjoint for one candidate, every contact pair in float-float.  Pairs are first
+// screened in float32 with a margin far above float32's rounding of the distance (so no contact is
+// lost), then the depth and the gradient terms are formed and summed in float-float.
+__device__ __forceinline__ ProxyOut proxy_eval_ff(const View& v, const DItem& it, FF c, FF s, float tx, float ty,
+                                                  int lane) {
+    FF p{0.0f, 0.0f}, gx{0.0f, 0.0f}, gy{0.0f, 0.0f}, gth{0.0f, 0.0f};
+    const int g = v.hp_g;
+    const float cf = ff_f(c), sf = ff_f(s);
+    for (uint32_t k = lane; k < it.n_poles; k += 32) {
+        const float4 pl = __ldg(&v.poles[it.pole_off + k]);
+        const float rxf = cf * pl.x - sf * pl.y, ryf = sf * pl.x + cf * pl.y;
+        const FF rx = ff_add(ff_mul_f(c, pl.x), ff_neg(ff_mul_f(s, pl.y)));
+        const FF ry = ff_add(ff_mul_f(s, pl.x), ff_mul_f(c, pl.y));
+        const float cx = rxf + tx, cy = ryf + ty;
+        const float reach = pl.z * 1.00001f + 1e-3f;   // the pole's box, grown by the screening margin
+        const float bx0 = cx - reach, by0 = cy - reach, bx1 = cx + reach, by1 = cy + reach;
+        const int ix0 = pole_cell(bx0, v.hp_x0, v.hp_inv_cs, g), ix1 = pole_cell(bx1, v.hp_x0, v.hp_inv_cs, g);
+        const int iy0 = pole_cell(by0, v.hp_y0, v.hp_inv_cs, g), iy1 = pole_cell(by1, v.hp_y0, v.hp_inv_cs, g);
+        for (int iy = iy0; iy <= iy1; iy++)
+            for (int ix = ix0; ix <= ix1; ix++) {
+                const uint32_t cell = (uint32_t)iy * (uint32_t)g + (uint32_t)ix;
+                const uint32_t a = __ldg(&v.hp_start[cell]), b = __ldg(&v.hp_start[cell + 1]);
+                for (uint32_t j = a; j < b; j++) {
+                    const float4 h = __ldg(&v.hpoles[j]);
+                    // each pair once: in the cell of the low corner of the two boxes' overlap
+                    const float mx = fmaxf(bx0, h.x - h.z), my = fmaxf(by0, h.y - h.z);
+                    if (mx > fminf(bx1, h.x + h.z) || my > fminf(by1, h.y + h.z)) continue;
+                    if (pole_cell(mx, v.hp_x0, v.hp_inv_cs, g) != ix || pole_cell(my, v.hp_y0, v.hp_inv_cs, g) != iy)
+                        continue;
+                    if (filtered(v, __float_as_uint(h.w))) continue;
+                    const float dxf = (tx - h.x) + rxf, dyf = (ty - h.y) + ryf;
+                    const float rm = (pl.z + h.z) * 1.00001f + 1e-3f;
+                    if (dxf * dxf + dyf * dyf >= rm * rm) continue;
+                    const FF dx = ff_add(ff_two_sum(tx, -h.x), rx), dy = ff_add(ff_two_sum(ty, -h.y), ry);
+                    const FF d2 = ff_add(ff_mul(dx, dx), ff_mul(dy, dy));
+                    const FF rr = ff_two_sum(pl.z, h.z);
+                    if (d2.hi <= 0.0f) {   // coincident centres: depth rr, no direction
+                        p = ff_add(p, ff_mul(rr, rr));
+                        continue;
+                    }
+                    const FF d = ff_sqrt(d2);
+                    const FF pen = ff_add(rr, ff_neg(d));
+                    if (pen.hi <= 0.0f) continue;
+                    p = ff_add(p, ff_mul(pen, pen));
+                    const FF f = ff_div(ff_mul_f(pen, -2.0f), d);
+                    gx = ff_add(gx, ff_mul(f, dx));
+                    gy = ff_add(gy, ff_mul(f, dy));
+                    gth = ff_add(gth, ff_mul(f, ff_add(ff_mul(dy, rx), ff_neg(ff_mul(dx, ry)))));
+                }
+            }
+    }
+    for (int sh = 16; sh; sh >>= 1) {
+        p = ff_add(p, FF{__shfl_xor_sync(FULL, p.hi, sh), __shfl_xor_sync(FULL, p.lo, sh)});
+        gx = ff_add(gx, FF{__shfl_xor_sync(FULL, gx.hi, sh), __shfl_xor_sync(FULL, gx.lo, sh)});
+        gy = ff_add(gy, FF{__shfl_xor_sync(FULL, gy.hi, sh), __shfl_xor_sync(FULL, gy.lo, sh)});
+        gth = ff_add(gth, FF{__shfl_xor_sync(FULL, gth.hi, sh), __shfl_xor_sync(FULL, gth.lo, sh)});
+    }
+    return ProxyOut{ff_f(p), ff_f(gx), ff_f(gy), ff_f(gth)};
+}
+
 constexpr int PROXY_WARPS = 8;
 
 // Forward and/or adjoint for a batch: params are (theta, tx, ty) per candidate.  `value` (may be
 // null) receives P; `grad` (may be null) receives dP/d(theta, tx, ty), times gscale[i] when
-// `gscale` is given (the backward of a loss L with dL/dP = gscale).
+// `gscale` is given (the backward of a loss L with dL/dP = gscale).  A warp takes 32 consecutive
+// candidates: each lane evaluates the float-float cos / sin of one of them, then the warp works
+// through the 32 together, lanes over the item's poles.
 __global__ void __launch_bounds__(PROXY_WARPS * 32) k_proxy(View v, const float* __restrict__ params,
                                                             const uint32_t* __restrict__ items, uint32_t n,
                                                             float* __restrict__ value, float* __restrict__ grad,
                                                             const float* __restrict__ gscale) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (uint32_t i = blockIdx.x * PROXY_WARPS + warp; i < n; i += gridDim.x * PROXY_WARPS) {
-        const uint32_t item = __ldg(&items[i]);
-        if (item >= v.n_items) {
-            if (lane == 0) {
-                if (value) value[i] = -1.0f;
-                if (grad) grad[3 * i] = grad[3 * i + 1] = grad[3 * i + 2] = 0.0f;
+    for (uint32_t base = (blockIdx.x * PROXY_WARPS + warp) * 32u; base < n; base += gridDim.x * PROXY_WARPS * 32u) {
+        FF my_s{0.0f, 0.0f}, my_c{1.0f, 0.0f};
+        if (base + lane < n) ff_sincos(__ldg(&params[3 * (base + lane)]), my_s, my_c);
+        const uint32_t m = min(32u, n - base);
+        for (uint32_t l = 0; l < m; l++) {
+            const uint32_t i = base + l;
+            const FF s{__shfl_sync(FULL, my_s.hi, l), __shfl_sync(FULL, my_s.lo, l)};
+            const FF c{__shfl_sync(FULL, my_c.hi, l), __shfl_sync(FULL, my_c.lo, l)};
+            const uint32_t item = __ldg(&items[i]);
+            if (item >= v.n_items) {
+                if (lane == 0) {
+                    if (value) value[i] = -1.0f;
+                    if (grad) grad[3 * i] = grad[3 * i + 1] = grad[3 * i + 2] = 0.0f;
+                }
+                continue;
             }
-            continue;
-        }
-        const DItem it = v.items[item];
-        float s, c;
-        sincosf(__ldg(&params[3 * i]), &s, &c);
-        const ProxyOut o = proxy_eval(v, it, c, s, __ldg(&params[3 * i + 1]), __ldg(&params[3 * i + 2]), lane, 32, FULL, 0.0f);
-        if (lane == 0) {
-            if (value) value[i] = o.p;
-            if (grad) {
-                const float g = gscale ? __ldg(&gscale[i]) : 1.0f;
-                grad[3 * i] = gscale ? o.gth * g : o.gth;
-                grad[3 * i + 1] = gscale ? o.gx * g : o.gx;
-                grad[3 * i + 2] = gscale ? o.gy * g : o.gy;
+            const DItem it = v.items[item];
+            const ProxyOut o = proxy_eval_ff(v, it, c, s, __ldg(&params[3 * i + 1]), __ldg(&params[3 * i + 2]), lane);
+            if (lane == 0) {
+                if (value) value[i] = o.p;
+                if (grad) {
+                    const float gs = gscale ? __ldg(&gscale[i]) : 1.0f;
+                    grad[3 * i] = gscale ? o.gth * gs : o.gth;
+                    grad[3 * i + 1] = gscale ? o.gx * gs : o.gx;
+                    grad[3 * i + 2] = gscale ? o.gy * gs : o.gy;
+                }
             }
         }
     }

@@ -272,14 +272,18 @@ class CDEngine:
             raise KeyError(key)
         check(st, "set_hazard_poles")
 
-    def proxy_batch(self, params, items, filter=None, stream=None):
-        """(value, grad) CUDA tensors of the proxy for (theta, tx, ty) params [n, 3] and items [n]."""
+    def proxy_batch(self, params, items, filter=None, stream=None, out=None):
+        """(value, grad) CUDA tensors of the proxy for (theta, tx, ty) params [n, 3] and items [n];
+        `out` = (value [n], grad [n, 3]) float32 tensors to write into."""
         import torch
 
         f = _Filter(filter)
         n = items.numel()
-        val = torch.empty(n, dtype=torch.float32, device=params.device)
-        grad = torch.empty((n, 3), dtype=torch.float32, device=params.device)
+        if out is not None:
+            val, grad = out
+        else:
+            val = torch.empty(n, dtype=torch.float32, device=params.device)
+            grad = torch.empty((n, 3), dtype=torch.float32, device=params.device)
         check(lib().jcde_proxy_batch(self.h, params.data_ptr(), items.data_ptr(), n, f.ref, val.data_ptr(),
                                      grad.data_ptr(), _stream_handle(stream)), "proxy_batch")
         return val, grad

@@ -1571,7 +1571,35 @@ extern "C" void or_proxy_f64(uint64_t n, const double* params, const uint32_t* i
         if (ignored[i] >= ign.size()) ign.resize(ignored[i] + 1, 0);
         ign[ignored[i]] = 1;
     }
+    // A uniform grid over the hazard poles' centres only prunes pairs that cannot overlap (centres
+    // further apart than r_i + r_max + 1); the pairs that remain are summed in ascending pole order,
+    // the order of a plain loop over every hazard pole.
+    double x0 = 1e300, y0 = 1e300, x1 = -1e300, y1 = -1e300, rmax = 0;
+    for (uint64_t j = 0; j < n_hpoles; j++) {
+        x0 = std::min(x0, (double)hpoles[4 * j]); x1 = std::max(x1, (double)hpoles[4 * j]);
+        y0 = std::min(y0, (double)hpoles[4 * j + 1]); y1 = std::max(y1, (double)hpoles[4 * j + 1]);
+        rmax = std::max(rmax, (double)hpoles[4 * j + 2]);
+    }
+    const double cs = std::max(1.0, 2.0 * rmax);
+    const int64_t gx_n = n_hpoles ? std::min<int64_t>(4096, (int64_t)((x1 - x0) / cs) + 1) : 1;
+    const int64_t gy_n = n_hpoles ? std::min<int64_t>(4096, (int64_t)((y1 - y0) / cs) + 1) : 1;
+    const double csx = n_hpoles ? std::max(cs, (x1 - x0) / (double)gx_n + 1e-9) : 1.0;
+    const double csy = n_hpoles ? std::max(cs, (y1 - y0) / (double)gy_n + 1e-9) : 1.0;
+    std::vector<uint32_t> start((size_t)(gx_n * gy_n + 1), 0), idx(n_hpoles);
+    auto cell_of = [&](double v, double o, double w, int64_t g) {
+        int64_t c = (int64_t)std::floor((v - o) / w);
+        return std::max<int64_t>(0, std::min<int64_t>(g - 1, c));
+    };
+    for (uint64_t j = 0; j < n_hpoles; j++)
+        start[cell_of(hpoles[4 * j + 1], y0, csy, gy_n) * gx_n + cell_of(hpoles[4 * j], x0, csx, gx_n) + 1]++;
+    for (size_t c = 1; c < start.size(); c++) start[c] += start[c - 1];
+    {
+        std::vector<uint32_t> fill(start.begin(), start.end() - 1);
+        for (uint64_t j = 0; j < n_hpoles; j++)
+            idx[fill[cell_of(hpoles[4 * j + 1], y0, csy, gy_n) * gx_n + cell_of(hpoles[4 * j], x0, csx, gx_n)]++] = (uint32_t)j;
+    }
     run_threads(n, n_threads, [&](uint64_t a, uint64_t b, int) {
+        std::vector<uint32_t> near;
         for (uint64_t i = a; i < b; i++) {
             const double th = params[3 * i], tx = params[3 * i + 1], ty = params[3 * i + 2];
             const double c = std::cos(th), s = std::sin(th);
@@ -1580,7 +1608,17 @@ extern "C" void or_proxy_f64(uint64_t n, const double* params, const uint32_t* i
             for (uint32_t k = pole_off[it]; k < pole_off[it + 1]; k++) {
                 const double px = item_poles[3 * k], py = item_poles[3 * k + 1], r = item_poles[3 * k + 2];
                 const double rx = c * px - s * py, ry = s * px + c * py;
-                for (uint64_t j = 0; j < n_hpoles; j++) {
+                const double cx = rx + tx, cy = ry + ty, reach = r + rmax + 1.0;
+                near.clear();
+                if (n_hpoles) {
+                    const int64_t ax = cell_of(cx - reach, x0, csx, gx_n), bx = cell_of(cx + reach, x0, csx, gx_n);
+                    const int64_t ay = cell_of(cy - reach, y0, csy, gy_n), by = cell_of(cy + reach, y0, csy, gy_n);
+                    for (int64_t yy = ay; yy <= by; yy++)
+                        for (int64_t xx = ax; xx <= bx; xx++)
+                            for (uint32_t q = start[yy * gx_n + xx]; q < start[yy * gx_n + xx + 1]; q++) near.push_back(idx[q]);
+                    std::sort(near.begin(), near.end());
+                }
+                for (uint32_t j : near) {
                     uint32_t key;
                     std::memcpy(&key, &hpoles[4 * j + 3], 4);
                     if (key < ign.size() && ign[key]) continue;

@@ -39,7 +39,7 @@ def test_f64_gradient_matches_central_differences(oracle_mod, strip_layout, stri
 def test_gpu_proxy_matches_f64(oracle_mod, jcde_mod, strip_layout, strip_poles):
     import torch
 
-    from test_gpu_parity import gpu_engine
+    from helpers import gpu_engine
 
     lay, _ = strip_layout
     eng = gpu_engine(lay)
@@ -57,8 +57,8 @@ def test_gpu_proxy_matches_f64(oracle_mod, jcde_mod, strip_layout, strip_poles):
     assert np.array_equal(val > 0, v64 > 0) or ((val > 0) != (v64 > 0)).sum() < 5
     rel_v = np.abs(val[on] - v64[on]) / v64[on]
     rel_g = np.linalg.norm(grad[on] - g64[on], axis=1) / np.linalg.norm(g64[on], axis=1)
-    assert np.median(rel_v) < 1e-5 and np.median(rel_g) < 1e-5, (np.median(rel_v), np.median(rel_g))
-    assert np.percentile(rel_g, 99) < 1e-4, np.percentile(rel_g, 99)
+    # float-float contact pairs: every candidate within 1e-4 (typically ~1e-8)
+    assert rel_v.max() < 1e-5 and rel_g.max() < 1e-4, (rel_v.max(), rel_g.max())
 
 
 @pytest.mark.gpu
@@ -66,7 +66,7 @@ def test_gpu_separation_then_exact_verdict(oracle_mod, jcde_mod, strip_layout, s
     """Descent moves colliding candidates; every final placement's verdict is the oracle's."""
     import torch
 
-    from test_gpu_parity import gpu_engine
+    from helpers import gpu_engine
 
     lay, oeng = strip_layout
     eng = gpu_engine(lay)
@@ -96,7 +96,7 @@ def test_gpu_proxy_forward_backward_pair_and_autograd(oracle_mod, jcde_mod, stri
     import torch
 
     import jcde
-    from test_gpu_parity import gpu_engine
+    from helpers import gpu_engine
 
     lay, _ = strip_layout
     eng = gpu_engine(lay)
