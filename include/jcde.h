@@ -148,14 +148,23 @@ jcde_status jcde_collect_batch(jcde_engine* e, const jcde_query* d_queries, uint
  * allocates a device bitmask and a per-node table the first time it sees a filter, and cudaMalloc
  * synchronizes the whole device and needs free memory — which a caller whose GPU memory is all
  * owned by its own pool, or that runs queries on a latency-critical stream next to other work,
- * cannot accept.  This entry point keeps the filter's keys, bitmask and per-node table in one static
- * device array of JCDE_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until the
- * process exits; it returns JCDE_ERR_CAPACITY when keys + bitmask + table exceed it.  Every call
- * shares that array and leaves its contents behind, so calls that overlap on the GPU (another
- * stream, another thread) race on it.  The engine's device copy must be current: after a
- * register / deregister / restore / register_item, run any other query first (jcde_detect_batch
- * with n = 0 suffices), else JCDE_ERR_STATE.  The first call on a device looks up the array's
- * device address with that device current; make that first call before any stream capture. */
+ * cannot accept.  This entry point keeps the two passes' work counters, the filter's bitmask and
+ * the per-node table in one static device array of JCDE_NOALLOC_SCRATCH_BYTES that every GPU
+ * loading the library holds until the process exits; it returns JCDE_ERR_CAPACITY when
+ * 256 B + n_slots / 8 B + one byte per quadtree node (each part rounded up to 256 B) exceed it,
+ * i.e. for engines of more than about 8 million hazard slots or 1 million nodes.  The ignored keys
+ * are turned into the bitmask on the host during the call and handed to the GPU by value in launch
+ * parameters, so the caller's key array may be reused as soon as the call returns, and its length
+ * costs no device memory.  Every call shares the array and leaves its contents behind, so calls
+ * that overlap on the GPU (another stream, another thread) race on it.  The engine's device copy
+ * must be current: after a register / deregister / restore / register_item, run any other query
+ * first (jcde_detect_batch with n = 0 suffices), else JCDE_ERR_STATE.  That first query of the
+ * engine also looks up the array's device address and loads this entry point's kernels on the
+ * current device (a call on a device where that has not happened does it itself; make such a call
+ * before any stream capture).  A cudaDeviceReset while the library is loaded is not supported.
+ * Visit ordering, whose buffers grow with the batch, is not used, so batches at or above the
+ * engine's order_min_batch (jcde_tuning; 4,096 by default) run somewhat slower than through
+ * jcde_detect_batch. */
 #define JCDE_NOALLOC_SCRATCH_BYTES 1048576u
 jcde_status jcde_detect_batch_noalloc(jcde_engine* e, const jcde_query* d_queries, uint32_t n,
                                       const jcde_filter* filter, uint8_t* d_verdicts, void* stream);
@@ -442,6 +451,12 @@ jcde_status jcde_tree_dump(const jcde_engine* e, uint32_t* out, uint64_t cap, ui
 jcde_status jcde_device_stats(jcde_engine* e, uint64_t* out5);
 /* number of kernels this engine has launched since creation (bench accounting) */
 uint64_t jcde_kernel_launches(const jcde_engine* e);
+/* Measurement helper (no counterpart in the reference): the L2 read bandwidth of the current device
+ * in GB/s for a buffer of `bytes` (>= 1 MiB) that stays L2-resident, read `reps` times by a
+ * hand-written streaming kernel (16-byte loads cached in L2 only), timed with CUDA events.  The
+ * query kernels read their layout from L2, so this is their bandwidth ceiling.  Allocates and frees
+ * its buffer; synchronizes the device. */
+jcde_status jcde_l2_read_peak(uint64_t bytes, uint32_t reps, double* out_gbs);
 /* Kernel timing (no counterpart in the reference): when enabled, every launch is bracketed by CUDA
  * events on its stream; jcde_profile_read synchronises on them and returns, per kind, the summed
  * milliseconds and launch counts (arrays of JCDE_PROF_KINDS), optionally resetting the totals. */

@@ -179,8 +179,13 @@ static jcde_status upload(DevBuf& b, const void* src, size_t bytes) {
 
 // Bring the device mirror up to date with the host quadtree and item table.  (The hazard-pole
 // grids of the proxy kernels are refreshed separately, by sync_poles, only where they are used.)
+static jcde_status noalloc_setup(void** out);
+
 static jcde_status sync_device(jcde_engine* e) {
     if (e->tree_version == e->tree.version() && !e->items_dirty) return JCDE_OK;
+    // the no-allocation entry point's set-up for this device, while allocating is still allowed
+    // (its own status is reported by that entry point, which repeats the set-up if it failed here)
+    (void)noalloc_setup(nullptr);
     // queries already queued on the caller's stream may still read the old image
     if (e->have_last_stream) CUDA_TRY(cudaStreamSynchronize(e->last_stream));
     if (e->tree_version != e->tree.version()) {
@@ -1033,19 +1038,37 @@ jcde_status jcde_profile_read(jcde_engine* e, double* ms, uint64_t* count, int r
 // Filtered detect that allocates nothing (jcde_detect_batch_noalloc).
 //
 // The regular filtered path keeps one device bitmask and one per-node strength array per distinct
-// filter, allocated on first use.  This variant keeps those in one static device array instead,
-// so a call never allocates device memory.  Every GPU that loads the library holds the array until
-// the process exits, every call shares it (it keeps the last call's contents), and calls that
-// overlap on the GPU race on it.
+// filter, allocated on first use.  This variant keeps those, and the two passes' work counters, in
+// one static device array instead, so a call never allocates device memory.  Every GPU that loads
+// the library holds the array until the process exits, every call shares it (it keeps the last
+// call's contents), and calls that overlap on the GPU race on it.
+//
+// Layout of the array: [0, 256) the two work counters (cleared by each call), then the filter's
+// key bitmask (n_slots bits, rounded up to 256 bytes), then the per-node strength table.
 // ---------------------------------------------------------------------------------------------
 static __device__ __align__(256) unsigned char g_noalloc_scratch[JCDE_NOALLOC_SCRATCH_BYTES];
 
 static std::mutex g_noalloc_mu;
 static void* g_noalloc_addr[256] = {};   // device address of g_noalloc_scratch, per device ordinal
 
-// The host name g_noalloc_scratch is only a stand-in; its device address is looked up once per
-// device, with that device current, on the first call made on it.
-static jcde_status noalloc_scratch_addr(void** out) {
+// Bitmask words handed over by value, in the launch parameters: nothing of the caller's key
+// buffer is read after the call returns, and nothing is staged through host memory.
+constexpr uint32_t NOALLOC_MASK_CHUNK = 960;
+struct MaskChunk {
+    uint32_t w[NOALLOC_MASK_CHUNK];
+};
+__global__ void k_mask_chunk(const MaskChunk c, uint32_t first, uint32_t count, uint32_t* __restrict__ mask) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < count) mask[first + i] = c.w[i];
+}
+
+// Set-up for the current device: the array's device address (the host name g_noalloc_scratch is
+// only a stand-in, not a device address) and the code of k_mask_chunk, loaded now so that a later
+// call loads nothing (CUDA loads kernels lazily by default).  Done once per device, with that
+// device current: by the engine's first query of any kind (sync_device), or else by the first
+// jcde_detect_batch_noalloc call on the device.  The address stays valid while the CUDA context
+// lives; a cudaDeviceReset while the library is loaded is not supported.
+static jcde_status noalloc_setup(void** out) {
     int dev = 0;
     CUDA_TRY(cudaGetDevice(&dev));
     if (dev < 0 || dev >= 256) return JCDE_ERR_STATE;
@@ -1053,21 +1076,19 @@ static jcde_status noalloc_scratch_addr(void** out) {
     if (!g_noalloc_addr[dev]) {
         void* p = nullptr;
         if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || p == nullptr) return JCDE_ERR_CUDA;
+        // every kernel the call can launch
+        cudaFuncAttributes fa;
+        const void* fns[] = {(const void*)k_mask_chunk, (const void*)k_strength,
+                             (const void*)k_surrogate_warp<uint32_t>, (const void*)k_surrogate_warp<uint64_t>,
+                             (const void*)k_surrogate<uint32_t, false>, (const void*)k_surrogate<uint64_t, false>,
+                             (const void*)k_poly_tab<uint32_t>, (const void*)k_poly_tab<uint64_t>,
+                             (const void*)k_poly<uint32_t, false>, (const void*)k_poly<uint64_t, false>};
+        for (const void* fn : fns)
+            if (cudaFuncGetAttributes(&fa, fn) != cudaSuccess) return JCDE_ERR_CUDA;
         g_noalloc_addr[dev] = p;
     }
-    *out = g_noalloc_addr[dev];
+    if (out) *out = g_noalloc_addr[dev];
     return JCDE_OK;
-}
-
-// Ignored keys -> bitmask over hazard keys; the mask is cleared first (the array keeps old contents).
-__global__ void k_mask_from_keys(const uint32_t* __restrict__ keys, uint32_t n_keys, uint32_t n_slots,
-                                 uint32_t* __restrict__ mask, uint32_t words) {
-    for (uint32_t w = threadIdx.x; w < words; w += blockDim.x) mask[w] = 0u;
-    __syncthreads();
-    for (uint32_t i = threadIdx.x; i < n_keys; i += blockDim.x) {
-        const uint32_t k = keys[i];
-        if (k < n_slots) atomicOr(&mask[k >> 5], 1u << (k & 31));
-    }
 }
 
 static inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
@@ -1079,30 +1100,44 @@ extern "C" jcde_status jcde_detect_batch_noalloc(jcde_engine* e, const jcde_quer
     if (n_keys && !f->ignored) return JCDE_ERR_ARG;
     // bringing the device mirror up to date may allocate: it must already be current
     if (e->tree_version != e->tree.version() || e->items_dirty) return JCDE_ERR_STATE;
-    const uint32_t words = mask_words(e);
-    const size_t keys_b = align256((size_t)n_keys * 4), mask_b = align256((size_t)words * 4);
+    const uint32_t words = mask_words(e), n_slots = e->tree.n_slots();
+    const size_t ctr_b = 256, mask_b = align256((size_t)words * 4);
     const size_t str_b = align256(e->n_nodes);
-    if (keys_b + mask_b + str_b > JCDE_NOALLOC_SCRATCH_BYTES) return JCDE_ERR_CAPACITY;
+    if (ctr_b + mask_b + str_b > JCDE_NOALLOC_SCRATCH_BYTES) return JCDE_ERR_CAPACITY;
     void* base = nullptr;
-    jcde_status st = noalloc_scratch_addr(&base);
+    jcde_status st = noalloc_setup(&base);
     if (st) return st;
     init_launch_shape(e);
     cudaStream_t s = (cudaStream_t)stream;
     unsigned char* b = static_cast<unsigned char*>(base);
-    uint32_t* keys = reinterpret_cast<uint32_t*>(b);
-    uint32_t* mask = reinterpret_cast<uint32_t*>(b + keys_b);
-    uint8_t* strength = b + keys_b + mask_b;
-    if (n_keys) CUDA_TRY(cudaMemcpyAsync(keys, f->ignored, (size_t)n_keys * 4, cudaMemcpyHostToDevice, s));
-    k_mask_from_keys<<<1, 256, 0, s>>>(keys, n_keys, e->tree.n_slots(), mask, words);
-    CUDA_TRY(cudaGetLastError());
+    uint32_t* next = reinterpret_cast<uint32_t*>(b);
+    uint32_t* mask = reinterpret_cast<uint32_t*>(b + ctr_b);
+    uint8_t* strength = b + ctr_b + mask_b;
+    // the bitmask, built here chunk by chunk and shipped by value (a chunk's words are all written,
+    // so the previous call's mask needs no clearing)
+    for (uint32_t w0 = 0; w0 < words; w0 += NOALLOC_MASK_CHUNK) {
+        const uint32_t cnt = std::min(NOALLOC_MASK_CHUNK, words - w0);
+        MaskChunk c;
+        std::memset(c.w, 0, sizeof(c.w));
+        for (uint32_t i = 0; i < n_keys; i++) {
+            const uint32_t k = f->ignored[i];
+            if (k < n_slots && (k >> 5) >= w0 && (k >> 5) < w0 + cnt) c.w[(k >> 5) - w0] |= 1u << (k & 31);
+        }
+        k_mask_chunk<<<(cnt + 255) / 256, 256, 0, s>>>(c, w0, cnt, mask);
+        CUDA_TRY(cudaGetLastError());
+        e->launches++;
+    }
     View v = base_view(e);
     v.mask = mask;
     k_strength<<<(e->n_nodes + 255) / 256, 256, 0, s>>>(v, e->n_nodes, strength);
     CUDA_TRY(cudaGetLastError());
     v.strength = strength;
-    e->launches += 2;
+    e->launches++;
     if (n) {
-        launch_passes(e, v, reinterpret_cast<const uint32_t*>(dq), n, dout, s, RawShape{nullptr, 0, 0, 0, 0}, 3);
+        // counter-fed passes (the counters are cleared on the stream by the passes themselves); no
+        // visit ordering, whose buffers grow with the batch
+        launch_passes(e, v, reinterpret_cast<const uint32_t*>(dq), n, dout, s, RawShape{nullptr, 0, 0, 0, 0}, 3,
+                      nullptr, next);
         CUDA_TRY(cudaGetLastError());
     }
     e->last_stream = s;
@@ -1348,7 +1383,7 @@ jcde_status jcde_proxy_batch(jcde_engine* e, const float* d_params, const uint32
     View v;
     jcde_status st = proxy_prepare(e, f, s, v);
     if (st || n == 0) return st;
-    const uint32_t grid = std::min<uint32_t>((n + PROXY_WARPS - 1) / PROXY_WARPS, (uint32_t)e->n_sms * 8);
+    const uint32_t grid = std::min<uint32_t>((n + PROXY_WARPS * 32 - 1) / (PROXY_WARPS * 32), (uint32_t)e->n_sms * 8);
     k_proxy<<<grid, PROXY_WARPS * 32, 0, s>>>(v, d_params, d_items, n, d_value, d_grad, nullptr);
     CUDA_TRY(cudaGetLastError());
     e->launches++;
@@ -1364,7 +1399,7 @@ jcde_status jcde_proxy_forward(jcde_engine* e, const float* d_params, const uint
     View v;
     jcde_status st = proxy_prepare(e, f, s, v);
     if (st || n == 0) return st;
-    const uint32_t grid = std::min<uint32_t>((n + PROXY_WARPS - 1) / PROXY_WARPS, (uint32_t)e->n_sms * 8);
+    const uint32_t grid = std::min<uint32_t>((n + PROXY_WARPS * 32 - 1) / (PROXY_WARPS * 32), (uint32_t)e->n_sms * 8);
     k_proxy<<<grid, PROXY_WARPS * 32, 0, s>>>(v, d_params, d_items, n, d_value, nullptr, nullptr);
     CUDA_TRY(cudaGetLastError());
     e->launches++;
@@ -1380,7 +1415,7 @@ jcde_status jcde_proxy_backward(jcde_engine* e, const float* d_params, const uin
     View v;
     jcde_status st = proxy_prepare(e, f, s, v);
     if (st || n == 0) return st;
-    const uint32_t grid = std::min<uint32_t>((n + PROXY_WARPS - 1) / PROXY_WARPS, (uint32_t)e->n_sms * 8);
+    const uint32_t grid = std::min<uint32_t>((n + PROXY_WARPS * 32 - 1) / (PROXY_WARPS * 32), (uint32_t)e->n_sms * 8);
     k_proxy<<<grid, PROXY_WARPS * 32, 0, s>>>(v, d_params, d_items, n, nullptr, d_grad_params, d_grad_value);
     CUDA_TRY(cudaGetLastError());
     e->launches++;

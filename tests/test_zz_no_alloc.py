@@ -38,47 +38,58 @@ def _filter(keys):
     return f, arr
 
 
-def test_noalloc_equals_detect_batch_two_calls(star_layout, jcde_mod):
+def _check_two_calls(eng, L, dq, n, filters, stream):
+    """jcde_detect_batch_noalloc equals jcde_detect_batch on each filter, called in a row; device
+    memory does not move across any call."""
     import torch
 
     from jcde import _ffi
-    from jcde import workload as W
 
-    lay, _ = star_layout
-    eng = _engine(lay)
-    L = jcde_mod.lib()
-    q = W.queries_for(lay, 1 << 17, 0xC1, sid=77)
-    dq = torch.from_numpy(q.view(np.uint8).copy()).cuda()
-    n = len(q)
-    stream = torch.cuda.current_stream().cuda_stream
-    placed = [hz.key for hz in lay.hazards if hz.dynamic][:25]
-    filters = [lay.filter_keys, placed + lay.filter_keys]   # second call: a different, larger filter
     ref = torch.empty(n, dtype=torch.uint8, device="cuda")
     got = torch.empty(n, dtype=torch.uint8, device="cuda")
     for i, keys in enumerate(filters):
         f, keep = _filter(keys)
         assert L.jcde_detect_batch(eng.h, dq.data_ptr(), n, C.byref(f), ref.data_ptr(), stream) == _ffi.OK
         torch.cuda.synchronize()
-        free_before = torch.cuda.mem_get_info()[0]
         got.fill_(0xAB)
+        free_before = torch.cuda.mem_get_info()[0]
         assert L.jcde_detect_batch_noalloc(eng.h, dq.data_ptr(), n, C.byref(f), got.data_ptr(), stream) == _ffi.OK
         torch.cuda.synchronize()
         free_after = torch.cuda.mem_get_info()[0]
-        assert torch.equal(ref, got), f"call {i}: {int((ref != got).sum())} verdicts differ"
-        if i == 1:   # the first call may load the new kernels' code; the second must not move memory
-            assert free_after >= free_before, (free_before, free_after)
+        assert torch.equal(ref, got), f"n={n} call {i}: {int((ref != got).sum())} verdicts differ"
+        assert free_after >= free_before, (n, i, free_before, free_after)
+
+
+@pytest.mark.parametrize("n", [256, 1 << 17, (1 << 18) + 5])
+def test_noalloc_equals_detect_batch_two_calls(star_layout, jcde_mod, n):
+    """Small batches (leaf-table polygon pass), the largest of those, and a large batch
+    (counter-fed large-batch passes)."""
+    import torch
+
+    from jcde import workload as W
+
+    lay, _ = star_layout
+    eng = _engine(lay)
+    L = jcde_mod.lib()
+    q = W.queries_for(lay, n, 0xC1, sid=77)
+    dq = torch.from_numpy(q.view(np.uint8).copy()).cuda()
+    stream = torch.cuda.current_stream().cuda_stream
+    placed = [hz.key for hz in lay.hazards if hz.dynamic][:25]
+    # second call: a different, larger filter (the array keeps the first call's mask)
+    _check_two_calls(eng, L, dq, n, [lay.filter_keys, placed + lay.filter_keys], stream)
     # the two filters give different answers somewhere, so the second call did not reuse the first's
-    f0, k0 = _filter(filters[0])
-    f1, k1 = _filter(filters[1])
-    a = torch.empty_like(got)
-    b = torch.empty_like(got)
-    L.jcde_detect_batch_noalloc(eng.h, dq.data_ptr(), n, C.byref(f0), a.data_ptr(), stream)
-    L.jcde_detect_batch_noalloc(eng.h, dq.data_ptr(), n, C.byref(f1), b.data_ptr(), stream)
-    torch.cuda.synchronize()
-    assert not torch.equal(a, b)
+    if n >= 1 << 17:
+        f0, k0 = _filter(lay.filter_keys)
+        f1, k1 = _filter(placed + lay.filter_keys)
+        a = torch.empty(n, dtype=torch.uint8, device="cuda")
+        b = torch.empty(n, dtype=torch.uint8, device="cuda")
+        L.jcde_detect_batch_noalloc(eng.h, dq.data_ptr(), n, C.byref(f0), a.data_ptr(), stream)
+        L.jcde_detect_batch_noalloc(eng.h, dq.data_ptr(), n, C.byref(f1), b.data_ptr(), stream)
+        torch.cuda.synchronize()
+        assert not torch.equal(a, b)
 
 
-def test_noalloc_refuses_what_it_cannot_do_without_allocating(strip_layout, jcde_mod):
+def test_noalloc_state_and_large_filters(strip_layout, jcde_mod):
     import torch
 
     from jcde import _ffi
@@ -96,7 +107,20 @@ def test_noalloc_refuses_what_it_cannot_do_without_allocating(strip_layout, jcde
     assert L.jcde_detect_batch_noalloc(eng.h, dq.data_ptr(), len(q), C.byref(f), out.data_ptr(), stream) == _ffi.ERR_STATE
     assert L.jcde_detect_batch(eng.h, dq.data_ptr(), 0, None, out.data_ptr(), stream) == _ffi.OK
     assert L.jcde_detect_batch_noalloc(eng.h, dq.data_ptr(), len(q), C.byref(f), out.data_ptr(), stream) == _ffi.OK
-    # more ignored keys than the static array holds
-    big, keep2 = _filter(np.arange(300_000) % 41)
-    assert L.jcde_detect_batch_noalloc(eng.h, dq.data_ptr(), len(q), C.byref(big), out.data_ptr(), stream) == _ffi.ERR_CAPACITY
+    # a filter of 300,000 keys (most beyond the engine's slots): the key list is turned into the
+    # bitmask on the host, so its length costs no device memory
+    _check_two_calls(eng, L, dq, len(q), [np.arange(300_000) % 41, [3, 5, 7]], stream)
+    # the caller's key buffer may be reused as soon as the call returns
+    keys = np.ascontiguousarray(np.array([1, 2, 3], np.uint32))
+    fk = _ffi.jcde_filter()
+    fk.ignored = keys.ctypes.data_as(C.POINTER(C.c_uint32))
+    fk.n_ignored = 3
+    a = torch.empty_like(out)
+    assert L.jcde_detect_batch_noalloc(eng.h, dq.data_ptr(), len(q), C.byref(fk), a.data_ptr(), stream) == _ffi.OK
+    keys[:] = [4, 5, 6]
     torch.cuda.synchronize()
+    f123, k123 = _filter([1, 2, 3])
+    ref = torch.empty_like(out)
+    assert L.jcde_detect_batch(eng.h, dq.data_ptr(), len(q), C.byref(f123), ref.data_ptr(), stream) == _ffi.OK
+    torch.cuda.synchronize()
+    assert torch.equal(a, ref)
