@@ -369,13 +369,16 @@ def replay(backend, lay: Layout):
 
 def strip_layout(backend, seed=0xC0, n_types=10, v_range=(8, 24), r_range=(20.0, 60.0), width=1000.0,
                  height=500.0, n_place=40, depth=DEFAULT_DEPTH, cd_threshold=DEFAULT_CD_THRESHOLD,
-                 chunk=256, max_attempts=1 << 16, name="strip"):
-    """Rectangular strip container with star items (the small CPU-runnable layout)."""
+                 chunk=256, max_attempts=1 << 16, name="strip", import_many=None):
+    """Rectangular strip container with star items (the small CPU-runnable layout).  `import_many`
+    (a list of raw shapes -> a list of Items, e.g. ``jcde.prep.import_items``) imports the item
+    types in one batch instead of one ``import_item`` call each; the Items must be the same."""
     st = Stream(seed, 1)
-    items = []
+    raws = []
     for _ in range(n_types):
         nv = int(st.randint(v_range[0], v_range[1], 1)[0])
-        items.append(import_item(backend, star_polygon(st, nv, *r_range)))
+        raws.append(star_polygon(st, nv, *r_range))
+    items = import_many(raws) if import_many is not None else [import_item(backend, r) for r in raws]
     outer = import_static(backend, rect_polygon(0.0, 0.0, width, height), EXTERIOR)
     lay = Layout(name, depth, cd_threshold, inflate_to_square(bbox_of(outer.xy)), items=items)
     lay.hazards.append(outer)
