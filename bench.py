@@ -12,7 +12,13 @@ detect_surrogate_collision || detect_poly_collision (lbf/benches/ci_bench.rs:107
             pinned host memory: host->device copy, kernel, device->host copy every step;
   roofline— algorithmic bytes per launch (oracle-counted per-query work of the same workload)
             over the kernel's event time, against the measured HBM peak;
-  cpu_baseline — the oracle (C++ restatement of the reference CDE) on all host cores, bounded sample.
+  cpu_baseline — the oracle (C++ restatement of the reference CDE) on all host cores, bounded sample;
+  roofline.l2 / roofline.issue — the dominant kernel against the project-measured L2 read peak
+            (jcde_l2_read_peak) and against its instruction-issue slots (ncu instruction count);
+  batched / proxy / lbf — the metric's other workloads in the same run (N=1): 64 layouts in one
+            launch sequence vs per-layout launches (configs[2]), grads/s and CDE-verified
+            placements/s of the pole-overlap proxy (configs[4]), and the device-resident LBF build
+            (configs[3]), each with its oracle check.
 
 `--impl reference` times the CPU restatement of the reference on the host cores instead (the
 reference itself is Rust and cannot be built here).
@@ -203,16 +209,35 @@ def cpu_baseline(lay, queries, n_sample: int, repeats: int = 3):
             "sample": f"first {n_sample} queries of the batch, best of {repeats}"}, work, verdicts
 
 
-def read_traffic(kernel: str):
-    """DRAM bytes per launch of `kernel` on this workload, from the committed ncu summary."""
+def read_profile(kernel: str) -> dict:
+    """Figures of `kernel` on this workload from its committed ncu summary (profiles/), per launch:
+    DRAM bytes, executed warp instructions, L2 sectors."""
     path = os.path.join(REPO, "profiles", f"{kernel}_star_1m.txt")
+    keys = {"dram_bytes_per_launch": "dram", "smsp__inst_executed.sum": "inst", "lts__t_sectors.sum": "l2_sectors"}
+    out = {}
     try:
         for line in open(path):
-            if line.startswith("dram_bytes_per_launch"):
-                return float(line.split("=")[1])
-    except OSError:
+            for k, name in keys.items():
+                if line.startswith(k):
+                    out[name] = float(line.split("=")[1])
+    except (OSError, ValueError):
         pass
-    return None
+    return out
+
+
+def read_traffic(kernel: str):
+    """DRAM bytes per launch of `kernel` on this workload, from the committed ncu summary."""
+    return read_profile(kernel).get("dram")
+
+
+def l2_read_peak(bytes_: int = 48 << 20, reps: int = 20):
+    """GB/s of the project's L2 streaming kernel (jcde_l2_read_peak) on an L2-resident buffer."""
+    import ctypes as C
+
+    from jcde._ffi import lib
+
+    g = C.c_double()
+    return g.value if lib().jcde_l2_read_peak(bytes_, reps, C.byref(g)) == 0 else None
 
 
 # ----------------------------------------------------------------------------------------------
@@ -398,6 +423,32 @@ def run_gpu(args):
     traffic = read_traffic(dom)
     order_ms, order_n = kprof["order"]
     clocks = clk.summary()
+    # the bounds this L2-resident, issue-limited kernel actually meets: L2 read bandwidth (the layout
+    # lives in L2) and instruction issue (4 schedulers per SM, one warp instruction each per cycle)
+    prof = read_profile(dom)
+    l2_peak = l2_read_peak()
+    n_sms = torch.cuda.get_device_properties(local).multi_processor_count
+    avg_s = kernels[dom]["avg_ms"] / 1e3
+    sm_hz = (clocks.get("sm_mhz") or 2070.0) * 1e6
+    issue = None
+    if prof.get("inst"):
+        issue = {"inst_per_launch": prof["inst"], "issue_slots_per_launch": n_sms * 4 * sm_hz * avg_s,
+                 "frac": prof["inst"] / (n_sms * 4 * sm_hz * avg_s), "sms": n_sms, "sm_mhz": sm_hz / 1e6,
+                 "inst_source": f"profiles/{dom}_star_1m.txt (ncu smsp__inst_executed.sum, one launch)"}
+    l2 = None
+    if l2_peak and prof.get("l2_sectors"):
+        l2_gbs = prof["l2_sectors"] * 32 / avg_s / 1e9
+        l2 = {"achieved": l2_gbs, "peak": l2_peak, "unit": "GB/s", "frac": l2_gbs / l2_peak,
+              "bytes_per_launch": prof["l2_sectors"] * 32,
+              "peak_source": "jcde_l2_read_peak: 48 MB L2-resident buffer, 20 passes of 16-byte ld.global.cg"}
+    sub = {}
+    if world == 1 and args.subrecords:
+        # the other headline workloads of the metric, measured on this GPU in the same run
+        t_sub = time.time()
+        sub["batched"] = measure_multi(min(args.steps, 20), args.warmup, bool(args.autotune))
+        sub["proxy"] = measure_proxy(min(args.steps, 5), 2, lay=lay)
+        sub["lbf"] = measure_lbf(min(args.steps, 5), 2, oracle_check=not args.no_cpu)
+        log(f"[bench] sub-records {time.time() - t_sub:.1f}s")
     line = {
         "metric": "collision queries/s", "value": value, "unit": "queries/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps,
@@ -408,6 +459,9 @@ def run_gpu(args):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "kernel": dom,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if peaks else "fallback 6.8 TB/s",
+                     "note": "achieved = oracle-counted algorithmic bytes / kernel time, a work rate: the layout is "
+                             "L2-resident, so the kernel's real limits are the l2 and issue entries",
+                     "l2": l2, "issue": issue,
                      "kernels": kernels, "ordering_ms_per_step": order_ms / max(1, order_n)},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": N_QUERIES * 20,
@@ -422,15 +476,17 @@ def run_gpu(args):
         "parity_sample": {"queries": args.cpu_sample, "bit_exact": sample_ok},
         "collision_rate": float(verdicts.mean()),
     }
+    line.update(sub)
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
 
 
-def run_multi(args):
-    """The multi-layout workload: 64 independent bin layouts, log-uniform 4,096-262,144 queries each, answered by
-    one launch sequence (CUDA graph) versus 64 per-layout jcde_detect_batch calls."""
+def measure_multi(steps: int, warmup: int, autotune: bool = True, parity_queries: int = 1024):
+    """configs[2]: 64 independent bin layouts, log-uniform 4,096-262,144 queries each, answered by one
+    launch sequence (CUDA graph) versus 64 per-layout jcde_detect_batch calls.  Returns the record;
+    the first `parity_queries` queries of every layout are checked against the oracle."""
     import torch
 
     import jcde
@@ -439,7 +495,8 @@ def run_multi(args):
     jcde.lib()
     t = time.time()
     lays = W.multi_layouts(jcde.GpuBackend)
-    log(f"[bench] {len(lays)} layouts, {sum(len(l.hazards) for l, _ in lays)} hazards ({time.time() - t:.1f}s)")
+    gen_s = time.time() - t
+    log(f"[bench] {len(lays)} layouts, {sum(len(l.hazards) for l, _ in lays)} hazards ({gen_s:.1f}s)")
     engines = [e.eng for _, e in lays]
     q, offs = W.multi_queries(lays)
     n = int(offs[-1])
@@ -451,7 +508,7 @@ def run_multi(args):
     m = jcde.MultiEngine(engines)
     qb = W.QUERY_DTYPE.itemsize
     # launch choices of the batched sequence timed on this batch (jcde_multi_autotune; verdicts checked)
-    multi_tuning, _ = m.autotune(dq, offs, stream=stream) if args.autotune else ({"poly_chunk": 2, "ordered": True}, 0)
+    multi_tuning, _ = m.autotune(dq, offs, stream=stream) if autotune else ({"poly_chunk": 2, "ordered": True}, 0)
 
     def plain():
         for l, eng in enumerate(engines):
@@ -464,11 +521,11 @@ def run_multi(args):
     res = {}
     with torch.cuda.stream(stream):
         for name, fn in (("plain", plain), ("batched", batched)):
-            for _ in range(args.warmup):
+            for _ in range(warmup):
                 fn()
             stream.synchronize()
             ms = []
-            for _ in range(args.steps):
+            for _ in range(steps):
                 flush.zero_()
                 a_ev, b_ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                 a_ev.record(stream)
@@ -476,39 +533,67 @@ def run_multi(args):
                 b_ev.record(stream)
                 ms.append((a_ev, b_ev))
             stream.synchronize()
-            res[name] = sum(a.elapsed_time(b) for a, b in ms) / args.steps
+            res[name] = sum(a.elapsed_time(b) for a, b in ms) / steps
     same = bool(torch.equal(out_plain, out_multi))
-    line = {
-        "metric": "multi-layout collision queries/s", "value": n / (res["batched"] / 1e3), "unit": "queries/s",
-        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["batched"],
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"{len(lays)} star-container bins (32-128 v), 20-400 items each from 40 star types "
-                               f"(8-200 v), log-uniform 4,096-262,144 queries per bin ({n} total)",
-                   "batched": "one ordering + surrogate + polygon launch sequence, CUDA-graph replay",
-                   "plain": f"{len(lays)} jcde_detect_batch calls, one per layout",
-                   "l2": "flushed between steps (256 MB write)"},
+    # oracle parity on a sample of every layout (CPU leg, after the timed region)
+    from oracle import oracle as O
+
+    O.build()
+    got = out_multi.cpu().numpy()
+    mism = 0
+    for l, (lay, _) in enumerate(lays):
+        a = int(offs[l])
+        ref = W.replay(O.OracleBackend, lay).detect_batch(q[a:a + parity_queries], n_threads=host_cores())
+        mism += int((ref != got[a:a + parity_queries]).sum())
+    return {
+        "value": n / (res["batched"] / 1e3), "unit": "queries/s", "ms_per_step": res["batched"],
+        "queries_per_step": n, "layouts": len(lays),
         "plain": {"value": n / (res["plain"] / 1e3), "ms_per_step": res["plain"]},
         "speedup_vs_plain": res["plain"] / res["batched"],
         "batched_tuning": multi_tuning,
-        "same_verdicts": same,
+        "same_verdicts_as_plain": same,
+        "oracle_parity": {"queries": parity_queries * len(lays), "mismatches": mism, "bit_exact": mism == 0},
+        "layout_generation_s": gen_s,
+    }
+
+
+def run_multi(args):
+    """The multi-layout workload as its own bench line."""
+    r = measure_multi(args.steps, args.warmup, bool(args.autotune))
+    line = {
+        "metric": "multi-layout collision queries/s", "value": r["value"], "unit": "queries/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": MULTI_WORKLOAD.format(n=r["queries_per_step"]),
+                   "batched": "one ordering + surrogate + polygon launch sequence, CUDA-graph replay",
+                   "plain": f"{r['layouts']} jcde_detect_batch calls, one per layout",
+                   "l2": "flushed between steps (256 MB write)"},
         "impl": "jcde",
     }
+    line.update({k: v for k, v in r.items() if k not in ("value", "unit", "ms_per_step")})
     print(json.dumps(line), flush=True)
     return 0
 
 
-def run_proxy(args):
-    """The gradient-separation workload: the star layout with surrogate poles on every interior hazard; 1,048,576 colliding
-    candidates; 20 gradient steps on the pole-overlap proxy then the exact verdict, versus 20 random
-    perturbations per candidate judged by the exact verdict.  Metric: verified collision-free
-    placements per second."""
+MULTI_WORKLOAD = ("64 star-container bins (32-128 v), 20-400 items each from 40 star types (8-200 v), "
+                  "log-uniform 4,096-262,144 queries per bin ({n} total)")
+
+
+def measure_proxy(steps: int, warmup: int, lay=None, grad_check: int = 1 << 16):
+    """configs[4], the gradient-separation workload: the star layout with surrogate poles on every
+    interior hazard; 1,048,576 colliding candidates.  Measures (a) grads/s: the pole-overlap proxy and
+    its adjoint d/d(theta, tx, ty) for every candidate (jcde_proxy_batch), (b) verified collision-free
+    placements/s: 20 descent steps on the proxy then the exact verdict, versus 20 random
+    perturbations per candidate judged by the exact verdict, (c) the gradient against an FP64
+    evaluation of the same float32 inputs on `grad_check` candidates."""
     import torch
 
     import jcde
     from jcde import workload as W
 
     jcde.lib()
-    lay, _ = make_layout(jcde.GpuBackend)
+    if lay is None:
+        lay, _ = make_layout(jcde.GpuBackend)
     eng = gpu_engine_for(lay)
     hp = W.hazard_poles(jcde.GpuBackend, lay)
     keys = hp[:, 3].view(np.uint32)
@@ -538,6 +623,12 @@ def run_proxy(args):
     CLEARANCE = 20.0   # poles under-cover the star items' spikes: separate the poles by a margin
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     out_k = torch.empty(n * K, dtype=torch.uint8, device="cuda")
+    g_val = torch.empty(n, dtype=torch.float32, device="cuda")
+    g_grad = torch.empty(n, 3, dtype=torch.float32, device="cuda")
+
+    def grads():
+        eng.proxy_batch(P0, I0, filter=filt, out=(g_val, g_grad))
+        return torch.zeros((), dtype=torch.int64, device="cuda") + n
 
     def gd():
         p = P0.clone()
@@ -551,12 +642,12 @@ def run_proxy(args):
         return (out_k.view(n, K) == 0).any(dim=1).sum()
 
     res = {}
-    for name, fn in (("gradient", gd), ("random", rnd)):
-        for _ in range(args.warmup):
+    for name, fn in (("grads", grads), ("gradient", gd), ("random", rnd)):
+        for _ in range(warmup):
             fn()
         torch.cuda.synchronize()
         ms, succ = 0.0, 0
-        for _ in range(args.steps):
+        for _ in range(steps):
             flush.zero_()
             a_ev, b_ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a_ev.record()
@@ -565,8 +656,7 @@ def run_proxy(args):
             torch.cuda.synchronize()
             ms += a_ev.elapsed_time(b_ev)
             succ += int(s_.item())
-        res[name] = {"placements_per_s": succ / (ms / 1e3), "verified_free": succ // args.steps,
-                     "ms_per_step": ms / args.steps, "candidates": n}
+        res[name] = {"per_s": succ / (ms / 1e3), "count": succ // steps, "ms_per_step": ms / steps, "candidates": n}
     # the other settings of both methods (one timed run each): descent lengths and copies per candidate
     def once(fn):
         fn()
@@ -580,12 +670,12 @@ def run_proxy(args):
         return int(s_.item()) / (a_ev.elapsed_time(b_ev) / 1e3)
 
     sweep = {}
-    for steps in (5, 10, 20):
-        def gd_s(steps=steps):
-            q, _ = eng.separate_batch(P0.clone(), I0, steps=steps, step_t=0.25, step_th=0.25, clearance=CLEARANCE,
+    for steps_ in (5, 10, 20):
+        def gd_s(steps_=steps_):
+            q, _ = eng.separate_batch(P0.clone(), I0, steps=steps_, step_t=0.25, step_th=0.25, clearance=CLEARANCE,
                                       filter=filt)
             return (eng.detect_batch(q, filter=filt) == 0).sum()
-        sweep[f"gradient_{steps}_steps"] = once(gd_s)
+        sweep[f"gradient_{steps_}_steps"] = once(gd_s)
     for kk in (1, 2, 5, 10, 20):
         out_kk = torch.empty(n * kk, dtype=torch.uint8, device="cuda")
         def rnd_k(kk=kk, out_kk=out_kk):
@@ -595,36 +685,53 @@ def run_proxy(args):
         sweep[f"random_{kk}_copies"] = once(rnd_k)
     best_g = max(v for k, v in sweep.items() if k.startswith("gradient"))
     best_r = max(v for k, v in sweep.items() if k.startswith("random"))
-    # gradient accuracy on a sample against the FP64 oracle (test infrastructure, CPU leg)
+    # gradient accuracy against the FP64 evaluation (test infrastructure, CPU leg)
     from oracle import oracle as O
 
     O.build()
-    ns = 4096
-    val, grad = eng.proxy_batch(P0[:ns].contiguous(), I0[:ns].contiguous(), filter=filt)
+    ns = min(grad_check, n)
+    v32 = g_val[:ns].cpu().numpy().astype(np.float64)
+    g32 = g_grad[:ns].cpu().numpy().astype(np.float64)
     v64, g64 = O.proxy_f64(P0[:ns].cpu().numpy(), I0[:ns].cpu().numpy().astype(np.uint32),
-                           [it.poles for it in lay.items], hp, ignored=filt)
-    g32 = grad.cpu().numpy().astype(np.float64)
-    on = v64 > 1e-2
-    rel = np.linalg.norm(g32[on] - g64[on], axis=1) / np.linalg.norm(g64[on], axis=1)
-    line = {
-        "metric": "CDE-verified collision-free placements/s (gradient separation)",
-        "value": res["gradient"]["placements_per_s"], "unit": "placements/s", "n_gpus": 1, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": res["gradient"]["ms_per_step"], "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"star layout with surrogate poles on {len(np.unique(keys))} hazards; {n} colliding "
-                               "candidates; 20 descent steps on the pole-overlap proxy (hazard poles grown by a "
-                               "20-unit clearance) then jcde_detect_batch",
-                   "random_arm": f"{K} Gaussian perturbations per candidate (sigma_t={mean_r:.1f}, sigma_th=0.25) "
-                                 "then jcde_detect_batch",
-                   "l2": "flushed between steps (256 MB write)"},
-        "gradient": res["gradient"], "random": res["random"],
-        "speedup_vs_random": res["gradient"]["placements_per_s"] / res["random"]["placements_per_s"],
+                           [it.poles for it in lay.items], hp, ignored=filt, n_threads=host_cores())
+    n64 = np.linalg.norm(g64, axis=1)
+    on = n64 > 0
+    rel = np.linalg.norm(g32[on] - g64[on], axis=1) / n64[on]
+    rel_v = np.abs(v32[v64 > 0] - v64[v64 > 0]) / v64[v64 > 0]
+    return {
+        "grads_per_s": res["grads"]["per_s"], "grads_ms_per_step": res["grads"]["ms_per_step"],
+        "value": res["gradient"]["per_s"], "unit": "placements/s", "ms_per_step": res["gradient"]["ms_per_step"],
+        "candidates": n, "hazards_with_poles": int(len(np.unique(keys))),
+        "gradient": {"placements_per_s": res["gradient"]["per_s"], "verified_free": res["gradient"]["count"],
+                     "ms_per_step": res["gradient"]["ms_per_step"]},
+        "random": {"placements_per_s": res["random"]["per_s"], "verified_free": res["random"]["count"],
+                   "ms_per_step": res["random"]["ms_per_step"]},
+        "speedup_vs_random": res["gradient"]["per_s"] / res["random"]["per_s"],
         "settings_sweep_placements_per_s": sweep,
         "best_setting_speedup": best_g / best_r,
         "grad_rel_err_vs_fp64": {"median": float(np.median(rel)), "p99": float(np.percentile(rel, 99)),
-                                 "max": float(rel.max()), "samples": int(on.sum())},
+                                 "max": float(rel.max()), "candidates": int(ns), "with_gradient": int(on.sum()),
+                                 "value_max_rel_err": float(rel_v.max()) if len(rel_v) else 0.0},
+        "random_arm": f"{K} Gaussian perturbations per candidate (sigma_t={mean_r:.1f}, sigma_th=0.25) then "
+                      "jcde_detect_batch",
+    }
+
+
+def run_proxy(args):
+    """The gradient-separation workload as its own bench line."""
+    r = measure_proxy(args.steps, args.warmup)
+    line = {
+        "metric": "CDE-verified collision-free placements/s (gradient separation)",
+        "value": r["value"], "unit": "placements/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"star layout with surrogate poles on {r['hazards_with_poles']} hazards; "
+                               f"{r['candidates']} colliding candidates; 20 descent steps on the pole-overlap proxy "
+                               "(hazard poles grown by a 20-unit clearance) then jcde_detect_batch",
+                   "random_arm": r["random_arm"], "l2": "flushed between steps (256 MB write)"},
         "impl": "jcde",
     }
+    line.update({k: v for k, v in r.items() if k not in ("value", "unit", "ms_per_step", "random_arm")})
     print(json.dumps(line), flush=True)
     return 0
 
@@ -834,13 +941,14 @@ def run_bpp(args):
     return 0
 
 
-def run_lbf(args):
-    """The LBF-style strip build on the device-resident engine.  2000 steps, each: 16384
+def measure_lbf(steps: int, warmup: int, oracle_check: bool = True, extras: bool = False, cpu_steps: int = 0):
+    """configs[3], the LBF-style strip build on the device-resident engine.  2000 steps, each: 16384
     candidates generated and searched as lbf's search does (surrogate pass for all; the polygon pass
     for those that could still beat the best free one, search.rs:52-56), the least-cost free one
     registered on the device, and a random placed item deregistered every 50 steps.  A timed step is
     one whole build from the strip's initial state.  Metric: candidate placements searched per
-    second over the build."""
+    second over the build.  With `oracle_check` the same build is driven through the oracle and its
+    placements, removals and final quadtree are compared with the device build's."""
     import torch
 
     import jcde
@@ -855,7 +963,7 @@ def run_lbf(args):
     stream = torch.cuda.Stream()   # a captured graph needs a stream other than the legacy default one
     sh = stream.cuda_stream
 
-    def build(timed):
+    def build():
         r.reset()
         r.lbf_begin(spec.seed, spec.n_cand, spec.n_types, spec.remove_every, spec.steps, spec.box)
         with torch.cuda.stream(stream):
@@ -867,110 +975,119 @@ def run_lbf(args):
         torch.cuda.synchronize()
         return a.elapsed_time(b)
 
-    for _ in range(args.warmup):
-        build(False)
+    for _ in range(warmup):
+        build()
     launches0 = r.kernel_launches()
     clk = ClockSampler(0)
     clk.__enter__()
     profiler_range(True)
-    times = [build(True) for _ in range(args.steps)]
+    times = [build() for _ in range(steps)]
     profiler_range(False)
     launches = r.kernel_launches() - launches0
     clk.__exit__()
     ms = float(np.sum(times))
     n_cand_total = spec.steps * spec.n_cand
-    value = n_cand_total * args.steps / (ms / 1e3)
     d = r.lbf_read()
     st = r.status()
-    # per-kernel shares from one eager, profiled build (events around every launch)
-    geng.eng.profile(True)
-    r.reset()
-    r.lbf_begin(spec.seed, spec.n_cand, spec.n_types, spec.remove_every, spec.steps, spec.box)
-    geng.eng.profile_read(reset=True)
-    r.lbf_steps(spec.steps, 0, stream=sh)
-    kp = geng.eng.profile_read(reset=True)
-    geng.eng.profile(False)
-    kinds = {k: {"ms_per_build": v[0], "launches": v[1]} for k, v in kp.items() if v[1]}
-    dominant = max(kinds, key=lambda k: kinds[k]["ms_per_build"])
+    dev_tree = r.tree_dump()
+    rec = {
+        "value": n_cand_total * steps / (ms / 1e3), "unit": "candidates/s", "ms_per_build": ms / steps,
+        "lbf_steps_per_s": spec.steps * steps / (ms / 1e3),
+        "placed": int(len(d["placements"])), "removed": int(len(d["removals"])), "live": d["n_live"],
+        "pool_use": st, "gpu_launches": int(launches), "clocks": clk.summary(),
+        "workload": (f"LBF strip build: {spec.n_types} star types ({spec.v_range[0]}-{spec.v_range[1]} vertices), "
+                     f"{spec.width:.0f} x {spec.height:.0f} strip, {spec.steps} steps x {spec.n_cand} candidates, "
+                     f"removal every {spec.remove_every} steps; one timed step = one whole build; register/deregister "
+                     f"on the device; {SPG} LBF steps per CUDA graph launch"),
+    }
     # end to end through the public API: resident copy from the host engine, the build, the log read back
     e2e_ms = []
     h2d = d2h = 0
-    for _ in range(max(1, min(args.steps, 5))):
+    for _ in range(max(1, min(steps, 3))):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         h2d = r.reset()
         log_e2e, _ = lbf.run_device(geng, spec, steps_per_graph=SPG, resident=r)
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
         d2h = (log_e2e.placements.nbytes + log_e2e.removals.nbytes + log_e2e.free_counts.nbytes + 16)
-    e2e_value = n_cand_total / (np.median(e2e_ms) / 1e3)
-    # the same build with three local-search rounds of 2048 candidates per step (search.rs:80-101 restated)
-    spec_ls = lbf.LbfSpec(ls_rounds=3, ls_cand=2048, ls_sigma_t=200.0, ls_sigma_turns=0.05)
-    ls_ms = []
-    for k in range(2):
-        r.reset()
-        r.lbf_begin(spec_ls.seed, spec_ls.n_cand, spec_ls.n_types, spec_ls.remove_every, spec_ls.steps, spec_ls.box, 0,
-                    spec_ls.ls_rounds, spec_ls.ls_cand, spec_ls.ls_sigma_t, spec_ls.ls_sigma_turns, spec_ls.ls_decay)
-        with torch.cuda.stream(stream):
-            flush.zero_()
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        r.lbf_steps(spec_ls.steps, SPG, stream=sh)
-        b.record(stream)
-        torch.cuda.synchronize()
-        if k:
-            ls_ms.append(a.elapsed_time(b))
-    d_ls = r.lbf_read()
-    ls_cands = spec_ls.steps * (spec_ls.n_cand + spec_ls.ls_rounds * spec_ls.ls_cand)
-    local_search = {"ms_per_build": ls_ms[0], "candidates_per_s": ls_cands / (ls_ms[0] / 1e3),
-                    "rounds": spec_ls.ls_rounds, "candidates_per_round": spec_ls.ls_cand,
-                    "placements_improved_by_local_search": int(((d_ls["placements"][:, 2] >> 24) > 0).sum())}
-    # the same build driven step by step from the host through the regular engine (host registration,
-    # a re-flattened tree upload per step): a bounded sample of its first steps
-    host_steps = 200
-    lay_h, geng_h = lbf.setup(jcde.GpuBackend, spec)
-    t0 = time.perf_counter()
-    hlog = lbf.run_host(lay_h, geng_h, spec, steps=host_steps)
-    host_s = time.perf_counter() - t0
-    host_ok = bool(np.array_equal(hlog.placements, d["placements"][: len(hlog.placements)]))
-    line = {
-        "metric": "LBF candidate placements searched per second (device-resident build)",
-        "value": value, "unit": "candidates/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"LBF strip build: {spec.n_types} star types ({spec.v_range[0]}-{spec.v_range[1]} "
-                               f"vertices), {spec.width:.0f} x {spec.height:.0f} strip, {spec.steps} steps x "
-                               f"{spec.n_cand} candidates, removal every {spec.remove_every} steps; one timed step = "
-                               "one whole build; register/deregister on the device; "
-                               f"{SPG} LBF steps per CUDA graph launch",
-                   "l2": "flushed between builds (256 MB write)"},
-        "lbf_steps_per_s": spec.steps * args.steps / (ms / 1e3),
-        "placed": int(len(d["placements"])), "removed": int(len(d["removals"])), "live": d["n_live"],
-        "pool_use": st,
-        "kernels_eager_build": kinds, "dominant": dominant,
-        "gpu_launches": int(launches),
-        "e2e": {"value": e2e_value, "unit": "candidates/s", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h), "ms_per_build": float(np.median(e2e_ms))},
-        "with_local_search": local_search,
-        "host_driven_gpu": {"value": host_steps * spec.n_cand / host_s, "unit": "candidates/s",
-                            "sample": f"first {host_steps} steps", "same_placements": host_ok},
-        "clocks": clk.summary(),
-        "impl": "jcde",
-    }
-    if not args.no_cpu:
+    rec["e2e"] = {"value": n_cand_total / (np.median(e2e_ms) / 1e3), "unit": "candidates/s",
+                  "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "ms_per_build": float(np.median(e2e_ms))}
+    if oracle_check:
         from oracle import oracle as O
 
         O.build()
-        cpu_steps = args.lbf_cpu_steps
         lay_o, oeng = lbf.setup(O.OracleBackend, spec)
         t0 = time.perf_counter()
-        olog = lbf.run_host(lay_o, oeng, spec, steps=cpu_steps)
+        olog = lbf.run_host(lay_o, oeng, spec)
         cpu_s = time.perf_counter() - t0
-        line["cpu_baseline"] = {"value": cpu_steps * spec.n_cand / cpu_s, "unit": "candidates/s",
-                                "cores": host_cores(), "kind": "port",
-                                "sample": f"first {cpu_steps} of {spec.steps} steps, oracle detect on all cores, "
-                                          "numpy choice, oracle register",
-                                "same_placements": bool(np.array_equal(olog.placements,
-                                                                       d["placements"][: len(olog.placements)]))}
+        rec["oracle_check"] = {
+            "same_placements": bool(np.array_equal(olog.placements, d["placements"])),
+            "same_removals": bool(np.array_equal(olog.removals, d["removals"])),
+            "same_final_tree": bool(np.array_equal(oeng.tree_dump(), dev_tree)),
+            "oracle_build_s": cpu_s, "oracle_cores": host_cores()}
+        rec["cpu_baseline"] = {"value": n_cand_total / cpu_s, "unit": "candidates/s", "cores": host_cores(),
+                               "kind": "port", "sample": "the whole build: oracle detect on all cores, numpy choice, "
+                                                         "oracle register"}
+    if extras:
+        # per-kernel shares from one eager, profiled build (events around every launch)
+        geng.eng.profile(True)
+        r.reset()
+        r.lbf_begin(spec.seed, spec.n_cand, spec.n_types, spec.remove_every, spec.steps, spec.box)
+        geng.eng.profile_read(reset=True)
+        r.lbf_steps(spec.steps, 0, stream=sh)
+        kp = geng.eng.profile_read(reset=True)
+        geng.eng.profile(False)
+        kinds = {k: {"ms_per_build": v[0], "launches": v[1]} for k, v in kp.items() if v[1]}
+        rec["kernels_eager_build"] = kinds
+        rec["dominant"] = max(kinds, key=lambda k: kinds[k]["ms_per_build"])
+        # the same build with three local-search rounds of 2048 candidates per step (search.rs:80-101)
+        spec_ls = lbf.LbfSpec(ls_rounds=3, ls_cand=2048, ls_sigma_t=200.0, ls_sigma_turns=0.05)
+        ls_ms = []
+        for k in range(2):
+            r.reset()
+            r.lbf_begin(spec_ls.seed, spec_ls.n_cand, spec_ls.n_types, spec_ls.remove_every, spec_ls.steps,
+                        spec_ls.box, 0, spec_ls.ls_rounds, spec_ls.ls_cand, spec_ls.ls_sigma_t, spec_ls.ls_sigma_turns,
+                        spec_ls.ls_decay)
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            r.lbf_steps(spec_ls.steps, SPG, stream=sh)
+            b.record(stream)
+            torch.cuda.synchronize()
+            if k:
+                ls_ms.append(a.elapsed_time(b))
+        d_ls = r.lbf_read()
+        ls_cands = spec_ls.steps * (spec_ls.n_cand + spec_ls.ls_rounds * spec_ls.ls_cand)
+        rec["with_local_search"] = {
+            "ms_per_build": ls_ms[0], "candidates_per_s": ls_cands / (ls_ms[0] / 1e3), "rounds": spec_ls.ls_rounds,
+            "candidates_per_round": spec_ls.ls_cand,
+            "placements_improved_by_local_search": int(((d_ls["placements"][:, 2] >> 24) > 0).sum())}
+        # the same build driven step by step from the host through the regular engine (host
+        # registration, a re-flattened tree upload per step): a bounded sample of its first steps
+        host_steps = 200
+        lay_h, geng_h = lbf.setup(jcde.GpuBackend, spec)
+        t0 = time.perf_counter()
+        hlog = lbf.run_host(lay_h, geng_h, spec, steps=host_steps)
+        host_s = time.perf_counter() - t0
+        rec["host_driven_gpu"] = {
+            "value": host_steps * spec.n_cand / host_s, "unit": "candidates/s", "sample": f"first {host_steps} steps",
+            "same_placements": bool(np.array_equal(hlog.placements, d["placements"][: len(hlog.placements)]))}
+    return rec
+
+
+def run_lbf(args):
+    """The LBF build as its own bench line."""
+    r = measure_lbf(args.steps, args.warmup, oracle_check=not args.no_cpu, extras=True)
+    line = {
+        "metric": "LBF candidate placements searched per second (device-resident build)",
+        "value": r["value"], "unit": "candidates/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": r["ms_per_build"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": r["workload"], "l2": "flushed between builds (256 MB write)"},
+        "impl": "jcde",
+    }
+    line.update({k: v for k, v in r.items() if k not in ("value", "unit", "workload")})
     print(json.dumps(line), flush=True)
     return 0
 
@@ -984,7 +1101,8 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=1 << 17)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--autotune", type=int, default=1, help="1: jcde_autotune on the batch before timing")
-    ap.add_argument("--lbf-cpu-steps", type=int, default=2000)
+    ap.add_argument("--subrecords", type=int, default=1,
+                    help="1: the default (star) line also measures the batched multi-layout, proxy and LBF workloads")
     ap.add_argument("--prep-shapes", type=int, default=1024, help="prep workload: shapes per batch")
     ap.add_argument("--workload", default="star", choices=["star", "multi", "proxy", "lbf", "prep", "bpp"],
                     help="star: the headline single-layout batch; multi: 64 layouts in one launch sequence; "

@@ -2230,3 +2230,17 @@ extern "C" jcde_status jcde_multi_autotune(jcde_multi* m, const jcde_query* dq, 
     if (best_ms) *best_ms = st ? 0.0 : best_t;
     return st;
 }
+
+#ifdef JCDE_POLY_STATS
+// The polygon pass's work counters (measurement builds only; see kernels.cuh).
+extern "C" jcde_status jcde_poly_stats(unsigned long long* out16, int reset) {
+    if (!out16) return JCDE_ERR_ARG;
+    CUDA_TRY(cudaDeviceSynchronize());
+    CUDA_TRY(cudaMemcpyFromSymbol(out16, g_poly_stats, 16 * sizeof(unsigned long long)));
+    if (reset) {
+        static const unsigned long long zero[16] = {};
+        CUDA_TRY(cudaMemcpyToSymbol(g_poly_stats, zero, sizeof(zero)));
+    }
+    return JCDE_OK;
+}
+#endif

@@ -29,6 +29,19 @@ namespace jcde {
 constexpr uint32_t FULL = 0xffffffffu;
 constexpr int MAX_DEPTH = 15;   // 4 pending bits per level in a 64-bit register
 
+// Work counters of the polygon pass, compiled in only with -DJCDE_POLY_STATS (a measurement build;
+// every count is an atomic add, so such a build is not for timing).  Slots: 0 loop iterations,
+// 1 active lanes summed over iterations, 2 iterations with <= 8 active lanes, 3 internal-node
+// visits, 4 leaf visits, 5 leaf entries scanned, 6 edge groups tested, 7 hazard edges tested,
+// 8 queries, 9 queries decided by the edge loop, 10 containment tests run as a warp, 11 jobs
+// (edges, or listed edge walks below the virtual root), 12 visits ending at Entire/None nodes.
+#ifdef JCDE_POLY_STATS
+static __device__ unsigned long long g_poly_stats[16];
+#define PSTAT(i, v) atomicAdd(&g_poly_stats[i], (unsigned long long)(v))
+#else
+#define PSTAT(i, v) ((void)0)
+#endif
+
 struct View {
     const DNode* __restrict__ nodes;
     const DEntry* __restrict__ entries;
@@ -163,6 +176,7 @@ __device__ __forceinline__ bool leaf_hits(const View& v, const P& p, const DNode
     for (uint32_t k = 0; k < nd.hz_cnt; k++) {
         if (stop && *stop) return false;
         DEntry e = ld_entry(v, nd.hz_off + k);
+        PSTAT(5, 1);
         // (the filter lookup, a dependent load, comes last: the tests commute)
         if (e.presence != PRES_PARTIAL || !p_hits_box(p, e.ff)) continue;   // qt_partial_hazard.rs:67-71
         if (filtered(v, e.hkey)) continue;
@@ -174,8 +188,10 @@ __device__ __forceinline__ bool leaf_hits(const View& v, const P& p, const DNode
                 const float py0 = fmn(p.s.y, p.e.y), py1 = fmx(p.s.y, p.e.y);
                 for (uint32_t g = 0; g * EDGE_GROUP < e.edge_cnt; g++) {
                     const float4 c = __ldg(&v.cbox[e.edge_off / EDGE_GROUP + g]);
+                    PSTAT(6, 1);
                     if (fmx(px0, c.x) > fmn(px1, c.z) || fmx(py0, c.y) > fmn(py1, c.w)) continue;
                     const uint32_t end = min(e.edge_cnt, g * EDGE_GROUP + EDGE_GROUP);
+                    PSTAT(7, end - g * EDGE_GROUP);
                     for (uint32_t j = g * EDGE_GROUP; j < end; j++)
                         if (p_hits_seg(p, ld_edge(v, e.edge_off + j))) {
                             if (stop) *stop = 1;
@@ -222,15 +238,22 @@ __device__ __forceinline__ bool leaf_hits(const View& v, const P& p, const DNode
 template <class P, typename PendT>
 __device__ __forceinline__ bool walk_step(const View& v, const P& p, WalkT<PendT>& w, volatile int* stop) {
     const uint32_t st = __ldg(&v.strength[w.node]);
-    if (st == PRES_ENTIRE) return true;
+    if (st == PRES_ENTIRE) {
+        PSTAT(12, 1);
+        return true;
+    }
     if (st == PRES_PARTIAL) {
         DNode nd = ld_node(v, w.node);
         if (nd.child >= 0) {
+            PSTAT(3, 1);
             const uint32_t m = p_quad_mask(p, nd.box);
             if (m) walk_push(w, m, nd.child);
-        } else if (leaf_hits(v, p, nd, stop)) {
-            return true;
+        } else {
+            PSTAT(4, 1);
+            if (leaf_hits(v, p, nd, stop)) return true;
         }
+    } else {
+        PSTAT(12, 1);
     }
     w.node = walk_next(v, w);
     return false;
@@ -929,6 +952,16 @@ __device__ __forceinline__ void poly_query(const View& v, const uint32_t* __rest
         next += __popc(need);
         const bool active = w.node >= 0;
         if (!__any_sync(FULL, active)) break;
+#ifdef JCDE_POLY_STATS
+        {
+            const uint32_t na = __popc(__ballot_sync(FULL, active));
+            if (lane == 0) {
+                PSTAT(0, 1);
+                PSTAT(1, na);
+                if (na <= 8) PSTAT(2, 1);
+            }
+        }
+#endif
         bool h = false;
         if (active) {
             if constexpr (TAB) h = walk_step_tab(v, e, w, stop, tab);
@@ -936,6 +969,11 @@ __device__ __forceinline__ void poly_query(const View& v, const uint32_t* __rest
             if (!h && w.node < 0) w.node = -1;
         }
         hit = __any_sync(FULL, h);
+    }
+    if (lane == 0) {
+        PSTAT(8, 1);
+        PSTAT(9, hit ? 1 : 0);
+        PSTAT(11, n_jobs);
     }
     if (!hit) {
         // containment of the shape in (or of) the partially present hazards of the virtual root
@@ -968,6 +1006,7 @@ __device__ __forceinline__ void poly_query(const View& v, const uint32_t* __rest
                 todo &= todo - 1;
                 const int nd = __shfl_sync(FULL, need, src);
                 const uint32_t hkk = __shfl_sync(FULL, hk, src);
+                if (lane == 0) PSTAT(10, 1);
                 hit = warp_containment(v, sh, sb, spoi, hkk, nd, lane);
             }
         }

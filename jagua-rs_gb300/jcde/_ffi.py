@@ -7,7 +7,9 @@ import subprocess
 
 PKG_DIR = os.path.dirname(os.path.abspath(__file__))
 ROOT_DIR = os.path.dirname(PKG_DIR)
-LIB_PATH = os.path.join(PKG_DIR, "libjcde.so")
+# JCDE_LIBRARY names another build of the same library (e.g. one compiled with other launch-shape
+# defaults); there is no fallback to anything but a libjcde build.
+LIB_PATH = os.environ.get("JCDE_LIBRARY") or os.path.join(PKG_DIR, "libjcde.so")
 
 OK, ERR_ARG, ERR_CUDA, ERR_CAPACITY, ERR_NOT_FOUND, ERR_TIMEOUT, ERR_STATE = 0, -1, -2, -3, -4, -5, -6
 
@@ -116,6 +118,7 @@ SIGNATURES = {
     "jcde_tree_dump": (C.c_int32, [P, u32p, C.c_uint64, u64p]),
     "jcde_device_stats": (C.c_int32, [P, u64p]),
     "jcde_kernel_launches": (C.c_uint64, [P]),
+    "jcde_l2_read_peak": (C.c_int32, [C.c_uint64, C.c_uint32, C.POINTER(C.c_double)]),
     "jcde_profile_enable": (C.c_int32, [P, C.c_int]),
     "jcde_multi_create": (C.c_int32, [C.POINTER(P), C.c_uint32, C.POINTER(P)]),
     "jcde_set_hazard_poles": (C.c_int32, [P, C.c_uint32, f32p, C.c_uint32]),
