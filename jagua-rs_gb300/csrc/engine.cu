@@ -102,6 +102,7 @@ struct jcde_engine {
     DevBuf d_q, d_out, d_raw, d_coll;
     DevBuf d_hist, d_order;   // spatial ordering of a query batch
     DevBuf d_next;            // work counters of the two passes (a pair per pipeline slot)
+    DevBuf d_pend, d_pendc;   // undecided queries of the surrogate pass and their count (per pipeline slot)
     // hazard poles binned in a uniform grid (overlap proxy)
     uint64_t pole_version = ~0ull;
     DevBuf d_hpoles, d_hpstart, d_hpoles_c, d_hpstart_c;
@@ -459,8 +460,13 @@ static const uint32_t* spatial_order_into(jcde_engine* e, const uint32_t* q, uin
 template <typename PendT>
 static bool launch_passes_t(jcde_engine* e, const View& v, const uint32_t* q, uint32_t n, uint8_t* dout,
                             cudaStream_t s, RawShape raw, int mode, const uint32_t* order, uint32_t* next,
-                            unsigned long long* best, uint32_t* n_pending, bool skip) {
+                            unsigned long long* best, uint32_t* n_pending, bool skip, PendList pend) {
     bool chose = false;
+    // the compacted list of undecided queries serves the large-batch passes of a full detect only
+    const bool large = n > e->tune.surrogate_warp_max && n > e->tune.leaf_table_max;
+    if (!(mode == 3 && large && next && JCDE_SURR_DYNAMIC && e->tune.poly_chunk && !raw.verts && !n_pending) ||
+        (pend.rec && cudaMemsetAsync(pend.count, 0, 4, s) != cudaSuccess))
+        pend = PendList{nullptr, nullptr};
     if (mode & 1) {
         const uint8_t miss = mode == 1 ? (uint8_t)0 : PENDING;
         cudaEvent_t pa = prof_begin(e, s);
@@ -475,11 +481,12 @@ static bool launch_passes_t(jcde_engine* e, const View& v, const uint32_t* q, ui
             const uint32_t grid = std::min<uint32_t>((n + SURR_THREADS - 1) / SURR_THREADS,
                                                      (uint32_t)e->n_sms * (uint32_t)std::max(per_sm, 1));
             k_surrogate<PendT, false><<<grid, SURR_THREADS, 0, s>>>(v, MultiSrc{}, q, n, dout, miss, order, next,
-                                                                    n_pending);
+                                                                    n_pending, pend);
         } else {
             const uint32_t grid = (n + SURR_THREADS - 1) / SURR_THREADS;
             k_surrogate<PendT, false><<<grid, SURR_THREADS, 0, s>>>(v, MultiSrc{}, q, n, dout, miss, order, nullptr,
                                                                     n_pending);
+            pend = PendList{nullptr, nullptr};   // this branch writes no list: the polygon pass reads the slots
         }
         prof_end(e, s, pa, JCDE_PROF_SURROGATE);
         e->launches++;
@@ -501,7 +508,7 @@ static bool launch_passes_t(jcde_engine* e, const View& v, const uint32_t* q, ui
             chose = best != nullptr;
         } else {
             k_poly<PendT, false><<<grid, POLY_WARPS * 32, 0, s>>>(v, MultiSrc{}, q, n, dout, raw, mode == 3, order, next,
-                                                                  std::max(e->tune.poly_chunk, 1u));
+                                                                  std::max(e->tune.poly_chunk, 1u), pend.rec, pend.count);
         }
         prof_end(e, s, pa, JCDE_PROF_POLY);
         e->launches++;
@@ -513,10 +520,23 @@ static bool launch_passes_t(jcde_engine* e, const View& v, const uint32_t* q, ui
 static bool launch_passes(jcde_engine* e, const View& v, const uint32_t* q, uint32_t n, uint8_t* dout,
                           cudaStream_t s, RawShape raw, int mode, const uint32_t* order = nullptr,
                           uint32_t* next = nullptr, unsigned long long* best = nullptr, uint32_t* n_pending = nullptr,
-                          bool skip = false) {
+                          bool skip = false, PendList pend = PendList{nullptr, nullptr}) {
     if (e->cfg.quadtree_depth <= 8)
-        return launch_passes_t<uint32_t>(e, v, q, n, dout, s, raw, mode, order, next, best, n_pending, skip);
-    return launch_passes_t<uint64_t>(e, v, q, n, dout, s, raw, mode, order, next, best, n_pending, skip);
+        return launch_passes_t<uint32_t>(e, v, q, n, dout, s, raw, mode, order, next, best, n_pending, skip, pend);
+    return launch_passes_t<uint64_t>(e, v, q, n, dout, s, raw, mode, order, next, best, n_pending, skip, pend);
+}
+
+// The pending-list buffers of pipeline slot `slot` for a batch of n (records of PEND_WORDS words),
+// or an empty list when they cannot be had (the passes then run without it).
+static PendList pend_list(jcde_engine* e, uint32_t n, int slot, uint32_t slot_cap) {
+    const size_t per_slot = std::max<size_t>(n, slot_cap) * PEND_WORDS * 4;
+    if (!e->d_pendc.ensure(2 * 4)) return PendList{nullptr, nullptr};
+    if (e->d_pend.cap < 2 * per_slot) {
+        // growing the buffer frees the old one, which queued batches may still read
+        if (e->have_last_stream && cudaStreamSynchronize(e->last_stream) != cudaSuccess) return PendList{nullptr, nullptr};
+        if (!e->d_pend.ensure(2 * per_slot)) return PendList{nullptr, nullptr};
+    }
+    return PendList{e->d_pend.as<uint32_t>() + (size_t)slot * (e->d_pend.cap / 8), e->d_pendc.as<uint32_t>() + slot};
 }
 
 // mode 1: surrogate only; 2: polygon only; 3: surrogate pass, then the polygon pass on the
@@ -532,7 +552,10 @@ static jcde_status launch_detect(jcde_engine* e, int mode, const jcde_query* dq,
     const uint32_t* q = reinterpret_cast<const uint32_t*>(dq);
     const uint32_t* order = raw.verts ? nullptr : spatial_order(e, q, n, s, slot, slot_cap);
     uint32_t* next = e->d_next.ensure(2 * 2 * 4) ? e->d_next.as<uint32_t>() + 2 * slot : nullptr;
-    launch_passes(e, v, q, n, dout, s, raw, mode, order, next);
+    const PendList pend = (mode == 3 && !raw.verts && n > e->tune.surrogate_warp_max && n > e->tune.leaf_table_max)
+                              ? pend_list(e, n, slot, slot_cap)
+                              : PendList{nullptr, nullptr};
+    launch_passes(e, v, q, n, dout, s, raw, mode, order, next, nullptr, nullptr, false, pend);
     CUDA_TRY(cudaGetLastError());
     e->last_stream = s;
     e->have_last_stream = true;

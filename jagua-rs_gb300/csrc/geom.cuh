@@ -52,10 +52,13 @@ JHD bool fpa_eq(float a, float b) {
     int32_t ad = d < 0 ? (d == INT32_MIN ? INT32_MAX : -d) : d;
     return ad <= 4;
 }
-JHD bool fpa_le(float a, float b) { return fpa_eq(a, b) || a < b; }
-JHD bool fpa_ge(float a, float b) { return fpa_eq(a, b) || a > b; }
-JHD bool fpa_lt(float a, float b) { return !fpa_eq(a, b) && a < b; }
-JHD bool fpa_gt(float a, float b) { return !fpa_eq(a, b) && a > b; }
+// FPA's PartialOrd (util/fpa.rs:25-31): Equal when approx-equal, else the f32 order.  The plain
+// comparison is tested first: the boolean is the same (both terms are pure), and it usually
+// decides without the approximate-equality test.
+JHD bool fpa_le(float a, float b) { return a < b || fpa_eq(a, b); }
+JHD bool fpa_ge(float a, float b) { return a > b || fpa_eq(a, b); }
+JHD bool fpa_lt(float a, float b) { return a < b && !fpa_eq(a, b); }
+JHD bool fpa_gt(float a, float b) { return a > b && !fpa_eq(a, b); }
 
 // rect.rs:266-271
 JHD bool box_hits_box(const Box& a, const Box& b) {

@@ -380,6 +380,20 @@ __device__ __forceinline__ int virtual_root(const View& v, const Box& sb) {
     }
 }
 
+// get_virtual_root with the four children of a level tested by lanes 0-3 at once; the first
+// surrounding child in quadrant order is the one `find` takes (cd_engine.rs:318-321).
+__device__ __forceinline__ int virtual_root_warp(const View& v, const Box& sb, int lane) {
+    int n = 0;
+    for (;;) {
+        const DNode nd = ld_node(v, n);
+        if (nd.child < 0) return n;
+        const bool ok = lane < 4 && box_surrounds(box_quadrant(nd.box, lane), sb);
+        const uint32_t m = __ballot_sync(FULL, ok);
+        if (!m) return n;
+        n = nd.child + __ffs(m) - 1;
+    }
+}
+
 // Ray-cast point-in-polygon (simple_polygon.rs:255-292) with the polygon's edges over the lanes.
 __device__ __forceinline__ bool warp_pip_hazard(const View& v, const DHaz& h, Pt p, int lane) {
     if (!box_hits_pt(h.box, p)) return false;
@@ -435,8 +449,8 @@ struct QueryHead {
     uint32_t item;
     float c, s, tx, ty;
 };
-__device__ __forceinline__ QueryHead load_query(const uint32_t* __restrict__ q, uint32_t qi, int lane) {
-    uint32_t w = lane < 5 ? __ldg(&q[(size_t)qi * 5 + lane]) : 0u;
+__device__ __forceinline__ QueryHead load_query_words(const uint32_t* __restrict__ w5, int lane) {
+    uint32_t w = lane < 5 ? __ldg(&w5[lane]) : 0u;
     QueryHead h;
     h.item = __shfl_sync(FULL, w, 0);
     h.c = __uint_as_float(__shfl_sync(FULL, w, 1));
@@ -445,6 +459,18 @@ __device__ __forceinline__ QueryHead load_query(const uint32_t* __restrict__ q, 
     h.ty = __uint_as_float(__shfl_sync(FULL, w, 4));
     return h;
 }
+__device__ __forceinline__ QueryHead load_query(const uint32_t* __restrict__ q, uint32_t qi, int lane) {
+    return load_query_words(q + (size_t)qi * 5, lane);
+}
+
+// Undecided queries of the surrogate pass, compacted for the polygon pass: record k is 6 words
+// (query index, then the query's 5 words) at rec + 6 k, appended with one atomic per warp; the
+// polygon pass then reads the records in order instead of re-reading every query's verdict slot.
+struct PendList {
+    uint32_t* rec;     // nullptr: no list
+    uint32_t* count;   // records written (zeroed before the surrogate pass)
+};
+constexpr uint32_t PEND_WORDS = 6;
 
 constexpr int MODE_SURROGATE = 1;
 constexpr int MODE_POLY = 2;
@@ -482,8 +508,9 @@ struct MultiSrc {
 };
 
 // With `n_pending`, every query the pass leaves undecided (miss = PENDING) is counted there.
+// Returns true when the query is left undecided (PENDING).
 template <typename PendT>
-__device__ __forceinline__ void surrogate_query(const View& v, const uint32_t* __restrict__ q, uint32_t qi,
+__device__ __forceinline__ bool surrogate_query(const View& v, const uint32_t* __restrict__ q, uint32_t qi,
                                                 uint8_t* __restrict__ out, uint8_t miss,
                                                 uint32_t* __restrict__ n_pending = nullptr) {
     const uint32_t* w5 = q + (size_t)qi * 5;
@@ -492,7 +519,7 @@ __device__ __forceinline__ void surrogate_query(const View& v, const uint32_t* _
     const float tx = __uint_as_float(__ldg(&w5[3])), ty = __uint_as_float(__ldg(&w5[4]));
     if (item >= v.n_items) {
         out[qi] = 2;
-        return;
+        return false;
     }
     const DItem it = v.items[item];
     bool hit = false;
@@ -510,6 +537,7 @@ __device__ __forceinline__ void surrogate_query(const View& v, const uint32_t* _
     }
     out[qi] = hit ? (uint8_t)1 : miss;
     if (n_pending && !hit && miss == PENDING) atomicAdd(n_pending, 1u);
+    return !hit && miss == PENDING;
 }
 
 template <typename PendT, bool MULTI>
@@ -517,7 +545,8 @@ __global__ void JCDE_SURR_BOUNDS k_surrogate(View v, MultiSrc ms, const uint32_t
                                                             uint32_t n, uint8_t* __restrict__ out, uint8_t miss,
                                                             const uint32_t* __restrict__ order,
                                                             uint32_t* __restrict__ next,
-                                                            uint32_t* __restrict__ n_pending = nullptr) {
+                                                            uint32_t* __restrict__ n_pending = nullptr,
+                                                            PendList pend = PendList{nullptr, nullptr}) {
     if (next) {   // each warp takes the next 32 queries from the counter as it finishes
         const int lane = threadIdx.x & 31;
         for (;;) {
@@ -526,10 +555,25 @@ __global__ void JCDE_SURR_BOUNDS k_surrogate(View v, MultiSrc ms, const uint32_t
             const uint32_t base = __shfl_sync(FULL, t, 0);
             if (base >= n) break;
             const uint32_t i = base + lane;
+            bool undecided = false;
+            uint32_t qi = 0;
             if (i < n) {
-                const uint32_t qi = order ? __ldg(&order[i]) : i;
-                if constexpr (MULTI) surrogate_query<PendT>(ms.views[ms.layout_of(qi)], q, qi, out, miss);
-                else surrogate_query<PendT>(v, q, qi, out, miss, n_pending);
+                qi = order ? __ldg(&order[i]) : i;
+                if constexpr (MULTI) undecided = surrogate_query<PendT>(ms.views[ms.layout_of(qi)], q, qi, out, miss);
+                else undecided = surrogate_query<PendT>(v, q, qi, out, miss, n_pending);
+            }
+            if (pend.rec) {
+                const uint32_t bal = __ballot_sync(FULL, undecided);
+                uint32_t at = 0;
+                if (lane == 0 && bal) at = atomicAdd(pend.count, (uint32_t)__popc(bal));
+                at = __shfl_sync(FULL, at, 0) + __popc(bal & ((1u << lane) - 1u));
+                if (undecided) {
+                    uint32_t* r = pend.rec + (size_t)at * PEND_WORDS;
+                    const uint32_t* w5 = q + (size_t)qi * 5;
+                    r[0] = qi;
+                    #pragma unroll
+                    for (int k = 0; k < 5; k++) r[1 + k] = __ldg(&w5[k]);
+                }
             }
         }
         return;
@@ -824,7 +868,7 @@ __device__ __forceinline__ bool walk_step_tab(const View& v, const P& p, WalkT<P
 #endif
 constexpr uint32_t POLY_MAXV = 256;   // items with more vertices transform edges on the fly
 template <typename PendT, bool TAB>
-__device__ __forceinline__ void poly_query(const View& v, const uint32_t* __restrict__ q, uint32_t qi,
+__device__ __forceinline__ void poly_query(const View& v, const uint32_t* __restrict__ qw, uint32_t qi,
                                            uint8_t* __restrict__ out, const RawShape& raw, volatile int* stop,
                                            float2* tv, uint32_t* jobsw, LeafTab* ltab, int lane,
                                            unsigned long long* best = nullptr, bool skip = false) {
@@ -834,7 +878,7 @@ __device__ __forceinline__ void poly_query(const View& v, const uint32_t* __rest
         sh = QShape{raw.verts, raw.nv, 1.0f, 0.0f, 0.0f, 0.0f, true};
         spoi = Pt{raw.poi_x, raw.poi_y};
     } else {
-        QueryHead qh = load_query(q, qi, lane);
+        QueryHead qh = load_query_words(qw, lane);
         if (qh.item >= v.n_items) {
             if (lane == 0) out[qi] = 2;
             return;
@@ -884,7 +928,7 @@ __device__ __forceinline__ void poly_query(const View& v, const uint32_t* __rest
     };
     // a shape not surrounded by the CDE box collides (cd_engine.rs:161-163)
     bool hit = !box_surrounds(v.cde, sb);
-    const int vr = hit ? 0 : virtual_root(v, sb);
+    const int vr = hit ? 0 : virtual_root_warp(v, sb, lane);
     const uint32_t lt = (1u << lane) - 1u;
     // Every edge's walk starts with a visit of the virtual root.  When the root of the walk is a
     // Partial internal node, that first visit is done here for all edges at once (uniform work,
@@ -1023,13 +1067,17 @@ template <typename PendT, bool MULTI>
 __global__ void __launch_bounds__(POLY_WARPS * 32, JCDE_POLY_MIN_BLOCKS)
     k_poly(View v, MultiSrc ms, const uint32_t* __restrict__ q, uint32_t n, uint8_t* __restrict__ out,
            RawShape raw, bool only_pending, const uint32_t* __restrict__ order, uint32_t* __restrict__ next,
-           uint32_t chunk) {
+           uint32_t chunk, const uint32_t* __restrict__ pend_rec = nullptr,
+           const uint32_t* __restrict__ pend_count = nullptr) {
     __shared__ int stops[POLY_WARPS];
     __shared__ float2 tverts[POLY_WARPS][POLY_MAXV];   // transformed item vertices
     __shared__ uint32_t jobs[POLY_WARPS][POLY_MAXV];   // edge index | children mask below the virtual root << 16
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     volatile int* stop = &stops[warp];
+    uint32_t* jobsw = jobs[warp];
     const uint32_t stride = gridDim.x * POLY_WARPS;
+    // with a pending list: its records, in the order the surrogate pass wrote them
+    if (pend_rec) n = *(volatile const uint32_t*)pend_count;
     // queries in grid-stride order, or `chunk` consecutive ones at a time from the counter `next`
     uint32_t i = 0, end = 0, gs = blockIdx.x * POLY_WARPS + warp;
     for (;;) {
@@ -1046,14 +1094,21 @@ __global__ void __launch_bounds__(POLY_WARPS * 32, JCDE_POLY_MIN_BLOCKS)
             }
             if (i >= n) break;
         }
+        if (pend_rec) {
+            const uint32_t* r = pend_rec + (size_t)i * PEND_WORDS;
+            i++;
+            const uint32_t qi = __ldg(&r[0]);
+            poly_query<PendT, false>(v, r + 1, qi, out, raw, stop, tverts[warp], jobsw, nullptr, lane);
+            continue;
+        }
         const uint32_t qi = order ? __ldg(&order[i]) : i;
         i++;
         if (only_pending && out[qi] != PENDING) continue;
         if constexpr (MULTI)
-            poly_query<PendT, false>(ms.views[ms.layout_of(qi)], q, qi, out, raw, stop, tverts[warp], jobs[warp],
-                                     nullptr, lane);
+            poly_query<PendT, false>(ms.views[ms.layout_of(qi)], q + (size_t)qi * 5, qi, out, raw, stop, tverts[warp],
+                                     jobsw, nullptr, lane);
         else
-            poly_query<PendT, false>(v, q, qi, out, raw, stop, tverts[warp], jobs[warp], nullptr, lane);
+            poly_query<PendT, false>(v, q + (size_t)qi * 5, qi, out, raw, stop, tverts[warp], jobsw, nullptr, lane);
     }
 }
 
@@ -1085,7 +1140,8 @@ __global__ void __launch_bounds__(POLY_WARPS * 32, JCDE_POLY_TAB_MIN_BLOCKS)
         if (i >= n) break;
         const uint32_t qi = order ? __ldg(&order[i]) : i;
         if (only_pending && out[qi] != PENDING) continue;
-        poly_query<PendT, true>(v, q, qi, out, raw, stop, tverts[warp], jobs[warp], &ltabs[warp], lane, best, skip);
+        poly_query<PendT, true>(v, q + (size_t)qi * 5, qi, out, raw, stop, tverts[warp], jobs[warp], &ltabs[warp], lane,
+                                best, skip);
     }
 }
 
@@ -1157,7 +1213,7 @@ __global__ void JCDE_COLLECT_BOUNDS k_collect(View v, const uint32_t* __restrict
             if (MODE & MODE_POLY) {
                 sb = warp_bbox(sh, lane);
                 if (!box_surrounds(v.cde, sb) && v.exterior >= 0 && lane == 0) bit_set(bits, (uint32_t)v.exterior);
-                vr = virtual_root(v, sb);
+                vr = virtual_root_warp(v, sb, lane);
             }
             const uint32_t n_pole = (MODE & MODE_SURROGATE) ? it.n_ff_poles : 0u;
             const uint32_t n_pier = (MODE & MODE_SURROGATE) ? it.n_piers : 0u;
