@@ -573,13 +573,18 @@ static jcde_status launch_collect(jcde_engine* e, int mode, const jcde_query* dq
     CUDA_TRY(cudaMemsetAsync(d_total, 0, 4, s));
     if (n == 0) return JCDE_OK;
     const uint32_t words = mask_words(e);
-    const size_t smem = (size_t)COLLECT_WARPS * words * 4;
-    if (smem > 200 * 1024) return JCDE_ERR_CAPACITY;   // > ~1.6M hazard slots
-    static bool attr_set[4] = {false, false, false, false};
-    const void* fn = mode == 1 ? (const void*)k_collect<1> : mode == 2 ? (const void*)k_collect<2> : (const void*)k_collect<3>;
-    if (smem > 48 * 1024 && !attr_set[mode]) {
+    // per warp: the key bitset and the item's transformed vertices
+    const size_t smem = (size_t)COLLECT_WARPS * (words * 4 + POLY_MAXV * sizeof(float2));
+    if (smem > 200 * 1024) return JCDE_ERR_CAPACITY;   // > ~1.5M hazard slots
+    const bool wide = e->cfg.quadtree_depth > 8;   // 64-bit walk masks above depth 8
+    static bool attr_set[2][4] = {};
+    const void* fn = wide ? (mode == 1 ? (const void*)k_collect<1, uint64_t> : mode == 2 ? (const void*)k_collect<2, uint64_t>
+                                                                                     : (const void*)k_collect<3, uint64_t>)
+                          : (mode == 1 ? (const void*)k_collect<1, uint32_t> : mode == 2 ? (const void*)k_collect<2, uint32_t>
+                                                                                     : (const void*)k_collect<3, uint32_t>);
+    if (smem > 48 * 1024 && !attr_set[wide][mode]) {
         CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-        attr_set[mode] = true;
+        attr_set[wide][mode] = true;
     }
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, COLLECT_WARPS * 32, smem);
@@ -593,11 +598,10 @@ static jcde_status launch_collect(jcde_engine* e, int mode, const jcde_query* dq
     if (JCDE_COLLECT_DYNAMIC && e->d_next.ensure(2 * 2 * 4) && cudaMemsetAsync(e->d_next.p, 0, 4, s) == cudaSuccess)
         next = e->d_next.as<uint32_t>();
     cudaEvent_t pa = prof_begin(e, s);
-    switch (mode) {
-        case 1: k_collect<1><<<grid, COLLECT_WARPS * 32, smem, s>>>(v, q, n, words, d_off, d_cnt, d_ids, cap, d_total, raw, order, next); break;
-        case 2: k_collect<2><<<grid, COLLECT_WARPS * 32, smem, s>>>(v, q, n, words, d_off, d_cnt, d_ids, cap, d_total, raw, order, next); break;
-        default: k_collect<3><<<grid, COLLECT_WARPS * 32, smem, s>>>(v, q, n, words, d_off, d_cnt, d_ids, cap, d_total, raw, order, next); break;
-    }
+    using K = void (*)(View, const uint32_t*, uint32_t, uint32_t, uint32_t*, uint32_t*, uint32_t*, uint32_t, uint32_t*,
+                       RawShape, const uint32_t*, uint32_t*);
+    const K k = reinterpret_cast<K>(const_cast<void*>(fn));
+    k<<<grid, COLLECT_WARPS * 32, smem, s>>>(v, q, n, words, d_off, d_cnt, d_ids, cap, d_total, raw, order, next);
     CUDA_TRY(cudaGetLastError());
     prof_end(e, s, pa, JCDE_PROF_COLLECT);
     e->launches++;

@@ -300,10 +300,9 @@ __device__ __forceinline__ bool seg_group_hits(const View& v, const P& p, const 
     return false;
 }
 
-// QTNode::collect_collisions (qt_node.rs:151-191) for one probe from node `start`.
-template <class P>
-__device__ void collect_walk(const View& v, const P& p, int start, uint32_t* bits) {
-    WalkT<uint64_t> w{start, 0, 0, 0ull};
+// QTNode::collect_collisions (qt_node.rs:151-191) for one probe, continuing walk `w`.
+template <class P, typename PendT>
+__device__ void collect_walk_w(const View& v, const P& p, WalkT<PendT>& w, uint32_t* bits) {
     while (w.node >= 0) {
         DNode nd = ld_node(v, w.node);
         const bool now = __ldg(&v.nedges[w.node]) <= v.cd_threshold;
@@ -323,6 +322,12 @@ __device__ void collect_walk(const View& v, const P& p, int start, uint32_t* bit
         }
         w.node = walk_next(v, w);
     }
+}
+// ... for one probe from node `start`.
+template <class P, typename PendT>
+__device__ __forceinline__ void collect_walk(const View& v, const P& p, int start, uint32_t* bits) {
+    WalkT<PendT> w{start, 0, 0, (PendT)0};
+    collect_walk_w(v, p, w, bits);
 }
 
 // Float bits mapped to unsigned integers of the same order (for 64-bit atomicMin of (cost, index)).
@@ -1147,7 +1152,7 @@ __global__ void __launch_bounds__(POLY_WARPS * 32, JCDE_POLY_TAB_MIN_BLOCKS)
 
 constexpr int COLLECT_WARPS = 4;
 #ifndef JCDE_COLLECT_MIN_BLOCKS
-#define JCDE_COLLECT_MIN_BLOCKS 0   // blocks per SM the collect pass is compiled for (0: ptxas decides)
+#define JCDE_COLLECT_MIN_BLOCKS 6   // blocks per SM the collect pass is compiled for (0: ptxas decides)
 #endif
 #if JCDE_COLLECT_MIN_BLOCKS > 0
 #define JCDE_COLLECT_BOUNDS __launch_bounds__(COLLECT_WARPS * 32, JCDE_COLLECT_MIN_BLOCKS)
@@ -1156,7 +1161,10 @@ constexpr int COLLECT_WARPS = 4;
 #endif
 
 // Collect: sorted colliding hazard keys per query, compacted with one atomicAdd per query.
-template <int MODE>
+// Dynamic shared memory: COLLECT_WARPS bitsets of `words` words, then per warp the item's
+// transformed vertices (POLY_MAXV float2).  (Listing the virtual root's first visit for all edges
+// at once, as the detect pass does, made this pass 30% slower: measured and left out.)
+template <int MODE, typename PendT>
 __global__ void JCDE_COLLECT_BOUNDS k_collect(View v, const uint32_t* __restrict__ q, uint32_t n,
                                                                 uint32_t words, uint32_t* __restrict__ offsets,
                                                                 uint32_t* __restrict__ counts, uint32_t* __restrict__ ids,
@@ -1166,6 +1174,7 @@ __global__ void JCDE_COLLECT_BOUNDS k_collect(View v, const uint32_t* __restrict
     extern __shared__ uint32_t smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     uint32_t* bits = smem + (size_t)warp * words;
+    float2* tv = reinterpret_cast<float2*>(smem + (size_t)COLLECT_WARPS * words) + (size_t)warp * POLY_MAXV;
     const uint32_t stride = gridDim.x * COLLECT_WARPS;
     // queries in grid-stride order, or two at a time from the counter `next`
     uint32_t i = 0, end = 0, gs = blockIdx.x * COLLECT_WARPS + warp;
@@ -1206,29 +1215,56 @@ __global__ void JCDE_COLLECT_BOUNDS k_collect(View v, const uint32_t* __restrict
         }
         // the ignored keys are pre-seeded into the collector (hazards/filter.rs:69-76)
         for (uint32_t w = lane; w < words; w += 32) bits[w] = v.mask ? __ldg(&v.mask[w]) : 0u;
+        // the transformed vertices (kept for items up to POLY_MAXV vertices) and the shape's bbox
+        // (SPolygon::generate_bounding_box, simple_polygon.rs:122-133)
+        const bool cached = (MODE & MODE_POLY) && valid && sh.nv <= POLY_MAXV;
+        Box sb{0, 0, 0, 0};
+        if ((MODE & MODE_POLY) && valid) {
+            float x0 = FLT_MAX, y0 = FLT_MAX, x1 = -FLT_MAX, y1 = -FLT_MAX;
+            for (uint32_t k = lane; k < sh.nv; k += 32) {
+                const Pt p = sh.vtx(k);
+                if (cached) tv[k] = make_float2(p.x, p.y);
+                x0 = fminf(x0, p.x);
+                y0 = fminf(y0, p.y);
+                x1 = fmaxf(x1, p.x);
+                y1 = fmaxf(y1, p.y);
+            }
+            JCDE_UNROLL
+            for (int o = 16; o; o >>= 1) {
+                x0 = fminf(x0, __shfl_xor_sync(FULL, x0, o));
+                y0 = fminf(y0, __shfl_xor_sync(FULL, y0, o));
+                x1 = fmaxf(x1, __shfl_xor_sync(FULL, x1, o));
+                y1 = fmaxf(y1, __shfl_xor_sync(FULL, y1, o));
+            }
+            sb = Box{x0, y0, x1, y1};
+        }
         __syncwarp();
+        auto edge_of = [&](uint32_t k) -> Seg {
+            if (!cached) return sh.edge(k);
+            const float2 a = tv[k], b = tv[k + 1 == sh.nv ? 0 : k + 1];
+            return Seg{Pt{a.x, a.y}, Pt{b.x, b.y}};
+        };
         if (valid) {
-            Box sb{0, 0, 0, 0};
             int vr = 0;
             if (MODE & MODE_POLY) {
-                sb = warp_bbox(sh, lane);
                 if (!box_surrounds(v.cde, sb) && v.exterior >= 0 && lane == 0) bit_set(bits, (uint32_t)v.exterior);
                 vr = virtual_root_warp(v, sb, lane);
             }
             const uint32_t n_pole = (MODE & MODE_SURROGATE) ? it.n_ff_poles : 0u;
             const uint32_t n_pier = (MODE & MODE_SURROGATE) ? it.n_piers : 0u;
+            const uint32_t n_sp = n_pole + n_pier;
             const uint32_t n_edge = (MODE & MODE_POLY) ? sh.nv : 0u;
-            const uint32_t np = n_pole + n_pier + n_edge;
+            const uint32_t np = n_sp + n_edge;
             for (uint32_t p = lane; p < np; p += 32) {   // lane l walks probes l, l+32, ...
                 if (p < n_pole) {
                     const float4 pl = __ldg(&v.poles[it.pole_off + p]);
-                    collect_walk(v, Disk{xform(Pt{pl.x, pl.y}, sh.c, sh.s, sh.tx, sh.ty), pl.z}, 0, bits);
-                } else if (p < n_pole + n_pier) {
+                    collect_walk<Disk, PendT>(v, Disk{xform(Pt{pl.x, pl.y}, sh.c, sh.s, sh.tx, sh.ty), pl.z}, 0, bits);
+                } else if (p < n_sp) {
                     const float4 pr = __ldg(&v.piers[it.pier_off + (p - n_pole)]);
-                    collect_walk(v, Seg{xform(Pt{pr.x, pr.y}, sh.c, sh.s, sh.tx, sh.ty), xform(Pt{pr.z, pr.w}, sh.c, sh.s, sh.tx, sh.ty)},
-                                 0, bits);
+                    collect_walk<Seg, PendT>(v, Seg{xform(Pt{pr.x, pr.y}, sh.c, sh.s, sh.tx, sh.ty),
+                                                    xform(Pt{pr.z, pr.w}, sh.c, sh.s, sh.tx, sh.ty)}, 0, bits);
                 } else {
-                    collect_walk(v, sh.edge(p - n_pole - n_pier), vr, bits);
+                    collect_walk<Seg, PendT>(v, edge_of(p - n_sp), vr, bits);
                 }
             }
             __syncwarp();
