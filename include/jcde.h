@@ -370,12 +370,15 @@ jcde_status jcde_set_tuning(jcde_engine* e, const jcde_tuning* t);
 /* Times all 16 combinations (surrogate pass warp/thread x polygon pass leaf tables/grabs of 1, 2, 4 x
  * Morton order on/off) on the caller's batch, checks that every combination gives the same verdicts
  * (JCDE_ERR_STATE otherwise), keeps the fastest in the engine (its thresholds set so that batches of
- * this size take it) and returns it with its median time.  Synchronises. */
+ * this size take it) and returns it with its median time.  Each timing starts from a cold L2 (a
+ * 256 MB buffer, allocated for the call, is written before it), as a fresh batch would.
+ * Synchronises. */
 jcde_status jcde_autotune(jcde_engine* e, const jcde_query* d_queries, uint32_t n, const jcde_filter* f, void* stream,
                           jcde_tuning* out, double* best_ms);
 /* The same for a jcde_multi batch: polygon-pass grabs of 1, 2, 4, 8 x Morton order on/off, verdicts
- * checked identical; d_out (device, total queries) receives verdicts; out2 = chosen grab size, order
- * flag.  The choice applies to later jcde_multi_detect / _graph calls.  Synchronises. */
+ * checked identical, timed from a cold L2; d_out (device, total queries) receives verdicts; out2 =
+ * chosen grab size, order flag.  The choice applies to later jcde_multi_detect / _graph calls.
+ * Synchronises. */
 jcde_status jcde_multi_autotune(jcde_multi* m, const jcde_query* d_queries, const uint32_t* offsets,
                                 const jcde_filter* filters, uint8_t* d_out, void* stream, uint32_t* out2,
                                 double* best_ms);

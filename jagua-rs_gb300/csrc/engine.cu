@@ -2119,13 +2119,22 @@ jcde_status jcde_set_tuning(jcde_engine* e, const jcde_tuning* t) {
 // Times every combination of the launch choices on the caller's batch (one warm-up, then the median
 // of three timed runs each, CUDA events on `stream`), checks that all of them give the same
 // verdicts, keeps the fastest in the engine and returns it.
+// The autotuners time every choice from a cold L2, as a fresh batch meets it: before each timed
+// repetition a buffer larger than L2 is written on the stream (outside the timed events).
+static constexpr size_t TUNE_FLUSH_BYTES = 256u << 20;
+static jcde_status tune_flush(DevBuf& f, cudaStream_t s) {
+    if (!f.p) return JCDE_OK;   // no buffer (allocation refused): timed warm
+    return cudaMemsetAsync(f.p, 0, f.cap, s) == cudaSuccess ? JCDE_OK : JCDE_ERR_CUDA;
+}
+
 jcde_status jcde_autotune(jcde_engine* e, const jcde_query* d_queries, uint32_t n, const jcde_filter* f, void* stream,
                           jcde_tuning* out, double* best_ms) {
     if (!e || !d_queries || !n) return JCDE_ERR_ARG;
     cudaStream_t s = (cudaStream_t)stream;
     const jcde_tuning saved = e->tune;
-    DevBuf d_ref, d_out;
+    DevBuf d_ref, d_out, d_flush;
     if (!d_ref.ensure(n) || !d_out.ensure(n)) return JCDE_ERR_CUDA;
+    d_flush.ensure(TUNE_FLUSH_BYTES);
     std::vector<uint8_t> ref(n), got(n);
     cudaEvent_t a = nullptr, b = nullptr;
     CUDA_TRY(cudaEventCreate(&a));
@@ -2149,7 +2158,8 @@ jcde_status jcde_autotune(jcde_engine* e, const jcde_query* d_queries, uint32_t 
                 e->tune = t;
                 float ms[3] = {0, 0, 0};
                 for (int r = -1; r < 3 && !st; r++) {
-                    if (r >= 0 && cudaEventRecord(a, s) != cudaSuccess) st = JCDE_ERR_CUDA;
+                    if (r >= 0) st = tune_flush(d_flush, s);
+                    if (!st && r >= 0 && cudaEventRecord(a, s) != cudaSuccess) st = JCDE_ERR_CUDA;
                     if (!st) st = launch_detect(e, 3, d_queries, n, f, d_out.as<uint8_t>(), s, RawShape{nullptr, 0, 0, 0, 0});
                     if (!st && r >= 0) {
                         if (cudaEventRecord(b, s) != cudaSuccess || cudaEventSynchronize(b) != cudaSuccess ||
@@ -2202,6 +2212,8 @@ extern "C" jcde_status jcde_multi_autotune(jcde_multi* m, const jcde_query* dq, 
     const uint32_t saved_chunk = m->poly_chunk;
     const bool saved_ordered = m->ordered;
     std::vector<uint8_t> ref(n), got(n);
+    DevBuf d_flush;
+    d_flush.ensure(TUNE_FLUSH_BYTES);
     cudaEvent_t a = nullptr, b = nullptr;
     CUDA_TRY(cudaEventCreate(&a));
     if (cudaEventCreate(&b) != cudaSuccess) {
@@ -2218,7 +2230,8 @@ extern "C" jcde_status jcde_multi_autotune(jcde_multi* m, const jcde_query* dq, 
             m->poly_chunk = chunk;
             float ms[3] = {0, 0, 0};
             for (int r = -1; r < 3 && !st; r++) {
-                if (r >= 0 && cudaEventRecord(a, s) != cudaSuccess) st = JCDE_ERR_CUDA;
+                if (r >= 0) st = tune_flush(d_flush, s);
+                if (!st && r >= 0 && cudaEventRecord(a, s) != cudaSuccess) st = JCDE_ERR_CUDA;
                 if (!st) st = jcde_multi_detect(m, dq, offsets, filters, d_out, s);
                 if (!st && r >= 0 &&
                     (cudaEventRecord(b, s) != cudaSuccess || cudaEventSynchronize(b) != cudaSuccess ||
