@@ -972,7 +972,8 @@ def measure_lbf(steps: int, warmup: int, oracle_check: bool = True, extras: bool
 
     def build():
         r.reset()
-        r.lbf_begin(spec.seed, spec.n_cand, spec.n_types, spec.remove_every, spec.steps, spec.box)
+        r.lbf_begin(spec.seed, spec.n_cand, spec.n_types, spec.remove_every, spec.steps, spec.box, 0, 0, 0, (),
+                    spec.uniform_rounds)
         with torch.cuda.stream(stream):
             flush.zero_()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -1019,6 +1020,44 @@ def measure_lbf(steps: int, warmup: int, oracle_check: bool = True, extras: bool
         d2h = (log_e2e.placements.nbytes + log_e2e.removals.nbytes + log_e2e.free_counts.nbytes + 16)
     rec["e2e"] = {"value": n_cand_total / (np.median(e2e_ms) / 1e3), "unit": "candidates/s",
                   "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "ms_per_build": float(np.median(e2e_ms))}
+    from jcde import workload as W
+
+    def strip_length(placements, removals):
+        """Largest x of the placed items still live (the strip length the build needs)."""
+        gone = set(int(k) for k in removals[:, 1]) if len(removals) else set()
+        xs = [W.transform_points(lay.items[int(p[3])].xy, *[np.uint32(v).view(np.float32) for v in p[4:8]])[:, 0].max()
+              for p in placements if int(p[1]) not in gone]
+        return float(max(xs)) if xs else 0.0
+
+    rec["strip_length"] = strip_length(d["placements"], d["removals"])
+    # lbf's search restated in rounds (search.rs:41-101): 4 uniform rounds of 4096, each over the box
+    # tightened to the best cost so far / 10, then 3 local-search rounds of 2048 with Normal offsets
+    spec_f = lbf.LbfSpec(uniform_rounds=4, ls_rounds=3, ls_cand=2048)
+    f_ms = []
+    for k in range(3):
+        r.reset()
+        r.lbf_begin(spec_f.seed, spec_f.n_cand, spec_f.n_types, spec_f.remove_every, spec_f.steps, spec_f.box, 0,
+                    spec_f.ls_rounds, spec_f.ls_cand, spec_f.ls_sigmas(), spec_f.uniform_rounds)
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        r.lbf_steps(spec_f.steps, SPG, stream=sh)
+        b.record(stream)
+        torch.cuda.synchronize()
+        if k:
+            f_ms.append(a.elapsed_time(b))
+    d_f = r.lbf_read()
+    f_cands = spec_f.steps * (spec_f.n_cand + spec_f.ls_rounds * spec_f.ls_cand)
+    rounds = d_f["placements"][:, 2] >> 24
+    rec["lbf_search"] = {
+        "ms_per_build": float(np.median(f_ms)), "candidates_per_s": f_cands / (np.median(f_ms) / 1e3),
+        "uniform_rounds": spec_f.uniform_rounds, "local_rounds": spec_f.ls_rounds,
+        "candidates_per_step": spec_f.n_cand + spec_f.ls_rounds * spec_f.ls_cand,
+        "strip_length": strip_length(d_f["placements"], d_f["removals"]),
+        "placements_from_tightened_rounds": int(((rounds >= 1) & (rounds < spec_f.uniform_rounds)).sum()),
+        "placements_improved_by_local_search": int((rounds >= spec_f.uniform_rounds).sum()),
+        "parity": "device build = oracle-driven build: tests/test_gpu_resident.py"}
     if oracle_check:
         from oracle import oracle as O
 
@@ -1039,7 +1078,8 @@ def measure_lbf(steps: int, warmup: int, oracle_check: bool = True, extras: bool
         # per-kernel shares from one eager, profiled build (events around every launch)
         geng.eng.profile(True)
         r.reset()
-        r.lbf_begin(spec.seed, spec.n_cand, spec.n_types, spec.remove_every, spec.steps, spec.box)
+        r.lbf_begin(spec.seed, spec.n_cand, spec.n_types, spec.remove_every, spec.steps, spec.box, 0, 0, 0, (),
+                    spec.uniform_rounds)
         geng.eng.profile_read(reset=True)
         r.lbf_steps(spec.steps, 0, stream=sh)
         kp = geng.eng.profile_read(reset=True)
@@ -1047,29 +1087,6 @@ def measure_lbf(steps: int, warmup: int, oracle_check: bool = True, extras: bool
         kinds = {k: {"ms_per_build": v[0], "launches": v[1]} for k, v in kp.items() if v[1]}
         rec["kernels_eager_build"] = kinds
         rec["dominant"] = max(kinds, key=lambda k: kinds[k]["ms_per_build"])
-        # the same build with three local-search rounds of 2048 candidates per step (search.rs:80-101)
-        spec_ls = lbf.LbfSpec(ls_rounds=3, ls_cand=2048, ls_sigma_t=200.0, ls_sigma_turns=0.05)
-        ls_ms = []
-        for k in range(2):
-            r.reset()
-            r.lbf_begin(spec_ls.seed, spec_ls.n_cand, spec_ls.n_types, spec_ls.remove_every, spec_ls.steps,
-                        spec_ls.box, 0, spec_ls.ls_rounds, spec_ls.ls_cand, spec_ls.ls_sigma_t, spec_ls.ls_sigma_turns,
-                        spec_ls.ls_decay)
-            with torch.cuda.stream(stream):
-                flush.zero_()
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            r.lbf_steps(spec_ls.steps, SPG, stream=sh)
-            b.record(stream)
-            torch.cuda.synchronize()
-            if k:
-                ls_ms.append(a.elapsed_time(b))
-        d_ls = r.lbf_read()
-        ls_cands = spec_ls.steps * (spec_ls.n_cand + spec_ls.ls_rounds * spec_ls.ls_cand)
-        rec["with_local_search"] = {
-            "ms_per_build": ls_ms[0], "candidates_per_s": ls_cands / (ls_ms[0] / 1e3), "rounds": spec_ls.ls_rounds,
-            "candidates_per_round": spec_ls.ls_cand,
-            "placements_improved_by_local_search": int(((d_ls["placements"][:, 2] >> 24) > 0).sum())}
         # the same build driven step by step from the host through the regular engine (host
         # registration, a re-flattened tree upload per step): a bounded sample of its first steps
         host_steps = 200

@@ -316,23 +316,29 @@ uint64_t jcde_resident_kernel_launches(const jcde_resident* r);
  * No host round trip per step; steps_per_graph > 0 replays that many steps per CUDA graph launch. */
 typedef struct jcde_lbf_params {
     uint64_t seed;
-    uint32_t n_candidates;
+    uint32_t n_candidates;         /* per step, over the uniform rounds */
     uint32_t n_types;              /* item types 0..n_types-1 of the engine */
     uint32_t remove_every;         /* 0: no removals */
     uint32_t max_steps;            /* log capacity; steps beyond it do nothing */
-    uint32_t verdict_log_steps;    /* keep the verdicts of the first steps (0: none; needs ls_rounds = 0) */
-    uint32_t reserved;
+    uint32_t verdict_log_steps;    /* keep the verdicts of the first steps (0: none; needs one round per step) */
+    /* the uniform phase of lbf's search (search.rs:41-66) in rounds of n_candidates / uniform_rounds
+     * (0 counts as 1): round 0 from stream (seed, 10000 + s), round u >= 1 from stream
+     * (seed, 2000000 + 64 s + u) over the sample box with x_max tightened to the step's best cost so
+     * far / 10 (LBFLoss::tighten_sample_bbox, loss.rs:34-44, after every improvement in search.rs:62-63,
+     * here after every round); draws i: item (unused), n+i: rotation, 2n+i: x, 3n+i: y */
+    uint32_t uniform_rounds;
     jcde_rect sample_box;
-    /* local search after the uniform round (lbf/src/opt/search.rs:80-101, restated with uniform
-     * offsets): round r = 1..ls_rounds draws ls_candidates placements of the step's item around the
-     * step's best so far from stream (seed, 1000000 + 64 s + r): turns + U[-1,1) sigma_turns_r,
-     * tx, ty + U[-sigma_t_r, sigma_t_r) (draws i, n+i, 2n+i), sigma_r = sigma * decay^(r-1); the
-     * round's least-cost free candidate replaces the best when it costs strictly less. */
+    /* local search after the uniform rounds (search.rs:80-101): round r = 1..ls_rounds draws
+     * ls_candidates placements of the step's item around the step's best so far from stream
+     * (seed, 1000000 + 64 s + r) with Normal offsets (a Box-Muller pair of draws i, m+i for x and y,
+     * another of draws 2m+i, 3m+i for the rotation, m = ls_candidates): translation deviation
+     * ls_sigma_t[r-1], rotation deviation ls_sigma_turns[r-1] (in turns; LSSampler's decaying
+     * deviations, ls_sampler.rs:84-90, one value per round); the round's least-cost free candidate
+     * replaces the best when it costs strictly less. */
     uint32_t ls_rounds;            /* 0..8 */
     uint32_t ls_candidates;        /* per round, at most n_candidates */
-    float ls_sigma_t;
-    float ls_decay;
-    double ls_sigma_turns;
+    float ls_sigma_t[8];
+    double ls_sigma_turns[8];
     /* instance mode (both optional, host arrays copied at jcde_lbf_begin): the item of step s is
      * item_sequence[s] instead of a type-stream draw; item t rotates to one of its allowed
      * orientations orientation_cs[2 * (offsets[t] + k)..] (cos, sin), k = (draw n+i) mod count, or

@@ -1539,6 +1539,7 @@ struct jcde_resident {
     DevBuf d_next;            // work counters of its two passes
     cudaGraphExec_t exec = nullptr;
     uint32_t exec_steps = 0;
+    uint64_t exec_launches = 0;   // kernels one launch of `exec` runs
     cudaStream_t exec_stream = nullptr;
     cudaStream_t own = nullptr;
     cudaStream_t last = nullptr;
@@ -1653,9 +1654,9 @@ static void lbf_step(jcde_resident* r, cudaStream_t s) {
     uint32_t* cand = r->d_cand.as<uint32_t>();
     double* cu = r->d_candu.as<double>();
     uint8_t* verd = r->d_verd.as<uint8_t>();
-    const uint32_t rounds = r->lp.ls_rounds;
-    for (uint32_t round = 0; round <= rounds; round++) {
-        const uint32_t n = round ? r->lp.ls_cand : r->lp.n_cand;
+    const uint32_t last = r->lp.uni_rounds + r->lp.ls_rounds - 1;   // uniform rounds, then local search
+    for (uint32_t round = 0; round <= last; round++) {
+        const uint32_t n = round < r->lp.uni_rounds ? r->lp.n_uni : r->lp.ls_cand;
         cudaEvent_t pa = prof_begin(e, s);
         res_launch_lbf_gen(r->lp, st, cand, cu, round, e->n_sms, s);
         prof_end(e, s, pa, JCDE_PROF_LBF);
@@ -1672,7 +1673,7 @@ static void lbf_step(jcde_resident* r, cudaStream_t s) {
             prof_end(e, s, pa, JCDE_PROF_LBF);
             r->launches++;
         }
-        if (round < rounds) {
+        if (round < last) {
             pa = prof_begin(e, s);
             res_launch_lbf_merge(st, cand, cu, round, s);
             prof_end(e, s, pa, JCDE_PROF_LBF);
@@ -1683,7 +1684,7 @@ static void lbf_step(jcde_resident* r, cudaStream_t s) {
                  r->d_live.as<uint32_t>(), r->lp.vlog_steps ? r->d_vlog.as<uint8_t>() : nullptr};
     cudaEvent_t pa = prof_begin(e, s);
     res_launch_lbf_commit(r->t, e->d_items.as<DItem>(), e->d_iverts.as<float2>(), (uint32_t)e->items.size(), r->lp,
-                          st, cand, cu, rounds, verd, logs, s);
+                          st, cand, cu, last, verd, logs, s);
     prof_end(e, s, pa, JCDE_PROF_UPDATE);
     r->launches++;
 }
@@ -1968,23 +1969,21 @@ jcde_status jcde_lbf_begin(jcde_resident* r, const jcde_lbf_params* p) {
     lp.y1_below = std::nextafter(b.y_max, b.y_min);
     if (p->ls_rounds > LBF_MAX_LS || (p->ls_rounds && (!p->ls_candidates || p->ls_candidates > p->n_candidates)))
         return JCDE_ERR_ARG;
+    const uint32_t uni = std::max(1u, p->uniform_rounds);
+    if (uni > LBF_MAX_UNIFORM || p->n_candidates % uni) return JCDE_ERR_ARG;
+    lp.uni_rounds = uni;
+    lp.n_uni = p->n_candidates / uni;
+    lp.uni_sid_base = 2000000ull;
     lp.ls_rounds = p->ls_rounds;
     lp.ls_cand = p->ls_rounds ? p->ls_candidates : 0;
     lp.ls_sid_base = 1000000ull;
-    {   // round r's half-widths: sigma * decay^(r-1), float32 (translation) and float64 (turns)
-        float sg = p->ls_sigma_t;
-        double sth = p->ls_sigma_turns;
-        for (uint32_t k = 1; k <= p->ls_rounds; k++) {
-            if (k > 1) {
-                sg = sg * p->ls_decay;
-                sth = sth * (double)p->ls_decay;
-            }
-            lp.ls_sig[k] = sg;
-            lp.ls_sig_below[k] = std::nextafter(sg, -sg);
-            lp.ls_sth[k] = sth;
-        }
+    for (uint32_t k = 1; k <= p->ls_rounds; k++) {   // round r's deviations, as given
+        if (!(p->ls_sigma_t[k - 1] >= 0.0f) || !(p->ls_sigma_turns[k - 1] >= 0.0)) return JCDE_ERR_ARG;
+        lp.ls_sig[k] = p->ls_sigma_t[k - 1];
+        lp.ls_sth[k] = p->ls_sigma_turns[k - 1];
     }
-    if (lp.ls_rounds && lp.vlog_steps) return JCDE_ERR_ARG;   // the verdict log keeps one round per step
+    // the verdict log keeps one round per step
+    if ((lp.ls_rounds || lp.uni_rounds > 1) && lp.vlog_steps) return JCDE_ERR_ARG;
     // instance mode: the item sequence and the allowed orientations
     const uint32_t n_items = (uint32_t)r->e->items.size();
     if (p->item_sequence) {
@@ -2046,6 +2045,7 @@ jcde_status jcde_lbf_steps(jcde_resident* r, uint32_t n_steps, uint32_t steps_pe
             e->prof = false;   // per-kernel events are not recorded inside graphs
             for (uint32_t i = 0; i < steps_per_graph; i++) lbf_step(r, s);
             e->prof = prof;
+            r->exec_launches = r->launches - before;   // kernels per graph launch
             r->launches = before;
             cudaError_t ce = cudaStreamEndCapture(s, &g);
             if (ce == cudaSuccess && g) ce = cudaGraphInstantiate(&r->exec, g, 0);
@@ -2059,7 +2059,7 @@ jcde_status jcde_lbf_steps(jcde_resident* r, uint32_t n_steps, uint32_t steps_pe
         }
         for (; done + steps_per_graph <= n_steps; done += steps_per_graph) {
             if (cudaGraphLaunch(r->exec, s) != cudaSuccess) return JCDE_ERR_CUDA;
-            r->launches += (4ull + 4ull * r->lp.ls_rounds) * steps_per_graph;
+            r->launches += r->exec_launches;
         }
     }
     for (; done < n_steps; done++) lbf_step(r, s);

@@ -588,7 +588,7 @@ __constant__ double COS_TAYLOR[13] = {
     0x1.a01a01a01a01ap-16,  -0x1.27e4fb7789f5cp-22, 0x1.1eed8eff8d898p-29, -0x1.93974a8c07c9dp-37,
     0x1.ae7f3e733b81fp-45,  -0x1.6827863b97d97p-53, 0x1.e542ba4020225p-62, -0x1.0ce396db7f853p-70,
     0x1.f2cf01972f578p-80};
-__device__ __forceinline__ void sincos_turns(double u, float& co, float& si) {
+__device__ __forceinline__ void sincos_turns_d(double u, double& dc, double& ds) {
     const double q = __dmul_rn(u, 4.0);
     const double k = floor(q);
     const double r = __dsub_rn(q, k);
@@ -598,15 +598,53 @@ __device__ __forceinline__ void sincos_turns(double u, float& co, float& si) {
     for (int j = 11; j >= 0; j--) s = __dadd_rn(__dmul_rn(s, p2), SIN_TAYLOR[j]);
     for (int j = 11; j >= 0; j--) c = __dadd_rn(__dmul_rn(c, p2), COS_TAYLOR[j]);
     s = __dmul_rn(s, phi);
-    double dc, ds;
     switch ((int)k & 3) {
         case 0: dc = c; ds = s; break;
         case 1: dc = -s; ds = c; break;
         case 2: dc = -c; ds = -s; break;
         default: dc = s; ds = -c; break;
     }
+}
+__device__ __forceinline__ void sincos_turns(double u, float& co, float& si) {
+    double dc, ds;
+    sincos_turns_d(u, dc, ds);
     co = __double2float_rn(dc);
     si = __double2float_rn(ds);
+}
+
+// Natural logarithm of a positive normal double with IEEE additions, multiplications and divisions
+// only, in the host generator's order (workload.ln_f64): x = m 2^e, m in [sqrt(1/2), sqrt(2)),
+// ln m = 2 atanh(z), z = (m-1)/(m+1), 13 terms of the atanh series.
+__constant__ double ATANH_C[13] = {
+    0x1.0000000000000p+0, 0x1.5555555555555p-2, 0x1.999999999999ap-3, 0x1.2492492492492p-3,
+    0x1.c71c71c71c71cp-4, 0x1.745d1745d1746p-4, 0x1.3b13b13b13b14p-4, 0x1.1111111111111p-4,
+    0x1.e1e1e1e1e1e1ep-5, 0x1.af286bca1af28p-5, 0x1.8618618618618p-5, 0x1.642c8590b2164p-5,
+    0x1.47ae147ae147bp-5};
+__device__ __forceinline__ double ln_f64(double x) {
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+    double e = (double)((long long)((bits >> 52) & 0x7FFull) - 1022);
+    double m = __longlong_as_double((long long)((bits & ((1ull << 52) - 1)) | (1022ull << 52)));
+    if (m < 0x1.6a09e667f3bcdp-1) {
+        m = __dmul_rn(m, 2.0);
+        e = __dsub_rn(e, 1.0);
+    }
+    const double z = __ddiv_rn(__dsub_rn(m, 1.0), __dadd_rn(m, 1.0));
+    const double z2 = __dmul_rn(z, z);
+    double sum = ATANH_C[12];
+    for (int j = 11; j >= 0; j--) sum = __dadd_rn(__dmul_rn(sum, z2), ATANH_C[j]);
+    const double t = __dmul_rn(__dmul_rn(2.0, z), sum);
+    return __dadd_rn(__dmul_rn(e, 0x1.62e42fefa39efp-1), __dadd_rn(__dmul_rn(e, 0x1.abc9e3b39803fp-56), t));
+}
+// Box-Muller pair (workload.normal_pair): u1 in (0, 1], u2 in [0, 1)
+__device__ __forceinline__ void normal_pair(double u1, double u2, double& z0, double& z1) {
+    const double r = __dsqrt_rn(__dmul_rn(-2.0, ln_f64(u1)));
+    double c, s;
+    sincos_turns_d(u2, c, s);
+    z0 = __dmul_rn(r, c);
+    z1 = __dmul_rn(r, s);
+}
+__device__ __forceinline__ double draw_f64(unsigned long long key, unsigned long long i) {
+    return (double)(draw(key, i) >> 11) * 0x1p-53;
 }
 __device__ __forceinline__ float draw_f32(unsigned long long key, unsigned long long i) {
     return __fmul_rn((float)(uint32_t)(draw(key, i) >> 40), 0x1p-24f);
@@ -660,21 +698,37 @@ __global__ void k_gen_candidates(GenSegs g, uint32_t n, uint32_t t, const float2
         gen_uniform(g.key[k], n, i, t, g.box[k], orient, ocnt, qk, uk);
 }
 
-// Candidates of round `round` of the current step.  Round 0: item type t ~ U{0..T-1} from the type
-// stream (one draw per step), rotation ~ U[0, 2pi) and translation ~ U(box) from the step's own
-// stream — the draws of make_queries in the workload generator (draw n+i: rotation, 2n+i: x,
-// 3n+i: y).  Round r >= 1 (local search): candidates around the step's best so far, from stream
-// (seed, ls_sid_base + 64 step + r): draw i: rotation offset in turns, ls_cand+i: x, 2 ls_cand+i: y;
-// with no best yet the round's candidates are marked invalid.  `qu` keeps each candidate's turns.
+// Float value of an order-preserving cost key (the inverse of `orderable`).
+__device__ __forceinline__ float cost_of_key(uint32_t v) {
+    return __uint_as_float((v & 0x80000000u) ? (v & 0x7FFFFFFFu) : ~v);
+}
+
+// Candidates of round `round` of the current step.  The item type t ~ U{0..T-1} comes from the type
+// stream (one draw per step).  Rounds 0 .. uni_rounds-1 are the uniform phase: round u draws
+// rotation ~ U[0, 2pi) and translation ~ U(box) (make_queries' draws: n+i rotation, 2n+i x, 3n+i y)
+// from the step's stream (seed, sid_base + s) for u = 0, else from (seed, uni_sid_base + 64 s + u)
+// over the box whose x1 is the step's best cost so far / 10 (LBFLoss::tighten_sample_bbox,
+// loss.rs:34-44) when there is a best.  Later rounds are local search: round r = round - uni_rounds + 1
+// draws around the step's best so far from stream (seed, ls_sid_base + 64 s + r): x and y offsets
+// float32(sigma * z) with the Box-Muller pair of draws i, m+i, the rotation sigma_turns * z' turns
+// with the pair of draws 2m+i, 3m+i; with no best yet the round's candidates are marked invalid.
+// `qu` keeps each candidate's turns.
 __global__ void k_lbf_gen(LbfParams p, LbfDev* __restrict__ st, uint32_t* __restrict__ q, double* __restrict__ qu,
                           uint32_t round) {
     const uint32_t step = *(volatile uint32_t*)&st->step;
     if (step >= p.max_steps) return;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
-        st->best = ~0ull;
         if (round == 0) {
             st->n_free = 0;
             st->rec_cost = ~0u;
+            st->best = ~0ull;
+        } else {
+            // The round's choice starts from the step's best so far (key: its cost, index ~0), as
+            // lbf's search tests a sample only if it beats the best so far (search.rs:52-56, :88): a
+            // candidate that cannot is left unjudged by the polygon pass, and when none beats it the
+            // merge keeps the best (its cost is not strictly lower).
+            const uint32_t rc = st->rec_cost;
+            st->best = rc == ~0u ? ~0ull : (((unsigned long long)rc << 32) | 0xFFFFFFFFull);
         }
     }
     const uint32_t t = p.seq ? p.seq[step] : (uint32_t)(draw(p.key_types, step) % p.n_types);
@@ -684,43 +738,51 @@ __global__ void k_lbf_gen(LbfParams p, LbfDev* __restrict__ st, uint32_t* __rest
         ooff = oo.x;
         ocnt = oo.y;
     }
-    if (round == 0) {
-        const unsigned long long key = stream_key(p.seed, (unsigned long long)p.sid_base + step);
-        const GenBox b{p.x0, p.x1, p.x1_below, p.y0, p.y1, p.y1_below};
-        for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < p.n_cand; i += gridDim.x * blockDim.x)
-            gen_uniform(key, p.n_cand, i, t, b, p.orient + ooff, ocnt, q, qu);
+    const volatile LbfDev* vs = st;
+    if (round < p.uni_rounds) {
+        const unsigned long long key = round == 0 ? stream_key(p.seed, (unsigned long long)p.sid_base + step)
+                                                  : stream_key(p.seed, p.uni_sid_base + 64ull * step + round);
+        GenBox b{p.x0, p.x1, p.x1_below, p.y0, p.y1, p.y1_below};
+        const uint32_t rc = round == 0 ? ~0u : vs->rec_cost;
+        if (rc != ~0u) {
+            b.x1 = fminf(p.x1, __fdiv_rn(cost_of_key(rc), 10.0f));
+            b.x1_below = nextafterf(b.x1, p.x0);
+        }
+        for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < p.n_uni; i += gridDim.x * blockDim.x)
+            gen_uniform(key, p.n_uni, i, t, b, p.orient + ooff, ocnt, q, qu);
         return;
     }
-    const volatile LbfDev* vs = st;
+    const uint32_t r = round - p.uni_rounds + 1;
     const bool have = vs->rec_cost != ~0u;
     const double ub = vs->rec_u;
     const float txb = __uint_as_float(vs->rec_q[3]), tyb = __uint_as_float(vs->rec_q[4]);
-    const unsigned long long key = stream_key(p.seed, p.ls_sid_base + 64ull * step + round);
+    const unsigned long long key = stream_key(p.seed, p.ls_sid_base + 64ull * step + r);
     const unsigned long long m = p.ls_cand;
-    const float sg = p.ls_sig[round], sgb = p.ls_sig_below[round];
-    const double sth = p.ls_sth[round];
+    const double sg = (double)p.ls_sig[r], sth = p.ls_sth[r];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < p.ls_cand; i += gridDim.x * blockDim.x) {
-        uint32_t* r = q + (size_t)i * 5;
+        uint32_t* o = q + (size_t)i * 5;
         if (!have) {
-            r[0] = 0xFFFFFFFFu;   // no best to search around: an invalid item, never free
+            o[0] = 0xFFFFFFFFu;   // no best to search around: an invalid item, never free
             continue;
         }
+        double zx, zy, zr, zu;
+        normal_pair(__dsub_rn(1.0, draw_f64(key, i)), draw_f64(key, m + i), zx, zy);
+        normal_pair(__dsub_rn(1.0, draw_f64(key, 2 * m + i)), draw_f64(key, 3 * m + i), zr, zu);
         float c, s;
         double u = ub;
         if (ocnt) {   // discrete orientations: the best's rotation is kept
             c = __uint_as_float(vs->rec_q[1]);
             s = __uint_as_float(vs->rec_q[2]);
         } else {
-            const double du = (double)(draw(key, i) >> 11) * 0x1p-53;
-            const double x = __dadd_rn(ub, __dmul_rn(__dsub_rn(__dmul_rn(2.0, du), 1.0), sth));
+            const double x = __dadd_rn(ub, __dmul_rn(sth, zr));
             u = __dsub_rn(x, floor(x));
             sincos_turns(u, c, s);
         }
-        r[0] = t;
-        r[1] = __float_as_uint(c);
-        r[2] = __float_as_uint(s);
-        r[3] = __float_as_uint(__fadd_rn(txb, draw_uniform(key, m + i, -sg, sg, sgb)));
-        r[4] = __float_as_uint(__fadd_rn(tyb, draw_uniform(key, 2 * m + i, -sg, sg, sgb)));
+        o[0] = t;
+        o[1] = __float_as_uint(c);
+        o[2] = __float_as_uint(s);
+        o[3] = __float_as_uint(__fadd_rn(txb, __double2float_rn(__dmul_rn(sg, zx))));
+        o[4] = __float_as_uint(__fadd_rn(tyb, __double2float_rn(__dmul_rn(sg, zy))));
         qu[i] = u;
     }
 }
@@ -825,7 +887,7 @@ void res_launch_insert_placed(const RTree& t, const DItem* items, const float2* 
 void res_launch_remove(const RTree& t, const uint32_t* key, cudaStream_t s) { k_res_remove<<<1, 32, 0, s>>>(t, key); }
 void res_launch_lbf_gen(const LbfParams& p, LbfDev* st, uint32_t* q, double* qu, uint32_t round, int n_sms,
                         cudaStream_t s) {
-    const uint32_t n = round ? p.ls_cand : p.n_cand;
+    const uint32_t n = round < p.uni_rounds ? p.n_uni : p.ls_cand;
     const uint32_t grid = std::min<uint32_t>((n + 255) / 256, (uint32_t)std::max(1, n_sms) * 4);
     k_lbf_gen<<<grid, 256, 0, s>>>(p, st, q, qu, round);
 }

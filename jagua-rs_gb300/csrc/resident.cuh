@@ -97,7 +97,8 @@ struct LbfDev {
     uint32_t pad[2];
 };
 
-constexpr int LBF_MAX_LS = 8;   // local-search rounds per step
+constexpr int LBF_MAX_LS = 8;        // local-search rounds per step
+constexpr int LBF_MAX_UNIFORM = 64;  // uniform rounds per step
 
 struct LbfParams {
     unsigned long long seed;   // candidate stream of step s: (seed, sid_base + s)
@@ -105,11 +106,16 @@ struct LbfParams {
     uint32_t sid_base, n_cand, n_types, remove_every, max_steps, vlog_steps;
     float x0, y0, x1, y1;      // sampling box of the translations
     float x1_below, y1_below;  // the largest float32 below x1 / y1 (draws stay inside the box)
+    // uniform phase: uni_rounds rounds of n_uni candidates; round u >= 1 draws from stream
+    // (seed, uni_sid_base + 64 s + u) with the box's x1 tightened to the step's best cost / 10
+    uint32_t uni_rounds, n_uni;
+    unsigned long long uni_sid_base;
     // local search: round r of step s draws ls_cand candidates around the step's best from stream
-    // (seed, ls_sid_base + 64 s + r): turns += U[-1,1) ls_sth[r], translation += U[-ls_sig[r], ls_sig[r])
+    // (seed, ls_sid_base + 64 s + r): Normal offsets with deviations ls_sig[r] (translation) and
+    // ls_sth[r] (rotation, in turns)
     uint32_t ls_rounds, ls_cand;
     unsigned long long ls_sid_base;
-    float ls_sig[LBF_MAX_LS + 1], ls_sig_below[LBF_MAX_LS + 1];
+    float ls_sig[LBF_MAX_LS + 1];
     double ls_sth[LBF_MAX_LS + 1];
     // instance mode: the item of step s is seq[s] (else drawn from the type stream); item t rotates
     // to one of orient[orient_of[t].x ..][0 .. orient_of[t].y) (count 0: continuous rotation)

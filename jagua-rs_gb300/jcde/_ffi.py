@@ -32,9 +32,9 @@ class jcde_resident_config(C.Structure):
 class jcde_lbf_params(C.Structure):
     _fields_ = [("seed", C.c_uint64), ("n_candidates", C.c_uint32), ("n_types", C.c_uint32),
                 ("remove_every", C.c_uint32), ("max_steps", C.c_uint32), ("verdict_log_steps", C.c_uint32),
-                ("reserved", C.c_uint32), ("sample_box", jcde_rect), ("ls_rounds", C.c_uint32),
-                ("ls_candidates", C.c_uint32), ("ls_sigma_t", C.c_float), ("ls_decay", C.c_float),
-                ("ls_sigma_turns", C.c_double), ("item_sequence", C.POINTER(C.c_uint32)), ("n_sequence", C.c_uint32),
+                ("uniform_rounds", C.c_uint32), ("sample_box", jcde_rect), ("ls_rounds", C.c_uint32),
+                ("ls_candidates", C.c_uint32), ("ls_sigma_t", C.c_float * 8), ("ls_sigma_turns", C.c_double * 8),
+                ("item_sequence", C.POINTER(C.c_uint32)), ("n_sequence", C.c_uint32),
                 ("n_orientation_items", C.c_uint32), ("orientation_offsets", C.POINTER(C.c_uint32)),
                 ("orientation_cs", C.POINTER(C.c_float))]
 

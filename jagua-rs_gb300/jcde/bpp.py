@@ -222,11 +222,8 @@ def quality_filter(bs: BinSetup, keys: list, min_quality) -> list | None:
 class BppSpec:
     seed: int = 0xB1
     n_cand: int = 4096
-    ls_rounds: int = 0
+    ls_rounds: int = 0   # local-search rounds after a layout's uniform round (lbf's deviations)
     ls_cand: int = 0
-    ls_sigma_t: float = 0.0
-    ls_sigma_turns: float = 0.0
-    ls_decay: float = 0.5
 
 
 @dataclass
@@ -266,10 +263,12 @@ def _round(spec: BppSpec, attempt: int, slot: int, t: int, box, orient):
     return q, u
 
 
-def _local_search(spec: BppSpec, su: BppSetup, eng, filt, attempt: int, t: int, rec):
-    """lbf's local-search rounds around a layout's best (strict improvement), on that layout's engine."""
-    ls = lbf.LbfSpec(seed=spec.seed, ls_rounds=spec.ls_rounds, ls_cand=spec.ls_cand, ls_sigma_t=spec.ls_sigma_t,
-                     ls_sigma_turns=spec.ls_sigma_turns, ls_decay=spec.ls_decay, orient=su.orient)
+def _local_search(spec: BppSpec, su: BppSetup, eng, filt, attempt: int, t: int, rec, box):
+    """lbf's local-search rounds around a layout's best (strict improvement), on that layout's engine;
+    the deviations scale with the bin's CDE box (its box inflated to a square)."""
+    box = np.asarray(box, dtype=np.float64)
+    ls = lbf.LbfSpec(seed=spec.seed, ls_rounds=spec.ls_rounds, ls_cand=spec.ls_cand, orient=su.orient,
+                     ls_max_dim=max(box[2] - box[0], box[3] - box[1]))
     for r, (sg, sth) in enumerate(ls.ls_sigmas(), start=1):
         # the rounds of attempt a draw lbf's local-search streams of step BPP_LS_STEP + a
         ql, ul = lbf._local_round(ls, BPP_LS_STEP + attempt, r, t, rec[1], rec[2], sg, sth)
@@ -318,7 +317,7 @@ def run_bpp(backend, su: BppSetup, spec: BppSpec, batched: bool = True) -> BppLo
             j, rec = found
             s, eng, keys, b = slots[j]
             if spec.ls_rounds:
-                rec = _local_search(spec, su, eng, filts[j], attempt, t, rec)
+                rec = _local_search(spec, su, eng, filts[j], attempt, t, rec, su.bins[b].box)
                 judged += spec.ls_rounds * spec.ls_cand
             if s >= CLOSED_SLOT:   # BPProblem::place_item opens a new layout (problem.rs:44-66)
                 eng, keys = _bin_engine(backend, su, b)

@@ -616,9 +616,10 @@ class ResidentEngine:
         return int(lib().jcde_resident_kernel_launches(self.h))
 
     def lbf_begin(self, seed, n_candidates, n_types, remove_every, max_steps, sample_box, verdict_log_steps=0,
-                  ls_rounds=0, ls_candidates=0, ls_sigma_t=0.0, ls_sigma_turns=0.0, ls_decay=0.5, item_sequence=None,
+                  ls_rounds=0, ls_candidates=0, ls_sigmas=(), uniform_rounds=1, item_sequence=None,
                   orientations=None):
-        """orientations: per engine item a float32 [k, 2] (cos, sin) table, or None for continuous rotation."""
+        """ls_sigmas: per local round (translation deviation, rotation deviation in turns);
+        orientations: per engine item a float32 [k, 2] (cos, sin) table, or None for continuous rotation."""
         p = jcde_lbf_params()
         keep = []
         if item_sequence is not None:
@@ -639,9 +640,10 @@ class ResidentEngine:
             p.orientation_cs = cs.ctypes.data_as(C.POINTER(C.c_float))
         p.ls_rounds = int(ls_rounds)
         p.ls_candidates = int(ls_candidates)
-        p.ls_sigma_t = float(np.float32(ls_sigma_t))
-        p.ls_decay = float(np.float32(ls_decay))
-        p.ls_sigma_turns = float(ls_sigma_turns)
+        for k, (sg, sth) in enumerate(ls_sigmas):
+            p.ls_sigma_t[k] = float(np.float32(sg))
+            p.ls_sigma_turns[k] = float(sth)
+        p.uniform_rounds = int(uniform_rounds)
         p.seed = int(seed)
         p.n_candidates = int(n_candidates)
         p.n_types = int(n_types)

@@ -6,9 +6,20 @@ verdicts, commits the candidate with the lowest LBF cost among the free ones
 ties keep the first, search.rs:52) by registering it as a hazard, and every `remove_every` steps
 deregisters a random placed item (as Layout::remove_item does, entities/layout.rs:88-100).
 
-Differences from lbf's search, chosen so that every engine sees the same candidates: the
-candidates of a step are drawn up front from a seeded stream (no sampling-box tightening between
-samples, search.rs:63-64, and no local-search phase, search.rs:80-101), uniformly over the strip.
+Each step restates lbf's search (search.rs:17-106) in rounds, so that every engine sees the same
+candidates and a whole round is one batch:
+* the uniform phase is `uniform_rounds` rounds of n_cand / uniform_rounds candidates drawn from a
+  seeded stream over the sampling box; after each round the box's x_max is tightened to the best
+  cost so far / 10 (LBFLoss::tighten_sample_bbox, loss.rs:34-44, applied by search.rs:62-63 after
+  every improvement; here after every round);
+* the optional local-search phase (search.rs:80-101) is `ls_rounds` rounds of `ls_cand`
+  candidates around the step's best so far, with Normal offsets whose standard deviations decay
+  exponentially from 1% to 0.05% of the CDE box's largest side (translation) and from 2 to 0.5
+  degrees (rotation), as LSSampler does (ls_sampler.rs:9-13, :84-90) per round instead of per
+  sample; the normals come from a project-owned Box-Muller generator (workload.normal_pair) fed by
+  the seeded streams, identical on the host and the device (lbf's own generator, rand_distr's
+  Normal, is not reproducible outside Rust);
+* a round's least-cost free candidate replaces the step's best when it costs strictly less.
 
 Two drivers share the definition: `run_host` (one engine call per step from Python: the oracle,
 or the GPU engine with host-side registration) and `run_device` (jcde_lbf_*: generation, verdicts,
@@ -21,6 +32,7 @@ verdict), which changes no choice.
 """
 from __future__ import annotations
 
+import math
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -29,7 +41,12 @@ from . import workload as W
 
 SEED = 0xC3
 TYPE_SID, REMOVE_SID, CAND_SID_BASE = 2, 4, 10_000   # stream ids of the driver's draws
-LS_SID_BASE = 1_000_000   # local-search round r of step s: stream LS_SID_BASE + 64 s + r
+LS_SID_BASE = 1_000_000    # local-search round r of step s: stream LS_SID_BASE + 64 s + r
+UNI_SID_BASE = 2_000_000   # uniform round u >= 1 of step s: stream UNI_SID_BASE + 64 s + u (round 0: CAND_SID_BASE + s)
+# LSSampler's default deviations (ls_sampler.rs:9-13): translation as fractions of the CDE box's
+# largest side, rotation in radians, each (start, end)
+SD_TRANSL = (0.01, 0.0005)
+SD_ROT = (2.0 * math.pi / 180.0, 0.5 * math.pi / 180.0)
 
 
 @dataclass
@@ -47,26 +64,35 @@ class LbfSpec:
     remove_every: int = 50
     depth: int = W.DEFAULT_DEPTH
     cd_threshold: int = W.DEFAULT_CD_THRESHOLD
-    # local search after the uniform round (0 rounds: off); half-widths shrink by ls_decay per round
+    # uniform phase in rounds (the sampling box tightened after each; 1: the benchmark's build, every
+    # candidate of a step drawn over the whole strip); local search after it (0: off)
+    uniform_rounds: int = 1
     ls_rounds: int = 0
     ls_cand: int = 0
-    ls_sigma_t: float = 0.0
-    ls_sigma_turns: float = 0.0
-    ls_decay: float = 0.5
+    ls_max_dim: float = 0.0   # largest side of the CDE box the deviations scale with (0: the strip's)
     # instance mode: the item of each step (else drawn from the type stream) and, per item, a float32
     # (cos, sin) table of allowed orientations or None for continuous rotation
     item_seq: np.ndarray | None = None
     orient: list | None = None
 
     def ls_sigmas(self):
-        """Per round r = 1..ls_rounds: (translation half-width float32, turns half-width float64)."""
-        out, sg, sth = [], np.float32(self.ls_sigma_t), float(self.ls_sigma_turns)
+        """Per local round r = 1..ls_rounds: (translation deviation float32, rotation deviation in
+        turns float64) at progress (r-1)/ls_rounds of LSSampler::decay_stddev's exponential curve
+        (ls_sampler.rs:84-90)."""
+        dim = float(self.ls_max_dim) or max(float(self.width), float(self.height))
+        out = []
         for r in range(1, self.ls_rounds + 1):
-            if r > 1:
-                sg = np.float32(sg * np.float32(self.ls_decay))
-                sth = sth * float(np.float32(self.ls_decay))
-            out.append((sg, sth))
+            pct = (r - 1) / self.ls_rounds
+            st = SD_TRANSL[0] * dim * (SD_TRANSL[1] / SD_TRANSL[0]) ** pct
+            sr = SD_ROT[0] * (SD_ROT[1] / SD_ROT[0]) ** pct
+            out.append((np.float32(st), sr / (2.0 * math.pi)))
         return out
+
+    @property
+    def n_uniform(self) -> int:
+        """Candidates per uniform round."""
+        assert self.n_cand % self.uniform_rounds == 0, "n_cand must be a multiple of uniform_rounds"
+        return self.n_cand // self.uniform_rounds
 
     @property
     def box(self) -> np.ndarray:
@@ -160,29 +186,35 @@ def _orient_of(spec: LbfSpec, t: int):
     return None if spec.orient is None else spec.orient[t]
 
 
-def _uniform_round(spec: LbfSpec, step: int, t: int):
-    """Round 0 of a step: make_queries' candidates and their rotations in turns (with allowed
-    orientations: orientation (draw n+i) mod count, turns unused)."""
-    q = W.make_queries(W.Stream(spec.seed, CAND_SID_BASE + step), spec.n_cand, 1, spec.box)
+def _uniform_round(spec: LbfSpec, step: int, u: int, t: int, x1):
+    """Uniform round u of a step over the sampling box with x_max = x1: make_queries' candidates
+    and their rotations in turns (with allowed orientations: orientation (draw n+i) mod count,
+    turns unused)."""
+    n = spec.n_uniform
+    sid = CAND_SID_BASE + step if u == 0 else UNI_SID_BASE + 64 * step + u
+    box = spec.box.copy()
+    box[2] = np.float32(x1)
+    q = W.make_queries(W.Stream(spec.seed, sid), n, 1, box)
     q["item"] = t
-    st = W.Stream(spec.seed, CAND_SID_BASE + step)
-    st.pos = spec.n_cand   # make_queries draws the items first, then the rotations
+    st = W.Stream(spec.seed, sid)
+    st.pos = n   # make_queries draws the items first, then the rotations
     o = _orient_of(spec, t)
     if o is None:
-        return q, st.f64(spec.n_cand)
-    k = (st.u64(spec.n_cand) % np.uint64(len(o))).astype(np.int64)
+        return q, st.f64(n)
+    k = (st.u64(n) % np.uint64(len(o))).astype(np.int64)
     q["cos"] = o[k, 0]
     q["sin"] = o[k, 1]
-    return q, np.zeros(spec.n_cand)
+    return q, np.zeros(n)
 
 
 def _local_round(spec: LbfSpec, step: int, r: int, t: int, best_u: float, best_q, sg, sth):
-    """Round r >= 1: candidates around the step's best (turns offset, then x, then y draws)."""
+    """Local round r >= 1: candidates around the step's best.  Draws i and m+i give the normals of
+    x and y (Box-Muller), 2m+i and 3m+i the rotation's; translation offsets are float32(sg * z), the
+    rotation moves by sth * z turns."""
     m = spec.ls_cand
-    st = W.Stream(spec.seed, LS_SID_BASE + 64 * step + r)
-    du = st.f64(m)
-    dx = st.uniform_f32(-sg, sg, m)
-    dy = st.uniform_f32(-sg, sg, m)
+    d = W.Stream(spec.seed, LS_SID_BASE + 64 * step + r).f64(4 * m)
+    zx, zy = W.normal_pair(1.0 - d[:m], d[m:2 * m])
+    zr, _ = W.normal_pair(1.0 - d[2 * m:3 * m], d[3 * m:])
     q = np.zeros(m, dtype=W.QUERY_DTYPE)
     q["item"] = t
     if _orient_of(spec, t) is not None:   # discrete orientations: the best's rotation is kept
@@ -190,13 +222,14 @@ def _local_round(spec: LbfSpec, step: int, r: int, t: int, best_u: float, best_q
         q["cos"] = best_q["cos"]
         q["sin"] = best_q["sin"]
     else:
-        x = best_u + (2.0 * du - 1.0) * sth
+        x = best_u + float(sth) * zr
         u = x - np.floor(x)
         c, s = W.sincos_turns(u)
         q["cos"] = c.astype(np.float32)
         q["sin"] = s.astype(np.float32)
-    q["tx"] = np.float32(best_q["tx"]) + dx
-    q["ty"] = np.float32(best_q["ty"]) + dy
+    sg64 = np.float64(np.float32(sg))
+    q["tx"] = np.float32(best_q["tx"]) + (sg64 * zx).astype(np.float32)
+    q["ty"] = np.float32(best_q["ty"]) + (sg64 * zy).astype(np.float32)
     return q, u
 
 
@@ -208,14 +241,21 @@ def run_host(lay, eng, spec: LbfSpec, steps: int | None = None, keep_verdicts: i
     sigmas = spec.ls_sigmas()
     placements, removals, free_counts, vkeep = [], [], [], []
     live = []   # keys of placed items, in placement order
+    n_uni = spec.uniform_rounds
     for step in range(steps):
         t = int(spec.item_seq[step]) if spec.item_seq is not None else int(types[step])
-        q, u = _uniform_round(spec, step, t)
-        verdicts, n_free = eng.detect_with_surrogate(q)
-        if step < keep_verdicts:
-            vkeep.append(np.asarray(verdicts).copy())
-        best, cost = select_host_cost(lay.items, q, verdicts)
-        rec = (cost, float(u[best]), q[best].copy(), best) if best >= 0 else None
+        rec, n_free = None, 0
+        for u in range(n_uni):
+            # LBFLoss::tighten_sample_bbox (loss.rs:34-44) by the best so far
+            x1 = spec.box[2] if rec is None else min(spec.box[2], np.float32(rec[0] / np.float32(10.0)))
+            q, uu = _uniform_round(spec, step, u, t, x1)
+            verdicts, nf = eng.detect_with_surrogate(q)
+            n_free += nf
+            if step < keep_verdicts:
+                vkeep.append(np.asarray(verdicts).copy())
+            b, cb = select_host_cost(lay.items, q, verdicts)
+            if b >= 0 and (rec is None or cb < rec[0]):   # strictly better replaces (search.rs:52 keeps the first)
+                rec = (cb, float(uu[b]), q[b].copy(), (u << 24) | b)
         for r, (sg, sth) in enumerate(sigmas, start=1):
             if rec is None:
                 break   # nothing to search around (the device marks the round's candidates invalid)
@@ -223,8 +263,8 @@ def run_host(lay, eng, spec: LbfSpec, steps: int | None = None, keep_verdicts: i
             vl, nf = eng.detect_with_surrogate(ql)
             n_free += nf
             b, cb = select_host_cost(lay.items, ql, vl)
-            if b >= 0 and cb < rec[0]:   # strictly better replaces (search.rs:52 keeps the first)
-                rec = (cb, float(ul[b]), ql[b].copy(), (r << 24) | b)
+            if b >= 0 and cb < rec[0]:
+                rec = (cb, float(ul[b]), ql[b].copy(), ((n_uni - 1 + r) << 24) | b)
         free_counts.append(n_free)
         if rec is not None:
             r_q = rec[2]
@@ -253,7 +293,7 @@ def run_device(eng, spec: LbfSpec, steps: int | None = None, steps_per_graph: in
     cde = eng.eng if hasattr(eng, "eng") else eng
     r = resident if resident is not None else ResidentEngine(cde)
     r.lbf_begin(spec.seed, spec.n_cand, spec.n_types, spec.remove_every, steps, spec.box, keep_verdicts,
-                spec.ls_rounds, spec.ls_cand, spec.ls_sigma_t, spec.ls_sigma_turns, spec.ls_decay,
+                spec.ls_rounds, spec.ls_cand, spec.ls_sigmas(), spec.uniform_rounds,
                 item_sequence=spec.item_seq, orientations=spec.orient)
     r.lbf_steps(steps, steps_per_graph)
     d = r.lbf_read()

@@ -111,6 +111,47 @@ def sincos_turns(u: np.ndarray):
     return cos, sin
 
 
+# 1 / (2k + 1), k = 0..12, and ln 2 split into two doubles (hi + lo)
+_ATANH_C = [float.fromhex(h) for h in (
+    "0x1.0000000000000p+0", "0x1.5555555555555p-2", "0x1.999999999999ap-3", "0x1.2492492492492p-3",
+    "0x1.c71c71c71c71cp-4", "0x1.745d1745d1746p-4", "0x1.3b13b13b13b14p-4", "0x1.1111111111111p-4",
+    "0x1.e1e1e1e1e1e1ep-5", "0x1.af286bca1af28p-5", "0x1.8618618618618p-5", "0x1.642c8590b2164p-5",
+    "0x1.47ae147ae147bp-5")]
+_LN2_HI = float.fromhex("0x1.62e42fefa39efp-1")
+_LN2_LO = float.fromhex("0x1.abc9e3b39803fp-56")
+_SQRT_HALF = float.fromhex("0x1.6a09e667f3bcdp-1")
+
+
+def ln_f64(x: np.ndarray) -> np.ndarray:
+    """Natural logarithm of positive normal float64 values using only IEEE additions, multiplications
+    and divisions (bit-identical on every platform, and restated in the device generator): x = m 2^e
+    with m in [sqrt(1/2), sqrt(2)), ln m = 2 atanh(z) = 2 (z + z^3/3 + ...) with z = (m-1)/(m+1),
+    |z| <= 0.172, 13 terms of the series (Horner form)."""
+    x = np.asarray(x, dtype=np.float64)
+    bits = x.view(np.uint64)
+    e = ((bits >> np.uint64(52)) & np.uint64(0x7FF)).astype(np.int64) - 1022
+    m = ((bits & np.uint64((1 << 52) - 1)) | np.uint64(1022 << 52)).view(np.float64)   # [0.5, 1)
+    low = m < _SQRT_HALF
+    m = np.where(low, m * 2.0, m)
+    e = np.where(low, e - 1, e).astype(np.float64)
+    z = (m - 1.0) / (m + 1.0)
+    z2 = z * z
+    s = np.full_like(z, _ATANH_C[-1])
+    for c in reversed(_ATANH_C[:-1]):
+        s = s * z2 + c
+    t = (2.0 * z) * s
+    return e * _LN2_HI + (e * _LN2_LO + t)
+
+
+def normal_pair(u1: np.ndarray, u2: np.ndarray):
+    """Two standard normal float64 draws from uniforms u1 in (0, 1] and u2 in [0, 1) by the
+    Box-Muller transform (G. E. P. Box and M. E. Muller, 1958): r = sqrt(-2 ln u1), (r cos 2 pi u2,
+    r sin 2 pi u2), with ln_f64 and the Taylor sin/cos of sincos_turns (every step an IEEE operation)."""
+    r = np.sqrt(-2.0 * ln_f64(u1))
+    c, s = sincos_turns(u2)
+    return r * c, r * s
+
+
 def transform_points(xy: np.ndarray, cos, sin, tx, ty) -> np.ndarray:
     """TRANSFORM_FORMULA (geometry/primitives/point.rs:259-264) in float32, no fused multiply-add.
 

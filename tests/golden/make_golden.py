@@ -33,7 +33,7 @@ def prep_shapes():
 
 
 def lbf_spec():
-    return lbf.LbfSpec(n_types=12, n_cand=512, steps=60, remove_every=20)
+    return lbf.LbfSpec(n_types=12, n_cand=512, steps=60, remove_every=20, uniform_rounds=1)
 
 
 def bpp_case():

@@ -14,7 +14,7 @@ def test_bpp_matches_oracle(oracle_mod, jcde_mod, ls):
     import jcde
 
     inst = bpp.load_bpp(bpp.synthetic_instance(n_types=16, n_bins=4))
-    spec = bpp.BppSpec(n_cand=2048, ls_rounds=ls, ls_cand=512 if ls else 0, ls_sigma_t=50.0, ls_sigma_turns=0.05)
+    spec = bpp.BppSpec(n_cand=2048, ls_rounds=ls, ls_cand=512 if ls else 0)
     ref = bpp.run_bpp(oracle_mod.OracleBackend, bpp.setup_bpp(oracle_mod.OracleBackend, inst), spec)
     su = bpp.setup_bpp(jcde.GpuBackend, inst)
     got = bpp.run_bpp(jcde.GpuBackend, su, spec, batched=True)

@@ -128,6 +128,22 @@ def test_lbf_full_size_matches_oracle(oracle_mod, jcde_mod):
     assert np.array_equal(r.tree_dump(), oeng.tree_dump())
 
 
+def test_lbf_search_with_box_tightening_and_normal_local_search_matches_oracle(oracle_mod, jcde_mod):
+    """lbf's search restated in rounds: 4 uniform rounds, each over the box tightened to the best
+    cost so far / 10 (search.rs:62-63, loss.rs:34-44), then 3 local-search rounds with Normal offsets
+    on LSSampler's decaying deviations (ls_sampler.rs): the device build equals the oracle-driven
+    one (placements, removals, per-step counts, final tree), eagerly and from a CUDA graph."""
+    spec = lbf.LbfSpec(steps=240, n_cand=4096, remove_every=40, uniform_rounds=4, ls_rounds=3, ls_cand=1024)
+    ref, oeng, got, r = _lbf_pair(oracle_mod, spec, steps_per_graph=16)
+    assert len(ref.placements) >= 200
+    assert got.same_as(ref)
+    assert r.status()["error"] == 0
+    assert np.array_equal(r.tree_dump(), oeng.tree_dump())
+    # the later rounds did choose (their round index is in the placement log)
+    rounds = ref.placements[:, 2] >> 24
+    assert (rounds >= 1).sum() > 20 and (rounds >= 4).sum() > 20
+
+
 def test_resident_capacity_error_is_sticky_and_reset_clears_it(strip_layout, jcde_mod):
     """A pool that runs out sets a sticky capacity error; later updates are skipped; reset recovers."""
     import torch
@@ -175,8 +191,7 @@ def test_lbf_select_entry_point_matches_host_choice(oracle_mod, jcde_mod):
 
 def test_lbf_with_local_search_matches_oracle(oracle_mod, jcde_mod):
     """Uniform round plus three local-search rounds per step, on the device and through the oracle."""
-    spec = lbf.LbfSpec(steps=160, n_cand=4096, remove_every=40, ls_rounds=3, ls_cand=1024, ls_sigma_t=150.0,
-                       ls_sigma_turns=0.05)
+    spec = lbf.LbfSpec(steps=160, n_cand=4096, remove_every=40, ls_rounds=3, ls_cand=1024)
     ref, oeng, got, r = _lbf_pair(oracle_mod, spec, steps_per_graph=16)
     rounds = ref.placements[:, 2] >> 24
     assert (rounds > 0).sum() > 20   # local search improved many steps
@@ -194,7 +209,7 @@ def test_instance_build_matches_oracle(oracle_mod, jcde_mod):
     inst = I.load_spp(DEMO)
     su_o = I.setup_spp(oracle_mod.OracleBackend, inst, 800.0)
     su_g = I.setup_spp(jcde.GpuBackend, inst, 800.0)
-    spec = lbf.spec_for_instance(su_o, n_cand=2048, ls_rounds=2, ls_cand=512, ls_sigma_t=30.0, ls_sigma_turns=0.05)
+    spec = lbf.spec_for_instance(su_o, n_cand=2048, ls_rounds=2, ls_cand=512)
     ref = lbf.run_host(su_o.layout, su_o.engine, spec)
     got, r = lbf.run_device(su_g.engine, spec, steps_per_graph=4)
     assert len(ref.placements) == 12 and got.same_as(ref)

@@ -50,7 +50,7 @@ def test_load_and_setup(oracle_mod):
 
 def test_instance_build_on_the_oracle(oracle_mod):
     su = I.setup_spp(oracle_mod.OracleBackend, I.load_spp(DEMO), 800.0)
-    spec = lbf.spec_for_instance(su, n_cand=1024, ls_rounds=2, ls_cand=256, ls_sigma_t=30.0, ls_sigma_turns=0.05)
+    spec = lbf.spec_for_instance(su, n_cand=1024, ls_rounds=2, ls_cand=256)
     log = lbf.run_host(su.layout, su.engine, spec)
     assert len(log.placements) == 12
     o0 = su.orient[0]
