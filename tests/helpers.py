@@ -1,9 +1,21 @@
 """Helpers shared by the test modules: a GPU engine holding a layout, batch calls on the GPU
 engine, and CSR key lists as per-query lists."""
+import os
+
 import numpy as np
 
 import jcde
 from jcde import workload as W
+
+
+# The reference's own instance files (its assets/ directory), read in place by a few CPU tests when
+# this variable names that directory; the tests skip otherwise.
+REFERENCE_ASSETS = os.environ.get("JCDE_REFERENCE_ASSETS", "")
+
+
+def reference_asset(name: str) -> str:
+    """Path of one of the reference's asset files, or "" when the directory is not given."""
+    return os.path.join(REFERENCE_ASSETS, name) if REFERENCE_ASSETS else ""
 
 
 def torch_queries(q):

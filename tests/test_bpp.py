@@ -8,7 +8,9 @@ import pytest
 from jcde import bpp
 from jcde import workload as W
 
-REF_BALDACCI = "/root/reference/assets/baldacci1.json"
+from helpers import reference_asset  # noqa: E402
+
+REF_BALDACCI = reference_asset("baldacci1.json")
 
 
 def test_load_rules():
@@ -76,7 +78,7 @@ def test_items_that_fit_nowhere(oracle_mod):
     assert 0 not in [int(r[3]) for r in log.placements]
 
 
-@pytest.mark.skipif(not os.path.exists(REF_BALDACCI), reason="reference assets not present")
+@pytest.mark.skipif(not (REF_BALDACCI and os.path.exists(REF_BALDACCI)), reason="JCDE_REFERENCE_ASSETS not set")
 def test_reference_instance_on_the_oracle(oracle_mod):
     """A reference bin-packing instance with quality zones, read in place, packed on the oracle."""
     inst = bpp.load_bpp(REF_BALDACCI)
@@ -87,7 +89,7 @@ def test_reference_instance_on_the_oracle(oracle_mod):
     _replay_free(oracle_mod, su, log)
 
 
-@pytest.mark.skipif(not os.path.exists(REF_BALDACCI), reason="reference assets not present")
+@pytest.mark.skipif(not (REF_BALDACCI and os.path.exists(REF_BALDACCI)), reason="JCDE_REFERENCE_ASSETS not set")
 def test_reference_instance_lbf_default_import(oracle_mod):
     """The reference instance imported as lbf's default config does (simplification 0.001 and
     concavities under 1% closed, items inflated, the container outers deflated) still packs."""

@@ -60,10 +60,12 @@ def test_instance_build_on_the_oracle(oracle_mod):
             assert (o0 == cs).all(axis=1).any()
 
 
-REF_ASSET = "/root/reference/assets/swim.json"
+from helpers import reference_asset  # noqa: E402
+
+REF_ASSET = reference_asset("swim.json")
 
 
-@pytest.mark.skipif(not os.path.exists(REF_ASSET), reason="reference assets not present")
+@pytest.mark.skipif(not (REF_ASSET and os.path.exists(REF_ASSET)), reason="JCDE_REFERENCE_ASSETS not set")
 def test_reference_instance_imports(oracle_mod):
     """A reference instance read in place: parsed, imported, and a few LBF steps run on the oracle."""
     inst = I.load_spp(REF_ASSET)

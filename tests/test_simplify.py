@@ -9,7 +9,7 @@ import pytest
 
 from jcde import workload as W
 
-REF_ASSETS = "/root/reference/assets"
+from helpers import REFERENCE_ASSETS as REF_ASSETS  # noqa: E402
 
 
 def _stars(n=24, seed=0xC2):
@@ -64,7 +64,7 @@ def _ref_instances():
     return sorted(glob.glob(os.path.join(REF_ASSETS, "*.json")))
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_ASSETS), reason="reference assets not present")
+@pytest.mark.skipif(not (REF_ASSETS and os.path.isdir(REF_ASSETS)), reason="JCDE_REFERENCE_ASSETS not set")
 def test_reference_instances_simplify(oracle_mod):
     """Every simple-polygon item of the reference's instances (read in place) simplifies at lbf's
     default tolerance within its invariants."""
