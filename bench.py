@@ -677,7 +677,7 @@ def measure_proxy(steps: int, warmup: int, lay=None, grad_check: int = 1 << 16):
         return int(s_.item()) / (a_ev.elapsed_time(b_ev) / 1e3)
 
     sweep = {}
-    for steps_ in (5, 10, 20):
+    for steps_ in (1, 2, 3, 5, 10, 20):
         def gd_s(steps_=steps_):
             q, _ = eng.separate_batch(P0.clone(), I0, steps=steps_, step_t=0.25, step_th=0.25, clearance=CLEARANCE,
                                       filter=filt)
