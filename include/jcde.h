@@ -370,23 +370,30 @@ typedef struct jcde_tuning {
     uint32_t leaf_table_max;       /* n <= this: polygon pass with per-query leaf tables, queries one by one */
     uint32_t poly_chunk;           /* otherwise: queries per counter grab in the polygon pass (0: grid stride) */
     uint32_t order_min_batch;      /* n >= this: queries visited in Morton order of their translation */
+    uint32_t surrogate_lanes;      /* lanes per query in the warp surrogate pass: 8, 16 or 32 */
+    uint32_t edge_tile;            /* edges per tile box a leaf test skips by (edge.rs:188-199): 4, 8 or 16 */
+    uint32_t staging_depth;        /* top quadtree levels the large-batch polygon pass keeps in shared
+                                      memory (0-4; levels whose nodes do not fit are left in global) */
 } jcde_tuning;
 jcde_status jcde_get_tuning(const jcde_engine* e, jcde_tuning* out);
 jcde_status jcde_set_tuning(jcde_engine* e, const jcde_tuning* t);
-/* Times all 16 combinations (surrogate pass warp/thread x polygon pass leaf tables/grabs of 1, 2, 4 x
- * Morton order on/off) on the caller's batch, checks that every combination gives the same verdicts
- * (JCDE_ERR_STATE otherwise), keeps the fastest in the engine (its thresholds set so that batches of
- * this size take it) and returns it with its median time.  Each timing starts from a cold L2 (a
- * 256 MB buffer, allocated for the call, is written before it), as a fresh batch would.
+/* Times, on the caller's batch, all 16 launch shapes (surrogate pass warp/thread x polygon pass leaf
+ * tables/grabs of 1, 2, 4 x Morton order on/off), then with the fastest the edge tiles 4/8/16, the
+ * staging depths 0-4 (when the large-batch polygon pass is chosen) and 8/16/32 lanes per query (when
+ * the warp surrogate pass is chosen), one knob at a time; checks that every choice gives the same
+ * verdicts (JCDE_ERR_STATE otherwise), keeps the fastest in the engine (its thresholds set so that
+ * batches of this size take it) and returns it with its median time.  Each timing starts from a
+ * cold L2 (a 256 MB buffer, allocated for the call, is written before it), as a fresh batch would.
  * Synchronises. */
 jcde_status jcde_autotune(jcde_engine* e, const jcde_query* d_queries, uint32_t n, const jcde_filter* f, void* stream,
                           jcde_tuning* out, double* best_ms);
-/* The same for a jcde_multi batch: polygon-pass grabs of 1, 2, 4, 8 x Morton order on/off, verdicts
- * checked identical, timed from a cold L2; d_out (device, total queries) receives verdicts; out2 =
- * chosen grab size, order flag.  The choice applies to later jcde_multi_detect / _graph calls.
+/* The same for a jcde_multi batch: polygon-pass grabs of 1, 2, 4, 8 x Morton order on/off, then edge
+ * tiles of 4, 8, 16 for every engine, verdicts checked identical, timed from a cold L2; d_out
+ * (device, total queries) receives verdicts; out3 = chosen grab size, order flag, edge tile.  The
+ * choice applies to later jcde_multi_detect / _graph calls (the edge tile is set in the engines).
  * Synchronises. */
 jcde_status jcde_multi_autotune(jcde_multi* m, const jcde_query* d_queries, const uint32_t* offsets,
-                                const jcde_filter* filters, uint8_t* d_out, void* stream, uint32_t* out2,
+                                const jcde_filter* filters, uint8_t* d_out, void* stream, uint32_t* out3,
                                 double* best_ms);
 
 /* --- snapshots: CDEngine::save / restore (cd_engine.rs:98-149) ------------------------------- */

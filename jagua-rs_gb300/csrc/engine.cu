@@ -93,9 +93,10 @@ struct jcde_engine {
     FlatTree flat;
     std::vector<DHaz> haz;
     std::vector<float2> hverts;
-    DevBuf d_nodes, d_nedges, d_strength0, d_entries, d_edges, d_cbox, d_haz, d_hverts;
+    DevBuf d_nodes, d_nedges, d_strength0, d_entries, d_edges, d_cbox[EDGE_TILES], d_haz, d_hverts;
     DevBuf d_items, d_iverts, d_poles, d_piers;
     uint32_t n_nodes = 0;
+    uint32_t level_end[MAX_STAGING_DEPTH + 1] = {};   // nodes of the top d + 1 levels, breadth-first
     // filters
     std::list<FilterSlot> filters;
     // staging for host entry points and single queries
@@ -118,7 +119,8 @@ struct jcde_engine {
     int n_sms = 0;
     int detect_blocks_per_sm = 0, collect_blocks_per_sm = 0, tab_blocks_per_sm = 0;
     // launch choices of the detect passes (jcde_set_tuning / jcde_autotune)
-    jcde_tuning tune{JCDE_SURR_WARP_MAX, JCDE_SURR_WARP_MAX, (uint32_t)JCDE_POLY_CHUNK, JCDE_ORDER_MIN_BATCH};
+    jcde_tuning tune{JCDE_SURR_WARP_MAX, JCDE_SURR_WARP_MAX, (uint32_t)JCDE_POLY_CHUNK, JCDE_ORDER_MIN_BATCH,
+                     (uint32_t)JCDE_SURR_GROUP, EDGE_TILE_DEFAULT, 0u};
     uint64_t launches = 0;
     // optional per-kernel timing (jcde_profile_enable): CUDA events around each launch
     bool prof = false;
@@ -211,10 +213,21 @@ static jcde_status sync_device(jcde_engine* e) {
         if ((st = upload(e->d_strength0, e->flat.strength.data(), e->flat.strength.size()))) return st;
         if ((st = upload(e->d_entries, e->flat.entries.data(), e->flat.entries.size() * sizeof(DEntry)))) return st;
         if ((st = upload(e->d_edges, e->flat.edges.data(), e->flat.edges.size() * 4))) return st;
-        if ((st = upload(e->d_cbox, e->flat.cbox.data(), e->flat.cbox.size() * sizeof(Box)))) return st;
+        for (int t = 0; t < EDGE_TILES; t++)
+            if ((st = upload(e->d_cbox[t], e->flat.cbox[t].data(), e->flat.cbox[t].size() * sizeof(Box)))) return st;
         if ((st = upload(e->d_haz, e->haz.data(), e->haz.size() * sizeof(DHaz)))) return st;
         if ((st = upload(e->d_hverts, e->hverts.data(), e->hverts.size() * sizeof(float2)))) return st;
         e->n_nodes = (uint32_t)e->flat.nodes.size();
+        {   // breadth-first level boundaries: a level's children quartets follow it in order
+            uint32_t a = 0, b = std::min<uint32_t>(1, e->n_nodes);
+            for (uint32_t d = 0; d <= MAX_STAGING_DEPTH; d++) {
+                e->level_end[d] = b;
+                uint32_t internal = 0;
+                for (uint32_t k = a; k < b; k++) internal += e->flat.nodes[k].child >= 0 ? 1u : 0u;
+                a = b;
+                b = std::min<uint32_t>(e->n_nodes, b + 4 * internal);
+            }
+        }
         e->tree_version = e->tree.version();
     }
     if (e->items_dirty) {
@@ -321,7 +334,11 @@ static View base_view(const jcde_engine* e) {
     v.strength = e->d_strength0.as<uint8_t>();
     v.mask = nullptr;
     v.nedges = e->d_nedges.as<uint32_t>();
-    v.cbox = e->d_cbox.as<float4>();
+    {   // the edge tile of the engine's launch choices: 4, 8 or 16 edges
+        const int t = e->tune.edge_tile == 4 ? 0 : e->tune.edge_tile == 16 ? 2 : 1;
+        v.cbox = e->d_cbox[t].as<float4>();
+        v.eg_shift = (uint32_t)(2 + t);
+    }
     v.cde = e->tree.bbox();
     v.coord_max = std::max(std::max(std::fabs(v.cde.x0), std::fabs(v.cde.x1)), std::max(std::fabs(v.cde.y0), std::fabs(v.cde.y1)));
     v.n_items = (uint32_t)e->items.size();
@@ -413,6 +430,7 @@ static void init_launch_shape(jcde_engine* e) {
 #ifndef JCDE_SPATIAL_ORDER
 #define JCDE_SPATIAL_ORDER 1
 #endif
+static constexpr size_t STAGE_MAX_BYTES = 8192;   // shared memory the polygon pass may use for staged nodes
 
 
 // Visit order of a batch: cell-by-cell over the CDE box (k_bucket_*), or nullptr for index order.
@@ -471,9 +489,12 @@ static bool launch_passes_t(jcde_engine* e, const View& v, const uint32_t* q, ui
         const uint8_t miss = mode == 1 ? (uint8_t)0 : PENDING;
         cudaEvent_t pa = prof_begin(e, s);
         if (n <= e->tune.surrogate_warp_max) {   // too few queries to fill the GPU one thread each
-            const uint32_t gpb = SURR_THREADS / JCDE_SURR_GROUP;   // query groups per block
+            const uint32_t lanes = e->tune.surrogate_lanes;
+            const uint32_t gpb = SURR_THREADS / lanes;   // query groups per block
             const uint32_t grid = std::min<uint32_t>((n + gpb - 1) / gpb, (uint32_t)e->n_sms * 8);
-            k_surrogate_warp<PendT><<<grid, SURR_THREADS, 0, s>>>(v, q, n, dout, miss, order, n_pending);
+            if (lanes == 8) k_surrogate_warp<PendT, 8><<<grid, SURR_THREADS, 0, s>>>(v, q, n, dout, miss, order, n_pending);
+            else if (lanes == 16) k_surrogate_warp<PendT, 16><<<grid, SURR_THREADS, 0, s>>>(v, q, n, dout, miss, order, n_pending);
+            else k_surrogate_warp<PendT, 32><<<grid, SURR_THREADS, 0, s>>>(v, q, n, dout, miss, order, n_pending);
         } else if (JCDE_SURR_DYNAMIC && next && cudaMemsetAsync(next, 0, 4, s) == cudaSuccess) {
             // persistent blocks; each warp takes the next 32 queries from a counter as it finishes
             int per_sm = 0;
@@ -507,8 +528,21 @@ static bool launch_passes_t(jcde_engine* e, const View& v, const uint32_t* q, ui
                                                                                         order, next, best, skip);
             chose = best != nullptr;
         } else {
-            k_poly<PendT, false><<<grid, POLY_WARPS * 32, 0, s>>>(v, MultiSrc{}, q, n, dout, raw, mode == 3, order, next,
-                                                                  std::max(e->tune.poly_chunk, 1u), pend.rec, pend.count);
+            // the top staging_depth levels of the tree in shared memory (at most STAGE_MAX_BYTES)
+            uint32_t staged = e->tune.staging_depth ? e->level_end[e->tune.staging_depth - 1] : 0u;
+            while (staged && (size_t)staged * (sizeof(DNode) + 1) > STAGE_MAX_BYTES) staged /= 4;
+            if (staged) {
+                View vs = v;
+                vs.n_staged = staged;
+                const size_t smem = ((size_t)staged * (sizeof(DNode) + 1) + 15) & ~size_t(15);
+                k_poly<PendT, false, true><<<grid, POLY_WARPS * 32, smem, s>>>(
+                    vs, MultiSrc{}, q, n, dout, raw, mode == 3, order, next, std::max(e->tune.poly_chunk, 1u), pend.rec,
+                    pend.count);
+            } else {
+                k_poly<PendT, false><<<grid, POLY_WARPS * 32, 0, s>>>(v, MultiSrc{}, q, n, dout, raw, mode == 3, order,
+                                                                      next, std::max(e->tune.poly_chunk, 1u), pend.rec,
+                                                                      pend.count);
+            }
         }
         prof_end(e, s, pa, JCDE_PROF_POLY);
         e->launches++;
@@ -1106,7 +1140,9 @@ static jcde_status noalloc_setup(void** out) {
         // every kernel the call can launch
         cudaFuncAttributes fa;
         const void* fns[] = {(const void*)k_mask_chunk, (const void*)k_strength,
-                             (const void*)k_surrogate_warp<uint32_t>, (const void*)k_surrogate_warp<uint64_t>,
+                             (const void*)k_surrogate_warp<uint32_t, 32>, (const void*)k_surrogate_warp<uint64_t, 32>,
+                             (const void*)k_surrogate_warp<uint32_t, 16>, (const void*)k_surrogate_warp<uint64_t, 16>,
+                             (const void*)k_surrogate_warp<uint32_t, 8>, (const void*)k_surrogate_warp<uint64_t, 8>,
                              (const void*)k_surrogate<uint32_t, false>, (const void*)k_surrogate<uint64_t, false>,
                              (const void*)k_poly_tab<uint32_t>, (const void*)k_poly_tab<uint64_t>,
                              (const void*)k_poly<uint32_t, false>, (const void*)k_poly<uint64_t, false>};
@@ -1568,7 +1604,8 @@ static View resident_view(const jcde_resident* r) {
     v.hverts = r->t.hverts;
     v.strength = r->t.strength;
     v.nedges = r->t.nedges;
-    v.cbox = nullptr;   // the resident pools keep no edge-group boxes
+    v.cbox = nullptr;   // the resident pools keep no edge-tile boxes
+    v.eg_shift = 3;
     v.mask = nullptr;
     v.n_slots = r->t.key_cap;
     v.exterior = r->exterior;
@@ -2112,6 +2149,9 @@ jcde_status jcde_get_tuning(const jcde_engine* e, jcde_tuning* out) {
 
 jcde_status jcde_set_tuning(jcde_engine* e, const jcde_tuning* t) {
     if (!e || !t) return JCDE_ERR_ARG;
+    const bool lanes = t->surrogate_lanes == 8 || t->surrogate_lanes == 16 || t->surrogate_lanes == 32;
+    const bool tile = t->edge_tile == 4 || t->edge_tile == 8 || t->edge_tile == 16;
+    if (!lanes || !tile || t->staging_depth > MAX_STAGING_DEPTH) return JCDE_ERR_ARG;
     e->tune = *t;
     return JCDE_OK;
 }
@@ -2142,47 +2182,70 @@ jcde_status jcde_autotune(jcde_engine* e, const jcde_query* d_queries, uint32_t 
         cudaEventDestroy(a);
         return JCDE_ERR_CUDA;
     }
+    bool have_ref = false;
+    // one choice: a warm-up, then the median of three runs from a cold L2; its verdicts must equal
+    // the first choice's (launch choices never change a verdict)
+    auto time_choice = [&](const jcde_tuning& t, double* ms_out) -> jcde_status {
+        e->tune = t;
+        float ms[3] = {0, 0, 0};
+        jcde_status st = JCDE_OK;
+        for (int r = -1; r < 3 && !st; r++) {
+            if (r >= 0) st = tune_flush(d_flush, s);
+            if (!st && r >= 0 && cudaEventRecord(a, s) != cudaSuccess) st = JCDE_ERR_CUDA;
+            if (!st) st = launch_detect(e, 3, d_queries, n, f, d_out.as<uint8_t>(), s, RawShape{nullptr, 0, 0, 0, 0});
+            if (!st && r >= 0 &&
+                (cudaEventRecord(b, s) != cudaSuccess || cudaEventSynchronize(b) != cudaSuccess ||
+                 cudaEventElapsedTime(&ms[r], a, b) != cudaSuccess))
+                st = JCDE_ERR_CUDA;
+        }
+        if (st) return st;
+        std::sort(ms, ms + 3);
+        if (cudaMemcpy(have_ref ? got.data() : ref.data(), d_out.p, n, cudaMemcpyDeviceToHost) != cudaSuccess)
+            return JCDE_ERR_CUDA;
+        if (have_ref && std::memcmp(ref.data(), got.data(), n) != 0) return JCDE_ERR_STATE;
+        have_ref = true;
+        *ms_out = ms[1];
+        return JCDE_OK;
+    };
     jcde_status st = JCDE_OK;
     jcde_tuning best = saved;
     double best_t = 1e300;
-    bool have_ref = false;
     const uint32_t all = 0xFFFFFFFFu;
-    for (int sm = 0; sm < 2 && !st; sm++)            // surrogate pass: warp per query / thread per query
-        for (int pm = 0; pm < 4 && !st; pm++)        // polygon pass: leaf tables / counter grabs of 1, 2, 4
-            for (int om = 0; om < 2 && !st; om++) {  // visit order: Morton / batch order
-                jcde_tuning t;
+    // 1. launch shapes: surrogate pass warp/thread x polygon pass leaf tables / grabs of 1, 2, 4 x order
+    for (int sm = 0; sm < 2 && !st; sm++)
+        for (int pm = 0; pm < 4 && !st; pm++)
+            for (int om = 0; om < 2 && !st; om++) {
+                jcde_tuning t = saved;
                 t.surrogate_warp_max = sm == 0 ? all : 0u;
                 t.leaf_table_max = pm == 0 ? all : 0u;
                 t.poly_chunk = pm == 0 ? 1u : (1u << (pm - 1));
                 t.order_min_batch = om == 0 ? 0u : all;
-                e->tune = t;
-                float ms[3] = {0, 0, 0};
-                for (int r = -1; r < 3 && !st; r++) {
-                    if (r >= 0) st = tune_flush(d_flush, s);
-                    if (!st && r >= 0 && cudaEventRecord(a, s) != cudaSuccess) st = JCDE_ERR_CUDA;
-                    if (!st) st = launch_detect(e, 3, d_queries, n, f, d_out.as<uint8_t>(), s, RawShape{nullptr, 0, 0, 0, 0});
-                    if (!st && r >= 0) {
-                        if (cudaEventRecord(b, s) != cudaSuccess || cudaEventSynchronize(b) != cudaSuccess ||
-                            cudaEventElapsedTime(&ms[r], a, b) != cudaSuccess)
-                            st = JCDE_ERR_CUDA;
-                    }
-                }
-                if (st) break;
-                std::sort(ms, ms + 3);
-                if (cudaMemcpy(have_ref ? got.data() : ref.data(), d_out.p, n, cudaMemcpyDeviceToHost) != cudaSuccess) {
-                    st = JCDE_ERR_CUDA;
-                    break;
-                }
-                if (have_ref && std::memcmp(ref.data(), got.data(), n) != 0) {
-                    st = JCDE_ERR_STATE;   // launch choices must never change a verdict
-                    break;
-                }
-                have_ref = true;
-                if (ms[1] < best_t) {
-                    best_t = ms[1];
+                double ms = 0;
+                if ((st = time_choice(t, &ms))) break;
+                if (ms < best_t) {
+                    best_t = ms;
                     best = t;
                 }
             }
+    // 2-4. with that shape: the edge tile, the staging depth (large-batch polygon kernel only) and the
+    // lanes per query of the warp surrogate pass (when that pass is chosen), one knob at a time
+    auto try_knob = [&](uint32_t jcde_tuning::*field, const uint32_t* values, int count) {
+        for (int k = 0; k < count && !st; k++) {
+            if (best.*field == values[k]) continue;
+            jcde_tuning t = best;
+            t.*field = values[k];
+            double ms = 0;
+            if ((st = time_choice(t, &ms))) return;
+            if (ms < best_t) {
+                best_t = ms;
+                best = t;
+            }
+        }
+    };
+    const uint32_t tiles[3] = {4, 8, 16}, depths[5] = {0, 1, 2, 3, 4}, lanes[3] = {8, 16, 32};
+    if (!st) try_knob(&jcde_tuning::edge_tile, tiles, 3);
+    if (!st && best.leaf_table_max == 0u) try_knob(&jcde_tuning::staging_depth, depths, 5);
+    if (!st && best.surrogate_warp_max == all) try_knob(&jcde_tuning::surrogate_lanes, lanes, 3);
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     // thresholds of the winner, extended to every batch at least this large / at most this small
@@ -2203,7 +2266,7 @@ jcde_status jcde_autotune(jcde_engine* e, const jcde_query* d_queries, uint32_t 
 }  // extern "C"
 
 extern "C" jcde_status jcde_multi_autotune(jcde_multi* m, const jcde_query* dq, const uint32_t* offsets,
-                                           const jcde_filter* filters, uint8_t* d_out, void* stream, uint32_t* out2,
+                                           const jcde_filter* filters, uint8_t* d_out, void* stream, uint32_t* out3,
                                            double* best_ms) {
     if (!m || !offsets || !dq || !d_out) return JCDE_ERR_ARG;
     const uint32_t n = offsets[m->engines.size()];
@@ -2224,10 +2287,24 @@ extern "C" jcde_status jcde_multi_autotune(jcde_multi* m, const jcde_query* dq, 
     double best_t = 1e300;
     uint32_t best_chunk = saved_chunk;
     bool best_ordered = saved_ordered, have_ref = false;
-    for (int om = 0; om < 2 && !st; om++)
-        for (uint32_t chunk = 1; chunk <= 8 && !st; chunk *= 2) {
-            m->ordered = om == 0;
-            m->poly_chunk = chunk;
+    std::vector<uint32_t> saved_tiles;
+    for (jcde_engine* e : m->engines) saved_tiles.push_back(e->tune.edge_tile);
+    uint32_t best_tile = saved_tiles.empty() ? EDGE_TILE_DEFAULT : saved_tiles[0];
+    // grab sizes 1-8 x order on/off with the engines' edge tile; then, with the fastest, edge tiles of
+    // 4, 8 and 16 for every engine
+    for (int om = 0; om < 3 && !st; om++)
+        for (uint32_t chunk = 1; chunk <= (om < 2 ? 8u : 16u) && !st; chunk *= (om < 2 ? 2u : 2u)) {
+            uint32_t tile = 0;
+            if (om < 2) {
+                m->ordered = om == 0;
+                m->poly_chunk = chunk;
+            } else {   // chunk walks 1, 2, 4, 8, 16: the tiles 4, 8 and 16 (1 and 2 are skipped)
+                if (chunk < 4) continue;
+                tile = chunk;
+                m->ordered = best_ordered;
+                m->poly_chunk = best_chunk;
+                for (jcde_engine* e : m->engines) e->tune.edge_tile = tile;
+            }
             float ms[3] = {0, 0, 0};
             for (int r = -1; r < 3 && !st; r++) {
                 if (r >= 0) st = tune_flush(d_flush, s);
@@ -2251,10 +2328,15 @@ extern "C" jcde_status jcde_multi_autotune(jcde_multi* m, const jcde_query* dq, 
             have_ref = true;
             if (ms[1] < best_t) {
                 best_t = ms[1];
-                best_chunk = chunk;
-                best_ordered = om == 0;
+                if (om < 2) {
+                    best_chunk = chunk;
+                    best_ordered = om == 0;
+                } else {
+                    best_tile = tile;
+                }
             }
         }
+    for (size_t k = 0; k < m->engines.size(); k++) m->engines[k]->tune.edge_tile = st ? saved_tiles[k] : best_tile;
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     m->poly_chunk = st ? saved_chunk : best_chunk;
@@ -2263,9 +2345,14 @@ extern "C" jcde_status jcde_multi_autotune(jcde_multi* m, const jcde_query* dq, 
         cudaGraphExecDestroy(m->exec);
         m->exec = nullptr;
     }
-    if (out2) {
-        out2[0] = m->poly_chunk;
-        out2[1] = m->ordered ? 1u : 0u;
+    if (m->exec && !st) {   // a changed edge tile changes the views: recapture next time
+        cudaGraphExecDestroy(m->exec);
+        m->exec = nullptr;
+    }
+    if (out3) {
+        out3[0] = m->poly_chunk;
+        out3[1] = m->ordered ? 1u : 0u;
+        out3[2] = st ? (saved_tiles.empty() ? EDGE_TILE_DEFAULT : saved_tiles[0]) : best_tile;
     }
     if (best_ms) *best_ms = st ? 0.0 : best_t;
     return st;

@@ -55,7 +55,13 @@ struct View {
     const uint8_t* __restrict__ strength;   // strongest unfiltered presence per node
     const uint32_t* __restrict__ mask;      // ignored-key bitmask, nullptr = NoFilter
     const uint32_t* __restrict__ nedges;    // active edges per node (collect)
-    const float4* __restrict__ cbox;        // box of each group of EDGE_GROUP edges (nullptr: not kept)
+    const float4* __restrict__ cbox;        // box of each tile of 1 << eg_shift edges (nullptr: not kept)
+    uint32_t eg_shift = 3;                  // log2 of the edge tile (2, 3 or 4)
+    // nodes [0, n_staged) (the top levels, breadth-first) and their strengths kept in shared memory by
+    // a staging kernel instance (read only where the code is compiled for staging)
+    const DNode* snode = nullptr;
+    const uint8_t* sstr = nullptr;
+    uint32_t n_staged = 0;
     Box cde;
     float coord_max;   // the largest coordinate magnitude of the CDE box (every hazard lies inside it)
     uint32_t n_items, n_slots, cd_threshold;
@@ -100,6 +106,29 @@ __device__ __forceinline__ DNode ld_node(const View& v, int i) {
 __device__ __forceinline__ int4 ld_node_links(const View& v, int i) {
     return __ldg(reinterpret_cast<const int4*>(v.nodes + i) + 1);
 }
+constexpr uint32_t MAX_STAGING_DEPTH = 4;
+// Node, strength and parent of node i: from shared memory when staged (S and i < n_staged).
+template <bool S>
+__device__ __forceinline__ DNode node_at(const View& v, int i) {
+    if constexpr (S) {
+        if (i < (int)v.n_staged) return v.snode[i];
+    }
+    return ld_node(v, i);
+}
+template <bool S>
+__device__ __forceinline__ uint32_t strength_at(const View& v, int i) {
+    if constexpr (S) {
+        if (i < (int)v.n_staged) return v.sstr[i];
+    }
+    return __ldg(&v.strength[i]);
+}
+template <bool S>
+__device__ __forceinline__ int parent_at(const View& v, int i) {
+    if constexpr (S) {
+        if (i < (int)v.n_staged) return v.snode[i].parent;
+    }
+    return __ldg(&v.nodes[i].parent);
+}
 __device__ __forceinline__ DEntry ld_entry(const View& v, uint32_t i) {
     const float4* p = reinterpret_cast<const float4*>(v.entries + i);
     float4 a = __ldg(p);
@@ -141,7 +170,7 @@ struct WalkT {
 };
 
 // Next node of the walk in depth-first order, or -1 when the walk is finished.
-template <typename PendT>
+template <typename PendT, bool S = false>
 __device__ __forceinline__ int walk_next(const View& v, WalkT<PendT>& w) {
     while (w.depth > 0) {
         const int sh = 4 * (w.depth - 1);
@@ -151,7 +180,7 @@ __device__ __forceinline__ int walk_next(const View& v, WalkT<PendT>& w) {
             w.pend &= ~((PendT)1 << (sh + i));
             return w.qb + i;
         }
-        if (--w.depth > 0) w.qb = quartet_base(__ldg(&v.nodes[w.qb].parent));
+        if (--w.depth > 0) w.qb = quartet_base(parent_at<S>(v, w.qb));
     }
     return -1;
 }
@@ -186,13 +215,14 @@ __device__ __forceinline__ bool leaf_hits(const View& v, const P& p, const DNode
                 // rejects every edge of such a group on the boxes' overlap (edge.rs:188-199)
                 const float px0 = fmn(p.s.x, p.e.x), px1 = fmx(p.s.x, p.e.x);
                 const float py0 = fmn(p.s.y, p.e.y), py1 = fmx(p.s.y, p.e.y);
-                for (uint32_t g = 0; g * EDGE_GROUP < e.edge_cnt; g++) {
-                    const float4 c = __ldg(&v.cbox[e.edge_off / EDGE_GROUP + g]);
+                const uint32_t eg = 1u << v.eg_shift;
+                for (uint32_t g = 0; g * eg < e.edge_cnt; g++) {
+                    const float4 c = __ldg(&v.cbox[(e.edge_off >> v.eg_shift) + g]);
                     PSTAT(6, 1);
                     if (fmx(px0, c.x) > fmn(px1, c.z) || fmx(py0, c.y) > fmn(py1, c.w)) continue;
-                    const uint32_t end = min(e.edge_cnt, g * EDGE_GROUP + EDGE_GROUP);
-                    PSTAT(7, end - g * EDGE_GROUP);
-                    for (uint32_t j = g * EDGE_GROUP; j < end; j++)
+                    const uint32_t end = min(e.edge_cnt, g * eg + eg);
+                    PSTAT(7, end - g * eg);
+                    for (uint32_t j = g * eg; j < end; j++)
                         if (p_hits_seg(p, ld_edge(v, e.edge_off + j))) {
                             if (stop) *stop = 1;
                             return true;
@@ -208,12 +238,13 @@ __device__ __forceinline__ bool leaf_hits(const View& v, const P& p, const DNode
                 // CDE box's coordinate magnitude, far above the rounding of the distance test
                 // (circle.rs:506-510 with edge.rs:63-87), so no skipped edge could count as hit
                 const float reach = p.r + v.coord_max * 0x1p-14f;
-                for (uint32_t g = 0; g * EDGE_GROUP < e.edge_cnt; g++) {
-                    const float4 c = __ldg(&v.cbox[e.edge_off / EDGE_GROUP + g]);
+                const uint32_t eg = 1u << v.eg_shift;
+                for (uint32_t g = 0; g * eg < e.edge_cnt; g++) {
+                    const float4 c = __ldg(&v.cbox[(e.edge_off >> v.eg_shift) + g]);
                     if (c.x - p.c.x > reach || p.c.x - c.z > reach || c.y - p.c.y > reach || p.c.y - c.w > reach)
                         continue;
-                    const uint32_t end = min(e.edge_cnt, g * EDGE_GROUP + EDGE_GROUP);
-                    for (uint32_t j = g * EDGE_GROUP; j < end; j++)
+                    const uint32_t end = min(e.edge_cnt, g * eg + eg);
+                    for (uint32_t j = g * eg; j < end; j++)
                         if (p_hits_seg(p, ld_edge(v, e.edge_off + j))) {
                             if (stop) *stop = 1;
                             return true;
@@ -235,15 +266,15 @@ __device__ __forceinline__ bool leaf_hits(const View& v, const P& p, const DNode
 }
 
 // Visit w.node for probe p (qt_node.rs:104-146) and advance the walk.  Returns true on a hit.
-template <class P, typename PendT>
+template <class P, typename PendT, bool S = false>
 __device__ __forceinline__ bool walk_step(const View& v, const P& p, WalkT<PendT>& w, volatile int* stop) {
-    const uint32_t st = __ldg(&v.strength[w.node]);
+    const uint32_t st = strength_at<S>(v, w.node);
     if (st == PRES_ENTIRE) {
         PSTAT(12, 1);
         return true;
     }
     if (st == PRES_PARTIAL) {
-        DNode nd = ld_node(v, w.node);
+        DNode nd = node_at<S>(v, w.node);
         if (nd.child >= 0) {
             PSTAT(3, 1);
             const uint32_t m = p_quad_mask(p, nd.box);
@@ -255,7 +286,7 @@ __device__ __forceinline__ bool walk_step(const View& v, const P& p, WalkT<PendT
     } else {
         PSTAT(12, 1);
     }
-    w.node = walk_next(v, w);
+    w.node = walk_next<PendT, S>(v, w);
     return false;
 }
 
@@ -272,11 +303,12 @@ __device__ __forceinline__ bool seg_group_hits(const View& v, const P& p, const 
         if (JCDE_EDGE_GROUPS && v.cbox) {
             const float px0 = fmn(p.s.x, p.e.x), px1 = fmx(p.s.x, p.e.x);
             const float py0 = fmn(p.s.y, p.e.y), py1 = fmx(p.s.y, p.e.y);
-            for (uint32_t g = 0; g * EDGE_GROUP < e.edge_cnt; g++) {
-                const float4 c = __ldg(&v.cbox[e.edge_off / EDGE_GROUP + g]);
+            const uint32_t eg = 1u << v.eg_shift;
+            for (uint32_t g = 0; g * eg < e.edge_cnt; g++) {
+                const float4 c = __ldg(&v.cbox[(e.edge_off >> v.eg_shift) + g]);
                 if (fmx(px0, c.x) > fmn(px1, c.z) || fmx(py0, c.y) > fmn(py1, c.w)) continue;
-                const uint32_t end = min(e.edge_cnt, g * EDGE_GROUP + EDGE_GROUP);
-                for (uint32_t j = g * EDGE_GROUP; j < end; j++)
+                const uint32_t end = min(e.edge_cnt, g * eg + eg);
+                for (uint32_t j = g * eg; j < end; j++)
                     if (p_hits_seg(p, ld_edge(v, e.edge_off + j))) return true;
             }
             return false;
@@ -285,11 +317,12 @@ __device__ __forceinline__ bool seg_group_hits(const View& v, const P& p, const 
     if constexpr (std::is_same<P, Disk>::value) {
         if (JCDE_EDGE_GROUPS && v.cbox) {   // the margin of leaf_hits
             const float reach = p.r + v.coord_max * 0x1p-14f;
-            for (uint32_t g = 0; g * EDGE_GROUP < e.edge_cnt; g++) {
-                const float4 c = __ldg(&v.cbox[e.edge_off / EDGE_GROUP + g]);
+            const uint32_t eg = 1u << v.eg_shift;
+            for (uint32_t g = 0; g * eg < e.edge_cnt; g++) {
+                const float4 c = __ldg(&v.cbox[(e.edge_off >> v.eg_shift) + g]);
                 if (c.x - p.c.x > reach || p.c.x - c.z > reach || c.y - p.c.y > reach || p.c.y - c.w > reach) continue;
-                const uint32_t end = min(e.edge_cnt, g * EDGE_GROUP + EDGE_GROUP);
-                for (uint32_t j = g * EDGE_GROUP; j < end; j++)
+                const uint32_t end = min(e.edge_cnt, g * eg + eg);
+                for (uint32_t j = g * eg; j < end; j++)
                     if (p_hits_seg(p, ld_edge(v, e.edge_off + j))) return true;
             }
             return false;
@@ -387,10 +420,11 @@ __device__ __forceinline__ int virtual_root(const View& v, const Box& sb) {
 
 // get_virtual_root with the four children of a level tested by lanes 0-3 at once; the first
 // surrounding child in quadrant order is the one `find` takes (cd_engine.rs:318-321).
+template <bool S = false>
 __device__ __forceinline__ int virtual_root_warp(const View& v, const Box& sb, int lane) {
     int n = 0;
     for (;;) {
-        const DNode nd = ld_node(v, n);
+        const DNode nd = node_at<S>(v, n);
         if (nd.child < 0) return n;
         const bool ok = lane < 4 && box_surrounds(box_quadrant(nd.box, lane), sb);
         const uint32_t m = __ballot_sync(FULL, ok);
@@ -872,7 +906,7 @@ __device__ __forceinline__ bool walk_step_tab(const View& v, const P& p, WalkT<P
 #define JCDE_POLY_MIN_BLOCKS 4   // 64 registers: four 256-thread blocks per SM
 #endif
 constexpr uint32_t POLY_MAXV = 256;   // items with more vertices transform edges on the fly
-template <typename PendT, bool TAB>
+template <typename PendT, bool TAB, bool S = false>
 __device__ __forceinline__ void poly_query(const View& v, const uint32_t* __restrict__ qw, uint32_t qi,
                                            uint8_t* __restrict__ out, const RawShape& raw, volatile int* stop,
                                            float2* tv, uint32_t* jobsw, LeafTab* ltab, int lane,
@@ -933,7 +967,7 @@ __device__ __forceinline__ void poly_query(const View& v, const uint32_t* __rest
     };
     // a shape not surrounded by the CDE box collides (cd_engine.rs:161-163)
     bool hit = !box_surrounds(v.cde, sb);
-    const int vr = hit ? 0 : virtual_root_warp(v, sb, lane);
+    const int vr = hit ? 0 : virtual_root_warp<S>(v, sb, lane);
     const uint32_t lt = (1u << lane) - 1u;
     // Every edge's walk starts with a visit of the virtual root.  When the root of the walk is a
     // Partial internal node, that first visit is done here for all edges at once (uniform work,
@@ -943,13 +977,13 @@ __device__ __forceinline__ void poly_query(const View& v, const uint32_t* __rest
     bool listed = false;
     int vr_child = -1;
     if (!hit) {
-        const uint32_t st = __ldg(&v.strength[vr]);
+        const uint32_t st = strength_at<S>(v, vr);
         if (st == PRES_ENTIRE) {
             hit = true;
         } else if (st == PRES_NONE) {
             n_jobs = 0;   // nothing to hit below; containment still runs
         } else {
-            const DNode vn = ld_node(v, vr);
+            const DNode vn = node_at<S>(v, vr);
             if (vn.child >= 0 && cached) {
                 listed = true;
                 vr_child = vn.child;
@@ -989,7 +1023,7 @@ __device__ __forceinline__ void poly_query(const View& v, const uint32_t* __rest
                     const uint32_t job = jobsw[p];
                     e = edge_of(job & 0xFFFFu);
                     w = WalkT<PendT>{-1, 1, vr_child, (PendT)(job >> 16)};
-                    w.node = walk_next(v, w);
+                    w.node = walk_next<PendT, S>(v, w);
                 } else {
                     e = edge_of(p);
                     w = WalkT<PendT>{vr, 0, 0, (PendT)0};
@@ -1014,7 +1048,7 @@ __device__ __forceinline__ void poly_query(const View& v, const uint32_t* __rest
         bool h = false;
         if (active) {
             if constexpr (TAB) h = walk_step_tab(v, e, w, stop, tab);
-            else h = walk_step(v, e, w, stop);
+            else h = walk_step<Seg, PendT, S>(v, e, w, stop);
             if (!h && w.node < 0) w.node = -1;
         }
         hit = __any_sync(FULL, h);
@@ -1026,7 +1060,7 @@ __device__ __forceinline__ void poly_query(const View& v, const uint32_t* __rest
     }
     if (!hit) {
         // containment of the shape in (or of) the partially present hazards of the virtual root
-        DNode vn = ld_node(v, vr);
+        DNode vn = node_at<S>(v, vr);
         for (uint32_t base = 0; !hit && base < vn.hz_cnt; base += 32) {
             const uint32_t k = base + lane;
             int need = 0;
@@ -1068,7 +1102,7 @@ __device__ __forceinline__ void poly_query(const View& v, const uint32_t* __rest
     }
 }
 
-template <typename PendT, bool MULTI>
+template <typename PendT, bool MULTI, bool STAGE = false>
 __global__ void __launch_bounds__(POLY_WARPS * 32, JCDE_POLY_MIN_BLOCKS)
     k_poly(View v, MultiSrc ms, const uint32_t* __restrict__ q, uint32_t n, uint8_t* __restrict__ out,
            RawShape raw, bool only_pending, const uint32_t* __restrict__ order, uint32_t* __restrict__ next,
@@ -1080,6 +1114,20 @@ __global__ void __launch_bounds__(POLY_WARPS * 32, JCDE_POLY_MIN_BLOCKS)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     volatile int* stop = &stops[warp];
     uint32_t* jobsw = jobs[warp];
+    if constexpr (STAGE) {
+        // the top levels of the tree (v.n_staged nodes, breadth-first) and their strengths under
+        // this batch's filter, copied into dynamic shared memory once per block
+        extern __shared__ float4 staged[];
+        DNode* sn = reinterpret_cast<DNode*>(staged);
+        uint8_t* ss = reinterpret_cast<uint8_t*>(sn + v.n_staged);
+        for (uint32_t k = threadIdx.x; k < v.n_staged; k += blockDim.x) {
+            sn[k] = ld_node(v, (int)k);
+            ss[k] = __ldg(&v.strength[k]);
+        }
+        __syncthreads();
+        v.snode = sn;
+        v.sstr = ss;
+    }
     const uint32_t stride = gridDim.x * POLY_WARPS;
     // with a pending list: its records, in the order the surrogate pass wrote them
     if (pend_rec) n = *(volatile const uint32_t*)pend_count;
@@ -1103,7 +1151,7 @@ __global__ void __launch_bounds__(POLY_WARPS * 32, JCDE_POLY_MIN_BLOCKS)
             const uint32_t* r = pend_rec + (size_t)i * PEND_WORDS;
             i++;
             const uint32_t qi = __ldg(&r[0]);
-            poly_query<PendT, false>(v, r + 1, qi, out, raw, stop, tverts[warp], jobsw, nullptr, lane);
+            poly_query<PendT, false, STAGE>(v, r + 1, qi, out, raw, stop, tverts[warp], jobsw, nullptr, lane);
             continue;
         }
         const uint32_t qi = order ? __ldg(&order[i]) : i;
@@ -1113,7 +1161,8 @@ __global__ void __launch_bounds__(POLY_WARPS * 32, JCDE_POLY_MIN_BLOCKS)
             poly_query<PendT, false>(ms.views[ms.layout_of(qi)], q + (size_t)qi * 5, qi, out, raw, stop, tverts[warp],
                                      jobsw, nullptr, lane);
         else
-            poly_query<PendT, false>(v, q + (size_t)qi * 5, qi, out, raw, stop, tverts[warp], jobsw, nullptr, lane);
+            poly_query<PendT, false, STAGE>(v, q + (size_t)qi * 5, qi, out, raw, stop, tverts[warp], jobsw, nullptr,
+                                            lane);
     }
 }
 

@@ -238,7 +238,7 @@ void QuadTree::flatten(FlatTree& out) const {
     out.strength.clear();
     out.entries.clear();
     out.edges.clear();
-    out.cbox.clear();
+    for (auto& c : out.cbox) c.clear();
     // breadth-first so that every quartet of children stays contiguous
     std::vector<int32_t> order{0};
     std::vector<int32_t> newid(nodes_.size(), -1);
@@ -275,7 +275,7 @@ void QuadTree::flatten(FlatTree& out) const {
             e.edge_off = (uint32_t)(out.edges.size() / 4);
             e.edge_cnt = 0;
             if (h.presence == PRES_PARTIAL && keep_edges) {
-                while ((out.edges.size() / 4) % EDGE_GROUP) out.edges.push_back(0.0f);   // lists start on a group
+                while ((out.edges.size() / 4) % EDGE_ALIGN) out.edges.push_back(0.0f);   // lists start on a tile
                 e.edge_off = (uint32_t)(out.edges.size() / 4);
                 for (size_t j = 0; j < h.edges->size(); j++) {
                     const Seg& s = (*h.edges)[j];
@@ -284,10 +284,13 @@ void QuadTree::flatten(FlatTree& out) const {
                     out.edges.push_back(s.e.x);
                     out.edges.push_back(s.e.y);
                     const Box b{fmn(s.s.x, s.e.x), fmn(s.s.y, s.e.y), fmx(s.s.x, s.e.x), fmx(s.s.y, s.e.y)};
-                    const size_t g = (e.edge_off + j) / EDGE_GROUP;
-                    if (out.cbox.size() <= g) out.cbox.resize(g + 1, Box{INFINITY, INFINITY, -INFINITY, -INFINITY});
-                    Box& c = out.cbox[g];
-                    c = Box{fmn(c.x0, b.x0), fmn(c.y0, b.y0), fmx(c.x1, b.x1), fmx(c.y1, b.y1)};
+                    for (int t = 0; t < EDGE_TILES; t++) {
+                        const size_t g = (e.edge_off + j) >> (2 + t);
+                        std::vector<Box>& cb = out.cbox[t];
+                        if (cb.size() <= g) cb.resize(g + 1, Box{INFINITY, INFINITY, -INFINITY, -INFINITY});
+                        Box& c = cb[g];
+                        c = Box{fmn(c.x0, b.x0), fmn(c.y0, b.y0), fmx(c.x1, b.x1), fmx(c.y1, b.y1)};
+                    }
                 }
                 e.edge_cnt = (uint32_t)h.edges->size();
             }

@@ -16,12 +16,12 @@ namespace jcde {
 
 enum Presence : uint32_t { PRES_NONE = 0, PRES_PARTIAL = 1, PRES_ENTIRE = 2 };
 
-// Edge lists of the flattened tree start on a multiple of EDGE_GROUP edges, and every group of
-// EDGE_GROUP consecutive edges of a list has a bounding box (FlatTree::cbox).
-#ifndef JCDE_EDGE_GROUP
-#define JCDE_EDGE_GROUP 8
-#endif
-constexpr uint32_t EDGE_GROUP = JCDE_EDGE_GROUP;
+// Edge tiles: the edge list of every entry starts on a multiple of EDGE_ALIGN edges, and for each
+// tile size 4 << t (t = 0, 1, 2) every tile of consecutive edges of a list has a bounding box
+// (FlatTree::cbox[t]); the query kernels use one of the three (jcde_tuning.edge_tile).
+constexpr uint32_t EDGE_ALIGN = 16;
+constexpr int EDGE_TILES = 3;
+constexpr uint32_t EDGE_TILE_DEFAULT = 8;
 enum Kind : int32_t { KIND_PLACED_ITEM = 0, KIND_EXTERIOR = 1, KIND_HOLE = 2, KIND_QUALITY_ZONE = 3 };
 inline bool kind_is_exterior(int32_t k) { return k == KIND_EXTERIOR; }  // hazard.rs:55-62
 
@@ -90,7 +90,7 @@ struct FlatTree {
     std::vector<uint8_t> strength;  // strongest presence per node with no filter
     std::vector<DEntry> entries;
     std::vector<float> edges;       // 4 floats per edge (x1, y1, x2, y2); every list starts at a group boundary
-    std::vector<Box> cbox;          // bounding box of each group of EDGE_GROUP edges of one list
+    std::vector<Box> cbox[EDGE_TILES];   // bounding box of each tile of 4 << t edges of one list
 };
 
 class QuadTree {

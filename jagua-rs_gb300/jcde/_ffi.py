@@ -41,7 +41,8 @@ class jcde_lbf_params(C.Structure):
 
 class jcde_tuning(C.Structure):
     _fields_ = [("surrogate_warp_max", C.c_uint32), ("leaf_table_max", C.c_uint32), ("poly_chunk", C.c_uint32),
-                ("order_min_batch", C.c_uint32)]
+                ("order_min_batch", C.c_uint32), ("surrogate_lanes", C.c_uint32), ("edge_tile", C.c_uint32),
+                ("staging_depth", C.c_uint32)]
 
 
 class jcde_config(C.Structure):

@@ -359,7 +359,8 @@ class CDEngine:
     def kernel_launches(self) -> int:
         return int(lib().jcde_kernel_launches(self.h))
 
-    TUNING_FIELDS = ("surrogate_warp_max", "leaf_table_max", "poly_chunk", "order_min_batch")
+    TUNING_FIELDS = ("surrogate_warp_max", "leaf_table_max", "poly_chunk", "order_min_batch", "surrogate_lanes",
+                     "edge_tile", "staging_depth")
 
     def get_tuning(self) -> dict:
         t = jcde_tuning()
@@ -534,17 +535,17 @@ class MultiEngine:
         return int(lib().jcde_multi_kernel_launches(self.h))
 
     def autotune(self, queries, offsets, filters=None, stream=None) -> tuple:
-        """jcde_multi_autotune: ({"poly_chunk", "ordered"}, median ms of the choice)."""
+        """jcde_multi_autotune: ({"poly_chunk", "ordered", "edge_tile"}, median ms of the choice)."""
         import torch
 
         offs = np.ascontiguousarray(offsets, dtype=np.uint32)
         out = torch.empty(int(offs[-1]), dtype=torch.uint8, device=queries.device)
         farr, keep = self._filters(filters)
-        o2 = (C.c_uint32 * 2)()
+        o3 = (C.c_uint32 * 3)()
         ms = C.c_double()
         check(lib().jcde_multi_autotune(self.h, queries.data_ptr(), offs.ctypes.data_as(C.POINTER(C.c_uint32)), farr,
-                                        out.data_ptr(), _stream_handle(stream), o2, C.byref(ms)), "multi_autotune")
-        return {"poly_chunk": int(o2[0]), "ordered": bool(o2[1])}, float(ms.value)
+                                        out.data_ptr(), _stream_handle(stream), o3, C.byref(ms)), "multi_autotune")
+        return {"poly_chunk": int(o3[0]), "ordered": bool(o3[1]), "edge_tile": int(o3[2])}, float(ms.value)
 
 
 

@@ -140,3 +140,17 @@ def test_batch_prep_and_generator_arguments(jcde_mod):
                                  bb.ctypes.data_as(f32p), ad.ctypes.data_as(f32p), None, C.c_void_p(st.ctypes.data),
                                  1) == 0
     assert st.tolist() == [0, ARG] and ad[0, 0] == 1.0
+
+
+def test_tuning_values_are_checked(jcde_mod):
+    """jcde_set_tuning rejects edge tiles, lane counts and staging depths outside the allowed sets."""
+    import jcde
+
+    eng = jcde.CDEngine((0.0, 0.0, 100.0, 100.0), (), jcde.CDEConfig())
+    t = eng.get_tuning()
+    assert t["edge_tile"] == 8 and t["surrogate_lanes"] == 32 and t["staging_depth"] == 0
+    for bad in ({"edge_tile": 5}, {"surrogate_lanes": 4}, {"staging_depth": 5}):
+        with pytest.raises(jcde.JcdeError):
+            eng.set_tuning(**bad)
+    eng.set_tuning(edge_tile=16, surrogate_lanes=8, staging_depth=3)
+    assert eng.get_tuning()["edge_tile"] == 16

@@ -193,6 +193,38 @@ def test_autotune_keeps_verdicts(star, oracle_mod):
         geng.set_tuning(**saved)
 
 
+@pytest.mark.parametrize("knob,values", [("edge_tile", (4, 8, 16)), ("staging_depth", (0, 1, 2, 3, 4)),
+                                         ("surrogate_lanes", (8, 16, 32))])
+def test_tuning_knobs_keep_verdicts(star, knob, values):
+    """Every value of the autotuner's knobs (edge tile, tree levels staged in shared memory, lanes
+    per query of the warp surrogate pass) gives the oracle's verdicts, in a small batch (leaf-table
+    polygon pass, warp surrogate pass) and a large one (staged large-batch polygon pass)."""
+    lay, oeng, geng = star
+    saved = geng.get_tuning()
+    try:
+        for n, sid in ((4096, 31), (1 << 18, 32)):
+            q = W.queries_for(lay, n, 0xC1, sid=sid)
+            ref = oeng.detect_batch(q, ignored=lay.filter_keys)
+            for val in values:
+                geng.set_tuning(**{knob: val})
+                got = gpu_detect(geng, q, filter=lay.filter_keys)
+                assert np.array_equal(got, ref), (knob, val, n, int((got != ref).sum()))
+    finally:
+        geng.set_tuning(**saved)
+
+
+def test_autotune_reports_the_three_knobs(star):
+    lay, oeng, geng = star
+    q = W.queries_for(lay, 1 << 17, 0xA8, sid=9)
+    saved = geng.get_tuning()
+    try:
+        t, ms = geng.autotune(torch_queries(q), filter=lay.filter_keys)
+        assert t["edge_tile"] in (4, 8, 16) and t["surrogate_lanes"] in (8, 16, 32) and 0 <= t["staging_depth"] <= 4
+        assert np.array_equal(gpu_detect(geng, q, filter=lay.filter_keys), oeng.detect_batch(q, ignored=lay.filter_keys))
+    finally:
+        geng.set_tuning(**saved)
+
+
 def test_boundary_queries_detect_and_collect(star, oracle_mod):
     lay, oeng, geng = star
     q = W.boundary_queries(lay, 1 << 16, 0xB0)
