@@ -1145,7 +1145,8 @@ static jcde_status noalloc_setup(void** out) {
                              (const void*)k_surrogate_warp<uint32_t, 8>, (const void*)k_surrogate_warp<uint64_t, 8>,
                              (const void*)k_surrogate<uint32_t, false>, (const void*)k_surrogate<uint64_t, false>,
                              (const void*)k_poly_tab<uint32_t>, (const void*)k_poly_tab<uint64_t>,
-                             (const void*)k_poly<uint32_t, false>, (const void*)k_poly<uint64_t, false>};
+                             (const void*)k_poly<uint32_t, false>, (const void*)k_poly<uint64_t, false>,
+                             (const void*)k_poly<uint32_t, false, true>, (const void*)k_poly<uint64_t, false, true>};
         for (const void* fn : fns)
             if (cudaFuncGetAttributes(&fa, fn) != cudaSuccess) return JCDE_ERR_CUDA;
         g_noalloc_addr[dev] = p;
