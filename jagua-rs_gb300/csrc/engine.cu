@@ -442,29 +442,40 @@ static const uint32_t* spatial_order(jcde_engine* e, const uint32_t* q, uint32_t
                                      uint32_t slot_cap) {
     if (!JCDE_SPATIAL_ORDER || n < e->tune.order_min_batch) return nullptr;
     const size_t per_slot = std::max<size_t>(n, slot_cap);
-    if (!e->d_hist.ensure(2 * N_BUCKETS * 4)) return nullptr;
+    if (!e->d_hist.ensure(2 * ORDER_HIST_WORDS * 4)) return nullptr;
     if (e->d_order.cap < 2 * per_slot * 4) {
         // growing the buffer frees the old one, which queued batches may still read
         if (e->have_last_stream && cudaStreamSynchronize(e->last_stream) != cudaSuccess) return nullptr;
         if (!e->d_order.ensure(2 * per_slot * 4)) return nullptr;
     }
-    uint32_t* hist = e->d_hist.as<uint32_t>() + (size_t)slot * N_BUCKETS;
+    uint32_t* hist = e->d_hist.as<uint32_t>() + (size_t)slot * ORDER_HIST_WORDS;
     uint32_t* order = e->d_order.as<uint32_t>() + (size_t)slot * (e->d_order.cap / 8);
     return spatial_order_into(e, q, n, s, hist, order);
 }
 
-// The ordering kernels over caller-owned buffers: hist of N_BUCKETS words, order of n words.
+// The ordering kernels over caller-owned buffers: hist of ORDER_HIST_WORDS words, order of n words.
 static const uint32_t* spatial_order_into(jcde_engine* e, const uint32_t* q, uint32_t n, cudaStream_t s,
                                           uint32_t* hist, uint32_t* order) {
-    if (cudaMemsetAsync(hist, 0, N_BUCKETS * 4, s) != cudaSuccess) return nullptr;
+    if (cudaMemsetAsync(hist, 0, ORDER_HIST_WORDS * 4, s) != cudaSuccess) return nullptr;
     const Box b = e->tree.bbox();
-    const uint32_t grid = std::min<uint32_t>((n + 255) / 256, (uint32_t)e->n_sms * 8);
+    const uint32_t tiles = (uint32_t)((n + (size_t)ORDER_TILE - 1) / ORDER_TILE);
+    const uint32_t grid = std::min<uint32_t>(tiles, (uint32_t)e->n_sms * 2);
+    if (ORDER_SMEM > 48 * 1024) {
+        static bool attr_set = false;
+        if (!attr_set) {
+            if (cudaFuncSetAttribute(k_order_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ORDER_SMEM) !=
+                    cudaSuccess ||
+                cudaFuncSetAttribute(k_order_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ORDER_SMEM) !=
+                    cudaSuccess)
+                return nullptr;
+            attr_set = true;
+        }
+    }
     cudaEvent_t pa = prof_begin(e, s);
-    k_bucket_count<<<grid, 256, 0, s>>>(q, n, b, hist);
-    k_bucket_scan<<<1, 1024, 0, s>>>(hist);
-    k_bucket_scatter<<<grid, 256, 0, s>>>(q, n, b, hist, order);
+    k_order_count<<<grid, ORDER_THREADS, ORDER_SMEM, s>>>(q, n, b, hist);
+    k_order_scatter<<<grid, ORDER_THREADS, ORDER_SMEM, s>>>(q, n, b, hist, order);
     prof_end(e, s, pa, JCDE_PROF_ORDER);
-    e->launches += 3;
+    e->launches += 2;
     return order;
 }
 
@@ -1661,7 +1672,7 @@ extern "C" jcde_status jcde_gen_candidates_segments(uint64_t seed, const uint64_
 
 // The resident's ordering buffers hold a batch of n queries (growing them waits for queued work).
 static jcde_status ensure_order_buffers(jcde_resident* r, uint32_t n) {
-    if (!r->d_hist.ensure(N_BUCKETS * 4)) return JCDE_ERR_CUDA;
+    if (!r->d_hist.ensure(ORDER_HIST_WORDS * 4)) return JCDE_ERR_CUDA;
     if (r->d_order.cap < (size_t)n * 4) {
         if (r->last) CUDA_TRY(cudaStreamSynchronize(r->last));
         if (!r->d_order.ensure((size_t)n * 4)) return JCDE_ERR_CUDA;
@@ -1679,7 +1690,7 @@ static bool resident_detect(jcde_resident* r, const uint32_t* q, uint32_t n, uin
         order = spatial_order_into(e, q, n, s, r->d_hist.as<uint32_t>(), r->d_order.as<uint32_t>());
     const bool chose =
         launch_passes(e, v, q, n, dout, s, RawShape{}, 3, order, r->d_next.as<uint32_t>(), best, n_pending, skip);
-    r->launches += (order ? 3 : 0) + 2;
+    r->launches += (order ? 2 : 0) + 2;
     return chose;
 }
 

@@ -1391,11 +1391,11 @@ constexpr uint32_t BUCKET_BITS = 6;
 constexpr uint32_t BUCKET_GRID = 1u << BUCKET_BITS;
 constexpr uint32_t N_BUCKETS = BUCKET_GRID * BUCKET_GRID;
 
-__device__ __forceinline__ uint32_t spread_bits(uint32_t x) {   // 6 bits -> even positions
-    x &= 0x3Fu;
-    x = (x | (x << 4)) & 0x30Fu;
-    x = (x | (x << 2)) & 0x333u;
-    x = (x | (x << 1)) & 0x555u;
+__device__ __forceinline__ uint32_t spread_bits(uint32_t x) {   // up to 8 bits -> even positions
+    x &= 0xFFu;
+    x = (x | (x << 4)) & 0x0F0Fu;
+    x = (x | (x << 2)) & 0x3333u;
+    x = (x | (x << 1)) & 0x5555u;
     return x;
 }
 __device__ __forceinline__ uint32_t bucket_of(const uint32_t* __restrict__ q, uint32_t qi, const Box& b) {
@@ -1406,40 +1406,121 @@ __device__ __forceinline__ uint32_t bucket_of(const uint32_t* __restrict__ q, ui
     const float fy = fmaxf(0.0f, fminf((ty - b.y0) / (b.y1 - b.y0) * g, g - 1.0f));
     return spread_bits((uint32_t)fx) | (spread_bits((uint32_t)fy) << 1);
 }
-__global__ void k_bucket_count(const uint32_t* __restrict__ q, uint32_t n, Box b, uint32_t* __restrict__ hist) {
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) atomicAdd(&hist[bucket_of(q, i, b)], 1u);
+// The same ordering in two kernels with the histogram in shared memory: one atomic per query to
+// shared memory and one per non-empty cell and block to global memory (global atomics on 4,096
+// counters were most of the three-kernel version's time).  ORDER_BITS bits per axis.
+#ifndef JCDE_ORDER_BITS
+#define JCDE_ORDER_BITS 6
+#endif
+constexpr uint32_t ORDER_BITS = JCDE_ORDER_BITS;
+constexpr uint32_t ORDER_CELLS = 1u << (2 * ORDER_BITS);
+constexpr uint32_t ORDER_HIST_WORDS = ORDER_CELLS + 32;   // the cells' counts, then the blocks-done counter
+constexpr uint32_t ORDER_THREADS = 1024;
+constexpr uint32_t ORDER_PER_THREAD = 8;                  // queries per thread and tile of the scatter
+constexpr uint32_t ORDER_TILE = ORDER_THREADS * ORDER_PER_THREAD;
+constexpr size_t ORDER_SMEM = ORDER_CELLS * 4;             // the block's histogram (dynamic shared memory)
+static_assert(ORDER_BITS <= 7, "the scan takes up to 16 cells per thread");
+
+__device__ __forceinline__ uint32_t order_cell(const uint32_t* __restrict__ q, uint32_t qi, const Box& b) {
+    const float tx = __uint_as_float(__ldg(&q[(size_t)qi * 5 + 3]));
+    const float ty = __uint_as_float(__ldg(&q[(size_t)qi * 5 + 4]));
+    const float g = (float)(1u << ORDER_BITS);
+    const float fx = fmaxf(0.0f, fminf((tx - b.x0) / (b.x1 - b.x0) * g, g - 1.0f));
+    const float fy = fmaxf(0.0f, fminf((ty - b.y0) / (b.y1 - b.y0) * g, g - 1.0f));
+    return spread_bits((uint32_t)fx) | (spread_bits((uint32_t)fy) << 1);
 }
-// exclusive scan of N_BUCKETS counts in place (one block of 1024 threads, 4 counts each)
-__global__ void __launch_bounds__(1024) k_bucket_scan(uint32_t* __restrict__ hist) {
+
+// Counts per cell (hist, zeroed by the caller, ORDER_HIST_WORDS words); the last block to finish
+// turns them into exclusive offsets and clears the blocks-done counter.
+__global__ void __launch_bounds__(ORDER_THREADS) k_order_count(const uint32_t* __restrict__ q, uint32_t n, Box b,
+                                                               uint32_t* __restrict__ hist) {
+    extern __shared__ uint32_t h[];   // ORDER_CELLS
     __shared__ uint32_t warp_sums[32];
-    const uint32_t t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    uint32_t c[4], s = 0;
-    for (int k = 0; k < 4; k++) { c[k] = hist[t * 4 + k]; s += c[k]; }
+    __shared__ bool is_last;
+    const uint32_t t = threadIdx.x;
+    for (uint32_t k = t; k < ORDER_CELLS; k += ORDER_THREADS) h[k] = 0;
+    __syncthreads();
+    for (uint32_t i = blockIdx.x * ORDER_THREADS + t; i < n; i += gridDim.x * ORDER_THREADS)
+        atomicAdd(&h[order_cell(q, i, b)], 1u);
+    __syncthreads();
+    for (uint32_t k = t; k < ORDER_CELLS; k += ORDER_THREADS)
+        if (h[k]) atomicAdd(&hist[k], h[k]);
+    __threadfence();
+    __syncthreads();
+    if (t == 0) is_last = atomicAdd(&hist[ORDER_CELLS], 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+    // exclusive scan of consecutive cells per thread (the counts are read from L2)
+    constexpr uint32_t PER = (ORDER_CELLS + ORDER_THREADS - 1) / ORDER_THREADS;
+    const uint32_t lane = t & 31, warp = t >> 5;
+    uint32_t c[PER], s = 0;
+    JCDE_UNROLL
+    for (uint32_t k = 0; k < PER; k++) {
+        const uint32_t j = t * PER + k;
+        c[k] = j < ORDER_CELLS ? __ldcg(&hist[j]) : 0u;
+        s += c[k];
+    }
     uint32_t incl = s;
+    JCDE_UNROLL
     for (int o = 1; o < 32; o <<= 1) {
-        uint32_t y = __shfl_up_sync(FULL, incl, o);
+        const uint32_t y = __shfl_up_sync(FULL, incl, o);
         if (lane >= (uint32_t)o) incl += y;
     }
     if (lane == 31) warp_sums[warp] = incl;
     __syncthreads();
     if (warp == 0) {
-        uint32_t w = warp_sums[lane], wi = w;
+        const uint32_t w = warp_sums[lane];
+        uint32_t wi = w;
+        JCDE_UNROLL
         for (int o = 1; o < 32; o <<= 1) {
-            uint32_t y = __shfl_up_sync(FULL, wi, o);
+            const uint32_t y = __shfl_up_sync(FULL, wi, o);
             if (lane >= (uint32_t)o) wi += y;
         }
         warp_sums[lane] = wi - w;
     }
     __syncthreads();
     uint32_t run = warp_sums[warp] + incl - s;
-    for (int k = 0; k < 4; k++) { hist[t * 4 + k] = run; run += c[k]; }
+    JCDE_UNROLL
+    for (uint32_t k = 0; k < PER; k++) {
+        const uint32_t j = t * PER + k;
+        if (j < ORDER_CELLS) hist[j] = run;
+        run += c[k];
+    }
+    if (t == 0) hist[ORDER_CELLS] = 0u;
 }
-__global__ void k_bucket_scatter(const uint32_t* __restrict__ q, uint32_t n, Box b, uint32_t* __restrict__ offs,
-                                 uint32_t* __restrict__ order) {
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
-        order[atomicAdd(&offs[bucket_of(q, i, b)], 1u)] = i;
+
+// Places every query at its cell's offset: per tile of ORDER_TILE queries the block ranks them in
+// shared memory, reserves one range per non-empty cell from the global offsets, then writes.
+__global__ void __launch_bounds__(ORDER_THREADS) k_order_scatter(const uint32_t* __restrict__ q, uint32_t n, Box b,
+                                                                 uint32_t* __restrict__ offs,
+                                                                 uint32_t* __restrict__ order) {
+    extern __shared__ uint32_t h[];   // ORDER_CELLS
+    const uint32_t t = threadIdx.x;
+    for (uint32_t tile = blockIdx.x; (size_t)tile * ORDER_TILE < n; tile += gridDim.x) {
+        for (uint32_t k = t; k < ORDER_CELLS; k += ORDER_THREADS) h[k] = 0;
+        __syncthreads();
+        const uint32_t i0 = tile * ORDER_TILE + t;
+        uint32_t cell[ORDER_PER_THREAD], rank[ORDER_PER_THREAD];
+        JCDE_UNROLL
+        for (uint32_t j = 0; j < ORDER_PER_THREAD; j++) {
+            const uint32_t i = i0 + j * ORDER_THREADS;
+            cell[j] = i < n ? order_cell(q, i, b) : 0u;
+            rank[j] = i < n ? atomicAdd(&h[cell[j]], 1u) : 0u;
+        }
+        __syncthreads();
+        for (uint32_t k = t; k < ORDER_CELLS; k += ORDER_THREADS) {
+            const uint32_t c = h[k];
+            if (c) h[k] = atomicAdd(&offs[k], c);
+        }
+        __syncthreads();
+        JCDE_UNROLL
+        for (uint32_t j = 0; j < ORDER_PER_THREAD; j++) {
+            const uint32_t i = i0 + j * ORDER_THREADS;
+            if (i < n) order[h[cell[j]] + rank[j]] = i;
+        }
+        __syncthreads();
+    }
 }
 
 // Several layouts in one batch: the bucket key is (layout, Morton cell of the layout's CDE box).
