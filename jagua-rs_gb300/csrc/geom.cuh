@@ -140,7 +140,15 @@ JCDE_UNROLL
     return !(all_pos || all_neg);
 }
 
-// edge.rs:180-228 (location not requested) — e1 is the querying edge, e2 the hazard edge
+// edge.rs:180-228 (location not requested) — e1 is the querying edge, e2 the hazard edge.
+// The reference divides (t = t_nom / t_den, u = u_nom / t_den) and tests 0 <= t, u <= 1.  With
+// the denominator's sign moved into the numerators (a / d with d = |t_den| > 0, negation is exact),
+// the rounded quotient is decided by comparisons in most cases:
+//   * RN(a / d) <= 1 exactly when a <= d: a float above d is at least d's successor, and the
+//     quotient of the two exceeds 1 + 2^-24, the midpoint that rounds to 1 (true for every d > 0);
+//   * RN(a / d) >= 0 exactly when a >= 0, unless a < 0 is so small against d that the quotient
+//     rounds to -0; with a <= -2^-60 and d <= 2^60 the quotient is at most -2^-120, so it cannot.
+// Outside those ranges (and for NaN or infinite terms) the divisions are done as the reference does.
 JHD bool seg_hits_seg(const Seg& e1, const Seg& e2) {
     float x1 = e1.s.x, y1 = e1.s.y, x2 = e1.e.x, y2 = e1.e.y;
     float x3 = e2.s.x, y3 = e2.s.y, x4 = e2.e.x, y4 = e2.e.y;
@@ -149,10 +157,28 @@ JHD bool seg_hits_seg(const Seg& e1, const Seg& e2) {
     float t_nom = (x2 - x4) * (y4 - y3) - (y2 - y4) * (x4 - x3);
     float t_den = (x2 - x1) * (y4 - y3) - (y2 - y1) * (x4 - x3);
     float u_nom = (x2 - x4) * (y2 - y1) - (y2 - y4) * (x2 - x1);
-    float u_den = t_den;  // edge.rs:210 is the same expression as edge.rs:208
-    if (t_den == 0.0f || u_den == 0.0f) return false;
+    // u's denominator (edge.rs:210) is the same expression as t's (edge.rs:208)
+    if (t_den == 0.0f) return false;
+    const bool neg = t_den < 0.0f;
+    const float a = neg ? -t_nom : t_nom, b = neg ? -u_nom : u_nom, d = neg ? -t_den : t_den;
+    if (d <= 0x1p60f && (a >= 0.0f || a <= -0x1p-60f) && (b >= 0.0f || b <= -0x1p-60f))
+        return a >= 0.0f && a <= d && b >= 0.0f && b <= d;
     float t = t_nom / t_den;
-    float u = u_nom / u_den;
+    float u = u_nom / t_den;
+    return 0.0f <= t && t <= 1.0f && 0.0f <= u && u <= 1.0f;
+}
+// The same test with the reference's two divisions always done (kept for the equivalence test).
+JHD bool seg_hits_seg_div(const Seg& e1, const Seg& e2) {
+    float x1 = e1.s.x, y1 = e1.s.y, x2 = e1.e.x, y2 = e1.e.y;
+    float x3 = e2.s.x, y3 = e2.s.y, x4 = e2.e.x, y4 = e2.e.y;
+    if (fmx(fmn(x1, x2), fmn(x3, x4)) > fmn(fmx(x1, x2), fmx(x3, x4))) return false;
+    if (fmx(fmn(y1, y2), fmn(y3, y4)) > fmn(fmx(y1, y2), fmx(y3, y4))) return false;
+    float t_nom = (x2 - x4) * (y4 - y3) - (y2 - y4) * (x4 - x3);
+    float t_den = (x2 - x1) * (y4 - y3) - (y2 - y1) * (x4 - x3);
+    float u_nom = (x2 - x4) * (y2 - y1) - (y2 - y4) * (x2 - x1);
+    if (t_den == 0.0f) return false;
+    float t = t_nom / t_den;
+    float u = u_nom / t_den;
     return 0.0f <= t && t <= 1.0f && 0.0f <= u && u <= 1.0f;
 }
 

@@ -1,0 +1,94 @@
+"""The division-free form of the edge crossing test (geom.cuh `seg_hits_seg`) against the
+reference's form with its two divisions (edge.rs:180-228, kept as `seg_hits_seg_div`), on tens of
+millions of segment pairs: random coordinates over many magnitudes, shared and nearly shared end
+points (quotients of exactly 0 and 1, and their neighbours), integer grids (exact collinear and
+touching cases), tiny and huge coordinates (the fallback ranges) and random bit patterns (NaN,
+infinities, subnormals).  The header is compiled for the host here, with the flags of the library's
+host code; the device compiles the same source with IEEE division and no contraction, so both
+round every operation alike.
+"""
+import os
+import shutil
+import subprocess
+
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(os.path.dirname(HERE), "jagua-rs_gb300", "csrc")
+
+PROGRAM = r"""
+#include <cstdio>
+#include <cstdint>
+#include <cstring>
+#include <cmath>
+#include "geom.cuh"
+using namespace jcde;
+static uint64_t s = 0x9E3779B97F4A7C15ull;
+static inline uint64_t nx() { s ^= s << 13; s ^= s >> 7; s ^= s << 17; return s; }
+static inline float unif(float lo, float hi) { return lo + (hi - lo) * (float)((nx() >> 40) * 0x1p-24); }
+static inline float bits() { uint32_t u = (uint32_t)nx(); float f; std::memcpy(&f, &u, 4); return f; }
+static inline float nudge(float f, int k) {   // k ulps up (k > 0) or down
+    for (; k > 0; k--) f = std::nextafter(f, INFINITY);
+    for (; k < 0; k++) f = std::nextafter(f, -INFINITY);
+    return f;
+}
+static long long n_pairs = 0, n_bad = 0, n_hits = 0;
+static void check(const Seg& a, const Seg& b) {
+    const bool x = seg_hits_seg(a, b), y = seg_hits_seg_div(a, b);
+    n_pairs++;
+    n_hits += y;
+    if (x != y && n_bad++ < 5)
+        std::printf("mismatch %a %a %a %a | %a %a %a %a: %d vs %d\n", a.s.x, a.s.y, a.e.x, a.e.y, b.s.x, b.s.y,
+                    b.e.x, b.e.y, (int)x, (int)y);
+}
+int main(int argc, char** argv) {
+    const long long N = argc > 1 ? atoll(argv[1]) : 4000000;
+    const float mags[] = {1e-30f, 1e-6f, 1e-3f, 1.0f, 100.0f, 2000.0f, 1e5f, 1e9f, 1e18f, 1e30f};
+    for (long long i = 0; i < N; i++) {
+        const float m = mags[nx() % 10];
+        Seg a{{unif(-m, m), unif(-m, m)}, {unif(-m, m), unif(-m, m)}};
+        Seg b{{unif(-m, m), unif(-m, m)}, {unif(-m, m), unif(-m, m)}};
+        check(a, b);
+        // b through an end point of a, or a point of a, nudged by a few ulps
+        const int k = (int)(nx() % 7) - 3;
+        Pt p = (nx() & 1) ? a.s : a.e;
+        if (nx() % 3 == 0) {
+            const float t = unif(0.0f, 1.0f);
+            p = Pt{a.s.x + t * (a.e.x - a.s.x), a.s.y + t * (a.e.y - a.s.y)};
+        }
+        Seg c{{nudge(p.x, k), nudge(p.y, (int)(nx() % 7) - 3)}, {unif(-m, m), unif(-m, m)}};
+        check(a, c);
+        check(c, a);
+        Seg c2{b.s, {nudge(p.x, -k), p.y}};
+        check(a, c2);
+        // shared end points, either orientation
+        check(a, Seg{a.e, b.e});
+        check(a, Seg{b.s, a.s});
+        // integer grid (exact ties, collinear overlaps)
+        Seg g{{(float)(nx() % 9), (float)(nx() % 9)}, {(float)(nx() % 9), (float)(nx() % 9)}};
+        Seg h{{(float)(nx() % 9), (float)(nx() % 9)}, {(float)(nx() % 9), (float)(nx() % 9)}};
+        check(g, h);
+        // raw bit patterns (NaN, infinities, subnormals)
+        if ((i & 7) == 0) {
+            check(Seg{{bits(), bits()}, {bits(), bits()}}, Seg{{bits(), bits()}, {bits(), bits()}});
+            Seg d{{bits(), bits()}, {bits(), bits()}};
+            check(d, Seg{d.e, {bits(), bits()}});
+        }
+    }
+    std::printf("pairs %lld hits %lld mismatches %lld\n", n_pairs, n_hits, n_bad);
+    return n_bad ? 1 : 0;
+}
+"""
+
+
+@pytest.mark.skipif(shutil.which("g++") is None, reason="needs g++")
+def test_division_free_edge_crossing_equals_reference_form(tmp_path):
+    src = tmp_path / "seg.cpp"
+    src.write_text(PROGRAM)
+    exe = tmp_path / "seg"
+    subprocess.run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fno-fast-math", "-I", CSRC, str(src), "-o",
+                    str(exe)], check=True)
+    r = subprocess.run([str(exe), "3000000"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    pairs, hits = int(r.stdout.split()[1]), int(r.stdout.split()[3])
+    assert pairs > 2e7 and hits > 1e6, r.stdout
