@@ -37,7 +37,7 @@ namespace {
 #define JCDE_COLLECT_DYNAMIC 1
 #endif
 #ifndef JCDE_HOST_CHUNKS
-#define JCDE_HOST_CHUNKS 2   // pipelined chunks of a large host batch (jcde_detect_batch_host)
+#define JCDE_HOST_CHUNKS 1   // pipelined chunks of a large host batch (jcde_detect_batch_host)
 #endif
 #ifndef JCDE_ORDER_MIN_BATCH
 #define JCDE_ORDER_MIN_BATCH 4096u
@@ -117,7 +117,7 @@ struct jcde_engine {
     cudaStream_t own[2] = {nullptr, nullptr};
     cudaEvent_t ev_ready = nullptr;   // the host entry point's filter is ready (orders the second stream)
     int n_sms = 0;
-    int detect_blocks_per_sm = 0, collect_blocks_per_sm = 0, tab_blocks_per_sm = 0;
+    int detect_blocks_per_sm = 0, collect_blocks_per_sm = 0, tab_blocks_per_sm = 0, surr_blocks_per_sm = 0;
     // launch choices of the detect passes (jcde_set_tuning / jcde_autotune)
     jcde_tuning tune{JCDE_SURR_WARP_MAX, JCDE_SURR_WARP_MAX, (uint32_t)JCDE_POLY_CHUNK, JCDE_ORDER_MIN_BATCH,
                      (uint32_t)JCDE_SURR_GROUP, EDGE_TILE_DEFAULT, 0u};
@@ -415,6 +415,11 @@ static void init_launch_shape(jcde_engine* e) {
     else
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&e->detect_blocks_per_sm, k_poly<uint64_t, false>, POLY_WARPS * 32, 0);
     if (e->detect_blocks_per_sm < 1) e->detect_blocks_per_sm = 1;
+    if (e->cfg.quadtree_depth <= 8)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&e->surr_blocks_per_sm, k_surrogate<uint32_t, false>, SURR_THREADS, 0);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&e->surr_blocks_per_sm, k_surrogate<uint64_t, false>, SURR_THREADS, 0);
+    if (e->surr_blocks_per_sm < 1) e->surr_blocks_per_sm = 1;
     // the small-batch polygon pass's leaf tables (dynamic shared memory) take its total above 48 KB
     const int tab_smem = (int)(POLY_WARPS * sizeof(LeafTab));
     cudaFuncSetAttribute(k_poly_tab<uint32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, tab_smem);
@@ -508,10 +513,8 @@ static bool launch_passes_t(jcde_engine* e, const View& v, const uint32_t* q, ui
             else k_surrogate_warp<PendT, 32><<<grid, SURR_THREADS, 0, s>>>(v, q, n, dout, miss, order, n_pending);
         } else if (JCDE_SURR_DYNAMIC && next && cudaMemsetAsync(next, 0, 4, s) == cudaSuccess) {
             // persistent blocks; each warp takes the next 32 queries from a counter as it finishes
-            int per_sm = 0;
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_surrogate<PendT, false>, SURR_THREADS, 0);
             const uint32_t grid = std::min<uint32_t>((n + SURR_THREADS - 1) / SURR_THREADS,
-                                                     (uint32_t)e->n_sms * (uint32_t)std::max(per_sm, 1));
+                                                     (uint32_t)e->n_sms * (uint32_t)e->surr_blocks_per_sm);
             k_surrogate<PendT, false><<<grid, SURR_THREADS, 0, s>>>(v, MultiSrc{}, q, n, dout, miss, order, next,
                                                                     n_pending, pend);
         } else {
@@ -816,6 +819,22 @@ jcde_status jcde_detect_batch_host(jcde_engine* e, const jcde_query* hq, uint32_
     for (auto& s : e->own)
         if (!s) CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
     if (!e->d_q.ensure((size_t)n * sizeof(jcde_query)) || !e->d_out.ensure(n)) return JCDE_ERR_CUDA;
+    const uint32_t n_chunks = n >= (1u << 18) ? (uint32_t)JCDE_HOST_CHUNKS : 1u;
+    if (n_chunks == 1) {
+        // The whole batch in one stream.  The copy is queued first, so that the engine's device image
+        // and the filter are resolved on the host while it runs.  (On GB300 the copy of a 1M batch
+        // takes ~4% of its kernels' time; splitting the batch into chunks whose copies overlap the
+        // other chunk's kernels costs more in per-batch kernel overhead than it hides.)
+        cudaStream_t s = e->own[0];
+        CUDA_TRY(cudaMemcpyAsync(e->d_q.p, hq, (size_t)n * sizeof(jcde_query), cudaMemcpyHostToDevice, s));
+        jcde_status st = launch_detect(e, 3, e->d_q.as<jcde_query>(), n, f, e->d_out.as<uint8_t>(), s,
+                                       RawShape{nullptr, 0, 0, 0, 0});
+        if (!st) st = cudaMemcpyAsync(hout, e->d_out.p, n, cudaMemcpyDeviceToHost, s) == cudaSuccess ? JCDE_OK
+                                                                                                 : JCDE_ERR_CUDA;
+        const bool synced = cudaStreamSynchronize(s) == cudaSuccess;
+        e->have_last_stream = false;
+        return st ? st : (synced ? JCDE_OK : JCDE_ERR_CUDA);
+    }
     jcde_status st = sync_device(e);
     if (st) return st;
     // resolve the filter once, on the first stream, before the pipelined chunks (the second stream
@@ -826,7 +845,6 @@ jcde_status jcde_detect_batch_host(jcde_engine* e, const jcde_query* hq, uint32_
     CUDA_TRY(cudaEventRecord(e->ev_ready, e->own[0]));
     CUDA_TRY(cudaStreamWaitEvent(e->own[1], e->ev_ready, 0));
     // chunks alternate between two streams so that copies overlap the other chunk's kernels
-    const uint32_t n_chunks = n >= (1u << 18) ? (uint32_t)JCDE_HOST_CHUNKS : 1u;
     const uint32_t chunk = (n + n_chunks - 1) / n_chunks;
     jcde_query* dq = e->d_q.as<jcde_query>();
     uint8_t* dout = e->d_out.as<uint8_t>();
