@@ -209,19 +209,40 @@ def cpu_baseline(lay, queries, n_sample: int, repeats: int = 3):
             "sample": f"first {n_sample} queries of the batch, best of {repeats}"}, work, verdicts
 
 
+# committed ncu summaries per kernel and figure, in order of preference: the instruction count from
+# the reduced-batch capture of the current build (it scales with the batch: the same query
+# generator, the same undecided fraction), memory figures from the full-size capture (cache hit
+# rates depend on the batch size, so those are taken at the size they describe)
+PROFILE_FILES = {"k_poly": {"inst": ("k_poly_star_262k.txt", "k_poly_star_1m.txt"),
+                            "l2_sectors": ("k_poly_star_1m.txt", "k_poly_star_262k.txt"),
+                            "dram": ("k_poly_star_1m.txt",)}}
+
+
 def read_profile(kernel: str) -> dict:
-    """Figures of `kernel` on this workload from its committed ncu summary (profiles/), per launch:
-    DRAM bytes, executed warp instructions, L2 sectors."""
-    path = os.path.join(REPO, "profiles", f"{kernel}_star_1m.txt")
+    """Figures of `kernel` on this workload from its committed ncu summaries (profiles/), per launch of
+    a batch of N_QUERIES: DRAM bytes, executed warp instructions, L2 sectors, and the file each came from."""
     keys = {"dram_bytes_per_launch": "dram", "smsp__inst_executed.sum": "inst", "lts__t_sectors.sum": "l2_sectors"}
+    default = (f"{kernel}_star_1m.txt",)
+    files = PROFILE_FILES.get(kernel, {})
     out = {}
-    try:
-        for line in open(path):
-            for k, name in keys.items():
-                if line.startswith(k):
-                    out[name] = float(line.split("=")[1])
-    except (OSError, ValueError):
-        pass
+    for name in keys.values():
+        for fn in files.get(name, default):
+            val, queries = None, float(1 << 20)
+            try:
+                for line in open(os.path.join(REPO, "profiles", fn)):
+                    if line.startswith("queries_per_launch"):
+                        queries = float(line.split("=")[1])
+                    for k, nm in keys.items():
+                        if nm == name and line.startswith(k):
+                            val = float(line.split("=")[1])
+            except (OSError, ValueError):
+                continue
+            if val is None:
+                continue
+            out[name] = val * N_QUERIES / queries
+            out[name + "_source"] = f"profiles/{fn}" + ("" if queries == N_QUERIES
+                                                         else f" scaled by {N_QUERIES}/{int(queries)} queries")
+            break
     return out
 
 
@@ -440,12 +461,12 @@ def run_gpu(args):
     if prof.get("inst"):
         issue = {"inst_per_launch": prof["inst"], "issue_slots_per_launch": n_sms * 4 * sm_hz * avg_s,
                  "frac": prof["inst"] / (n_sms * 4 * sm_hz * avg_s), "sms": n_sms, "sm_mhz": sm_hz / 1e6,
-                 "inst_source": f"profiles/{dom}_star_1m.txt (ncu smsp__inst_executed.sum, one launch)"}
+                 "inst_source": prof["inst_source"] + " (ncu smsp__inst_executed.sum, one launch)"}
     l2 = None
     if l2_peak and prof.get("l2_sectors"):
         l2_gbs = prof["l2_sectors"] * 32 / avg_s / 1e9
         l2 = {"achieved": l2_gbs, "peak": l2_peak, "unit": "GB/s", "frac": l2_gbs / l2_peak,
-              "bytes_per_launch": prof["l2_sectors"] * 32,
+              "bytes_per_launch": prof["l2_sectors"] * 32, "sectors_source": prof["l2_sectors_source"],
               "peak_source": "jcde_l2_read_peak: best of 3 runs x 16/32/48 MB L2-resident buffers, 20 passes of "
                              "16-byte ld.global.cg"}
     sub = {}
