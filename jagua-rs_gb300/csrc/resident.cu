@@ -49,6 +49,10 @@ __device__ __forceinline__ void r_fail(RState& s, uint32_t code) {
     if (!s.error) s.error = code;
 }
 
+__device__ __forceinline__ RTask* r_task(const RTree& t, uint32_t i) {
+    return (t.stasks && i < RT_SMEM_TASKS) ? &t.stasks[i] : &t.tasks[i];
+}
+
 __device__ __forceinline__ bool r_push(const RTree& t, RState& s, uint32_t& top, int32_t node, uint32_t kind,
                                        const DEntry& e, int lane) {
     if (top >= t.task_cap) {
@@ -56,7 +60,7 @@ __device__ __forceinline__ bool r_push(const RTree& t, RState& s, uint32_t& top,
         return false;
     }
     if (lane == 0) {
-        RTask* k = &t.tasks[top];
+        RTask* k = r_task(t, top);
         k->node = node;
         k->kind = kind;
         k->e = e;
@@ -318,7 +322,7 @@ __device__ void r_constrict(const RTree& t, RState& s, uint32_t& top, int32_t n,
 __device__ void r_run_register(const RTree& t, RState& s, uint32_t top, int lane) {
     while (top > 0 && !s.error) {
         __syncwarp();
-        const RTask tk = t.tasks[--top];
+        const RTask tk = *r_task(t, --top);
         __syncwarp();
         const int32_t n = tk.node;
         if (tk.kind == RT_CONSTRICT) {
@@ -415,7 +419,7 @@ __device__ bool r_remove(const RTree& t, RState& s, uint32_t key, int lane) {
     const uint32_t lt_all = FULL;
     while (top > 0 && !s.error) {
         __syncwarp();
-        const RTask tk = t.tasks[--top];
+        const RTask tk = *r_task(t, --top);
         __syncwarp();
         const int32_t n = tk.node;
         if (tk.kind == RT_FREE) {   // free a quartet and, below it, every descendant quartet
@@ -488,9 +492,12 @@ __device__ bool r_remove(const RTree& t, RState& s, uint32_t key, int lane) {
 // ---------------------------------------------------------------------------------------------
 
 // Copy of a host tree: the root node, then every live hazard registered under its own key.
-__global__ void __launch_bounds__(32) k_res_init(RTree t, const float2* __restrict__ verts, const uint4* __restrict__ recs,
+__global__ void __launch_bounds__(32) k_res_init(RTree tg, const float2* __restrict__ verts, const uint4* __restrict__ recs,
                                                  const float2* __restrict__ pois, uint32_t n, uint32_t n_slots,
                                                  const uint32_t* __restrict__ kfree, uint32_t n_kfree) {
+    __shared__ RTask stasks[RT_SMEM_TASKS];
+    RTree t = tg;
+    t.stasks = stasks;
     const int lane = threadIdx.x;
     RState s{};
     s.n_nodes = 1;
@@ -536,9 +543,12 @@ __device__ uint32_t r_insert_item(const RTree& t, RState& s, const DItem* items,
     return r_insert(t, s, iverts + it.v_off, it.v_cnt, true, q.c, q.s, q.tx, q.ty, poi, false, -1, lane);
 }
 
-__global__ void __launch_bounds__(32) k_res_insert_placed(RTree t, const DItem* __restrict__ items,
+__global__ void __launch_bounds__(32) k_res_insert_placed(RTree tg, const DItem* __restrict__ items,
                                                           const float2* __restrict__ iverts, uint32_t n_items,
                                                           const uint32_t* __restrict__ q, uint32_t* __restrict__ out_key) {
+    __shared__ RTask stasks[RT_SMEM_TASKS];
+    RTree t = tg;
+    t.stasks = stasks;
     const int lane = threadIdx.x;
     RState s = r_load(t.ctl);
     uint32_t key = ~0u;
@@ -555,7 +565,10 @@ __global__ void __launch_bounds__(32) k_res_insert_placed(RTree t, const DItem* 
     }
 }
 
-__global__ void __launch_bounds__(32) k_res_remove(RTree t, const uint32_t* __restrict__ key) {
+__global__ void __launch_bounds__(32) k_res_remove(RTree tg, const uint32_t* __restrict__ key) {
+    __shared__ RTask stasks[RT_SMEM_TASKS];
+    RTree t = tg;
+    t.stasks = stasks;
     const int lane = threadIdx.x;
     RState s = r_load(t.ctl);
     if (!s.error) r_remove(t, s, *key, lane);
@@ -806,11 +819,14 @@ __global__ void k_lbf_merge(LbfDev* __restrict__ st, const uint32_t* __restrict_
 
 // End of a step: log it, register the chosen candidate, and every `remove_every` steps remove the
 // placed item at a random position of the placement list (Layout::remove_item, layout.rs:88-100).
-__global__ void __launch_bounds__(32) k_lbf_commit(RTree t, const DItem* __restrict__ items,
+__global__ void __launch_bounds__(32) k_lbf_commit(RTree tg, const DItem* __restrict__ items,
                                                    const float2* __restrict__ iverts, uint32_t n_items, LbfParams p,
                                                    LbfDev* __restrict__ st, const uint32_t* __restrict__ q,
                                                    const double* __restrict__ qu, uint32_t round,
                                                    const uint8_t* __restrict__ verdicts, LbfLogs logs) {
+    __shared__ RTask stasks[RT_SMEM_TASKS];
+    RTree t = tg;
+    t.stasks = stasks;
     const int lane = threadIdx.x;
     volatile LbfDev* vs = st;
     const uint32_t step = vs->step;

@@ -62,6 +62,10 @@ struct RTask {
     DEntry e;
 };
 
+// The task stack's bottom entries live in the update kernel's shared memory (a warp pops a task right
+// after pushing it, so a global-memory stack put a round trip through L2 on every task).
+constexpr uint32_t RT_SMEM_TASKS = 512;
+
 struct RTree {
     DNode* nodes;
     uint32_t* ncap;      // entry slab capacity per node
@@ -76,6 +80,7 @@ struct RTree {
     int32_t* qfree;
     uint32_t* kfree;
     RTask* tasks;
+    RTask* stasks;   // in a kernel: the bottom RT_SMEM_TASKS entries of the stack, in shared memory
     RCtl* ctl;
     uint32_t node_cap, entry_cap, edge_cap, hvert_cap, key_cap, task_cap;
     Box cde;
