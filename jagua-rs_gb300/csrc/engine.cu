@@ -1250,6 +1250,7 @@ struct jcde_multi {
     std::vector<uint32_t> up_offs;
     DevBuf d_views, d_offs, d_hist, d_order;
     DevBuf d_next;                    // work counters of the two passes
+    DevBuf d_pend, d_pendc;           // the surrogate pass's list of undecided queries, its length
     bool wide = false;                // a tree deeper than 8 levels needs 64-bit walk masks
     int surr_blocks = 1;
     uint32_t poly_chunk = JCDE_POLY_CHUNK > 0 ? JCDE_POLY_CHUNK : 1;   // launch choices (jcde_multi_autotune)
@@ -1289,9 +1290,12 @@ static jcde_status multi_prepare(jcde_multi* m, const uint32_t* offsets, const j
         if (!m->d_views.ensure(L * sizeof(View)) || !m->d_offs.ensure((L + 1) * 4)) return JCDE_ERR_CUDA;
         m->up_views.clear();
     }
-    if (m->d_hist.cap < (size_t)L * N_BUCKETS * 4 || m->d_order.cap < std::max<size_t>(total, 1) * 4) {
+    const size_t pend_bytes = std::max<size_t>(total, 1) * PEND_WORDS * 4;
+    if (m->d_hist.cap < (size_t)L * N_BUCKETS * 4 || m->d_order.cap < std::max<size_t>(total, 1) * 4 ||
+        m->d_pend.cap < pend_bytes || !m->d_pendc.p) {
         CUDA_TRY(cudaStreamSynchronize(s));   // growing frees buffers that queued launches may read
-        if (!m->d_hist.ensure((size_t)L * N_BUCKETS * 4) || !m->d_order.ensure(std::max<size_t>(total, 1) * 4))
+        if (!m->d_hist.ensure((size_t)L * N_BUCKETS * 4) || !m->d_order.ensure(std::max<size_t>(total, 1) * 4) ||
+            !m->d_pend.ensure(pend_bytes) || !m->d_pendc.ensure(4))
             return JCDE_ERR_CUDA;
         m->up_views.clear();
     }
@@ -1330,14 +1334,17 @@ static void multi_launch_t(jcde_multi* m, const uint32_t* q, uint8_t* out, cudaS
         k_mbucket_scatter<<<grid, 256, 0, s>>>(q, n, ms, hist, order);
         m->launches += 3;
     }
-    // both passes take their queries from counters (see launch_passes_t)
+    // both passes take their queries from counters (see launch_passes_t); the polygon pass reads the
+    // surrogate pass's list of undecided queries
     uint32_t* next = m->d_next.as<uint32_t>();
+    const PendList pend{m->d_pend.as<uint32_t>(), m->d_pendc.as<uint32_t>()};
     cudaMemsetAsync(next, 0, 2 * 4, s);
+    cudaMemsetAsync(pend.count, 0, 4, s);
     const uint32_t sgrid = std::min<uint32_t>((n + SURR_THREADS - 1) / SURR_THREADS, (uint32_t)(m->n_sms * m->surr_blocks));
-    k_surrogate<PendT, true><<<sgrid, SURR_THREADS, 0, s>>>(View{}, ms, q, n, out, PENDING, order, next);
+    k_surrogate<PendT, true><<<sgrid, SURR_THREADS, 0, s>>>(View{}, ms, q, n, out, PENDING, order, next, nullptr, pend);
     const uint32_t pgrid = std::min<uint32_t>((n + POLY_WARPS - 1) / POLY_WARPS, (uint32_t)(m->n_sms * m->poly_blocks));
     k_poly<PendT, true><<<pgrid, POLY_WARPS * 32, 0, s>>>(View{}, ms, q, n, out, RawShape{nullptr, 0, 0, 0, 0}, true,
-                                                          order, next + 1, m->poly_chunk);
+                                                          order, next + 1, m->poly_chunk, pend.rec, pend.count);
     m->launches += 2;
 }
 static void multi_launch(jcde_multi* m, const uint32_t* q, uint8_t* out, cudaStream_t s) {

@@ -1151,7 +1151,11 @@ __global__ void __launch_bounds__(POLY_WARPS * 32, JCDE_POLY_MIN_BLOCKS)
             const uint32_t* r = pend_rec + (size_t)i * PEND_WORDS;
             i++;
             const uint32_t qi = __ldg(&r[0]);
-            poly_query<PendT, false, STAGE>(v, r + 1, qi, out, raw, stop, tverts[warp], jobsw, nullptr, lane);
+            if constexpr (MULTI)
+                poly_query<PendT, false>(ms.views[ms.layout_of(qi)], r + 1, qi, out, raw, stop, tverts[warp], jobsw,
+                                         nullptr, lane);
+            else
+                poly_query<PendT, false, STAGE>(v, r + 1, qi, out, raw, stop, tverts[warp], jobsw, nullptr, lane);
             continue;
         }
         const uint32_t qi = order ? __ldg(&order[i]) : i;
