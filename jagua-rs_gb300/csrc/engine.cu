@@ -823,7 +823,7 @@ jcde_status jcde_detect_batch_host(jcde_engine* e, const jcde_query* hq, uint32_
     if (n_chunks == 1) {
         // The whole batch in one stream.  The copy is queued first, so that the engine's device image
         // and the filter are resolved on the host while it runs.  (On GB300 the copy of a 1M batch
-        // takes ~4% of its kernels' time; splitting the batch into chunks whose copies overlap the
+        // takes ~8% of its kernels' time; splitting the batch into chunks whose copies overlap the
         // other chunk's kernels costs more in per-batch kernel overhead than it hides.)
         cudaStream_t s = e->own[0];
         CUDA_TRY(cudaMemcpyAsync(e->d_q.p, hq, (size_t)n * sizeof(jcde_query), cudaMemcpyHostToDevice, s));
