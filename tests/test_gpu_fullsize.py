@@ -153,3 +153,18 @@ def test_proxy_gradient_every_configs4_candidate(star_gpu):
     assert np.abs(g32[~on]).max(initial=0.0) <= 1e-6
     rel_v = np.abs(v32 - v64) / np.maximum(v64, 1e-30)
     assert rel_v[v64 > 0].max() <= 1e-5, rel_v.max()
+
+
+@pytest.mark.parametrize("n", [(1 << 18) + 7, 1 << 20])
+def test_host_entry_point_equals_device_path_and_oracle(star_gpu, n):
+    """jcde_detect_batch_host (host buffers: copy in, the passes, copy out) at the benchmark's size
+    gives the device path's verdicts, with and without a filter, and the oracle's on samples."""
+    from helpers import gpu_detect
+
+    lay, geng, oeng = star_gpu
+    q = W.queries_for(lay, n, 0xC1, sid=91)
+    for filt in (None, lay.filter_keys):
+        host = geng.detect_batch(q, filter=filt)
+        assert np.array_equal(host, gpu_detect(geng, q, filter=filt)), filt
+        assert np.array_equal(host[:8192], oeng.detect_batch(q[:8192], ignored=filt)), filt
+        assert np.array_equal(host[-4096:], oeng.detect_batch(q[-4096:], ignored=filt)), filt
