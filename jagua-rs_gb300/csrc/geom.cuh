@@ -239,6 +239,30 @@ JCDE_UNROLL
     }
     return hit;
 }
+// The same mask, first for an edge that lies strictly on one side of both bisectors: its extent
+// then misses the other three quadrants' extents (their overlap tests compare a bound beyond the
+// bisector with one short of it), so only quadrant i can be set, by the very tests the full form
+// makes for it; an edge whose quadrant is then still undetermined (it overlaps the quadrant with
+// neither end point inside) takes the full form.  A NaN coordinate fails the strict comparisons,
+// so such an edge takes the full form too.  (Faster in the collect walks, where every lane walks its
+// own edge to the end; slower in the polygon pass's lockstep walk, which keeps the full form.)
+JHD uint32_t seg_quadrant_mask_short(const Seg& e, const Box& r) {
+    const float ex0 = fmn(e.s.x, e.e.x), ex1 = fmx(e.s.x, e.e.x);
+    const float ey0 = fmn(e.s.y, e.e.y), ey1 = fmx(e.s.y, e.e.y);
+    const Pt c = box_mid(r);
+    const bool lft = ex1 < c.x, rgt = ex0 > c.x, bot = ey1 < c.y, top = ey0 > c.y;
+    if ((lft || rgt) && (bot || top)) {
+        const int i = rgt ? (top ? 0 : 3) : (top ? 1 : 2);
+        const float qx0 = rgt ? c.x : r.x0, qx1 = rgt ? r.x1 : c.x;
+        const float qy0 = top ? c.y : r.y0, qy1 = top ? r.y1 : c.y;
+        const bool ov = !(fmx(ex0, qx0) > fmn(ex1, qx1)) && !(fmx(ey0, qy0) > fmn(ey1, qy1));
+        if (!ov) return 0u;
+        const bool in_s = e.s.x >= qx0 && e.s.x <= qx1 && e.s.y >= qy0 && e.s.y <= qy1;
+        const bool in_e = e.e.x >= qx0 && e.e.x <= qx1 && e.e.y >= qy0 && e.e.y <= qy1;
+        if (in_s || in_e) return 1u << i;
+    }
+    return seg_quadrant_mask(e, r);
+}
 
 // edge.rs:63-87 + edge.rs:152-159 — squared distance from p to the segment
 JHD float seg_sq_dist(const Seg& e, Pt p) {

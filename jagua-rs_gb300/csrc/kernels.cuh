@@ -153,6 +153,9 @@ __device__ __forceinline__ bool p_hits_seg(const Disk& d, const Seg& e) { return
 __device__ __forceinline__ bool p_hits_seg(const Seg& s, const Seg& e) { return seg_hits_seg(s, e); }
 __device__ __forceinline__ uint32_t p_quad_mask(const Disk& d, const Box& b) { return disk_quadrant_mask(d, b); }
 __device__ __forceinline__ uint32_t p_quad_mask(const Seg& s, const Box& b) { return seg_quadrant_mask(s, b); }
+// The collect walks' form (each lane walks its probe to the end): the one-quadrant shortcut for edges.
+__device__ __forceinline__ uint32_t p_quad_mask_walk(const Disk& d, const Box& b) { return disk_quadrant_mask(d, b); }
+__device__ __forceinline__ uint32_t p_quad_mask_walk(const Seg& s, const Box& b) { return seg_quadrant_mask_short(s, b); }
 
 // Breadth-first flattening stores the children of every node as one quartet, and quartets fill
 // indices 1, 5, 9, ... in order, so the quartet holding node i >= 1 starts at quartet_base(i).
@@ -340,7 +343,7 @@ __device__ void collect_walk_w(const View& v, const P& p, WalkT<PendT>& w, uint3
         DNode nd = ld_node(v, w.node);
         const bool now = __ldg(&v.nedges[w.node]) <= v.cd_threshold;
         if (nd.child >= 0 && !now) {
-            const uint32_t m = p_quad_mask(p, nd.box);
+            const uint32_t m = p_quad_mask_walk(p, nd.box);
             if (m) walk_push(w, m, nd.child);
         } else {
             for (uint32_t k = 0; k < nd.hz_cnt; k++) {

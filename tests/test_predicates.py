@@ -1,9 +1,11 @@
 """The division-free form of the edge crossing test (geom.cuh `seg_hits_seg`) against the
-reference's form with its two divisions (edge.rs:180-228, kept as `seg_hits_seg_div`), on tens of
-millions of segment pairs: random coordinates over many magnitudes, shared and nearly shared end
-points (quotients of exactly 0 and 1, and their neighbours), integer grids (exact collinear and
-touching cases), tiny and huge coordinates (the fallback ranges) and random bit patterns (NaN,
-infinities, subnormals).  The header is compiled for the host here, with the flags of the library's
+reference's form with its two divisions (edge.rs:180-228, kept as `seg_hits_seg_div`), and the
+quadrant mask's one-quadrant shortcut (`seg_quadrant_mask_short`) against its full form
+(qt_traits.rs:19-106, `seg_quadrant_mask`), on tens of millions of cases: random coordinates
+over many magnitudes, shared and nearly shared end points (quotients of exactly 0 and 1, and their
+neighbours), integer grids (exact collinear and touching cases), tiny and huge coordinates (the
+fallback ranges), random bit patterns (NaN, infinities, subnormals), and for the mask node boxes of
+many scales and of zero width with edges on, one ulp off and across the bisectors.  The header is compiled for the host here, with the flags of the library's
 host code; the device compiles the same source with IEEE division and no contraction, so both
 round every operation alike.
 """
@@ -75,8 +77,38 @@ int main(int argc, char** argv) {
             check(d, Seg{d.e, {bits(), bits()}});
         }
     }
-    std::printf("pairs %lld hits %lld mismatches %lld\n", n_pairs, n_hits, n_bad);
-    return n_bad ? 1 : 0;
+    // the quadrant mask's one-quadrant shortcut against its full form: node boxes of many scales and
+    // of zero width, edges inside, across and beyond them, on and one ulp off the bisectors, NaN
+    long long n_masks = 0, n_mask_bad = 0, n_short = 0;
+    for (long long i = 0; i < N; i++) {
+        const float m = mags[nx() % 10];
+        const float x0 = unif(-m, m), y0 = unif(-m, m);
+        const float w = (nx() % 16 == 0) ? 0.0f : unif(0.0f, m), h = (nx() % 16 == 0) ? 0.0f : unif(0.0f, m);
+        const Box r{x0, y0, x0 + w, y0 + h};
+        const Pt c = box_mid(r);
+        for (int k = 0; k < 6; k++) {
+            auto coord = [&](float lo, float hi, float mid) {
+                switch (nx() % 6) {
+                    case 0: return nudge(mid, (int)(nx() % 5) - 2);
+                    case 1: return nudge(nx() & 1 ? lo : hi, (int)(nx() % 5) - 2);
+                    case 2: return unif(lo - (hi - lo), hi + (hi - lo));
+                    case 3: return (nx() % 64 == 0) ? NAN : unif(lo, hi);
+                    default: return unif(lo, hi);
+                }
+            };
+            Seg e{{coord(r.x0, r.x1, c.x), coord(r.y0, r.y1, c.y)}, {coord(r.x0, r.x1, c.x), coord(r.y0, r.y1, c.y)}};
+            if (k == 5) e.e = Pt{nudge(e.s.x, (int)(nx() % 3) - 1), nudge(e.s.y, (int)(nx() % 3) - 1)};
+            const uint32_t a = seg_quadrant_mask_short(e, r), b = seg_quadrant_mask(e, r);
+            n_masks++;
+            n_short += (a != 0 && (a & (a - 1)) == 0);
+            if (a != b && n_mask_bad++ < 5)
+                std::printf("mask mismatch %a %a %a %a | %a %a %a %a: %u vs %u\n", e.s.x, e.s.y, e.e.x, e.e.y, r.x0,
+                            r.y0, r.x1, r.y1, a, b);
+        }
+    }
+    std::printf("pairs %lld hits %lld mismatches %lld masks %lld single %lld mask_mismatches %lld\n", n_pairs, n_hits,
+                n_bad, n_masks, n_short, n_mask_bad);
+    return (n_bad || n_mask_bad) ? 1 : 0;
 }
 """
 
@@ -90,5 +122,7 @@ def test_division_free_edge_crossing_equals_reference_form(tmp_path):
                     str(exe)], check=True)
     r = subprocess.run([str(exe), "3000000"], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
-    pairs, hits = int(r.stdout.split()[1]), int(r.stdout.split()[3])
+    tok = r.stdout.split()
+    pairs, hits, masks, single = int(tok[1]), int(tok[3]), int(tok[7]), int(tok[9])
     assert pairs > 2e7 and hits > 1e6, r.stdout
+    assert masks > 1e7 and single > 1e6, r.stdout
