@@ -279,8 +279,38 @@ JHD float seg_sq_dist(const Seg& e, Pt p) {
     float dx = p.x - xx, dy = p.y - yy;
     return dx * dx + dy * dy;
 }
+// The same squared distance with the end-point cases decided without the division: for a finite
+// len_sq > 0, RN(dot / len_sq) > 1 exactly when dot > len_sq (a float above len_sq is at least its
+// successor, whose quotient exceeds the midpoint 1 + 2^-24), and dot < 0 gives a negative quotient
+// or -0, whose projection x1 + (-0) c is x1 again (c finite), so both pick the first end point.
+// The division stays for the projection itself and for a non-finite len_sq.
+JHD float seg_sq_dist_ep(const Seg& e, Pt p) {
+    float x1 = e.s.x, y1 = e.s.y, x2 = e.e.x, y2 = e.e.y;
+    float a = p.x - x1, b = p.y - y1, c = x2 - x1, d = y2 - y1;
+    float dot = a * c + b * d;
+    float len_sq = c * c + d * d;
+    float xx, yy;
+    const bool fin = len_sq <= 3.40282347e+38f;
+    if (len_sq == 0.0f || (fin && dot < 0.0f)) {
+        xx = x1;
+        yy = y1;
+    } else if (fin && dot > len_sq) {
+        xx = x2;
+        yy = y2;
+    } else {
+        float param = -1.0f;
+        if (len_sq != 0.0f) param = dot / len_sq;
+        if (param < 0.0f) { xx = x1; yy = y1; }
+        else if (param > 1.0f) { xx = x2; yy = y2; }
+        else { xx = x1 + param * c; yy = y1 + param * d; }
+    }
+    float dx = p.x - xx, dy = p.y - yy;
+    return dx * dx + dy * dy;
+}
 // circle.rs:506-510
-JHD bool disk_hits_seg(const Disk& c, const Seg& e) { return seg_sq_dist(e, c.c) <= c.r * c.r; }
+JHD bool disk_hits_seg(const Disk& c, const Seg& e) { return seg_sq_dist_ep(e, c.c) <= c.r * c.r; }
+// ... with the reference's division always done (the lane-group surrogate pass, the equivalence test)
+JHD bool disk_hits_seg_div(const Disk& c, const Seg& e) { return seg_sq_dist(e, c.c) <= c.r * c.r; }
 // circle.rs:512-525
 JHD bool disk_hits_box(const Disk& c, const Box& r) {
     float nx = fmx(r.x0, fmn(c.c.x, r.x1));

@@ -151,6 +151,10 @@ __device__ __forceinline__ bool p_hits_box(const Disk& d, const Box& b) { return
 __device__ __forceinline__ bool p_hits_box(const Seg& s, const Box& b) { return box_hits_seg(b, s); }
 __device__ __forceinline__ bool p_hits_seg(const Disk& d, const Seg& e) { return disk_hits_seg(d, e); }
 __device__ __forceinline__ bool p_hits_seg(const Seg& s, const Seg& e) { return seg_hits_seg(s, e); }
+// The lane groups of the small-batch surrogate pass keep the pole-edge test with its division: its
+// end-point branches cost the groups' lockstep leaf loops more than the division they save.
+__device__ __forceinline__ bool p_hits_seg_group(const Disk& d, const Seg& e) { return disk_hits_seg_div(d, e); }
+__device__ __forceinline__ bool p_hits_seg_group(const Seg& s, const Seg& e) { return seg_hits_seg(s, e); }
 __device__ __forceinline__ uint32_t p_quad_mask(const Disk& d, const Box& b) { return disk_quadrant_mask(d, b); }
 __device__ __forceinline__ uint32_t p_quad_mask(const Seg& s, const Box& b) { return seg_quadrant_mask(s, b); }
 // The collect walks' form (each lane walks its probe to the end): the one-quadrant shortcut for edges.
@@ -666,7 +670,7 @@ __device__ __forceinline__ bool leaf_hits_group(const View& v, const P& p, const
             const uint32_t cnt = __shfl_sync(g.mask, ec, (int)g.base + src);
             for (uint32_t jb = 0; jb < cnt; jb += G) {
                 const uint32_t j = jb + g.lig;
-                if (__any_sync(g.mask, j < cnt && p_hits_seg(p, ld_edge(v, off + j)))) return true;
+                if (__any_sync(g.mask, j < cnt && p_hits_seg_group(p, ld_edge(v, off + j)))) return true;
             }
         }
     }

@@ -5,7 +5,9 @@ quadrant mask's one-quadrant shortcut (`seg_quadrant_mask_short`) against its fu
 over many magnitudes, shared and nearly shared end points (quotients of exactly 0 and 1, and their
 neighbours), integer grids (exact collinear and touching cases), tiny and huge coordinates (the
 fallback ranges), random bit patterns (NaN, infinities, subnormals), and for the mask node boxes of
-many scales and of zero width with edges on, one ulp off and across the bisectors.  The header is compiled for the host here, with the flags of the library's
+many scales and of zero width with edges on, one ulp off and across the bisectors; and the pole-edge
+distance with its end-point branches decided without the division (`seg_sq_dist_ep`) against the
+reference form (`seg_sq_dist`, edge.rs:63-87), bit for bit.  The header is compiled for the host here, with the flags of the library's
 host code; the device compiles the same source with IEEE division and no contraction, so both
 round every operation alike.
 """
@@ -106,9 +108,40 @@ int main(int argc, char** argv) {
                             r.y0, r.x1, r.y1, a, b);
         }
     }
-    std::printf("pairs %lld hits %lld mismatches %lld masks %lld single %lld mask_mismatches %lld\n", n_pairs, n_hits,
-                n_bad, n_masks, n_short, n_mask_bad);
-    return (n_bad || n_mask_bad) ? 1 : 0;
+    // the pole-edge test with its end-point cases decided without the division, against the reference
+    // form: the squared distances must be the same bits, and so the verdicts
+    long long n_disks = 0, n_disk_bad = 0;
+    for (long long i = 0; i < N; i++) {
+        const float m = mags[nx() % 10];
+        Seg e{{unif(-m, m), unif(-m, m)}, {unif(-m, m), unif(-m, m)}};
+        if (nx() % 8 == 0) e.e = e.s;                                              // zero length
+        if (nx() % 8 == 0) e.e = Pt{nudge(e.s.x, (int)(nx() % 3) - 1), e.s.y};   // nearly zero
+        Pt p{unif(-m, m), unif(-m, m)};
+        switch (nx() % 5) {
+            case 0: p = Pt{nudge(e.s.x, (int)(nx() % 5) - 2), nudge(e.s.y, (int)(nx() % 5) - 2)}; break;
+            case 1: p = Pt{nudge(e.e.x, (int)(nx() % 5) - 2), nudge(e.e.y, (int)(nx() % 5) - 2)}; break;
+            case 2: {   // on the perpendicular through an end point (dot ~ 0 or ~ len_sq)
+                const Pt q = nx() & 1 ? e.s : e.e;
+                const float t = unif(-1.0f, 1.0f);
+                p = Pt{q.x - t * (e.e.y - e.s.y), q.y + t * (e.e.x - e.s.x)};
+                break;
+            }
+            default: break;
+        }
+        if ((i & 15) == 0) { e = Seg{{bits(), bits()}, {bits(), bits()}}; p = Pt{bits(), bits()}; }
+        const Disk dk{p, unif(0.0f, m)};
+        const float a = seg_sq_dist_ep(e, p), b = seg_sq_dist(e, p);
+        uint32_t ua, ub;
+        std::memcpy(&ua, &a, 4);
+        std::memcpy(&ub, &b, 4);
+        n_disks++;
+        if ((ua != ub && !(a != a && b != b)) || disk_hits_seg(dk, e) != disk_hits_seg_div(dk, e))
+            if (n_disk_bad++ < 5)
+                std::printf("disk mismatch %a %a %a %a | %a %a: %a vs %a\n", e.s.x, e.s.y, e.e.x, e.e.y, p.x, p.y, a, b);
+    }
+    std::printf("pairs %lld hits %lld mismatches %lld masks %lld single %lld mask_mismatches %lld disks %lld "
+                "disk_mismatches %lld\n", n_pairs, n_hits, n_bad, n_masks, n_short, n_mask_bad, n_disks, n_disk_bad);
+    return (n_bad || n_mask_bad || n_disk_bad) ? 1 : 0;
 }
 """
 
@@ -126,3 +159,4 @@ def test_division_free_edge_crossing_equals_reference_form(tmp_path):
     pairs, hits, masks, single = int(tok[1]), int(tok[3]), int(tok[7]), int(tok[9])
     assert pairs > 2e7 and hits > 1e6, r.stdout
     assert masks > 1e7 and single > 1e6, r.stdout
+    assert int(tok[13]) >= 3e6 and int(tok[15]) == 0, r.stdout
