@@ -345,7 +345,7 @@ def run_gpu(args):
     torch.cuda.synchronize()
     clk = ClockSampler(local)
     clk.__enter__()   # sampled through the device loop, its profiled twin and the e2e loop
-    profiler_range(True)
+    profiler_range(args.profile_range == "detect")
     t0 = time.perf_counter()
     for i in range(args.steps):
         flush.zero_()
@@ -354,7 +354,8 @@ def run_gpu(args):
         ev[i][1].record(stream)
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
-    profiler_range(False)
+    if args.profile_range == "detect":
+        profiler_range(False)
     launches = eng.kernel_launches() - launches0
     step_ms = [a.elapsed_time(b) for a, b in ev]
     # per-kernel event times of the same steps (a second, profiled run of the timed loop)
@@ -401,6 +402,8 @@ def run_gpu(args):
     for _ in range(args.warmup):
         collect_once()
     c_ms = []
+    if args.profile_range == "collect":
+        profiler_range(True)
     for i in range(args.steps):
         flush.zero_()
         a_ev, b_ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -409,6 +412,8 @@ def run_gpu(args):
         b_ev.record(stream)
         c_ms.append((a_ev, b_ev))
     torch.cuda.synchronize()
+    if args.profile_range == "collect":
+        profiler_range(False)
     collect_s = sum(a.elapsed_time(b) for a, b in c_ms) / 1e3
     collect_total = int(c_tot.item())
     clk.__exit__(None, None, None)
@@ -1149,6 +1154,8 @@ def main():
     ap.add_argument("--subrecords", type=int, default=1,
                     help="1: the default (star) line also measures the batched multi-layout, proxy and LBF workloads")
     ap.add_argument("--prep-shapes", type=int, default=1024, help="prep workload: shapes per batch")
+    ap.add_argument("--profile-range", default="detect", choices=["detect", "collect"],
+                    help="star workload: the timed loop bracketed by cudaProfilerStart/Stop (for ncu captures)")
     ap.add_argument("--queries", type=int, default=1 << 20,
                     help="star workload: queries per step (smaller batches serve profiling captures)")
     ap.add_argument("--workload", default="star", choices=["star", "multi", "proxy", "lbf", "prep", "bpp"],
