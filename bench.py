@@ -16,9 +16,8 @@ detect_surrogate_collision || detect_poly_collision (lbf/benches/ci_bench.rs:107
   roofline.l2 / roofline.issue — the dominant kernel against the project-measured L2 read peak
             (jcde_l2_read_peak) and against its instruction-issue slots (ncu instruction count);
   batched / proxy / lbf — the metric's other workloads in the same run (N=1): 64 layouts in one
-            launch sequence vs per-layout launches (configs[2]), grads/s and CDE-verified
-            placements/s of the pole-overlap proxy (configs[4]), and the device-resident LBF build
-            (configs[3]), each with its oracle check.
+            launch sequence vs per-layout launches, grads/s and CDE-verified placements/s of the
+            pole-overlap proxy, and the device-resident LBF build, each with its oracle check.
 
 `--impl reference` times the CPU restatement of the reference on the host cores instead (the
 reference itself is Rust and cannot be built here).
@@ -517,7 +516,7 @@ def run_gpu(args):
 
 
 def measure_multi(steps: int, warmup: int, autotune: bool = True, parity_queries: int = 1024):
-    """configs[2]: 64 independent bin layouts, log-uniform 4,096-262,144 queries each, answered by one
+    """The batched workload: 64 independent bin layouts, log-uniform 4,096-262,144 queries each, answered by one
     launch sequence (CUDA graph) versus 64 per-layout jcde_detect_batch calls.  Returns the record;
     the first `parity_queries` queries of every layout are checked against the oracle."""
     import torch
@@ -613,7 +612,7 @@ MULTI_WORKLOAD = ("64 star-container bins (32-128 v), 20-400 items each from 40 
 
 
 def measure_proxy(steps: int, warmup: int, lay=None, grad_check: int = 1 << 16):
-    """configs[4], the gradient-separation workload: the star layout with surrogate poles on every
+    """The gradient-separation workload: the star layout with surrogate poles on every
     interior hazard; 1,048,576 colliding candidates.  Measures (a) grads/s: the pole-overlap proxy and
     its adjoint d/d(theta, tx, ty) for every candidate (jcde_proxy_batch), (b) verified collision-free
     placements/s: 20 descent steps on the proxy then the exact verdict, versus 20 random
@@ -975,7 +974,7 @@ def run_bpp(args):
 
 
 def measure_lbf(steps: int, warmup: int, oracle_check: bool = True, extras: bool = False, cpu_steps: int = 0):
-    """configs[3], the LBF-style strip build on the device-resident engine.  2000 steps, each: 16384
+    """The LBF-style strip build on the device-resident engine.  2000 steps, each: 16384
     candidates generated and searched as lbf's search does (surrogate pass for all; the polygon pass
     for those that could still beat the best free one, search.rs:52-56), the least-cost free one
     registered on the device, and a random placed item deregistered every 50 steps.  A timed step is

@@ -1,7 +1,8 @@
 // ORACLE — TEST INFRASTRUCTURE ONLY.
 //
 // A plain C++ restatement of jagua-rs's f32 collision detection engine (crate jagua-rs 0.6.4),
-// used by the test-suite, by smoke() and by the CPU-baseline leg of bench.py as the checker.
+// used by the test-suite, by smoke() and by the CPU-baseline leg of bench.py as the reference the
+// product's results are compared with.
 // Nothing in the product library links, loads or calls this file.
 //
 // PARITY UNPINNED: the reference is Rust, no Rust toolchain exists where this is built, and the

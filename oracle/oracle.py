@@ -2,7 +2,7 @@
 
 The oracle (``cde_oracle.cpp``) is a C++ restatement of the reference's f32 collision detection
 engine.  Only the test-suite, ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py``
-load it, as the checker.  Parity of the oracle itself is UNPINNED (the reference is Rust and
+load it, as the reference the product's results are compared with.  Parity of the oracle itself is UNPINNED (the reference is Rust and
 cannot be built here, and it ships no golden vectors); see the header of ``cde_oracle.cpp``.
 
 The classes mirror the duck-typed backend interface of ``jcde.workload`` so that the same seeded

@@ -23,7 +23,7 @@ def _cuda(q):
 
 @pytest.fixture(scope="module")
 def star_gpu(jcde_mod, oracle_mod):
-    """The configs[1] layout (300 items of 8-200 vertices, holes, zones), with a GPU and an oracle engine."""
+    """The star benchmark layout (300 items of 8-200 vertices, holes, zones), with a GPU and an oracle engine."""
     from helpers import gpu_engine
 
     lay, _ = W.star_container_layout(jcde.GpuBackend)
@@ -31,7 +31,7 @@ def star_gpu(jcde_mod, oracle_mod):
 
 
 def test_multi_64_layouts_every_layout_vs_oracle(jcde_mod, oracle_mod):
-    """configs[2]: the 64 default layouts (20-400 items of 8-200 vertices, 32-128-vertex containers,
+    """The batched workload: the 64 default layouts (20-400 items of 8-200 vertices, 32-128-vertex containers,
     4,096-262,144 queries each) in one batched launch sequence with graph replay: every verdict equals
     the per-layout launch's, and the first 4,096 queries of every layout equal the oracle's."""
     import torch
@@ -58,7 +58,7 @@ def test_multi_64_layouts_every_layout_vs_oracle(jcde_mod, oracle_mod):
 
 
 def test_collect_full_configs1_batch(star_gpu):
-    """configs[1] in collect mode: all 1,048,576 queries with the zone filter; every count and every
+    """The star benchmark batch in collect mode: all 1,048,576 queries with the zone filter; every count and every
     sorted key list equals the oracle's."""
     lay, geng, oeng = star_gpu
     q = W.queries_for(lay, 1 << 20, 0xC1)
@@ -112,7 +112,7 @@ def test_big_items_collect_and_touch(big_items):
 
 
 def _proxy_candidates(eng, lay, n_target, filt):
-    """configs[4]'s candidate pool: uniform placements that collide (exact verdict) and overlap
+    """The gradient-separation workload's candidate pool: uniform placements that collide (exact verdict) and overlap
     some hazard pole."""
     import torch
 
@@ -132,7 +132,7 @@ def _proxy_candidates(eng, lay, n_target, filt):
 
 
 def test_proxy_gradient_every_configs4_candidate(star_gpu):
-    """configs[4]: 1,048,576 colliding candidates on the configs[1] layout; the proxy and its
+    """The gradient-separation workload: 1,048,576 colliding candidates on the star layout; the proxy and its
     gradient d/d(theta, tx, ty) from the GPU against an FP64 evaluation of the same float32 inputs:
     every candidate's gradient within 1e-4 relative (norm-wise), every value within 1e-5."""
     lay, geng, _ = star_gpu

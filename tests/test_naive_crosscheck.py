@@ -99,7 +99,7 @@ def star_nc(star_layout):
 
 
 def test_strip_uniform_queries(strip_layout, strip_nc):
-    """configs[0] (65,536 uniform queries, NoFilter): verdicts and collected sets agree exactly."""
+    """The strip workload (65,536 uniform queries, NoFilter): verdicts and collected sets agree exactly."""
     lay, oeng = strip_layout
     q = W.queries_for(lay, 65536, 0xC0)
     assert compare_verdicts(strip_nc, q, oeng.detect_batch(q)) == []
@@ -108,7 +108,7 @@ def test_strip_uniform_queries(strip_layout, strip_nc):
 
 
 def test_star_uniform_sample(star_layout, star_nc):
-    """configs[1] layout with its zone filter: a 16,384-query sample agrees exactly."""
+    """The star benchmark layout with its zone filter: a 16,384-query sample agrees exactly."""
     lay, oeng = star_layout
     q = W.queries_for(lay, 16384, 0xC1, sid=21)
     assert compare_verdicts(star_nc, q, oeng.detect_batch(q, ignored=lay.filter_keys), lay.filter_keys) == []
@@ -168,16 +168,16 @@ def _three_way(geng, oeng, nc, q, ign, collect_n):
 
 
 @pytest.mark.gpu
-def test_gpu_three_way_configs0(strip_layout, strip_nc, gpu_engines):
-    """configs[0]: all 65,536 queries, the oracle, the GPU and the naive checker agree."""
+def test_gpu_three_way_strip(strip_layout, strip_nc, gpu_engines):
+    """The strip workload: all 65,536 queries, the oracle, the GPU and the naive checker agree."""
     lay, oeng = strip_layout
     bad, corners = _three_way(gpu_engines[0], oeng, strip_nc, W.queries_for(lay, 65536, 0xC0), None, 65536)
     assert bad == [] and corners == []
 
 
 @pytest.mark.gpu
-def test_gpu_three_way_configs1_sample(star_layout, star_nc, gpu_engines):
-    """configs[1]: a 65,536-query sample of the benchmark batch, with the zone filter."""
+def test_gpu_three_way_star_sample(star_layout, star_nc, gpu_engines):
+    """The star benchmark: a 65,536-query sample of its batch, with the zone filter."""
     lay, oeng = star_layout
     q = W.queries_for(lay, 1 << 20, 0xC1)[:65536]
     bad, corners = _three_way(gpu_engines[1], oeng, star_nc, q, lay.filter_keys, 65536)
