@@ -1616,11 +1616,18 @@ struct jcde_resident {
     cudaStream_t exec_stream = nullptr;
     cudaStream_t own = nullptr;
     cudaStream_t last = nullptr;
+    // the next step's first candidates are drawn on `side` while a step commits (fork and join)
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     uint64_t launches = 0;
     uint64_t load_bytes = 0;   // host-to-device bytes of the last load of the engine's hazards
     ~jcde_resident() {
         if (last) cudaStreamSynchronize(last);
+        if (side) cudaStreamSynchronize(side);
         if (exec) cudaGraphExecDestroy(exec);
+        if (ev_fork) cudaEventDestroy(ev_fork);
+        if (ev_join) cudaEventDestroy(ev_join);
+        if (side) cudaStreamDestroy(side);
         if (own) {
             // the engine must not wait on a stream that no longer exists
             if (e && e->have_last_stream && e->last_stream == own) {
@@ -1721,8 +1728,11 @@ static bool resident_detect(jcde_resident* r, const uint32_t* q, uint32_t n, uin
 
 // One step of the LBF-style build: a uniform round and ls_rounds local-search rounds, each
 // generate -> surrogate pass -> polygon pass + choice (-> merge into the step's best), then the
-// commit (4 launches without local search, 4 more per local-search round).
-static void lbf_step(jcde_resident* r, cudaStream_t s) {
+// commit.  With `drawn`, the first round's candidates were generated while the previous step
+// committed; with `ahead`, the next step's are generated on the side stream while this step
+// commits (the commit touches neither the candidates nor the generator's inputs, and the generation
+// neither the tree nor the step state).
+static void lbf_step(jcde_resident* r, cudaStream_t s, bool drawn, bool ahead) {
     jcde_engine* e = r->e;
     LbfDev* st = r->d_lbf.as<LbfDev>();
     uint32_t* cand = r->d_cand.as<uint32_t>();
@@ -1731,10 +1741,13 @@ static void lbf_step(jcde_resident* r, cudaStream_t s) {
     const uint32_t last = r->lp.uni_rounds + r->lp.ls_rounds - 1;   // uniform rounds, then local search
     for (uint32_t round = 0; round <= last; round++) {
         const uint32_t n = round < r->lp.uni_rounds ? r->lp.n_uni : r->lp.ls_cand;
-        cudaEvent_t pa = prof_begin(e, s);
-        res_launch_lbf_gen(r->lp, st, cand, cu, round, e->n_sms, s);
-        prof_end(e, s, pa, JCDE_PROF_LBF);
-        r->launches++;
+        cudaEvent_t pa = nullptr;
+        if (round > 0 || !drawn) {
+            pa = prof_begin(e, s);
+            res_launch_lbf_gen(r->lp, st, cand, cu, round, e->n_sms, s);
+            prof_end(e, s, pa, JCDE_PROF_LBF);
+            r->launches++;
+        }
         // the polygon pass makes the choice itself when it runs its small-batch kernel, skipping the
         // candidates that can no longer win unless every verdict is logged; n_free counts the
         // candidates the surrogate pass leaves to the polygon pass
@@ -1756,11 +1769,26 @@ static void lbf_step(jcde_resident* r, cudaStream_t s) {
     }
     LbfLogs logs{r->d_place.as<uint32_t>(), r->d_remv.as<uint32_t>(), r->d_free.as<uint32_t>(),
                  r->d_live.as<uint32_t>(), r->lp.vlog_steps ? r->d_vlog.as<uint8_t>() : nullptr};
-    cudaEvent_t pa = prof_begin(e, s);
+    cudaEvent_t pa = nullptr;
+    if (ahead) {
+        pa = prof_begin(e, s);
+        res_launch_lbf_merge(st, cand, cu, last, s, true);
+        prof_end(e, s, pa, JCDE_PROF_LBF);
+        r->launches++;
+        cudaEventRecord(r->ev_fork, s);
+        cudaStreamWaitEvent(r->side, r->ev_fork, 0);
+        pa = prof_begin(e, r->side);
+        res_launch_lbf_gen(r->lp, st, cand, cu, 0, e->n_sms, r->side, true);
+        prof_end(e, r->side, pa, JCDE_PROF_LBF);
+        r->launches++;
+        cudaEventRecord(r->ev_join, r->side);
+    }
+    pa = prof_begin(e, s);
     res_launch_lbf_commit(r->t, e->d_items.as<DItem>(), e->d_iverts.as<float2>(), (uint32_t)e->items.size(), r->lp,
-                          st, cand, cu, last, verd, logs, s);
+                          st, cand, cu, last, verd, logs, s, ahead);
     prof_end(e, s, pa, JCDE_PROF_UPDATE);
     r->launches++;
+    if (ahead) cudaStreamWaitEvent(s, r->ev_join, 0);
 }
 
 // Loads the engine's live hazards, each under its own key, into empty pools (jcde_resident_create
@@ -2097,6 +2125,9 @@ jcde_status jcde_lbf_begin(jcde_resident* r, const jcde_lbf_params* p) {
     }
     jcde_status st = ensure_order_buffers(r, p->n_candidates);
     if (st) return st;
+    if (!r->side) CUDA_TRY(cudaStreamCreateWithFlags(&r->side, cudaStreamNonBlocking));
+    if (!r->ev_fork) CUDA_TRY(cudaEventCreateWithFlags(&r->ev_fork, cudaEventDisableTiming));
+    if (!r->ev_join) CUDA_TRY(cudaEventCreateWithFlags(&r->ev_join, cudaEventDisableTiming));
     r->lbf_ready = true;
     return JCDE_OK;
 }
@@ -2117,7 +2148,9 @@ jcde_status jcde_lbf_steps(jcde_resident* r, uint32_t n_steps, uint32_t steps_pe
             if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return JCDE_ERR_CUDA;
             const uint64_t before = r->launches;
             e->prof = false;   // per-kernel events are not recorded inside graphs
-            for (uint32_t i = 0; i < steps_per_graph; i++) lbf_step(r, s);
+            // every graph launch is self-contained: its first step draws its own candidates and its
+            // last step draws none ahead
+            for (uint32_t i = 0; i < steps_per_graph; i++) lbf_step(r, s, i > 0, i + 1 < steps_per_graph);
             e->prof = prof;
             r->exec_launches = r->launches - before;   // kernels per graph launch
             r->launches = before;
@@ -2136,7 +2169,7 @@ jcde_status jcde_lbf_steps(jcde_resident* r, uint32_t n_steps, uint32_t steps_pe
             r->launches += r->exec_launches;
         }
     }
-    for (; done < n_steps; done++) lbf_step(r, s);
+    for (uint32_t i = 0; done < n_steps; done++, i++) lbf_step(r, s, i > 0, done + 1 < n_steps);
     CUDA_TRY(cudaGetLastError());
     r->last = s;
     e->last_stream = s;

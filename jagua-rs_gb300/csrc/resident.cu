@@ -727,10 +727,12 @@ __device__ __forceinline__ float cost_of_key(uint32_t v) {
 // with the pair of draws 2m+i, 3m+i; with no best yet the round's candidates are marked invalid.
 // `qu` keeps each candidate's turns.
 __global__ void k_lbf_gen(LbfParams p, LbfDev* __restrict__ st, uint32_t* __restrict__ q, double* __restrict__ qu,
-                          uint32_t round) {
-    const uint32_t step = *(volatile uint32_t*)&st->step;
+                          uint32_t round, bool ahead) {
+    // `ahead`: the first round of the next step, drawn while this step commits (the step state is
+    // the commit's to clear)
+    const uint32_t step = ahead ? *(volatile uint32_t*)&st->gen_step : *(volatile uint32_t*)&st->step;
     if (step >= p.max_steps) return;
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (blockIdx.x == 0 && threadIdx.x == 0 && !ahead) {
         if (round == 0) {
             st->n_free = 0;
             st->rec_cost = ~0u;
@@ -813,8 +815,11 @@ __device__ __forceinline__ void lbf_merge(LbfDev* st, const uint32_t* q, const d
     st->rec_cand = (round << 24) | idx;
 }
 __global__ void k_lbf_merge(LbfDev* __restrict__ st, const uint32_t* __restrict__ q, const double* __restrict__ qu,
-                            uint32_t round) {
-    if (threadIdx.x == 0) lbf_merge(st, q, qu, round);
+                            uint32_t round, bool ahead) {
+    if (threadIdx.x == 0) {
+        lbf_merge(st, q, qu, round);
+        if (ahead) st->gen_step = st->step + 1;
+    }
 }
 
 // End of a step: log it, register the chosen candidate, and every `remove_every` steps remove the
@@ -823,7 +828,7 @@ __global__ void __launch_bounds__(32) k_lbf_commit(RTree tg, const DItem* __rest
                                                    const float2* __restrict__ iverts, uint32_t n_items, LbfParams p,
                                                    LbfDev* __restrict__ st, const uint32_t* __restrict__ q,
                                                    const double* __restrict__ qu, uint32_t round,
-                                                   const uint8_t* __restrict__ verdicts, LbfLogs logs) {
+                                                   const uint8_t* __restrict__ verdicts, LbfLogs logs, bool ahead) {
     __shared__ RTask stasks[RT_SMEM_TASKS];
     RTree t = tg;
     t.stasks = stasks;
@@ -833,7 +838,7 @@ __global__ void __launch_bounds__(32) k_lbf_commit(RTree tg, const DItem* __rest
     if (step >= p.max_steps) return;
     RState s = r_load(t.ctl);
     if (s.error) return;
-    if (lane == 0) lbf_merge(st, q, qu, round);   // the last round's choice
+    if (lane == 0 && !ahead) lbf_merge(st, q, qu, round);   // the last round's choice (else merged before)
     __syncwarp();
     uint32_t n_live = vs->n_live, n_removed = vs->n_removed, n_placed = vs->n_placed;
     if (lane == 0) logs.free_counts[step] = vs->n_free;
@@ -886,6 +891,11 @@ __global__ void __launch_bounds__(32) k_lbf_commit(RTree tg, const DItem* __rest
         vs->n_removed = n_removed;
         vs->n_placed = n_placed;
         vs->step = step + 1;
+        if (ahead) {   // the next step's state (its first round was generated alongside this commit)
+            vs->n_free = 0;
+            vs->rec_cost = ~0u;
+            vs->best = ~0ull;
+        }
     }
 }
 
@@ -902,10 +912,10 @@ void res_launch_insert_placed(const RTree& t, const DItem* items, const float2* 
 }
 void res_launch_remove(const RTree& t, const uint32_t* key, cudaStream_t s) { k_res_remove<<<1, 32, 0, s>>>(t, key); }
 void res_launch_lbf_gen(const LbfParams& p, LbfDev* st, uint32_t* q, double* qu, uint32_t round, int n_sms,
-                        cudaStream_t s) {
+                        cudaStream_t s, bool ahead) {
     const uint32_t n = round < p.uni_rounds ? p.n_uni : p.ls_cand;
     const uint32_t grid = std::min<uint32_t>((n + 255) / 256, (uint32_t)std::max(1, n_sms) * 4);
-    k_lbf_gen<<<grid, 256, 0, s>>>(p, st, q, qu, round);
+    k_lbf_gen<<<grid, 256, 0, s>>>(p, st, q, qu, round, ahead);
 }
 void res_launch_gen_candidates(const unsigned long long* keys, const float (*bx)[4], uint32_t m, uint32_t n,
                                uint32_t item, const float2* orient, uint32_t n_orient, uint32_t* q, double* qu,
@@ -920,13 +930,14 @@ void res_launch_gen_candidates(const unsigned long long* keys, const float (*bx)
     const uint32_t gx = std::max<uint32_t>(1u, std::min<uint32_t>((n + 255) / 256, per_seg));
     k_gen_candidates<<<dim3(gx, m), 256, 0, s>>>(g, n, item, orient, n_orient, q, qu);
 }
-void res_launch_lbf_merge(LbfDev* st, const uint32_t* q, const double* qu, uint32_t round, cudaStream_t s) {
-    k_lbf_merge<<<1, 32, 0, s>>>(st, q, qu, round);
+void res_launch_lbf_merge(LbfDev* st, const uint32_t* q, const double* qu, uint32_t round, cudaStream_t s,
+                          bool ahead) {
+    k_lbf_merge<<<1, 32, 0, s>>>(st, q, qu, round, ahead);
 }
 void res_launch_lbf_commit(const RTree& t, const DItem* items, const float2* iverts, uint32_t n_items,
                            const LbfParams& p, LbfDev* st, const uint32_t* q, const double* qu, uint32_t round,
-                           const uint8_t* verdicts, const LbfLogs& logs, cudaStream_t s) {
-    k_lbf_commit<<<1, 32, 0, s>>>(t, items, iverts, n_items, p, st, q, qu, round, verdicts, logs);
+                           const uint8_t* verdicts, const LbfLogs& logs, cudaStream_t s, bool ahead) {
+    k_lbf_commit<<<1, 32, 0, s>>>(t, items, iverts, n_items, p, st, q, qu, round, verdicts, logs, ahead);
 }
 
 }  // namespace jcde

@@ -99,7 +99,8 @@ struct LbfDev {
     double rec_u;              //   its rotation in turns
     uint32_t rec_q[5];         //   its query record
     uint32_t rec_cand;         //   round << 24 | candidate index
-    uint32_t pad[2];
+    uint32_t gen_step;         // the step whose first round is generated while this step commits
+    uint32_t pad[1];
 };
 
 constexpr int LBF_MAX_LS = 8;        // local-search rounds per step
@@ -150,10 +151,14 @@ void res_launch_gen_candidates(const unsigned long long* keys, const float (*bx)
                                uint32_t item, const float2* orient, uint32_t n_orient, uint32_t* q, double* qu,
                                int n_sms, cudaStream_t s);
 void res_launch_lbf_gen(const LbfParams& p, LbfDev* st, uint32_t* q, double* qu, uint32_t round, int n_sms,
-                        cudaStream_t s);
-void res_launch_lbf_merge(LbfDev* st, const uint32_t* q, const double* qu, uint32_t round, cudaStream_t s);
+                        cudaStream_t s, bool ahead = false);
+// With `ahead`: the last round's merge before the commit, which then overlaps the next step's first
+// generation (gen with `ahead` draws for st->gen_step, set by that merge, and leaves the step's state
+// alone; the commit skips the merge and clears that state for the next step when it ends).
+void res_launch_lbf_merge(LbfDev* st, const uint32_t* q, const double* qu, uint32_t round, cudaStream_t s,
+                          bool ahead = false);
 void res_launch_lbf_commit(const RTree& t, const DItem* items, const float2* iverts, uint32_t n_items,
                            const LbfParams& p, LbfDev* st, const uint32_t* q, const double* qu, uint32_t round,
-                           const uint8_t* verdicts, const LbfLogs& logs, cudaStream_t s);
+                           const uint8_t* verdicts, const LbfLogs& logs, cudaStream_t s, bool ahead = false);
 
 }  // namespace jcde
