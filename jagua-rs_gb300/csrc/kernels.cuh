@@ -962,13 +962,19 @@ __device__ __forceinline__ void poly_query(const View& v, const uint32_t* __rest
     // lbf's search tests a sample's polygon only if it could still beat the best free sample
     // (search.rs:52-56): with `skip`, a query whose (cost, index) exceeds the batch's best so far
     // is left unjudged (3); the best only falls, so no skipped query could have been the choice.
+    unsigned long long skip_key = ~0ull;
     if (skip && best && !raw.verts) {
-        const unsigned long long key = ((unsigned long long)orderable(sb.x1 * 10.0f + sb.y1) << 32) | qi;
-        if (key > *(volatile unsigned long long*)best) {
+        skip_key = ((unsigned long long)orderable(sb.x1 * 10.0f + sb.y1) << 32) | qi;
+        if (skip_key > *(volatile unsigned long long*)best) {
             if (lane == 0) out[qi] = 3;
             return;
         }
     }
+    // the same test while the query is judged: a query whose key falls behind a best found since can
+    // no longer be the choice, so its judgment stops there (unjudged, 3)
+    auto overtaken = [&]() -> bool {
+        return skip_key != ~0ull && skip_key > *(volatile unsigned long long*)best;
+    };
     auto edge_of = [&](uint32_t k) -> Seg {
         if (!cached) return sh.edge(k);
         const float2 a = tv[k], b = tv[k + 1 == sh.nv ? 0 : k + 1];
@@ -1022,7 +1028,12 @@ __device__ __forceinline__ void poly_query(const View& v, const uint32_t* __rest
     uint32_t next = 0;
     WalkT<PendT> w{-1, 0, 0, (PendT)0};
     Seg e{};
+    uint32_t iter = 0;
     while (!hit) {
+        if (((++iter & 7) == 0) && overtaken()) {
+            if (lane == 0) out[qi] = 3;
+            return;
+        }
         const bool want = w.node == -1;
         const uint32_t need = __ballot_sync(FULL, want);
         if (want) {
@@ -1066,6 +1077,10 @@ __device__ __forceinline__ void poly_query(const View& v, const uint32_t* __rest
         PSTAT(8, 1);
         PSTAT(9, hit ? 1 : 0);
         PSTAT(11, n_jobs);
+    }
+    if (!hit && overtaken()) {
+        if (lane == 0) out[qi] = 3;
+        return;
     }
     if (!hit) {
         // containment of the shape in (or of) the partially present hazards of the virtual root
