@@ -970,8 +970,9 @@ __device__ __forceinline__ void poly_query(const View& v, const uint32_t* __rest
             return;
         }
     }
-    // the same test while the query is judged: a query whose key falls behind a best found since can
-    // no longer be the choice, so its judgment stops there (unjudged, 3)
+    // the same test while the query is judged (before its leaf table, then every 4 iterations of the
+    // edge loop, then before the containment scan): a query whose key falls behind a best found since
+    // can no longer be the choice, so its judgment stops there (unjudged, 3)
     auto overtaken = [&]() -> bool {
         return skip_key != ~0ull && skip_key > *(volatile unsigned long long*)best;
     };
@@ -1017,6 +1018,10 @@ __device__ __forceinline__ void poly_query(const View& v, const uint32_t* __rest
     }
     const LeafTab* tab = nullptr;
     if constexpr (TAB) {
+        if (!hit && n_jobs > 0 && overtaken()) {
+            if (lane == 0) out[qi] = 3;
+            return;
+        }
         if (!hit && n_jobs > 0) {
             build_leaf_tab<PendT>(v, vr, sb, ltab, lane);
             tab = ltab;
@@ -1030,7 +1035,7 @@ __device__ __forceinline__ void poly_query(const View& v, const uint32_t* __rest
     Seg e{};
     uint32_t iter = 0;
     while (!hit) {
-        if (((++iter & 7) == 0) && overtaken()) {
+        if (((++iter & 3) == 0) && overtaken()) {
             if (lane == 0) out[qi] = 3;
             return;
         }
