@@ -501,6 +501,8 @@ static bool launch_passes_t(jcde_engine* e, const View& v, const uint32_t* q, ui
     if (!(mode == 3 && large && next && JCDE_SURR_DYNAMIC && e->tune.poly_chunk && !raw.verts && !n_pending) ||
         (pend.rec && cudaMemsetAsync(pend.count, 0, 4, s) != cudaSuccess))
         pend = PendList{nullptr, nullptr};
+    // the small-batch polygon pass's counter, cleared by the warp surrogate pass when both run here
+    bool poly_counter_zeroed = false;
     if (mode & 1) {
         const uint8_t miss = mode == 1 ? (uint8_t)0 : PENDING;
         cudaEvent_t pa = prof_begin(e, s);
@@ -508,9 +510,14 @@ static bool launch_passes_t(jcde_engine* e, const View& v, const uint32_t* q, ui
             const uint32_t lanes = e->tune.surrogate_lanes;
             const uint32_t gpb = SURR_THREADS / lanes;   // query groups per block
             const uint32_t grid = std::min<uint32_t>((n + gpb - 1) / gpb, (uint32_t)e->n_sms * 8);
-            if (lanes == 8) k_surrogate_warp<PendT, 8><<<grid, SURR_THREADS, 0, s>>>(v, q, n, dout, miss, order, n_pending);
-            else if (lanes == 16) k_surrogate_warp<PendT, 16><<<grid, SURR_THREADS, 0, s>>>(v, q, n, dout, miss, order, n_pending);
-            else k_surrogate_warp<PendT, 32><<<grid, SURR_THREADS, 0, s>>>(v, q, n, dout, miss, order, n_pending);
+            uint32_t* zero = (mode & 2) && next && n <= e->tune.leaf_table_max ? next + 1 : nullptr;
+            poly_counter_zeroed = zero != nullptr;
+            if (lanes == 8)
+                k_surrogate_warp<PendT, 8><<<grid, SURR_THREADS, 0, s>>>(v, q, n, dout, miss, order, n_pending, zero);
+            else if (lanes == 16)
+                k_surrogate_warp<PendT, 16><<<grid, SURR_THREADS, 0, s>>>(v, q, n, dout, miss, order, n_pending, zero);
+            else
+                k_surrogate_warp<PendT, 32><<<grid, SURR_THREADS, 0, s>>>(v, q, n, dout, miss, order, n_pending, zero);
         } else if (JCDE_SURR_DYNAMIC && next && cudaMemsetAsync(next, 0, 4, s) == cudaSuccess) {
             // persistent blocks; each warp takes the next 32 queries from a counter as it finishes
             const uint32_t grid = std::min<uint32_t>((n + SURR_THREADS - 1) / SURR_THREADS,
@@ -535,7 +542,9 @@ static bool launch_passes_t(jcde_engine* e, const View& v, const uint32_t* q, ui
         // batches are latency-bound and also build per-query leaf tables.
         const bool tab = n <= e->tune.leaf_table_max;
         if (next) next += 1;   // the polygon pass's own counter
-        if (!next || (!tab && !e->tune.poly_chunk) || cudaMemsetAsync(next, 0, 4, s) != cudaSuccess) next = nullptr;
+        if (!next || (!tab && !e->tune.poly_chunk) ||
+            (!(tab && poly_counter_zeroed) && cudaMemsetAsync(next, 0, 4, s) != cudaSuccess))
+            next = nullptr;
         if (tab) {
             grid = std::min<uint32_t>(want, (uint32_t)(e->n_sms * e->tab_blocks_per_sm));
             k_poly_tab<PendT><<<grid, POLY_WARPS * 32, POLY_WARPS * sizeof(LeafTab), s>>>(v, q, n, dout, raw, mode == 3,

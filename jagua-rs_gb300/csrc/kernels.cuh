@@ -703,7 +703,11 @@ template <typename PendT, int G = JCDE_SURR_GROUP>
 __global__ void JCDE_SURR_BOUNDS k_surrogate_warp(View v, const uint32_t* __restrict__ q, uint32_t n,
                                                                  uint8_t* __restrict__ out, uint8_t miss,
                                                                  const uint32_t* __restrict__ order,
-                                                                 uint32_t* __restrict__ n_pending = nullptr) {
+                                                                 uint32_t* __restrict__ n_pending = nullptr,
+                                                                 uint32_t* __restrict__ zero = nullptr) {
+    // `zero`: the polygon pass's work counter, cleared here (the polygon pass runs after this one on
+    // the stream) instead of by a memset of its own
+    if (zero && blockIdx.x == 0 && threadIdx.x == 0) *zero = 0u;
     const LaneGroup<G> g(threadIdx.x & 31);
     constexpr uint32_t gpb = SURR_THREADS / G;   // groups per block
     for (uint32_t i = blockIdx.x * gpb + threadIdx.x / G; i < n; i += gridDim.x * gpb) {
