@@ -1616,6 +1616,7 @@ struct jcde_resident {
     bool lbf_ready = false;
     LbfParams lp{};
     DevBuf d_lbf, d_cand, d_candu, d_verd, d_place, d_remv, d_free, d_live, d_vlog;
+    DevBuf d_cand2, d_candu2;   // the other candidate buffer: step k of a launch uses buffer k % 2
     DevBuf d_seq, d_orient, d_orient_of;   // instance mode: item sequence, allowed orientations
     DevBuf d_hist, d_order;   // spatial ordering of the resident's own query batches
     DevBuf d_next;            // work counters of its two passes
@@ -1741,11 +1742,12 @@ static bool resident_detect(jcde_resident* r, const uint32_t* q, uint32_t n, uin
 // committed; with `ahead`, the next step's are generated on the side stream while this step
 // commits (the commit touches neither the candidates nor the generator's inputs, and the generation
 // neither the tree nor the step state).
-static void lbf_step(jcde_resident* r, cudaStream_t s, bool drawn, bool ahead) {
+static void lbf_step(jcde_resident* r, cudaStream_t s, uint32_t k, bool ahead) {
     jcde_engine* e = r->e;
     LbfDev* st = r->d_lbf.as<LbfDev>();
-    uint32_t* cand = r->d_cand.as<uint32_t>();
-    double* cu = r->d_candu.as<double>();
+    const bool drawn = k > 0;   // the first round was generated while the previous step committed
+    uint32_t* cand = (k & 1u) ? r->d_cand2.as<uint32_t>() : r->d_cand.as<uint32_t>();
+    double* cu = (k & 1u) ? r->d_candu2.as<double>() : r->d_candu.as<double>();
     uint8_t* verd = r->d_verd.as<uint8_t>();
     const uint32_t last = r->lp.uni_rounds + r->lp.ls_rounds - 1;   // uniform rounds, then local search
     for (uint32_t round = 0; round <= last; round++) {
@@ -1753,7 +1755,7 @@ static void lbf_step(jcde_resident* r, cudaStream_t s, bool drawn, bool ahead) {
         cudaEvent_t pa = nullptr;
         if (round > 0 || !drawn) {
             pa = prof_begin(e, s);
-            res_launch_lbf_gen(r->lp, st, cand, cu, round, e->n_sms, s);
+            res_launch_lbf_gen(r->lp, st, cand, cu, round, e->n_sms, s, false, k & 1u);
             prof_end(e, s, pa, JCDE_PROF_LBF);
             r->launches++;
         }
@@ -1779,15 +1781,13 @@ static void lbf_step(jcde_resident* r, cudaStream_t s, bool drawn, bool ahead) {
     LbfLogs logs{r->d_place.as<uint32_t>(), r->d_remv.as<uint32_t>(), r->d_free.as<uint32_t>(),
                  r->d_live.as<uint32_t>(), r->lp.vlog_steps ? r->d_vlog.as<uint8_t>() : nullptr};
     cudaEvent_t pa = nullptr;
-    if (ahead) {
-        pa = prof_begin(e, s);
-        res_launch_lbf_merge(st, cand, cu, last, s, true);
-        prof_end(e, s, pa, JCDE_PROF_LBF);
-        r->launches++;
+    if (ahead) {   // the next step's first round, into the other buffer, while this step commits
+        uint32_t* cand_n = (k & 1u) ? r->d_cand.as<uint32_t>() : r->d_cand2.as<uint32_t>();
+        double* cu_n = (k & 1u) ? r->d_candu.as<double>() : r->d_candu2.as<double>();
         cudaEventRecord(r->ev_fork, s);
         cudaStreamWaitEvent(r->side, r->ev_fork, 0);
         pa = prof_begin(e, r->side);
-        res_launch_lbf_gen(r->lp, st, cand, cu, 0, e->n_sms, r->side, true);
+        res_launch_lbf_gen(r->lp, st, cand_n, cu_n, 0, e->n_sms, r->side, true, (k + 1) & 1u);
         prof_end(e, r->side, pa, JCDE_PROF_LBF);
         r->launches++;
         cudaEventRecord(r->ev_join, r->side);
@@ -2123,6 +2123,7 @@ jcde_status jcde_lbf_begin(jcde_resident* r, const jcde_lbf_params* p) {
     }
     const size_t n = p->n_candidates, ms = p->max_steps;
     const bool ok = r->d_lbf.ensure(sizeof(LbfDev)) && r->d_cand.ensure(n * 20) && r->d_candu.ensure(n * 8) &&
+                    r->d_cand2.ensure(n * 20) && r->d_candu2.ensure(n * 8) &&
                     r->d_verd.ensure(n) &&
                     r->d_place.ensure(ms * 32) && r->d_remv.ensure(ms * 8) && r->d_free.ensure(ms * 4) &&
                     r->d_live.ensure(ms * 4) && (!lp.vlog_steps || r->d_vlog.ensure((size_t)lp.vlog_steps * n));
@@ -2159,7 +2160,7 @@ jcde_status jcde_lbf_steps(jcde_resident* r, uint32_t n_steps, uint32_t steps_pe
             e->prof = false;   // per-kernel events are not recorded inside graphs
             // every graph launch is self-contained: its first step draws its own candidates and its
             // last step draws none ahead
-            for (uint32_t i = 0; i < steps_per_graph; i++) lbf_step(r, s, i > 0, i + 1 < steps_per_graph);
+            for (uint32_t i = 0; i < steps_per_graph; i++) lbf_step(r, s, i, i + 1 < steps_per_graph);
             e->prof = prof;
             r->exec_launches = r->launches - before;   // kernels per graph launch
             r->launches = before;
@@ -2178,7 +2179,7 @@ jcde_status jcde_lbf_steps(jcde_resident* r, uint32_t n_steps, uint32_t steps_pe
             r->launches += r->exec_launches;
         }
     }
-    for (uint32_t i = 0; done < n_steps; done++, i++) lbf_step(r, s, i > 0, done + 1 < n_steps);
+    for (uint32_t i = 0; done < n_steps; done++, i++) lbf_step(r, s, i, done + 1 < n_steps);
     CUDA_TRY(cudaGetLastError());
     r->last = s;
     e->last_stream = s;

@@ -727,10 +727,11 @@ __device__ __forceinline__ float cost_of_key(uint32_t v) {
 // with the pair of draws 2m+i, 3m+i; with no best yet the round's candidates are marked invalid.
 // `qu` keeps each candidate's turns.
 __global__ void k_lbf_gen(LbfParams p, LbfDev* __restrict__ st, uint32_t* __restrict__ q, double* __restrict__ qu,
-                          uint32_t round, bool ahead) {
+                          uint32_t round, bool ahead, uint32_t slot) {
     // `ahead`: the first round of the next step, drawn while this step commits (the step state is
-    // the commit's to clear)
-    const uint32_t step = ahead ? *(volatile uint32_t*)&st->gen_step : *(volatile uint32_t*)&st->step;
+    // the commit's to clear); its step is gen_step[slot]
+    const uint32_t step = ahead ? *(volatile uint32_t*)&st->gen_step[slot] : *(volatile uint32_t*)&st->step;
+    if (round == 0 && blockIdx.x == 0 && threadIdx.x == 0) st->gen_step[slot ^ 1u] = step + 1;
     if (step >= p.max_steps) return;
     if (blockIdx.x == 0 && threadIdx.x == 0 && !ahead) {
         if (round == 0) {
@@ -815,11 +816,8 @@ __device__ __forceinline__ void lbf_merge(LbfDev* st, const uint32_t* q, const d
     st->rec_cand = (round << 24) | idx;
 }
 __global__ void k_lbf_merge(LbfDev* __restrict__ st, const uint32_t* __restrict__ q, const double* __restrict__ qu,
-                            uint32_t round, bool ahead) {
-    if (threadIdx.x == 0) {
-        lbf_merge(st, q, qu, round);
-        if (ahead) st->gen_step = st->step + 1;
-    }
+                            uint32_t round) {
+    if (threadIdx.x == 0) lbf_merge(st, q, qu, round);
 }
 
 // End of a step: log it, register the chosen candidate, and every `remove_every` steps remove the
@@ -838,7 +836,7 @@ __global__ void __launch_bounds__(32) k_lbf_commit(RTree tg, const DItem* __rest
     if (step >= p.max_steps) return;
     RState s = r_load(t.ctl);
     if (s.error) return;
-    if (lane == 0 && !ahead) lbf_merge(st, q, qu, round);   // the last round's choice (else merged before)
+    if (lane == 0) lbf_merge(st, q, qu, round);   // the last round's choice
     __syncwarp();
     uint32_t n_live = vs->n_live, n_removed = vs->n_removed, n_placed = vs->n_placed;
     if (lane == 0) logs.free_counts[step] = vs->n_free;
@@ -912,10 +910,10 @@ void res_launch_insert_placed(const RTree& t, const DItem* items, const float2* 
 }
 void res_launch_remove(const RTree& t, const uint32_t* key, cudaStream_t s) { k_res_remove<<<1, 32, 0, s>>>(t, key); }
 void res_launch_lbf_gen(const LbfParams& p, LbfDev* st, uint32_t* q, double* qu, uint32_t round, int n_sms,
-                        cudaStream_t s, bool ahead) {
+                        cudaStream_t s, bool ahead, uint32_t slot) {
     const uint32_t n = round < p.uni_rounds ? p.n_uni : p.ls_cand;
     const uint32_t grid = std::min<uint32_t>((n + 255) / 256, (uint32_t)std::max(1, n_sms) * 4);
-    k_lbf_gen<<<grid, 256, 0, s>>>(p, st, q, qu, round, ahead);
+    k_lbf_gen<<<grid, 256, 0, s>>>(p, st, q, qu, round, ahead, slot);
 }
 void res_launch_gen_candidates(const unsigned long long* keys, const float (*bx)[4], uint32_t m, uint32_t n,
                                uint32_t item, const float2* orient, uint32_t n_orient, uint32_t* q, double* qu,
@@ -930,9 +928,8 @@ void res_launch_gen_candidates(const unsigned long long* keys, const float (*bx)
     const uint32_t gx = std::max<uint32_t>(1u, std::min<uint32_t>((n + 255) / 256, per_seg));
     k_gen_candidates<<<dim3(gx, m), 256, 0, s>>>(g, n, item, orient, n_orient, q, qu);
 }
-void res_launch_lbf_merge(LbfDev* st, const uint32_t* q, const double* qu, uint32_t round, cudaStream_t s,
-                          bool ahead) {
-    k_lbf_merge<<<1, 32, 0, s>>>(st, q, qu, round, ahead);
+void res_launch_lbf_merge(LbfDev* st, const uint32_t* q, const double* qu, uint32_t round, cudaStream_t s) {
+    k_lbf_merge<<<1, 32, 0, s>>>(st, q, qu, round);
 }
 void res_launch_lbf_commit(const RTree& t, const DItem* items, const float2* iverts, uint32_t n_items,
                            const LbfParams& p, LbfDev* st, const uint32_t* q, const double* qu, uint32_t round,

@@ -99,8 +99,10 @@ struct LbfDev {
     double rec_u;              //   its rotation in turns
     uint32_t rec_q[5];         //   its query record
     uint32_t rec_cand;         //   round << 24 | candidate index
-    uint32_t gen_step;         // the step whose first round is generated while this step commits
-    uint32_t pad[1];
+    // the step the next first-round generation draws for, in two slots: the generation of a graph
+    // launch's k-th step reads slot k % 2 (when drawn ahead) and writes slot (k + 1) % 2, so that a
+    // generation never writes the slot its own blocks read
+    uint32_t gen_step[2];
 };
 
 constexpr int LBF_MAX_LS = 8;        // local-search rounds per step
@@ -151,12 +153,12 @@ void res_launch_gen_candidates(const unsigned long long* keys, const float (*bx)
                                uint32_t item, const float2* orient, uint32_t n_orient, uint32_t* q, double* qu,
                                int n_sms, cudaStream_t s);
 void res_launch_lbf_gen(const LbfParams& p, LbfDev* st, uint32_t* q, double* qu, uint32_t round, int n_sms,
-                        cudaStream_t s, bool ahead = false);
-// With `ahead`: the last round's merge before the commit, which then overlaps the next step's first
-// generation (gen with `ahead` draws for st->gen_step, set by that merge, and leaves the step's state
-// alone; the commit skips the merge and clears that state for the next step when it ends).
-void res_launch_lbf_merge(LbfDev* st, const uint32_t* q, const double* qu, uint32_t round, cudaStream_t s,
-                          bool ahead = false);
+                        cudaStream_t s, bool ahead = false, uint32_t slot = 0);
+// The next step's first round can be generated while a step commits (into the other candidate
+// buffer): gen with `ahead` draws for st->gen_step[slot] and leaves the step's state alone, and the
+// commit, with `ahead`, clears that state for the next step when it ends.  A first-round generation
+// writes st->gen_step[slot ^ 1] (its step + 1).
+void res_launch_lbf_merge(LbfDev* st, const uint32_t* q, const double* qu, uint32_t round, cudaStream_t s);
 void res_launch_lbf_commit(const RTree& t, const DItem* items, const float2* iverts, uint32_t n_items,
                            const LbfParams& p, LbfDev* st, const uint32_t* q, const double* qu, uint32_t round,
                            const uint8_t* verdicts, const LbfLogs& logs, cudaStream_t s, bool ahead = false);
