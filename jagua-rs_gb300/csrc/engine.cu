@@ -512,12 +512,11 @@ static bool launch_passes_t(jcde_engine* e, const View& v, const uint32_t* q, ui
             const uint32_t grid = std::min<uint32_t>((n + gpb - 1) / gpb, (uint32_t)e->n_sms * 8);
             uint32_t* zero = (mode & 2) && next && n <= e->tune.leaf_table_max ? next + 1 : nullptr;
             poly_counter_zeroed = zero != nullptr;
-            if (lanes == 8)
-                k_surrogate_warp<PendT, 8><<<grid, SURR_THREADS, 0, s>>>(v, q, n, dout, miss, order, n_pending, zero);
-            else if (lanes == 16)
-                k_surrogate_warp<PendT, 16><<<grid, SURR_THREADS, 0, s>>>(v, q, n, dout, miss, order, n_pending, zero);
-            else
-                k_surrogate_warp<PendT, 32><<<grid, SURR_THREADS, 0, s>>>(v, q, n, dout, miss, order, n_pending, zero);
+            // a chained launch: scheduled while the kernel before it (the LBF commit, in a build) ends
+            auto kern = lanes == 8 ? k_surrogate_warp<PendT, 8>
+                        : lanes == 16 ? k_surrogate_warp<PendT, 16> : k_surrogate_warp<PendT, 32>;
+            launch_chained(kern, dim3(grid), dim3(SURR_THREADS), 0, s, true, v, q, n, dout, miss, order, n_pending,
+                           zero);
         } else if (JCDE_SURR_DYNAMIC && next && cudaMemsetAsync(next, 0, 4, s) == cudaSuccess) {
             // persistent blocks; each warp takes the next 32 queries from a counter as it finishes
             const uint32_t grid = std::min<uint32_t>((n + SURR_THREADS - 1) / SURR_THREADS,
@@ -547,8 +546,8 @@ static bool launch_passes_t(jcde_engine* e, const View& v, const uint32_t* q, ui
             next = nullptr;
         if (tab) {
             grid = std::min<uint32_t>(want, (uint32_t)(e->n_sms * e->tab_blocks_per_sm));
-            k_poly_tab<PendT><<<grid, POLY_WARPS * 32, POLY_WARPS * sizeof(LeafTab), s>>>(v, q, n, dout, raw, mode == 3,
-                                                                                        order, next, best, skip);
+            launch_chained(k_poly_tab<PendT>, dim3(grid), dim3(POLY_WARPS * 32), POLY_WARPS * sizeof(LeafTab), s, true,
+                           v, q, n, dout, raw, mode == 3, order, next, best, skip);
             chose = best != nullptr;
         } else {
             // the top staging_depth levels of the tree in shared memory (at most STAGE_MAX_BYTES)

@@ -23,6 +23,22 @@
 
 namespace jcde {
 
+#ifdef __CUDACC__
+// Programmatic dependent launch: a grid launched with the programmatic stream-serialization
+// attribute may be scheduled as soon as every block of the grid before it on the stream has
+// exited, ahead of that grid's completion and the launch processing that would otherwise follow
+// it.  pdl_wait() returns once that grid has completed and its memory writes are visible (at once
+// when there is none, or when the grid was launched without the attribute), so a kernel that calls
+// it before its first global memory access gives the same results launched either way.  (Letting
+// the successor be scheduled earlier still, with griddepcontrol.launch_dependents at the start of
+// the predecessor, made the LBF build slower: its blocks sit waiting on SMs the predecessor uses.)
+__device__ __forceinline__ void pdl_wait() {
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 900
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+#endif
+}
+#endif
+
 struct Pt { float x, y; };
 struct Seg { Pt s, e; };
 struct Box { float x0, y0, x1, y1; };

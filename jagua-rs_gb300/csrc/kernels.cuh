@@ -705,6 +705,7 @@ __global__ void JCDE_SURR_BOUNDS k_surrogate_warp(View v, const uint32_t* __rest
                                                                  const uint32_t* __restrict__ order,
                                                                  uint32_t* __restrict__ n_pending = nullptr,
                                                                  uint32_t* __restrict__ zero = nullptr) {
+    pdl_wait();
     // `zero`: the polygon pass's work counter, cleared here (the polygon pass runs after this one on
     // the stream) instead of by a memset of its own
     if (zero && blockIdx.x == 0 && threadIdx.x == 0) *zero = 0u;
@@ -1219,6 +1220,7 @@ __global__ void __launch_bounds__(POLY_WARPS * 32, JCDE_POLY_TAB_MIN_BLOCKS)
     __shared__ float2 tverts[POLY_WARPS][POLY_MAXV];
     __shared__ uint32_t jobs[POLY_WARPS][POLY_MAXV];
     extern __shared__ LeafTab ltabs[];   // one per warp
+    pdl_wait();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     volatile int* stop = &stops[warp];
     const uint32_t stride = gridDim.x * POLY_WARPS;

@@ -828,6 +828,7 @@ __global__ void __launch_bounds__(32) k_lbf_commit(RTree tg, const DItem* __rest
                                                    const double* __restrict__ qu, uint32_t round,
                                                    const uint8_t* __restrict__ verdicts, LbfLogs logs, bool ahead) {
     __shared__ RTask stasks[RT_SMEM_TASKS];
+    pdl_wait();
     RTree t = tg;
     t.stasks = stasks;
     const int lane = threadIdx.x;
@@ -934,7 +935,8 @@ void res_launch_lbf_merge(LbfDev* st, const uint32_t* q, const double* qu, uint3
 void res_launch_lbf_commit(const RTree& t, const DItem* items, const float2* iverts, uint32_t n_items,
                            const LbfParams& p, LbfDev* st, const uint32_t* q, const double* qu, uint32_t round,
                            const uint8_t* verdicts, const LbfLogs& logs, cudaStream_t s, bool ahead) {
-    k_lbf_commit<<<1, 32, 0, s>>>(t, items, iverts, n_items, p, st, q, qu, round, verdicts, logs, ahead);
+    launch_chained(k_lbf_commit, dim3(1), dim3(32), 0, s, true, t, items, iverts, n_items, p, st, q, qu, round,
+                   verdicts, logs, ahead);
 }
 
 }  // namespace jcde

@@ -27,7 +27,31 @@
 #include "geom.cuh"
 #include "qtree.hpp"
 
+#ifndef JCDE_PDL
+#define JCDE_PDL 1   // chained kernels of the small-batch passes and the LBF step: programmatic launch
+#endif
+
 namespace jcde {
+
+// Launches `kern` on `s`, with the programmatic stream-serialization attribute when `pdl` (and
+// JCDE_PDL): the grid may then be scheduled before the grid ahead of it has completed, so `kern`
+// must call pdl_wait() before its first global access.  In the LBF build's graph (three chained
+// kernels per step) this takes 150.7 -> 146.8 ms per 2000-step build.
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_chained(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, bool pdl,
+                                  Args... args) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = (JCDE_PDL && pdl) ? 1u : 0u;
+    return cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
+}
 
 enum : uint32_t {
     RES_OK = 0,
