@@ -40,7 +40,7 @@ import numpy as np
 from . import workload as W
 
 SEED = 0xC3
-TYPE_SID, REMOVE_SID, CAND_SID_BASE = 2, 4, 10_000   # stream ids of the driver's draws
+TYPE_SID, REMOVE_SID, CAND_SID_BASE = 2, 4, 10_000   # stream ids of the build's draws
 LS_SID_BASE = 1_000_000    # local-search round r of step s: stream LS_SID_BASE + 64 s + r
 UNI_SID_BASE = 2_000_000   # uniform round u >= 1 of step s: stream UNI_SID_BASE + 64 s + u (round 0: CAND_SID_BASE + s)
 # LSSampler's default deviations (ls_sampler.rs:9-13): translation as fractions of the CDE box's
