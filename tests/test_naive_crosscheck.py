@@ -143,6 +143,76 @@ def test_touch_queries(strip_layout, star_layout, strip_nc, star_nc):
     assert len(bad) <= 4, bad
 
 
+@pytest.fixture(scope="module")
+def bin_layouts(oracle_mod):
+    """Three bins of the batched multi-layout workload: star containers of 32-128 vertices holding
+    log-uniform 20-160 items drawn from 40 star types of 8-200 vertices."""
+    return W.multi_layouts(oracle_mod.OracleBackend, seed=0x7C2, n_layouts=3, items_range=(20, 160))
+
+
+def test_bin_layouts(bin_layouts):
+    """Random star containers and items of up to 200 vertices: queries inside the container, on the
+    quadtree's split lines and touching hazards agree, verdicts and collected sets."""
+    for l, (lay, oeng) in enumerate(bin_layouts):
+        nc = N.NaiveChecker.from_layout(lay)
+        xy = lay.hazards[0].xy
+        cx, cy = (xy[:, 0].min() + xy[:, 0].max()) / 2, (xy[:, 1].min() + xy[:, 1].max()) / 2
+        h = 0.6 * (xy[:, 0].max() - xy[:, 0].min()) / 2
+        box = np.array([cx - h, cy - h, cx + h, cy + h], np.float32)
+        q = W.make_queries(W.Stream(0x7C4 + l, 1), 8192, len(lay.items), box)
+        assert compare_verdicts(nc, q, oeng.detect_batch(q)) == []
+        assert compare(nc, q[:4096], *oeng.collect_batch(q[:4096])) == []
+        qb = W.boundary_queries(lay, 8192, 0xB2 + l)
+        compare_verdicts(nc, qb, oeng.detect_batch(qb))
+        compare(nc, qb[:4096], *oeng.collect_batch(qb[:4096]))
+        qt = W.touch_queries(lay, 16384, 0x71 + l)
+        compare_verdicts(nc, qt, oeng.detect_batch(qt))
+        compare(nc, qt[:4096], *oeng.collect_batch(qt[:4096]))
+
+
+def test_lbf_end_state_after_registrations_and_removals(oracle_mod):
+    """The oracle's quadtree after 300 LBF steps (300 registrations, a deregistration every 50 steps,
+    freed keys reused by later placements) against the tree-free checker built from the hazards
+    still live: what register_hazard / deregister_hazard_by_key (cd_engine.rs:59-96) leave behind
+    answers like the live set alone."""
+    from jcde import lbf
+
+    spec = lbf.LbfSpec(steps=300, n_cand=2048)
+    lay, eng = lbf.setup(oracle_mod.OracleBackend, spec)
+    log = lbf.run_host(lay, eng, spec)
+    keys = log.placements[:, 1].astype(np.int64)
+    assert len(log.removals) == 6 and len(set(keys.tolist())) < len(keys)   # keys were reused
+    placed = {int(r[0]): r for r in log.placements}
+    removed = {int(s): int(k) for s, k in log.removals}
+    live = {}
+    for step in range(spec.steps):   # a step places, then removes
+        if step in placed:
+            r = placed[step]
+            t = int(r[3])
+            c, s, tx, ty = np.asarray(r[4:8], np.uint32).view(np.float32)
+            hz = W.placed_hazard(lay.items[t], t, c, s, tx, ty)
+            hz.key = int(r[1])
+            assert hz.key not in live
+            live[hz.key] = hz
+        if step in removed:
+            del live[removed[step]]
+    assert len(live) == len(keys) - len(log.removals)
+    end = W.Layout(lay.name, lay.depth, lay.cd_threshold, lay.cde_bbox, items=lay.items,
+                   hazards=[lay.hazards[0]] + list(live.values()))
+    nc = N.NaiveChecker.from_layout(end)
+    q = W.make_queries(W.Stream(0x1BF, 5), 16384, len(lay.items), np.array([0, 0, 4000, 2000], np.float32))
+    v = eng.detect_batch(q)
+    assert 0.1 < v.mean() < 0.9
+    assert compare_verdicts(nc, q, v) == []
+    assert compare(nc, q[:8192], *eng.collect_batch(q[:8192])) == []
+    qt = W.touch_queries(end, 32768, 0x72)
+    compare_verdicts(nc, qt, eng.detect_batch(qt))
+    compare(nc, qt[:8192], *eng.collect_batch(qt[:8192]))
+    qb = W.boundary_queries(end, 16384, 0xB3)
+    compare_verdicts(nc, qb, eng.detect_batch(qb))
+    compare(nc, qb[:8192], *eng.collect_batch(qb[:8192]))
+
+
 # ----------------------------------------------------------------------------------------------
 # GPU: the sm_103a kernels against the oracle (bit-exact) and the naive checker (as above)
 # ----------------------------------------------------------------------------------------------
