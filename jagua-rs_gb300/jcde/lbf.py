@@ -144,6 +144,41 @@ def select_host_cost(items, q: np.ndarray, verdicts: np.ndarray):
     return int(free[k]), costs[k]
 
 
+NO_KEY = (1 << 64) - 1   # the key of a round with no free candidate
+
+
+def cost_key(cost, index: int) -> int:
+    """The 64-bit choice key of a free candidate: the order-preserving bits of its float32 cost
+    above its index, so that the least key is the least cost, first on ties (the order the
+    device's 64-bit atomicMin choice uses).  -0 is keyed as +0: the two compare equal."""
+    u = int(np.asarray(np.float32(cost) + np.float32(0.0), dtype=np.float32).view(np.uint32))
+    u = (~u & 0xFFFFFFFF) if u & 0x80000000 else (u | 0x80000000)
+    return (u << 32) | int(index)
+
+
+def _judge(lay, eng, q: np.ndarray, ranks):
+    """One round's (choice index or -1, its float32 cost, candidates the surrogate pass left to the
+    polygon pass, verdicts).  With ranks = (rank, world size) a rank judges its contiguous slice of
+    the candidates; the choice is the least cost_key over the ranks and the count their sum, and
+    every rank recomputes the winner's cost from its record (verdicts are then None)."""
+    if ranks is None:
+        verdicts, n_free = eng.detect_with_surrogate(q)
+        b, cb = select_host_cost(lay.items, q, verdicts)
+        return b, cb, n_free, verdicts
+    from . import shards
+
+    r, w = ranks
+    lo, hi = len(q) * r // w, len(q) * (r + 1) // w
+    v, n_free = eng.detect_with_surrogate(q[lo:hi]) if hi > lo else (np.zeros(0, np.uint8), 0)
+    b, cb = select_host_cost(lay.items, q[lo:hi], v)
+    key = shards.min_u64_over_ranks(NO_KEY if b < 0 else cost_key(cb, lo + b))
+    n_free = shards.sum_over_ranks(n_free)
+    if key == NO_KEY:
+        return -1, None, n_free, None
+    b = key & 0xFFFFFFFF
+    return b, select_host_cost(lay.items, q[b : b + 1], np.zeros(1, np.uint8))[1], n_free, None
+
+
 def _select_host_scalar(items, q: np.ndarray, verdicts: np.ndarray) -> int:
     best, best_cost = -1, None
     for i in np.flatnonzero(verdicts == 0):
@@ -233,8 +268,13 @@ def _local_round(spec: LbfSpec, step: int, r: int, t: int, best_u: float, best_q
     return q, u
 
 
-def run_host(lay, eng, spec: LbfSpec, steps: int | None = None, keep_verdicts: int = 0, on_step=None) -> LbfLog:
-    """The build with one engine call per round (oracle or GPU engine)."""
+def run_host(lay, eng, spec: LbfSpec, steps: int | None = None, keep_verdicts: int = 0, on_step=None,
+             ranks: tuple | None = None) -> LbfLog:
+    """The build with one engine call per round (oracle or GPU engine).  With ranks = (rank, world
+    size) under an initialised process group, each rank judges a slice of every round's candidates
+    against its own replica and the ranks agree on each round's choice (see `_judge`): every rank
+    returns the log of the one-process build."""
+    assert ranks is None or keep_verdicts == 0, "a rank holds only its slice's verdicts"
     steps = spec.steps if steps is None else steps
     s_rm = W.Stream(spec.seed, REMOVE_SID)
     types = W.Stream(spec.seed, TYPE_SID).u64(steps) % np.uint64(max(spec.n_types, 1))
@@ -249,20 +289,18 @@ def run_host(lay, eng, spec: LbfSpec, steps: int | None = None, keep_verdicts: i
             # LBFLoss::tighten_sample_bbox (loss.rs:34-44) by the best so far
             x1 = spec.box[2] if rec is None else min(spec.box[2], np.float32(rec[0] / np.float32(10.0)))
             q, uu = _uniform_round(spec, step, u, t, x1)
-            verdicts, nf = eng.detect_with_surrogate(q)
+            b, cb, nf, verdicts = _judge(lay, eng, q, ranks)
             n_free += nf
             if step < keep_verdicts:
                 vkeep.append(np.asarray(verdicts).copy())
-            b, cb = select_host_cost(lay.items, q, verdicts)
             if b >= 0 and (rec is None or cb < rec[0]):   # strictly better replaces (search.rs:52 keeps the first)
                 rec = (cb, float(uu[b]), q[b].copy(), (u << 24) | b)
         for r, (sg, sth) in enumerate(sigmas, start=1):
             if rec is None:
                 break   # nothing to search around (the device marks the round's candidates invalid)
             ql, ul = _local_round(spec, step, r, t, rec[1], rec[2], sg, sth)
-            vl, nf = eng.detect_with_surrogate(ql)
+            b, cb, nf, _ = _judge(lay, eng, ql, ranks)
             n_free += nf
-            b, cb = select_host_cost(lay.items, ql, vl)
             if b >= 0 and cb < rec[0]:
                 rec = (cb, float(ul[b]), ql[b].copy(), ((n_uni - 1 + r) << 24) | b)
         free_counts.append(n_free)

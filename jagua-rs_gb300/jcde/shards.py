@@ -4,6 +4,11 @@ Queries are independent and a layout is read-only while a batch runs (cd_engine.
 &self), so every rank answers its own batch against its own replica of the layout and no data
 moves between ranks on the query path.  The exchanges are the step-time reduction (the slowest
 rank sets the time of a step) and, where a caller wants every verdict in one place, a gather.
+
+An LBF-style build (lbf/src/opt/search.rs:41-66) has one real exchange per round: every rank
+judges its slice of the round's candidates, and the choice is the least (cost, index) key over
+the ranks (`min_u64_over_ranks`; `lbf.run_host(..., ranks=...)`).  Every rank then registers the
+same winner in its own replica, so the replicas stay equal with no further transfer.
 """
 from __future__ import annotations
 
@@ -60,3 +65,28 @@ def gather_verdicts(v: np.ndarray) -> np.ndarray:
     parts = [torch.empty_like(t) for _ in range(dist.get_world_size())]
     dist.all_gather(parts, t)
     return np.concatenate([p.cpu().numpy() for p in parts])
+
+
+def min_u64_over_ranks(key: int) -> int:
+    """The least of every rank's unsigned 64-bit key.  Carried as int64 with the top bit flipped,
+    which keeps the unsigned order (a < b unsigned iff a ^ 2^63 < b ^ 2^63 signed)."""
+    dist = _dist()
+    if dist is None:
+        return int(key)
+    import torch
+
+    t = torch.tensor([int(key) - (1 << 63)], dtype=torch.int64, device=_device())
+    dist.all_reduce(t, op=dist.ReduceOp.MIN)
+    return int(t.item()) + (1 << 63)
+
+
+def sum_over_ranks(x: int) -> int:
+    """The sum of every rank's count."""
+    dist = _dist()
+    if dist is None:
+        return int(x)
+    import torch
+
+    t = torch.tensor([int(x)], dtype=torch.int64, device=_device())
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return int(t.item())
